@@ -1,0 +1,295 @@
+"""Python mirror of the reference's operator interface, backed by libeb_gb300.so.
+
+The reference (Fortran 77) exposes its hot path as subroutines that share the geometry
+through COMMON blocks. Here a `Context` holds that geometry on the GPU and offers the
+same operations under the reference's names:
+
+    fasmvp / matvec            Stokes operator          (stokesbubb.f:419-614)
+    fasmvp_lap / matvec_lapl   Laplace operator         (laplace.f:159-262, 429-465)
+    cadapdr / cadapmod         Stokes layer sums        (cadapdrop.f, cadapmod.f)
+    dapif2                     Cauchy sum, IFLAG7 = 3   (dapif1.f:458-1077)
+    solvei / solve_lapl        GMRES solves             (stokesbubb.f:294-415, laplace.f:335-425)
+    fdifff                     spectral derivative      (dcfft.f:1371-1428)
+    pvintev, dirich_neu_map    PV integral, DtN map     (pv_integral.f:53-204, laplace.f:266-331)
+    interfacenew               interface velocity       (electric.f:791-912)
+    extractdat                 geometry from the RK state (electric.f:636-716)
+
+Arrays may be numpy arrays (host memory; copied in and out) or CUDA tensors exposing
+`data_ptr()` and `is_cuda` (device memory; used in place). Errors raise `EbError`,
+where the reference would print and STOP. There is no CPU fallback: without the built
+library or a CUDA device, construction fails.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import (EB_DEVICE, EB_FP32, EB_FP64, EB_HOST, EB_SOLVE_FP32_REFINED, EB_SOLVE_FP64,
+                   EbError, Opts, SolveInfo, TreeInfo, check)
+
+PRECISION = {"fp64": EB_FP64, "fp32": EB_FP32}
+SOLVE_MODE = {"fp64": EB_SOLVE_FP64, "fp32_refined": EB_SOLVE_FP32_REFINED}
+
+
+def _is_device(a):
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_device(a):
+        return ctypes.c_void_p(a.data_ptr())
+    if not (isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]):
+        raise TypeError("expected a C-contiguous numpy array or a CUDA tensor")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _mem(*arrays):
+    dev = [_is_device(a) for a in arrays if a is not None]
+    if all(dev):
+        return EB_DEVICE
+    if not any(dev):
+        return EB_HOST
+    raise TypeError("mix of host and device arrays in one call")
+
+
+def _host(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+class Context:
+    """One GPU context: geometry, trees, expansion work space and a CUDA stream."""
+
+    def __init__(self, p64=0, p32=0, leaf64=0, leaf32=0, tol64=0.0, tol32=0.0, maxl=0,
+                 gmres_tol=0.0, inner_tol=0.0, max_outer=0, device=0):
+        self._lib = _lib.load()
+        o = Opts()
+        self._lib.eb_opts_default(ctypes.byref(o))
+        for name, v in (("p64", p64), ("p32", p32), ("leaf64", leaf64), ("leaf32", leaf32),
+                        ("tol64", tol64), ("tol32", tol32), ("maxl", maxl),
+                        ("gmres_tol", gmres_tol), ("inner_tol", inner_tol),
+                        ("max_outer", max_outer)):
+            if v:
+                setattr(o, name, v)
+        o.device = device
+        h = ctypes.c_void_p()
+        check("eb_ctx_create", self._lib.eb_ctx_create(ctypes.byref(h), ctypes.byref(o)))
+        self._h = h
+        self.k = 0
+        self.nbk = 0
+        self.nd = None
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.eb_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- context -------------------------------------------------------------
+    def set_stream(self, stream_handle):
+        """Run on an existing CUDA stream (an integer cudaStream_t), or None."""
+        check("eb_ctx_set_stream", self._lib.eb_ctx_set_stream(
+            self._h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def sync(self):
+        check("eb_ctx_sync", self._lib.eb_ctx_sync(self._h))
+
+    def launch_count(self):
+        return int(self._lib.eb_ctx_launch_count(self._h))
+
+    def set_profiling(self, on=True):
+        check("eb_ctx_set_profiling", self._lib.eb_ctx_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_time(self, cls):
+        n = ctypes.c_longlong()
+        ms = ctypes.c_double()
+        check("eb_ctx_kernel_time", self._lib.eb_ctx_kernel_time(self._h, cls, ctypes.byref(n),
+                                                                 ctypes.byref(ms)))
+        return n.value, ms.value
+
+    def tree_info(self):
+        t = TreeInfo()
+        check("eb_ctx_tree_info", self._lib.eb_ctx_tree_info(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    # ---- geometry ------------------------------------------------------------
+    def set_geometry(self, nd, z, dz, dsda, kappa, zk):
+        """Install the geometry (COMMON /inteqn/ and /problem/)."""
+        nd = _host(nd, np.int32)
+        arrs = [z, dz, dsda, kappa, zk]
+        mem = _mem(*arrs)
+        if mem == EB_HOST:
+            z, dz, zk = (_host(a, np.complex128) for a in (z, dz, zk))
+            dsda, kappa = (_host(a, np.float64) for a in (dsda, kappa))
+        check("eb_set_geometry", self._lib.eb_set_geometry(
+            self._h, int(nd.shape[0]), _ptr(nd), _ptr(z), _ptr(dz), _ptr(dsda), _ptr(kappa),
+            _ptr(zk), mem))
+        self.k = int(nd.shape[0])
+        self.nbk = int(nd.sum())
+        self.nd = nd
+        self._keep = (z, dz, dsda, kappa, zk)
+
+    def extractdat(self, nd, rku):
+        """EXTRACTDAT on the GPU: install the geometry of the RK state `rku`
+        (interleaved x, y) and return it as a dict of host arrays."""
+        nd = _host(nd, np.int32)
+        k = int(nd.shape[0])
+        nbk = int(nd.sum())
+        rku = _host(rku, np.float64)
+        out = {"zk": np.zeros(k, np.complex128), "dz": np.zeros(nbk, np.complex128),
+               "dsda": np.zeros(nbk), "kappa": np.zeros(nbk), "ckern": np.zeros(nbk, np.complex128),
+               "tha": np.zeros(nbk), "area": np.zeros(k)}
+        check("eb_extractdat", self._lib.eb_extractdat(
+            self._h, k, _ptr(nd), _ptr(rku), _ptr(out["zk"]), _ptr(out["dz"]), _ptr(out["dsda"]),
+            _ptr(out["kappa"]), _ptr(out["ckern"]), _ptr(out["tha"]), _ptr(out["area"]), EB_HOST))
+        self.k = k
+        self.nbk = nbk
+        self.nd = nd
+        out["z"] = rku.view(np.complex128).copy()
+        return out
+
+    def extractdat_device(self, nd, rku_dev):
+        """EXTRACTDAT from a device RK state; nothing is copied back."""
+        nd = _host(nd, np.int32)
+        k = int(nd.shape[0])
+        check("eb_extractdat", self._lib.eb_extractdat(
+            self._h, k, _ptr(nd), _ptr(rku_dev), None, None, None, None, None, None, None,
+            EB_DEVICE))
+        self.k = k
+        self.nbk = int(nd.sum())
+        self.nd = nd
+
+    # ---- operators -----------------------------------------------------------
+    def _out(self, x, n, dtype):
+        if _is_device(x):
+            import torch
+            tdt = {np.float64: torch.float64, np.complex128: torch.complex128}[dtype]
+            return torch.empty(n, dtype=tdt, device=x.device)
+        return np.empty(n, dtype)
+
+    def fasmvp(self, x, precision="fp64", out=None):
+        """Stokes operator FASMVP / MATVEC: x, y real of length 2 nbk."""
+        if not _is_device(x):
+            x = _host(x, np.float64)
+        y = out if out is not None else self._out(x, 2 * self.nbk, np.float64)
+        check("eb_stokes_matvec", self._lib.eb_stokes_matvec(
+            self._h, 2 * self.nbk, _ptr(x), _ptr(y), PRECISION[precision], _mem(x, y)))
+        return y
+
+    matvec = fasmvp
+
+    def fasmvp_lap(self, x, precision="fp64", out=None):
+        """Laplace operator FASMVP_LAP / MATVEC_LAPL: x, y real of length nbk."""
+        if not _is_device(x):
+            x = _host(x, np.float64)
+        y = out if out is not None else self._out(x, self.nbk, np.float64)
+        check("eb_laplace_matvec", self._lib.eb_laplace_matvec(
+            self._h, self.nbk, _ptr(x), _ptr(y), PRECISION[precision], _mem(x, y)))
+        return y
+
+    matvec_lapl = fasmvp_lap
+
+    def laplace_constraints(self, x):
+        x = _host(x, np.float64)
+        s = np.empty(self.k)
+        check("eb_laplace_constraints", self._lib.eb_laplace_constraints(
+            self._h, self.nbk, _ptr(x), _ptr(s), EB_HOST))
+        return s
+
+    def stokes_sum(self, dens, sign, precision="fp64"):
+        """GRADW of CADAPDR (sign -1) or CADAPMOD (sign +1) at the installed nodes."""
+        if not _is_device(dens):
+            dens = _host(dens, np.complex128)
+        g = self._out(dens, self.nbk, np.complex128)
+        check("eb_stokes_sum", self._lib.eb_stokes_sum(
+            self._h, self.nbk, _ptr(dens), int(sign), _ptr(g), PRECISION[precision], _mem(dens, g)))
+        return g
+
+    def cadapdr(self, dens, precision="fp64"):
+        return self.stokes_sum(dens, -1, precision)
+
+    def cadapmod(self, dens, precision="fp64"):
+        return self.stokes_sum(dens, +1, precision)
+
+    def dapif2(self, z, q, precision="fp64"):
+        """FIELD of DAPIF2 with IFLAG7 = 3: sum_{j != i} q_j / (z_i - z_j)."""
+        if not _is_device(z):
+            z = _host(z, np.complex128)
+            q = _host(q, np.complex128)
+        n = int(z.shape[0])
+        f = self._out(z, n, np.complex128)
+        check("eb_cauchy_sum", self._lib.eb_cauchy_sum(
+            self._h, n, _ptr(z), _ptr(q), _ptr(f), PRECISION[precision], _mem(z, q, f)))
+        return f
+
+    def _solve(self, fn, n, rhs, mode, out):
+        if not _is_device(rhs):
+            rhs = _host(rhs, np.float64)
+        x = out if out is not None else self._out(rhs, n, np.float64)
+        info = SolveInfo()
+        st = getattr(self._lib, fn)(self._h, n, _ptr(rhs), _ptr(x), SOLVE_MODE[mode],
+                                    ctypes.byref(info), _mem(rhs, x))
+        check(fn, st)
+        return x, info.as_dict()
+
+    def solvei(self, rhs, mode="fp64", out=None):
+        """SOLVEI: GMRES on the Stokes operator, x0 = rhs. Returns (soln, info)."""
+        return self._solve("eb_stokes_solve", 2 * self.nbk, rhs, mode, out)
+
+    def solve_lapl(self, rhs, mode="fp64", out=None):
+        """SOLVE_LAPL: GMRES on the Laplace operator, x0 = rhs. Returns (soln, info)."""
+        return self._solve("eb_laplace_solve", self.nbk, rhs, mode, out)
+
+    def fdifff(self, f):
+        """FDIFFF per drop of the installed geometry (complex samples)."""
+        f = _host(f, np.complex128)
+        df = np.empty_like(f)
+        check("eb_fdiff", self._lib.eb_fdiff(self._h, _ptr(f), _ptr(df), EB_HOST))
+        return df
+
+    def pvintev(self, ucmplx, precision="fp64"):
+        u = _host(ucmplx, np.complex128)
+        phi = np.empty_like(u)
+        check("eb_pvintev", self._lib.eb_pvintev(self._h, _ptr(u), _ptr(phi),
+                                                 PRECISION[precision], EB_HOST))
+        return phi
+
+    def dirich_neu_map(self, u, precision="fp64"):
+        u = _host(u, np.float64)
+        phi = np.empty(self.nbk)
+        psi = np.empty(self.nbk)
+        dphi = np.empty(self.nbk)
+        check("eb_dirich_neu_map", self._lib.eb_dirich_neu_map(
+            self._h, _ptr(u), _ptr(phi), _ptr(psi), _ptr(dphi), PRECISION[precision], EB_HOST))
+        return phi, psi, dphi
+
+    def interfacenew(self, u, zc, cap=0.0, precision="fp64"):
+        """INTERFACENEW: (Un, FLUX) from the Stokes density u (complex)."""
+        u = _host(u, np.complex128)
+        zc = _host(zc, np.complex128)
+        un = np.empty(self.nbk)
+        flux = ctypes.c_double()
+        check("eb_interface_velocity", self._lib.eb_interface_velocity(
+            self._h, _ptr(u), _ptr(zc), float(cap), _ptr(un), ctypes.byref(flux),
+            PRECISION[precision], EB_HOST))
+        return un, flux.value
+
+
+def geometry_from_extract(ctx, cfg):
+    """Install cfg's geometry by EXTRACTDAT on the GPU; returns the geometry dict."""
+    return ctx.extractdat(cfg.nd, cfg.rku())
+
+
+__all__ = ["Context", "EbError", "geometry_from_extract", "PRECISION", "SOLVE_MODE"]

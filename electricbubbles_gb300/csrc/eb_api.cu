@@ -1,0 +1,518 @@
+// C ABI of libeb_gb300: context, geometry, operator applies and the Fortran shims.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "eb_internal.h"
+
+// ---------------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------------
+static thread_local std::string g_last_error;
+
+void eb_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  g_last_error = buf;
+}
+void eb_set_last_error_msg(const char* msg) { g_last_error = msg; }
+
+int eb_check_launch(eb_ctx* ctx, const char* name) {
+  (void)ctx;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    eb_set_last_cuda_error(e, name, __FILE__, __LINE__);
+    return EB_ERR_CUDA;
+  }
+  return EB_OK;
+}
+
+cudaStream_t eb_stream(eb_ctx* ctx) { return ctx->stream; }
+
+namespace {
+
+inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+// Per-drop reductions of FASMVP (stokesbubb.f:549-565): za_k = h sum dens,
+// pk_k = sum 2 h Re(dens dz/(z - zk)^2) / pi. One block per drop.
+__global__ void k_drop_reduce_stokes(const int* __restrict__ start, const double2* __restrict__ dens,
+                                     const double2* __restrict__ dz, const double2* __restrict__ z,
+                                     const double2* __restrict__ zk, double2* __restrict__ za,
+                                     double* __restrict__ pk) {
+  __shared__ double s[3][256];
+  int b = blockIdx.x;
+  int i0 = start[b], i1 = start[b + 1];
+  double h = 2.0 * EB_PI / (double)(i1 - i0);
+  double ax = 0.0, ay = 0.0, pp = 0.0;
+  double2 c = zk[b];
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    double2 u = dens[i];
+    double2 d = make_double2(z[i].x - c.x, z[i].y - c.y);
+    double2 d2 = cmul<double>(d, d);
+    double2 num = cmul<double>(u, dz[i]);
+    double2 q = cdiv<double>(num, d2);
+    pp += 2.0 * h * q.x / EB_PI;
+    ax += u.x;
+    ay += u.y;
+  }
+  s[0][threadIdx.x] = ax; s[1][threadIdx.x] = ay; s[2][threadIdx.x] = pp;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s[0][threadIdx.x] += s[0][threadIdx.x + o];
+      s[1][threadIdx.x] += s[1][threadIdx.x + o];
+      s[2][threadIdx.x] += s[2][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    za[b] = make_double2(h * s[0][0], h * s[1][0]);
+    pk[b] = s[2][0];
+  }
+}
+
+// Identity, self and singular terms of FASMVP (stokesbubb.f:585-612).
+__global__ void k_fasmvp_post(int nbk, const int* __restrict__ drop_of, const double2* __restrict__ dens,
+                              const double2* __restrict__ z, const double2* __restrict__ dz,
+                              const double* __restrict__ dsda, const double* __restrict__ kappa,
+                              const double* __restrict__ hpt, const double2* __restrict__ za,
+                              const double* __restrict__ pk, const double2* __restrict__ stress,
+                              double2* __restrict__ w) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbk) return;
+  int b = drop_of[t];
+  double2 u = dens[t];
+  double qwi = hpt[t], s = dsda[t], kap = kappa[t];
+  double2 zn = make_double2(dz[t].y / s, -dz[t].x / s);  // -i dz / s'
+  double c1 = qwi * s * 0.5 * kap / EB_PI;
+  double2 zn2 = cmul<double>(zn, zn);
+  double2 zself = cscale<double>(u, c1);
+  zself = csub<double>(zself, cscale<double>(cmul<double>(cconj<double>(u), zn2), c1));
+  double pinf = -pk[0];
+  double pkb = pk[b] + pinf;
+  double f = -0.5 * (pinf - pkb);  // times i z
+  double2 zz = z[t];
+  double2 st = stress[t];
+  st.x += zself.x - f * zz.y;
+  st.y += zself.y + f * zz.x;
+  double2 zab = za[b];
+  w[t] = make_double2(u.x + zab.x + st.x, u.y + zab.y + st.y);
+}
+
+// Charges of FASMVP_LAP (laplace.f:190-200): q = u dz h.
+__global__ void k_lap_charges(int nbk, const double* __restrict__ u, const double2* __restrict__ dz,
+                              const double* __restrict__ hpt, double2* __restrict__ q) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbk) return;
+  double f = u[t] * hpt[t];
+  q[t] = make_double2(f * dz[t].x, f * dz[t].y);
+}
+
+// Discrete operator of FASMVP_LAP (laplace.f:225-243).
+__global__ void k_lap_post(int nbk, const double* __restrict__ u, const double* __restrict__ dsda,
+                           const double* __restrict__ kappa, const double* __restrict__ hpt,
+                           const double2* __restrict__ cf, double* __restrict__ w) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbk) return;
+  double hs = hpt[t];
+  double self = 0.25 * hs * kappa[t] * dsda[t] / EB_PI;
+  // Re(cf / (2 pi i)) = Im(cf) / (2 pi)
+  double zc = self * u[t] - cf[t].y / (2.0 * EB_PI);
+  double wt = u[t] + 2.0 * zc;
+  double du = hs * u[t] * dsda[t];
+  w[t] = wt - 2.0 * du;
+}
+
+// Constraint sums the reference writes past YY(N) (laplace.f:252-259): h s' u per drop.
+__global__ void k_lap_constraints(const int* __restrict__ start, const double* __restrict__ u,
+                                  const double* __restrict__ dsda, double* __restrict__ sums) {
+  __shared__ double s[256];
+  int b = blockIdx.x;
+  int i0 = start[b], i1 = start[b + 1];
+  double h = 2.0 * EB_PI / (double)(i1 - i0), acc = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += h * dsda[i] * u[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[b] = s[0];
+}
+
+__global__ void k_fill_drop(int k, const int* __restrict__ start, int* __restrict__ drop_of,
+                            double* __restrict__ hpt) {
+  int b = blockIdx.x;
+  if (b >= k) return;
+  int i0 = start[b], i1 = start[b + 1];
+  double h = 2.0 * EB_PI / (double)(i1 - i0);
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    drop_of[i] = b;
+    hpt[i] = h;
+  }
+}
+
+int copy_in(eb_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem) {
+  EB_TRY(buf.ensure(bytes));
+  EB_CUDA_TRY(cudaMemcpyAsync(buf.p, src, bytes,
+                              mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                              ctx->stream));
+  return EB_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// Context. The public functions are declared extern "C" in eb_gb300.h, which gives
+// these definitions C linkage.
+// ---------------------------------------------------------------------------------
+
+int eb_version(void) { return EB_GB300_VERSION; }
+
+const char* eb_status_string(int s) {
+  switch (s) {
+    case EB_OK: return "ok";
+    case EB_ERR_ARG: return "invalid argument";
+    case EB_ERR_CUDA: return "CUDA error";
+    case EB_ERR_NOGEOM: return "no geometry installed";
+    case EB_ERR_WORKSPACE: return "size exceeds capacity";
+    case EB_ERR_TOL: return "tolerance needs too many expansion terms";
+    case EB_ERR_NAN: return "non-finite value";
+    case EB_ERR_NOT_CONVERGED: return "GMRES did not converge";
+    case EB_ERR_NODEVICE: return "no CUDA device";
+    case EB_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+const char* eb_last_error(void) { return g_last_error.c_str(); }
+
+void eb_opts_default(eb_opts* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->p64 = 44;
+  o->p32 = 20;
+  o->leaf64 = 32;
+  o->leaf32 = 32;
+  o->tol64 = 1e-15;
+  o->tol32 = 1e-7;
+  o->maxl = 100;
+  o->gmres_tol = 1e-10;
+  o->inner_tol = 1e-5;
+  o->max_outer = 8;
+  o->device = 0;
+}
+
+int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
+  if (!out) return EB_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev <= 0) {
+    eb_set_last_error_msg("no CUDA device is available");
+    return EB_ERR_NODEVICE;
+  }
+  eb_ctx* c = new eb_ctx();
+  eb_opts_default(&c->opts);
+  if (opts) {
+    eb_opts o = *opts;
+    eb_opts d;
+    eb_opts_default(&d);
+    if (o.p64 <= 0) o.p64 = d.p64;
+    if (o.p32 <= 0) o.p32 = d.p32;
+    if (o.leaf64 <= 0) o.leaf64 = d.leaf64;
+    if (o.leaf32 <= 0) o.leaf32 = d.leaf32;
+    if (o.tol64 <= 0) o.tol64 = d.tol64;
+    if (o.tol32 <= 0) o.tol32 = d.tol32;
+    if (o.maxl <= 0) o.maxl = d.maxl;
+    if (o.gmres_tol <= 0) o.gmres_tol = d.gmres_tol;
+    if (o.inner_tol <= 0) o.inner_tol = d.inner_tol;
+    if (o.max_outer <= 0) o.max_outer = d.max_outer;
+    c->opts = o;
+  }
+  if (c->opts.device < 0 || c->opts.device >= ndev) {
+    delete c;
+    eb_set_last_error_msg("device ordinal out of range");
+    return EB_ERR_ARG;
+  }
+  c->device = c->opts.device;
+  e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e != cudaSuccess) {
+    eb_set_last_cuda_error(e, "context setup", __FILE__, __LINE__);
+    delete c;
+    return EB_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  int st = eb_tables_init(c);
+  if (st != EB_OK) {
+    eb_ctx_destroy(c);
+    return st;
+  }
+  *out = c;
+  return EB_OK;
+}
+
+int eb_ctx_destroy(eb_ctx* ctx) {
+  if (!ctx) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return EB_OK;
+}
+
+int eb_ctx_set_stream(eb_ctx* ctx, void* s) {
+  if (!ctx) return EB_ERR_ARG;
+  ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
+  return EB_OK;
+}
+
+int eb_ctx_sync(eb_ctx* ctx) {
+  if (!ctx) return EB_ERR_ARG;
+  EB_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return EB_OK;
+}
+
+long long eb_ctx_launch_count(eb_ctx* ctx) { return ctx ? ctx->launches : -1; }
+
+int eb_ctx_set_profiling(eb_ctx* ctx, int enable) {
+  if (!ctx) return EB_ERR_ARG;
+  ctx->profiling = enable != 0;
+  ctx->prof_launch[0] = ctx->prof_launch[1] = 0;
+  ctx->prof_ms[0] = ctx->prof_ms[1] = 0.0;
+  return EB_OK;
+}
+
+int eb_ctx_kernel_time(eb_ctx* ctx, int cls, long long* launches, double* total_ms) {
+  if (!ctx || cls < 0 || cls > 1) return EB_ERR_ARG;
+  if (launches) *launches = ctx->prof_launch[cls];
+  if (total_ms) *total_ms = ctx->prof_ms[cls];
+  return EB_OK;
+}
+
+int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info) {
+  if (!ctx || !info) return EB_ERR_ARG;
+  if (!ctx->tree.valid) return EB_ERR_NOGEOM;
+  info->npoints = ctx->tree.n;
+  info->levels = ctx->tree.L;
+  info->nboxes = ctx->tree.nbox;
+  info->nleaves = ctx->tree.nleaf;
+  info->v_pairs = ctx->tree.v_pairs;
+  info->u_pairs = ctx->tree.u_pairs;
+  info->p = ctx->last_p;
+  return EB_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Geometry
+// ---------------------------------------------------------------------------------
+int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const double* dz,
+                    const double* dsda, const double* kappa, const double* zk, int mem) {
+  if (!ctx || k <= 0 || !nd || !z || !dz || !dsda || !kappa || !zk) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  std::vector<int> st(k + 1, 0);
+  for (int b = 0; b < k; ++b) {
+    if (nd[b] < 2) {
+      eb_set_last_error_msg("every drop needs at least 2 nodes");
+      return EB_ERR_ARG;
+    }
+    st[b + 1] = st[b] + nd[b];
+  }
+  int nbk = st[k];
+  ctx->geom_valid = false;
+  ctx->ckern_valid = false;
+  ctx->k = k;
+  ctx->nbk = nbk;
+  ctx->nd_host.assign(nd, nd + k);
+  ctx->start_host = st;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->nd.ensure(sizeof(int) * k));
+  EB_TRY(ctx->start.ensure(sizeof(int) * (k + 1)));
+  EB_TRY(ctx->drop_of.ensure(sizeof(int) * nbk));
+  EB_TRY(ctx->hpt.ensure(sizeof(double) * nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->nd.p, nd, sizeof(int) * k, cudaMemcpyHostToDevice, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->start.p, st.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, s));
+  EB_TRY(copy_in(ctx, ctx->z, z, sizeof(double2) * nbk, mem));
+  EB_TRY(copy_in(ctx, ctx->dz, dz, sizeof(double2) * nbk, mem));
+  EB_TRY(copy_in(ctx, ctx->dsda, dsda, sizeof(double) * nbk, mem));
+  EB_TRY(copy_in(ctx, ctx->kappa, kappa, sizeof(double) * nbk, mem));
+  EB_TRY(copy_in(ctx, ctx->zk, zk, sizeof(double2) * k, mem));
+  k_fill_drop<<<k, 256, 0, s>>>(k, ctx->start.as<int>(), ctx->drop_of.as<int>(), ctx->hpt.as<double>());
+  eb_count_launch(ctx);
+  EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
+  ctx->tree_pv.valid = false;
+  ctx->geom_valid = true;
+  return EB_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Operators on device vectors
+// ---------------------------------------------------------------------------------
+int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw, int prec) {
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  return eb_fmm_apply(ctx, ctx->tree, 0, sign, prec, dens, ctx->dz.as<double2>(),
+                      ctx->hpt.as<double>(), gradw);
+}
+
+int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  cudaStream_t s = ctx->stream;
+  int nbk = ctx->nbk, k = ctx->k;
+  const double2* dens = reinterpret_cast<const double2*>(x);
+  EB_TRY(ctx->za.ensure(sizeof(double2) * k));
+  EB_TRY(ctx->pk.ensure(sizeof(double) * k));
+  EB_TRY(ctx->stress.ensure(sizeof(double2) * nbk));
+  k_drop_reduce_stokes<<<k, 256, 0, s>>>(ctx->start.as<int>(), dens, ctx->dz.as<double2>(),
+                                         ctx->z.as<double2>(), ctx->zk.as<double2>(),
+                                         ctx->za.as<double2>(), ctx->pk.as<double>());
+  eb_count_launch(ctx);
+  EB_TRY(eb_stokes_sum_dev(ctx, dens, -1, ctx->stress.as<double2>(), prec));
+  k_fasmvp_post<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->drop_of.as<int>(), dens, ctx->z.as<double2>(),
+                                               ctx->dz.as<double2>(), ctx->dsda.as<double>(),
+                                               ctx->kappa.as<double>(), ctx->hpt.as<double>(),
+                                               ctx->za.as<double2>(), ctx->pk.as<double>(),
+                                               ctx->stress.as<double2>(), reinterpret_cast<double2*>(y));
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "stokes matvec");
+}
+
+int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  cudaStream_t s = ctx->stream;
+  int nbk = ctx->nbk;
+  EB_TRY(ctx->vtmp.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->stress.ensure(sizeof(double2) * nbk));
+  k_lap_charges<<<nblk(nbk, 256), 256, 0, s>>>(nbk, x, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
+                                               ctx->vtmp.as<double2>());
+  eb_count_launch(ctx);
+  EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, ctx->vtmp.as<double2>(), ctx->stress.as<double2>()));
+  k_lap_post<<<nblk(nbk, 256), 256, 0, s>>>(nbk, x, ctx->dsda.as<double>(), ctx->kappa.as<double>(),
+                                            ctx->hpt.as<double>(), ctx->stress.as<double2>(), y);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "laplace matvec");
+}
+
+// Host/device dispatch for an operator y = A x with nin, nout doubles.
+template <typename F>
+static int run_op(eb_ctx* ctx, const double* x, size_t nin, double* y, size_t nout, int mem, F f) {
+  if (mem == EB_DEVICE) return f(x, y);
+  if (mem != EB_HOST) return EB_ERR_ARG;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->vin.ensure(sizeof(double) * nin));
+  EB_TRY(ctx->vout.ensure(sizeof(double) * nout));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, x, sizeof(double) * nin, cudaMemcpyHostToDevice, s));
+  EB_TRY(f(ctx->vin.as<double>(), ctx->vout.as<double>()));
+  EB_CUDA_TRY(cudaMemcpyAsync(y, ctx->vout.p, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_stokes_matvec(eb_ctx* ctx, int n, const double* x, double* y, int prec, int mem) {
+  if (!ctx || !x || !y) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != 2 * ctx->nbk || (prec != EB_FP64 && prec != EB_FP32)) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return run_op(ctx, x, n, y, n, mem, [&](const double* xd, double* yd) {
+    return eb_stokes_matvec_dev(ctx, xd, yd, prec);
+  });
+}
+
+int eb_laplace_matvec(eb_ctx* ctx, int n, const double* x, double* y, int prec, int mem) {
+  if (!ctx || !x || !y) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != ctx->nbk || (prec != EB_FP64 && prec != EB_FP32)) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return run_op(ctx, x, n, y, n, mem, [&](const double* xd, double* yd) {
+    return eb_laplace_matvec_dev(ctx, xd, yd, prec);
+  });
+}
+
+int eb_laplace_constraints(eb_ctx* ctx, int n, const double* x, double* sums, int mem) {
+  if (!ctx || !x || !sums) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != ctx->nbk) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return run_op(ctx, x, n, sums, ctx->k, mem, [&](const double* xd, double* yd) {
+    k_lap_constraints<<<ctx->k, 256, 0, ctx->stream>>>(ctx->start.as<int>(), xd, ctx->dsda.as<double>(), yd);
+    eb_count_launch(ctx);
+    return eb_check_launch(ctx, "laplace constraints");
+  });
+}
+
+int eb_stokes_sum(eb_ctx* ctx, int n, const double* dens, int sign, double* gradw, int prec,
+                  int mem) {
+  if (!ctx || !dens || !gradw || (sign != 1 && sign != -1)) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != ctx->nbk || (prec != EB_FP64 && prec != EB_FP32)) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return run_op(ctx, dens, 2 * (size_t)n, gradw, 2 * (size_t)n, mem, [&](const double* xd, double* yd) {
+    return eb_stokes_sum_dev(ctx, reinterpret_cast<const double2*>(xd), sign,
+                             reinterpret_cast<double2*>(yd), prec);
+  });
+}
+
+int eb_cauchy_sum(eb_ctx* ctx, int n, const double* z, const double* q, double* field, int prec,
+                  int mem) {
+  if (!ctx || !z || !q || !field || n <= 0) return EB_ERR_ARG;
+  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const double2* zd = reinterpret_cast<const double2*>(z);
+  const double2* qd = reinterpret_cast<const double2*>(q);
+  double2* fd = reinterpret_cast<double2*>(field);
+  if (mem == EB_HOST) {
+    EB_TRY(copy_in(ctx, ctx->pvz, z, sizeof(double2) * n, mem));
+    EB_TRY(copy_in(ctx, ctx->pvq, q, sizeof(double2) * n, mem));
+    EB_TRY(ctx->pvout.ensure(sizeof(double2) * n));
+    zd = ctx->pvz.as<double2>();
+    qd = ctx->pvq.as<double2>();
+    fd = ctx->pvout.as<double2>();
+  }
+  EB_TRY(eb_tree_build(ctx, ctx->tree_tmp, zd, n, ctx->opts.leaf64));
+  EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree_tmp, prec, qd, fd));
+  if (mem == EB_HOST) {
+    EB_CUDA_TRY(cudaMemcpyAsync(field, fd, sizeof(double2) * n, cudaMemcpyDeviceToHost, s));
+    EB_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return EB_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// gfortran shims: MATVEC(N, XX, YY, NELT, IA, JA, A, ISYM) as DPIGMR calls it.
+// ---------------------------------------------------------------------------------
+static eb_ctx* g_default_ctx = nullptr;
+
+int eb_set_default_ctx(eb_ctx* ctx) {
+  g_default_ctx = ctx;
+  return EB_OK;
+}
+
+static void shim_fail(const char* who, int st) {
+  fprintf(stderr, "%s: %s: %s\n", who, eb_status_string(st), eb_last_error());
+  abort();
+}
+
+void matvec_(const int* n, const double* xx, double* yy, const int* nelt, const int* ia,
+             const int* ja, const double* a, const int* isym) {
+  (void)nelt; (void)ia; (void)ja; (void)a; (void)isym;
+  if (!g_default_ctx) shim_fail("matvec_", EB_ERR_NOGEOM);
+  int st = eb_stokes_matvec(g_default_ctx, *n, xx, yy, EB_FP64, EB_HOST);
+  if (st != EB_OK) shim_fail("matvec_", st);
+}
+
+void matvec_lapl_(const int* n, const double* xx, double* yy, const int* nelt, const int* ia,
+                  const int* ja, const double* a, const int* isym) {
+  (void)nelt; (void)ia; (void)ja; (void)a; (void)isym;
+  if (!g_default_ctx) shim_fail("matvec_lapl_", EB_ERR_NOGEOM);
+  int st = eb_laplace_matvec(g_default_ctx, *n, xx, yy, EB_FP64, EB_HOST);
+  if (st != EB_OK) shim_fail("matvec_lapl_", st);
+}

@@ -1,0 +1,136 @@
+// Internal declarations shared by the translation units of libeb_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "eb_common.cuh"
+
+// Deepest level of the point keys (2*EB_KEY_LEVELS bits of Morton code).
+#define EB_KEY_LEVELS 20
+#define EB_MAX_P 60
+#define EB_VMAX 27
+#define EB_UMAX 9
+#define EB_NCODE 49
+
+// ---------------------------------------------------------------------------------
+// Device buffer that grows on demand (never shrinks) and frees itself.
+// ---------------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t nbytes);
+  void release();
+  ~DevBuf() { release(); }
+  template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+// Sparse uniform-depth quadtree over a point set, built on the GPU.
+// Boxes of level l are stored in Morton order in the global box range
+// [lev_off[l], lev_off[l+1]); every box owns a contiguous range of the sorted points.
+struct EbTree {
+  int n = 0;
+  int L = 0;                 // leaf level
+  int nbox = 0;
+  int nleaf = 0;
+  int lev_off[EB_KEY_LEVELS + 2] = {0};
+  double x0 = 0, y0 = 0, W = 1;  // root square [x0, x0+W] x [y0, y0+W]
+  long long v_pairs = 0, u_pairs = 0;
+  bool valid = false;
+
+  DevBuf perm;     // int[n]: sorted index -> original index
+  DevBuf zs;       // double2[n]: sorted positions
+  DevBuf zhi, zlo; // float2[n]: sorted positions as float hi + lo
+  DevBuf keys, keys_alt, idx_alt;  // sort buffers
+  DevBuf bkey;     // unsigned long long[nbox]: Morton key of the box at its level
+  DevBuf pt0, pt1; // int[nbox]: point range
+  DevBuf parent;   // int[nbox]
+  DevBuf child0, nchild;  // int[nbox]
+  DevBuf vlist;    // int[nbox*EB_VMAX]
+  DevBuf vcode;    // unsigned char[nbox*EB_VMAX]
+  DevBuf vcount;   // int[nbox]
+  DevBuf ulist;    // int[nleaf*EB_UMAX] (global box ids)
+  DevBuf ucount;   // int[nleaf]
+  DevBuf flags, scan, hist, bbox, partial, cubtmp;
+};
+
+// Per-precision constant tables for the translation operators.
+struct EbTables {
+  int p = 0;
+  DevBuf binom;   // T[(2p+2)*(2p+2)] binomial coefficients C(i, j) at [i*(2p+2)+j]
+  DevBuf dinv;    // c_t<T>[EB_NCODE*(p+2)]: d^-j for the 49 offset codes
+  DevBuf pd;      // int[EB_NCODE]: per-offset truncation order
+  DevBuf epow;    // c_t<T>[4*(p+2)]: e_q^j for the 4 child offsets (child units)
+  DevBuf einv;    // c_t<T>[4*(p+2)]: e_q^-j
+};
+
+struct EbFmmWork {
+  DevBuf qa, qb;     // c_t<T>[n] sorted charges (P2M)
+  DevBuf pq, aa;     // near-field source data (P2P)
+  DevBuf mpole;      // c_t<T>[nbox*E*p]
+  DevBuf local;      // c_t<T>[nbox*E*(p+1)]
+};
+
+struct eb_ctx {
+  eb_opts opts;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  long long launches = 0;
+  bool profiling = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long prof_launch[2] = {0, 0};
+  double prof_ms[2] = {0, 0};
+  int last_p = 0;
+
+  // installed geometry (COMMON /inteqn/ and /problem/)
+  int k = 0, nbk = 0;
+  std::vector<int> nd_host;
+  std::vector<int> start_host;
+  DevBuf nd, start, drop_of;     // int[k], int[k+1], int[nbk]
+  DevBuf z, dz, zk, ckern;       // double2
+  DevBuf dsda, kappa, tha, hpt;  // double
+  bool geom_valid = false;
+  bool ckern_valid = false;       // ckern/tha filled by eb_extractdat
+
+  EbTree tree;      // tree over the nodes
+  EbTree tree_pv;   // tree over the 2N fine points of PVINTEV
+  EbTree tree_tmp;  // tree for eb_cauchy_sum on caller points
+  EbTables tab64, tab32;
+  EbFmmWork work64, work32;
+
+  // operator scratch
+  DevBuf za, pk, redpart;          // per-drop reductions
+  DevBuf vin, vout, vtmp, vtmp2;   // host-path staging and temporaries
+  DevBuf stress;                   // double2[nbk]
+  DevBuf pvz, pvq, pvout;          // PVINTEV fine grid
+  DevBuf fftbuf, fftbuf2;          // spectral scratch
+
+  // GMRES workspace
+  DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ;
+  std::vector<double> hH;
+};
+
+// tree.cu
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target);
+
+// fmm.cu
+int eb_tables_init(eb_ctx* ctx);
+// kernel: 0 = Stokes (sign from `sign`), 1 = Cauchy
+int eb_fmm_apply(eb_ctx* ctx, EbTree& t, int kernel, int sign, int precision,
+                 const double2* dens, const double2* dz, const double* hpt, double2* out);
+int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q,
+                        double2* out);
+
+// api.cu: operators on device vectors (x, y device pointers)
+int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw, int prec);
+int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
+int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
+
+// api.cu helpers
+cudaStream_t eb_stream(eb_ctx* ctx);
+inline void eb_count_launch(eb_ctx* ctx) { ctx->launches++; }
+int eb_check_launch(eb_ctx* ctx, const char* name);

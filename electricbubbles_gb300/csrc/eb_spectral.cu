@@ -1,0 +1,548 @@
+// Per-drop spectral kernels: one thread block per drop, the drop's samples and the
+// FFT twiddles resident in shared memory (one HBM read and one write per transform).
+// The FFT is an in-place radix-2 decimation-in-time transform with the unnormalised
+// DCFFTF (exp(-i..)) / DCFFTB (exp(+i..)) conventions (dcfft.f:1-77, 715-790);
+// drop sizes must be powers of two (as in every configuration of the reference runs).
+//
+// Routines: FDIFFF (dcfft.f:1371-1428), EXTRACTDAT (electric.f:636-716), the FINTERC /
+// FINTER interpolation and alternating-point rule of PVINTEV (pv_integral.f:53-345),
+// DIRICH_NEU_MAP (laplace.f:266-331) and INTERFACENEW (electric.f:791-912).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "eb_internal.h"
+
+namespace {
+
+inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+constexpr int SBS = 512;
+
+// tw[j] = exp(+2 pi i j / N), j < N/2: one table serves both directions (the forward
+// transform uses the conjugate) and every size n dividing N.
+__device__ __forceinline__ void make_twiddles(double2* tw, int N) {
+  for (int j = threadIdx.x; j < N / 2; j += blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)j / (double)N, &s, &c);
+    tw[j] = make_double2(c, s);
+  }
+}
+
+// In-place FFT of a[0..n): sign = -1 is DCFFTF's exp(-i..), +1 is DCFFTB's exp(+i..).
+__device__ void smem_fft(double2* a, int n, const double2* tw, int N, int sign) {
+  int logn = 31 - __clz(n);
+  int mult = N / n;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int j = (int)(__brev((unsigned)i) >> (32 - logn));
+    if (i < j) {
+      double2 t = a[i];
+      a[i] = a[j];
+      a[j] = t;
+    }
+  }
+  __syncthreads();
+  for (int len = 2; len <= n; len <<= 1) {
+    int half = len >> 1, step = (n / len) * mult;
+    for (int b = threadIdx.x; b < n / 2; b += blockDim.x) {
+      int grp = b / half, j = b - grp * half;
+      int i = grp * len + j;
+      double2 t = tw[j * step];
+      if (sign < 0) t.y = -t.y;
+      double2 u = a[i], v = cmul<double>(a[i + half], t);
+      a[i] = make_double2(u.x + v.x, u.y + v.y);
+      a[i + half] = make_double2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+}
+
+// Derivative in Fourier space: c_k -> i k c_k / n for |k| < n/2, Nyquist and mean zeroed
+// (FDIFFF, dcfft.f:1395-1425).
+__device__ void spectral_deriv(double2* a, int n) {
+  double inv = 1.0 / (double)n;
+  for (int m = threadIdx.x; m < n; m += blockDim.x) {
+    int k = (m <= n / 2) ? m : m - n;
+    if (m == n / 2 || m == 0) {
+      a[m] = make_double2(0.0, 0.0);
+    } else {
+      double2 c = a[m];
+      double f = (double)k * inv;
+      a[m] = make_double2(-f * c.y, f * c.x);
+    }
+  }
+  __syncthreads();
+}
+
+// FDIFFF of each drop's complex samples.
+__global__ void k_fdiff(const int* __restrict__ start, const double2* __restrict__ f,
+                        double2* __restrict__ df, int nmax) {
+  extern __shared__ double2 sm[];
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0;
+  double2* a = sm;
+  double2* tw = sm + nmax;
+  make_twiddles(tw, n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = f[i0 + i];
+  smem_fft(a, n, tw, n, -1);
+  spectral_deriv(a, n);
+  smem_fft(a, n, tw, n, +1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) df[i0 + i] = a[i];
+}
+
+// Same, for a real input (imaginary part zero).
+__global__ void k_fdiff_real(const int* __restrict__ start, const double* __restrict__ f,
+                             double2* __restrict__ df, int nmax) {
+  extern __shared__ double2 sm[];
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0;
+  double2* a = sm;
+  double2* tw = sm + nmax;
+  make_twiddles(tw, n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(f[i0 + i], 0.0);
+  smem_fft(a, n, tw, n, -1);
+  spectral_deriv(a, n);
+  smem_fft(a, n, tw, n, +1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) df[i0 + i] = a[i];
+}
+
+__device__ double block_sum_d(double v, double* red) {
+  v = warp_sum<double>(v);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
+    r = warp_sum<double>(r);
+    if (l == 0) red[0] = r;
+  }
+  __syncthreads();
+  r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// EXTRACTDAT per drop: zk = mean of z (its zero Fourier mode / n), z' = FDIFFF(z),
+// z'' = FDIFFF(z'), kappa = -(x'y'' - y'x'')/|z'|^3, ckern = -z''/z', tha = -kappa |z'|,
+// dz = -z', dsda = |dz|, area = 2 pi mean(y Re(dz)).
+__global__ void k_extractdat(const int* __restrict__ start, const double2* __restrict__ z,
+                             double2* __restrict__ zk, double2* __restrict__ dz,
+                             double* __restrict__ dsda, double* __restrict__ kappa,
+                             double2* __restrict__ ckern, double* __restrict__ tha,
+                             double* __restrict__ area, int nmax) {
+  extern __shared__ double2 sm[];
+  __shared__ double red[32];
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0;
+  double2* a = sm;
+  double2* d1 = sm + nmax;
+  double2* tw = d1 + nmax;
+  make_twiddles(tw, n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = z[i0 + i];
+  smem_fft(a, n, tw, n, -1);
+  if (threadIdx.x == 0) zk[b] = make_double2(a[0].x / n, a[0].y / n);
+  __syncthreads();
+  spectral_deriv(a, n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) d1[i] = a[i];
+  smem_fft(d1, n, tw, n, +1);  // d1 = z'
+  // second derivative from the samples of z' (FDIFFF applied twice, as the reference)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = d1[i];
+  smem_fft(a, n, tw, n, -1);
+  spectral_deriv(a, n);
+  smem_fft(a, n, tw, n, +1);  // a = z''
+  double ysum = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double xd = d1[i].x, yd = d1[i].y, xdd = a[i].x, ydd = a[i].y;
+    double dsdt = sqrt(xd * xd + yd * yd);
+    double kap = -(xd * ydd - yd * xdd) / (dsdt * dsdt * dsdt);
+    int t = i0 + i;
+    kappa[t] = kap;
+    double2 ck = cdiv<double>(make_double2(xdd, ydd), make_double2(xd, yd));
+    ckern[t] = make_double2(-ck.x, -ck.y);
+    tha[t] = -kap * dsdt;
+    dz[t] = make_double2(-xd, -yd);
+    dsda[t] = dsdt;
+    ysum += z[t].y * (-xd);
+  }
+  ysum = block_sum_d(ysum, red);
+  if (threadIdx.x == 0) area[b] = 2.0 * EB_PI * ysum / (double)n;
+}
+
+// PVINTEV interpolation (pv_integral.f:143-166): per drop, FINTERC of ucmplx and FINTER
+// of x and y from n to 2n points; charges QA = U2 h on the odd fine nodes (0-based),
+// zero on the even ones (the original nodes).
+__global__ void k_pv_interp(const int* __restrict__ start, const double2* __restrict__ z,
+                            const double2* __restrict__ uc, double2* __restrict__ zf,
+                            double2* __restrict__ qf, int nmax, int want_positions) {
+  extern __shared__ double2 sm[];
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0, nf = 2 * n;
+  double2* w = sm;             // 2n: coarse transform in w[0..n), then the padded spectrum
+  double2* tw = sm + 2 * nmax; // n twiddles of the size-2n transform
+  make_twiddles(tw, nf);
+  double h = 2.0 * EB_PI / (double)n, inv = 1.0 / (double)n;
+  int ny = n / 2;
+  int ncomp = want_positions ? 3 : 1;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      double2 v;
+      if (comp == 0) v = uc[i0 + i];
+      else if (comp == 1) v = make_double2(z[i0 + i].x, 0.0);
+      else v = make_double2(z[i0 + i].y, 0.0);
+      w[i] = v;
+    }
+    smem_fft(w, n, tw, nf, -1);
+    if (threadIdx.x == 0) {
+      if (comp == 0) {
+        w[ny] = make_double2(0.0, 0.0);  // FINTERC, pv_integral.f:307
+      } else {
+        // FINTER zeroes WORK(IPT+2*NYK-1) and WORK(IPT+2*NYK) (pv_integral.f:235-236):
+        // the imaginary part of mode n/2-1 and the real part of mode n/2.
+        w[ny - 1].y = 0.0;
+        w[ny].x = 0.0;
+      }
+    }
+    __syncthreads();
+    // negative modes n/2+1..n-1 move to 2n-(n-m) = n+m; the gap in between is zero
+    for (int m = ny + 1 + threadIdx.x; m < n; m += blockDim.x) w[m + n] = w[m];
+    __syncthreads();
+    for (int m = ny + 1 + threadIdx.x; m <= n + ny; m += blockDim.x) w[m] = make_double2(0.0, 0.0);
+    __syncthreads();
+    for (int m = threadIdx.x; m < nf; m += blockDim.x) w[m] = make_double2(w[m].x * inv, w[m].y * inv);
+    smem_fft(w, nf, tw, nf, +1);
+    for (int m = threadIdx.x; m < nf; m += blockDim.x) {
+      int t = 2 * i0 + m;
+      if (comp == 0) qf[t] = (m & 1) ? make_double2(w[m].x * h, w[m].y * h) : make_double2(0.0, 0.0);
+      else if (comp == 1) zf[t].x = w[m].x;
+      else zf[t].y = w[m].x;
+    }
+  }
+}
+
+// PHICMPLX = -FIELD/(2 pi i) at the even fine nodes (pv_integral.f:194-201).
+__global__ void k_pv_extract(int nbk, const double2* __restrict__ cf, double2* __restrict__ phi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbk) return;
+  double2 c = cf[2 * i];
+  // -c/(2 pi i) = i c / (2 pi)
+  phi[i] = make_double2(-c.y / (2.0 * EB_PI), c.x / (2.0 * EB_PI));
+}
+
+__global__ void k_dtn_pre(int nbk, const double* __restrict__ u, const double2* __restrict__ dz,
+                          double2* __restrict__ uc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbk) return;
+  uc[i] = make_double2(u[i] * dz[i].x, u[i] * dz[i].y);
+}
+
+// zphi = -u/2 - PV - z; phi = Re, psi = Im (laplace.f:304-311).
+__global__ void k_dtn_mid(int nbk, const double* __restrict__ u, const double2* __restrict__ pv,
+                          const double2* __restrict__ z, double* __restrict__ phi,
+                          double* __restrict__ psi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbk) return;
+  double zx = -0.5 * u[i] - pv[i].x - z[i].x;
+  double zy = -pv[i].y - z[i].y;
+  phi[i] = zx;
+  psi[i] = zy;
+}
+
+__global__ void k_dtn_post(int nbk, const double2* __restrict__ dpsi, const double* __restrict__ dsda,
+                           double* __restrict__ dphi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbk) return;
+  dphi[i] = -dpsi[i].x / dsda[i];
+}
+
+// INTERFACENEW corrections and normal velocity (electric.f:845-882), free space.
+__global__ void k_velocity(int nbk, int k, const int* __restrict__ drop_of,
+                           const double2* __restrict__ z, const double2* __restrict__ dz,
+                           const double* __restrict__ dsda, const double* __restrict__ kappa,
+                           const double* __restrict__ hpt, const double2* __restrict__ ckern,
+                           const double2* __restrict__ u, const double2* __restrict__ udot,
+                           const double2* __restrict__ gw, const double2* __restrict__ zc,
+                           const double2* __restrict__ zk, int any_zc, double cap,
+                           double* __restrict__ un, double* __restrict__ fluxpart) {
+  __shared__ double red[32];
+  double fl = 0.0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbk; t += gridDim.x * blockDim.x) {
+    double hb = hpt[t], s = dsda[t];
+    double2 zn = make_double2(dz[t].y / s, -dz[t].x / s);  // -i dz / |dz|
+    double2 zz = z[t], uu = u[t];
+    // zcorr = (0.5 h 2 Re(ckern) u - 2 h udot) / (2 pi i)
+    double2 zcorr = make_double2(hb * ckern[t].x * uu.x - 2.0 * hb * udot[t].x,
+                                 hb * ckern[t].x * uu.y - 2.0 * hb * udot[t].y);
+    zcorr = make_double2(zcorr.y / (2.0 * EB_PI), -zcorr.x / (2.0 * EB_PI));
+    double adz = sqrt(dz[t].x * dz[t].x + dz[t].y * dz[t].y);
+    double c1 = hb * adz * 0.5 * kappa[t] / EB_PI;
+    double2 zself = cscale<double>(cmul<double>(cconj<double>(uu), cmul<double>(zn, zn)), c1);
+    double2 g = gw[t];
+    g = cadd<double>(g, cadd<double>(zself, zcorr));
+    double2 zck = make_double2(0.0, 0.0);
+    if (any_zc) {
+      for (int nb = 0; nb < k; ++nb) {
+        double2 zd = csub<double>(zz, zk[nb]);
+        double2 c = zc[nb];
+        double lg = log(sqrt(zd.x * zd.x + zd.y * zd.y));
+        zck = cadd<double>(zck, cscale<double>(c, 2.0 * lg));
+        zck = cadd<double>(zck, cdiv<double>(cmul<double>(cconj<double>(c), zd), cconj<double>(zd)));
+      }
+    }
+    // far field: zpsi = -i cap z / 2, gradwr = conj(zpsi)
+    double2 zpsi = make_double2(0.5 * cap * zz.y, -0.5 * cap * zz.x);
+    g = cadd<double>(g, cadd<double>(cconj<double>(zpsi), zck));
+    double2 zvel = make_double2(g.y, -g.x);  // -i g
+    double unt = zvel.x * zn.x + zvel.y * zn.y;  // Re(zvel conj(zn))
+    un[t] = unt;
+    fl += hb * unt * s;
+  }
+  fl = block_sum_d(fl, red);
+  if (threadIdx.x == 0) fluxpart[blockIdx.x] = fl;
+}
+
+__global__ void k_sum_final(int nb, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < nb; ++i) s += part[i];
+  *out = s;
+}
+
+int check_pow2(eb_ctx* ctx, int& nmax) {
+  nmax = 0;
+  for (int n : ctx->nd_host) {
+    if (n < 4 || (n & (n - 1)) != 0) {
+      eb_set_last_error_msg("spectral routines need power-of-two drop sizes >= 4");
+      return EB_ERR_ARG;
+    }
+    nmax = std::max(nmax, n);
+  }
+  return EB_OK;
+}
+
+int set_smem(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024)
+    EB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return EB_OK;
+}
+
+int fdiff_dev(eb_ctx* ctx, const double2* f, double2* df) {
+  int nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  size_t sm = sizeof(double2) * ((size_t)nmax + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_fdiff, sm));
+  k_fdiff<<<ctx->k, SBS, sm, ctx->stream>>>(ctx->start.as<int>(), f, df, nmax);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "fdiff");
+}
+
+// PVINTEV on device: ucmplx (nbk complex) -> phicmplx (nbk complex).
+int pvintev_dev(eb_ctx* ctx, const double2* uc, double2* phi, int prec) {
+  int nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  int nbk = ctx->nbk;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->pvz.ensure(sizeof(double2) * 2 * (size_t)nbk));
+  EB_TRY(ctx->pvq.ensure(sizeof(double2) * 2 * (size_t)nbk));
+  EB_TRY(ctx->pvout.ensure(sizeof(double2) * 2 * (size_t)nbk));
+  size_t sm = sizeof(double2) * (size_t)nmax * 3;
+  EB_TRY(set_smem((const void*)k_pv_interp, sm));
+  bool need_tree = !ctx->tree_pv.valid;
+  k_pv_interp<<<ctx->k, SBS, sm, s>>>(ctx->start.as<int>(), ctx->z.as<double2>(), uc,
+                                      ctx->pvz.as<double2>(), ctx->pvq.as<double2>(), nmax,
+                                      need_tree ? 1 : 0);
+  eb_count_launch(ctx);
+  if (need_tree) EB_TRY(eb_tree_build(ctx, ctx->tree_pv, ctx->pvz.as<double2>(), 2 * nbk, ctx->opts.leaf64));
+  EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree_pv, prec, ctx->pvq.as<double2>(), ctx->pvout.as<double2>()));
+  k_pv_extract<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->pvout.as<double2>(), phi);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "pvintev");
+}
+
+}  // namespace
+
+int eb_extractdat(eb_ctx* ctx, int k, const int* nd, const double* rku, double* zk, double* dz,
+                  double* dsda, double* kappa, double* ckern, double* tha, double* area, int mem) {
+  if (!ctx || k <= 0 || !nd || !rku) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = 0, nmax = 0;
+  for (int b = 0; b < k; ++b) {
+    if (nd[b] < 4 || (nd[b] & (nd[b] - 1)) != 0) {
+      eb_set_last_error_msg("EXTRACTDAT needs power-of-two drop sizes >= 4");
+      return EB_ERR_ARG;
+    }
+    nbk += nd[b];
+    nmax = std::max(nmax, nd[b]);
+  }
+  cudaStream_t s = ctx->stream;
+  std::vector<int> st(k + 1, 0);
+  for (int b = 0; b < k; ++b) st[b + 1] = st[b] + nd[b];
+  EB_TRY(ctx->start.ensure(sizeof(int) * (k + 1)));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->start.p, st.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, s));
+  EB_TRY(ctx->fftbuf.ensure(sizeof(double2) * nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->fftbuf.p, rku, sizeof(double2) * nbk,
+                              mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+  // geometry buffers of the context receive the results
+  DevBuf zk_d, dz_d, ds_d, ka_d, area_d;
+  EB_TRY(zk_d.ensure(sizeof(double2) * k));
+  EB_TRY(dz_d.ensure(sizeof(double2) * nbk));
+  EB_TRY(ds_d.ensure(sizeof(double) * nbk));
+  EB_TRY(ka_d.ensure(sizeof(double) * nbk));
+  EB_TRY(area_d.ensure(sizeof(double) * k));
+  EB_TRY(ctx->ckern.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->tha.ensure(sizeof(double) * nbk));
+  size_t sm = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_extractdat, sm));
+  k_extractdat<<<k, SBS, sm, s>>>(ctx->start.as<int>(), ctx->fftbuf.as<double2>(), zk_d.as<double2>(),
+                                  dz_d.as<double2>(), ds_d.as<double>(), ka_d.as<double>(),
+                                  ctx->ckern.as<double2>(), ctx->tha.as<double>(), area_d.as<double>(), nmax);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "extractdat"));
+  // install (the ckern / tha buffers are kept; eb_set_geometry leaves them alone)
+  EB_TRY(eb_set_geometry(ctx, k, nd, ctx->fftbuf.as<double>(), dz_d.as<double>(), ds_d.as<double>(),
+                         ka_d.as<double>(), zk_d.as<double>(), EB_DEVICE));
+  cudaMemcpyKind ko = mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (zk) EB_CUDA_TRY(cudaMemcpyAsync(zk, zk_d.p, sizeof(double2) * k, ko, s));
+  if (dz) EB_CUDA_TRY(cudaMemcpyAsync(dz, dz_d.p, sizeof(double2) * nbk, ko, s));
+  if (dsda) EB_CUDA_TRY(cudaMemcpyAsync(dsda, ds_d.p, sizeof(double) * nbk, ko, s));
+  if (kappa) EB_CUDA_TRY(cudaMemcpyAsync(kappa, ka_d.p, sizeof(double) * nbk, ko, s));
+  if (ckern) EB_CUDA_TRY(cudaMemcpyAsync(ckern, ctx->ckern.p, sizeof(double2) * nbk, ko, s));
+  if (tha) EB_CUDA_TRY(cudaMemcpyAsync(tha, ctx->tha.p, sizeof(double) * nbk, ko, s));
+  if (area) EB_CUDA_TRY(cudaMemcpyAsync(area, area_d.p, sizeof(double) * k, ko, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  ctx->ckern_valid = true;
+  return EB_OK;
+}
+
+int eb_fdiff(eb_ctx* ctx, const double* f, double* df, int mem) {
+  if (!ctx || !f || !df) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = ctx->nbk;
+  cudaStream_t s = ctx->stream;
+  if (mem == EB_DEVICE)
+    return fdiff_dev(ctx, reinterpret_cast<const double2*>(f), reinterpret_cast<double2*>(df));
+  EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vout.ensure(sizeof(double2) * nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, f, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
+  EB_TRY(fdiff_dev(ctx, ctx->vin.as<double2>(), ctx->vout.as<double2>()));
+  EB_CUDA_TRY(cudaMemcpyAsync(df, ctx->vout.p, sizeof(double2) * nbk, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_pvintev(eb_ctx* ctx, const double* uc, double* phi, int prec, int mem) {
+  if (!ctx || !uc || !phi) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = ctx->nbk;
+  cudaStream_t s = ctx->stream;
+  if (mem == EB_DEVICE)
+    return pvintev_dev(ctx, reinterpret_cast<const double2*>(uc), reinterpret_cast<double2*>(phi), prec);
+  EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vout.ensure(sizeof(double2) * nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, uc, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
+  EB_TRY(pvintev_dev(ctx, ctx->vin.as<double2>(), ctx->vout.as<double2>(), prec));
+  EB_CUDA_TRY(cudaMemcpyAsync(phi, ctx->vout.p, sizeof(double2) * nbk, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, double* dphi_dn,
+                      int prec, int mem) {
+  if (!ctx || !u || !dphi_dn) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = ctx->nbk, nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->vin.ensure(sizeof(double) * nbk));
+  EB_TRY(ctx->vtmp.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vtmp2.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vout.ensure(sizeof(double) * 3 * nbk));
+  const double* ud = u;
+  if (mem == EB_HOST) {
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, u, sizeof(double) * nbk, cudaMemcpyHostToDevice, s));
+    ud = ctx->vin.as<double>();
+  }
+  double* phd = ctx->vout.as<double>();
+  double* psd = phd + nbk;
+  double* dpd = psd + nbk;
+  k_dtn_pre<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ud, ctx->dz.as<double2>(), ctx->vtmp.as<double2>());
+  eb_count_launch(ctx);
+  EB_TRY(pvintev_dev(ctx, ctx->vtmp.as<double2>(), ctx->vtmp2.as<double2>(), prec));
+  k_dtn_mid<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ud, ctx->vtmp2.as<double2>(), ctx->z.as<double2>(), phd, psd);
+  eb_count_launch(ctx);
+  size_t sm = sizeof(double2) * ((size_t)nmax + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_fdiff_real, sm));
+  k_fdiff_real<<<ctx->k, SBS, sm, s>>>(ctx->start.as<int>(), psd, ctx->vtmp.as<double2>(), nmax);
+  eb_count_launch(ctx);
+  k_dtn_post<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->vtmp.as<double2>(), ctx->dsda.as<double>(), dpd);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "dirich_neu_map"));
+  cudaMemcpyKind ko = mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (phi) EB_CUDA_TRY(cudaMemcpyAsync(phi, phd, sizeof(double) * nbk, ko, s));
+  if (psi) EB_CUDA_TRY(cudaMemcpyAsync(psi, psd, sizeof(double) * nbk, ko, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(dphi_dn, dpd, sizeof(double) * nbk, ko, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
+                          double* flux, int prec, int mem) {
+  if (!ctx || !u || !zc || !un) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (!ctx->ckern_valid) {
+    eb_set_last_error_msg("INTERFACENEW needs ckern: install the geometry with eb_extractdat");
+    return EB_ERR_NOGEOM;
+  }
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = ctx->nbk, k = ctx->k;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vtmp.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vtmp2.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->vout.ensure(sizeof(double) * nbk));
+  EB_TRY(ctx->redpart.ensure(sizeof(double) * 2048));
+  EB_TRY(ctx->za.ensure(sizeof(double2) * k));
+  const double2* ud = reinterpret_cast<const double2*>(u);
+  if (mem == EB_HOST) {
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, u, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
+    ud = ctx->vin.as<double2>();
+  }
+  std::vector<double> zch(2 * (size_t)k);
+  EB_CUDA_TRY(cudaMemcpyAsync(zch.data(), zc, sizeof(double2) * k,
+                              mem == EB_HOST ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  int any_zc = 0;
+  for (double v : zch) if (v != 0.0) any_zc = 1;
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->za.p, zch.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, s));
+  EB_TRY(fdiff_dev(ctx, ud, ctx->vtmp.as<double2>()));
+  EB_TRY(eb_stokes_sum_dev(ctx, ud, +1, ctx->vtmp2.as<double2>(), prec));
+  int nbv = std::min(nblk(nbk, 256), 2048);
+  double* und = mem == EB_HOST ? ctx->vout.as<double>() : un;
+  k_velocity<<<nbv, 256, 0, s>>>(nbk, k, ctx->drop_of.as<int>(), ctx->z.as<double2>(), ctx->dz.as<double2>(),
+                                 ctx->dsda.as<double>(), ctx->kappa.as<double>(), ctx->hpt.as<double>(),
+                                 ctx->ckern.as<double2>(), ud, ctx->vtmp.as<double2>(), ctx->vtmp2.as<double2>(),
+                                 ctx->za.as<double2>(), ctx->zk.as<double2>(), any_zc, cap, und,
+                                 ctx->redpart.as<double>());
+  eb_count_launch(ctx);
+  k_sum_final<<<1, 32, 0, s>>>(nbv, ctx->redpart.as<double>(), ctx->redpart.as<double>() + 2047);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "interface velocity"));
+  if (mem == EB_HOST) EB_CUDA_TRY(cudaMemcpyAsync(un, und, sizeof(double) * nbk, cudaMemcpyDeviceToHost, s));
+  double fl = 0.0;
+  EB_CUDA_TRY(cudaMemcpyAsync(&fl, ctx->redpart.as<double>() + 2047, sizeof(double), cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flux) *flux = fl;
+  return EB_OK;
+}

@@ -1,0 +1,452 @@
+// GPU quadtree construction for the boundary-node FMM.
+//
+// The reference bins the nodes into a uniform 2^l x 2^l grid at every level with a
+// counting sort (ASSIGN1, cadap2.f:252-409) and loops over all 4^l boxes, empty or
+// not (DOINT0DR, cadapdrop2.f:84-197). Here the nodes are sorted once by a Morton key
+// at depth 20; the occupied boxes of every level are then the distinct key prefixes,
+// each owning a contiguous range of the sorted nodes. Only occupied boxes exist.
+// The leaf level is the shallowest one whose mean occupancy is at most `leaf_target`.
+// Interaction lists follow MKINTL (cadap2.f:780-828: children of the parent's
+// neighbours that are not adjacent, at most 27) and MKNBOR (cadap2.f:705-742: the
+// 3 x 3 neighbourhood at the leaf level).
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cmath>
+
+#include "eb_internal.h"
+
+namespace {
+
+struct __align__(16) Box4 {
+  double x, y, z, w;
+};
+__host__ __device__ __forceinline__ Box4 mk_box4(double a, double b, double c, double d) {
+  Box4 r;
+  r.x = a; r.y = b; r.z = c; r.w = d;
+  return r;
+}
+
+__host__ __device__ __forceinline__ unsigned long long spread2(unsigned int v) {
+  unsigned long long x = v;
+  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
+}
+__host__ __device__ __forceinline__ unsigned int compact2(unsigned long long x) {
+  x &= 0x5555555555555555ull;
+  x = (x | (x >> 1)) & 0x3333333333333333ull;
+  x = (x | (x >> 2)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x >> 4)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x >> 8)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x >> 16)) & 0x00000000FFFFFFFFull;
+  return (unsigned int)x;
+}
+__host__ __device__ __forceinline__ unsigned long long morton(unsigned int ix, unsigned int iy) {
+  return spread2(ix) | (spread2(iy) << 1);
+}
+
+__global__ void k_bbox(const double2* __restrict__ z, int n, Box4* __restrict__ part,
+                       int* __restrict__ bad) {
+  __shared__ double s[4][256];
+  double mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
+  int nonfinite = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 p = z[i];
+    if (!isfinite(p.x) || !isfinite(p.y)) { nonfinite = 1; continue; }
+    mnx = fmin(mnx, p.x); mxx = fmax(mxx, p.x);
+    mny = fmin(mny, p.y); mxy = fmax(mxy, p.y);
+  }
+  if (nonfinite) atomicOr(bad, 1);
+  s[0][threadIdx.x] = mnx; s[1][threadIdx.x] = mxx; s[2][threadIdx.x] = mny; s[3][threadIdx.x] = mxy;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + o]);
+      s[1][threadIdx.x] = fmax(s[1][threadIdx.x], s[1][threadIdx.x + o]);
+      s[2][threadIdx.x] = fmin(s[2][threadIdx.x], s[2][threadIdx.x + o]);
+      s[3][threadIdx.x] = fmax(s[3][threadIdx.x], s[3][threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = mk_box4(s[0][0], s[1][0], s[2][0], s[3][0]);
+}
+
+__global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Box4 r = mk_box4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+  for (int i = 0; i < nb; ++i) {
+    Box4 p = part[i];
+    r.x = fmin(r.x, p.x); r.y = fmax(r.y, p.y); r.z = fmin(r.z, p.z); r.w = fmax(r.w, p.w);
+  }
+  *out = r;
+}
+
+__global__ void k_keys(const double2* __restrict__ z, int n, double x0, double y0,
+                       double inv_cell, unsigned long long* __restrict__ keys,
+                       int* __restrict__ idx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double maxc = (double)((1u << EB_KEY_LEVELS) - 1);
+  double fx = floor((z[i].x - x0) * inv_cell), fy = floor((z[i].y - y0) * inv_cell);
+  fx = fmin(fmax(fx, 0.0), maxc);
+  fy = fmin(fmax(fy, 0.0), maxc);
+  keys[i] = morton((unsigned int)fx, (unsigned int)fy);
+  idx[i] = i;
+}
+
+// Histogram of the first level at which consecutive sorted keys fall in different
+// boxes: occupied boxes at level l = 1 + sum_{l' <= l} hist[l'].
+__global__ void k_level_hist(const unsigned long long* __restrict__ keys, int n,
+                             int* __restrict__ hist) {
+  __shared__ int sh[EB_KEY_LEVELS + 1];
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += gridDim.x * blockDim.x) {
+    unsigned long long x = keys[i] ^ keys[i - 1];
+    if (x == 0) continue;
+    int hb = 63 - __clzll((long long)x);
+    int lfirst = EB_KEY_LEVELS - hb / 2;
+    atomicAdd(&sh[lfirst], 1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+__global__ void k_gather_points(const double2* __restrict__ z, const int* __restrict__ perm,
+                                int n, double2* __restrict__ zs, float2* __restrict__ zhi,
+                                float2* __restrict__ zlo) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 p = z[perm[i]];
+  zs[i] = p;
+  float hx = (float)p.x, hy = (float)p.y;
+  zhi[i] = make_float2(hx, hy);
+  zlo[i] = make_float2((float)(p.x - (double)hx), (float)(p.y - (double)hy));
+}
+
+__global__ void k_heads(const unsigned long long* __restrict__ keys, int n, int shift,
+                        int* __restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flags[i] = (i == 0) || ((keys[i] >> shift) != (keys[i - 1] >> shift));
+}
+
+__global__ void k_leaf_fill(const unsigned long long* __restrict__ keys, int n, int shift,
+                            const int* __restrict__ flags, const int* __restrict__ scan,
+                            int off, unsigned long long* __restrict__ bkey,
+                            int* __restrict__ pt0, int* __restrict__ child0,
+                            int* __restrict__ nchild) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flags[i]) return;
+  int b = off + scan[i];
+  bkey[b] = keys[i] >> shift;
+  pt0[b] = i;
+  child0[b] = -1;
+  nchild[b] = 0;
+}
+
+__global__ void k_level_pt1(const int* __restrict__ pt0, int* __restrict__ pt1, int off,
+                            int nb, int n) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  pt1[off + b] = (b + 1 < nb) ? pt0[off + b + 1] : n;
+}
+
+__global__ void k_parent_fill(unsigned long long* __restrict__ bkey, int offc, int nbc,
+                              int offp, const int* __restrict__ flags,
+                              const int* __restrict__ scan, int* __restrict__ pt0,
+                              int* __restrict__ parent, int* __restrict__ child0) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbc) return;
+  int P = offp + scan[b];
+  parent[offc + b] = P;
+  if (flags[b]) {
+    bkey[P] = bkey[offc + b] >> 2;
+    pt0[P] = pt0[offc + b];
+    child0[P] = offc + b;
+  }
+}
+
+__global__ void k_parent_fin(int offp, int nbp, int offc, int nbc, int n,
+                             const int* __restrict__ child0, int* __restrict__ nchild,
+                             const int* __restrict__ pt0, int* __restrict__ pt1) {
+  int P = blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= nbp) return;
+  int next = (P + 1 < nbp) ? child0[offp + P + 1] : offc + nbc;
+  nchild[offp + P] = next - child0[offp + P];
+  pt1[offp + P] = (P + 1 < nbp) ? pt0[offp + P + 1] : n;
+}
+
+__device__ __forceinline__ int find_box(const unsigned long long* __restrict__ bkey, int off,
+                                        int nb, unsigned long long key) {
+  int lo = 0, hi = nb - 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    unsigned long long v = bkey[off + mid];
+    if (v == key) return off + mid;
+    if (v < key) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+__global__ void k_vlist(const unsigned long long* __restrict__ bkey, int off, int nb, int lev,
+                        int* __restrict__ vlist, unsigned char* __restrict__ vcode,
+                        int* __restrict__ vcount) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  int gid = off + b;
+  unsigned long long key = bkey[gid];
+  int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
+  int px = ix >> 1, py = iy >> 1, half = 1 << (lev - 1), side = 1 << lev;
+  int cnt = 0;
+  for (int qy = py - 1; qy <= py + 1; ++qy) {
+    if (qy < 0 || qy >= half) continue;
+    for (int qx = px - 1; qx <= px + 1; ++qx) {
+      if (qx < 0 || qx >= half) continue;
+      for (int cy = 0; cy < 2; ++cy)
+        for (int cx = 0; cx < 2; ++cx) {
+          int sx = 2 * qx + cx, sy = 2 * qy + cy;
+          int dx = ix - sx, dy = iy - sy;
+          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) continue;
+          if (sx >= side || sy >= side) continue;
+          int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
+          if (s < 0) continue;
+          vlist[(size_t)gid * EB_VMAX + cnt] = s;
+          vcode[(size_t)gid * EB_VMAX + cnt] = (unsigned char)((dy + 3) * 7 + (dx + 3));
+          ++cnt;
+        }
+    }
+  }
+  vcount[gid] = cnt;
+}
+
+__global__ void k_ulist(const unsigned long long* __restrict__ bkey, int off, int nb, int lev,
+                        int* __restrict__ ulist, int* __restrict__ ucount) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  unsigned long long key = bkey[off + b];
+  int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
+  int side = 1 << lev, cnt = 0;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      int sx = ix + dx, sy = iy + dy;
+      if (sx < 0 || sy < 0 || sx >= side || sy >= side) continue;
+      int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
+      if (s < 0) continue;
+      ulist[(size_t)b * EB_UMAX + cnt] = s;
+      ++cnt;
+    }
+  ucount[b] = cnt;
+}
+
+__global__ void k_pair_counts(int off, int nleaf, const int* __restrict__ pt0,
+                              const int* __restrict__ pt1, const int* __restrict__ ulist,
+                              const int* __restrict__ ucount, int vfirst, int vlast,
+                              const int* __restrict__ vcount,
+                              unsigned long long* __restrict__ out) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long up = 0, vp = 0;
+  if (b < nleaf) {
+    int nt = pt1[off + b] - pt0[off + b];
+    long long ns = 0;
+    for (int j = 0; j < ucount[b]; ++j) {
+      int s = ulist[(size_t)b * EB_UMAX + j];
+      ns += pt1[s] - pt0[s];
+    }
+    up = (unsigned long long)(nt * ns - nt);
+  }
+  for (int g = vfirst + blockIdx.x * blockDim.x + threadIdx.x; g < vlast; g += gridDim.x * blockDim.x)
+    vp += (unsigned long long)vcount[g];
+  up = warp_sum<unsigned long long>(up);
+  vp = warp_sum<unsigned long long>(vp);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&out[0], up);
+    atomicAdd(&out[1], vp);
+  }
+}
+
+inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+}  // namespace
+
+int DevBuf::ensure(size_t nbytes) {
+  if (nbytes <= bytes && p) return EB_OK;
+  release();
+  size_t want = nbytes < 256 ? 256 : nbytes;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    bytes = 0;
+    eb_set_last_cuda_error(e, "cudaMalloc", __FILE__, __LINE__);
+    return EB_ERR_CUDA;
+  }
+  bytes = want;
+  return EB_OK;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target) {
+  cudaStream_t st = eb_stream(ctx);
+  t.valid = false;
+  if (n <= 0) return EB_ERR_ARG;
+  if (leaf_target < 1) leaf_target = 32;
+  t.n = n;
+  const int BS = 256;
+  // 1. bounding square
+  int nbb = std::min(nblk(n, BS), 1024);
+  EB_TRY(t.partial.ensure(sizeof(Box4) * (size_t)nbb));
+  EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(int) * 4));
+  int* bad = reinterpret_cast<int*>(t.bbox.as<char>() + sizeof(Box4));
+  EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
+  eb_count_launch(ctx);
+  k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>());
+  eb_count_launch(ctx);
+  Box4 bb;
+  int hbad = 0;
+  EB_CUDA_TRY(cudaMemcpyAsync(&bb, t.bbox.p, sizeof(Box4), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hbad) {
+    eb_set_last_error_msg("non-finite node coordinate");
+    return EB_ERR_NAN;
+  }
+  double w = std::max(bb.y - bb.x, bb.w - bb.z);
+  if (!(w > 0)) w = 1.0;
+  w *= 1.0 + 1e-9;
+  t.W = w;
+  t.x0 = 0.5 * (bb.x + bb.y) - 0.5 * w;
+  t.y0 = 0.5 * (bb.z + bb.w) - 0.5 * w;
+  // 2. keys and sort
+  EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
+  EB_TRY(t.keys_alt.ensure(sizeof(unsigned long long) * (size_t)n));
+  EB_TRY(t.idx_alt.ensure(sizeof(int) * (size_t)n));
+  EB_TRY(t.perm.ensure(sizeof(int) * (size_t)n));
+  double inv_cell = (double)(1u << EB_KEY_LEVELS) / w;
+  k_keys<<<nblk(n, BS), BS, 0, st>>>(z, n, t.x0, t.y0, inv_cell, t.keys_alt.as<unsigned long long>(),
+                                     t.idx_alt.as<int>());
+  eb_count_launch(ctx);
+  size_t tmp_sort = 0, tmp_scan = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, tmp_sort, t.keys_alt.as<unsigned long long>(),
+                                  t.keys.as<unsigned long long>(), t.idx_alt.as<int>(),
+                                  t.perm.as<int>(), n, 0, 2 * EB_KEY_LEVELS, st);
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, t.flags.as<int>(), t.scan.as<int>(), n, st);
+  EB_TRY(t.cubtmp.ensure(std::max(tmp_sort, tmp_scan)));
+  size_t tb = t.cubtmp.bytes;
+  EB_CUDA_TRY(cub::DeviceRadixSort::SortPairs(t.cubtmp.p, tb, t.keys_alt.as<unsigned long long>(),
+                                              t.keys.as<unsigned long long>(), t.idx_alt.as<int>(),
+                                              t.perm.as<int>(), n, 0, 2 * EB_KEY_LEVELS, st));
+  eb_count_launch(ctx);
+  // 3. sorted positions
+  EB_TRY(t.zs.ensure(sizeof(double2) * (size_t)n));
+  EB_TRY(t.zhi.ensure(sizeof(float2) * (size_t)n));
+  EB_TRY(t.zlo.ensure(sizeof(float2) * (size_t)n));
+  k_gather_points<<<nblk(n, BS), BS, 0, st>>>(z, t.perm.as<int>(), n, t.zs.as<double2>(),
+                                              t.zhi.as<float2>(), t.zlo.as<float2>());
+  eb_count_launch(ctx);
+  // 4. occupied boxes per level, leaf level
+  EB_TRY(t.hist.ensure(sizeof(int) * (EB_KEY_LEVELS + 1)));
+  EB_CUDA_TRY(cudaMemsetAsync(t.hist.p, 0, sizeof(int) * (EB_KEY_LEVELS + 1), st));
+  k_level_hist<<<std::min(nblk(n, BS), 1024), BS, 0, st>>>(t.keys.as<unsigned long long>(), n,
+                                                          t.hist.as<int>());
+  eb_count_launch(ctx);
+  int hist[EB_KEY_LEVELS + 1];
+  EB_CUDA_TRY(cudaMemcpyAsync(hist, t.hist.p, sizeof(hist), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  int nb[EB_KEY_LEVELS + 1];
+  nb[0] = 1;
+  for (int l = 1; l <= EB_KEY_LEVELS; ++l) nb[l] = nb[l - 1] + hist[l];
+  int L = EB_KEY_LEVELS;
+  for (int l = 0; l <= EB_KEY_LEVELS; ++l)
+    if ((double)n / nb[l] <= (double)leaf_target) { L = l; break; }
+  t.L = L;
+  t.lev_off[0] = 0;
+  for (int l = 0; l <= L; ++l) t.lev_off[l + 1] = t.lev_off[l] + nb[l];
+  t.nbox = t.lev_off[L + 1];
+  t.nleaf = nb[L];
+  size_t NB = (size_t)t.nbox;
+  EB_TRY(t.bkey.ensure(sizeof(unsigned long long) * NB));
+  EB_TRY(t.pt0.ensure(sizeof(int) * NB));
+  EB_TRY(t.pt1.ensure(sizeof(int) * NB));
+  EB_TRY(t.parent.ensure(sizeof(int) * NB));
+  EB_TRY(t.child0.ensure(sizeof(int) * NB));
+  EB_TRY(t.nchild.ensure(sizeof(int) * NB));
+  EB_TRY(t.flags.ensure(sizeof(int) * (size_t)n));
+  EB_TRY(t.scan.ensure(sizeof(int) * (size_t)n));
+  // 5. leaf boxes
+  int shift = 2 * (EB_KEY_LEVELS - L);
+  k_heads<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, shift, t.flags.as<int>());
+  eb_count_launch(ctx);
+  tb = t.cubtmp.bytes;
+  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), n, st));
+  eb_count_launch(ctx);
+  k_leaf_fill<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, shift, t.flags.as<int>(),
+                                          t.scan.as<int>(), t.lev_off[L],
+                                          t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                          t.child0.as<int>(), t.nchild.as<int>());
+  eb_count_launch(ctx);
+  k_level_pt1<<<nblk(nb[L], BS), BS, 0, st>>>(t.pt0.as<int>(), t.pt1.as<int>(), t.lev_off[L], nb[L], n);
+  eb_count_launch(ctx);
+  // 6. coarser levels from the finer level's box keys
+  for (int l = L - 1; l >= 0; --l) {
+    int offc = t.lev_off[l + 1], nbc = nb[l + 1], offp = t.lev_off[l];
+    k_heads<<<nblk(nbc, BS), BS, 0, st>>>(t.bkey.as<unsigned long long>() + offc, nbc, 2,
+                                          t.flags.as<int>());
+    eb_count_launch(ctx);
+    tb = t.cubtmp.bytes;
+    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nbc, st));
+    eb_count_launch(ctx);
+    k_parent_fill<<<nblk(nbc, BS), BS, 0, st>>>(t.bkey.as<unsigned long long>(), offc, nbc, offp,
+                                                t.flags.as<int>(), t.scan.as<int>(), t.pt0.as<int>(),
+                                                t.parent.as<int>(), t.child0.as<int>());
+    eb_count_launch(ctx);
+    k_parent_fin<<<nblk(nb[l], BS), BS, 0, st>>>(offp, nb[l], offc, nbc, n, t.child0.as<int>(),
+                                                 t.nchild.as<int>(), t.pt0.as<int>(), t.pt1.as<int>());
+    eb_count_launch(ctx);
+  }
+  int minus1 = -1;
+  EB_CUDA_TRY(cudaMemcpyAsync(t.parent.as<int>(), &minus1, sizeof(int), cudaMemcpyHostToDevice, st));
+  // 7. interaction lists
+  EB_TRY(t.vlist.ensure(sizeof(int) * NB * EB_VMAX));
+  EB_TRY(t.vcode.ensure(NB * EB_VMAX));
+  EB_TRY(t.vcount.ensure(sizeof(int) * NB));
+  EB_CUDA_TRY(cudaMemsetAsync(t.vcount.p, 0, sizeof(int) * NB, st));
+  for (int l = 2; l <= L; ++l) {
+    k_vlist<<<nblk(nb[l], 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[l], nb[l], l,
+                                              t.vlist.as<int>(), t.vcode.as<unsigned char>(),
+                                              t.vcount.as<int>());
+    eb_count_launch(ctx);
+  }
+  EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)t.nleaf * EB_UMAX));
+  EB_TRY(t.ucount.ensure(sizeof(int) * (size_t)t.nleaf));
+  k_ulist<<<nblk(t.nleaf, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[L], t.nleaf, L,
+                                             t.ulist.as<int>(), t.ucount.as<int>());
+  eb_count_launch(ctx);
+  // 8. pair counts (the algorithmic work of the near field and M2L)
+  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(t.partial.p);
+  EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
+  int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
+  k_pair_counts<<<std::max(nblk(t.nleaf, BS), 1), BS, 0, st>>>(
+      t.lev_off[L], t.nleaf, t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(),
+      vfirst, vlast, t.vcount.as<int>(), cnt);
+  eb_count_launch(ctx);
+  unsigned long long hc[2];
+  EB_CUDA_TRY(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  EB_TRY(eb_check_launch(ctx, "tree build"));
+  t.u_pairs = (long long)hc[0];
+  t.v_pairs = (long long)hc[1];
+  t.valid = true;
+  return EB_OK;
+}

@@ -1,0 +1,182 @@
+/*
+ * eb_gb300.h - C ABI of the GB300-native ElectricBubbles hot path.
+ *
+ * The reference (mcetal/ElectricBubbles, Fortran 77) applies its boundary-integral
+ * operators through GMRES callbacks with the SLATEC signature
+ *     MATVEC(N, X, Y, NELT, IA, JA, A, ISYM)
+ * and passes the geometry through COMMON blocks. This library replaces that
+ * operator apply (and the solves, spectral derivatives and principal-value
+ * integrals around it) with CUDA kernels on one GPU. Plain C types only: pointers
+ * and sizes, no CUDA or PyTorch types in any signature.
+ *
+ * Conventions
+ *  - Complex arrays are interleaved (re, im) doubles, i.e. Fortran COMPLEX*16.
+ *  - Nodes of k drops are concatenated in drop order (nd[0] nodes of drop 0, ...).
+ *  - `mem` says whether the array arguments are host (EB_HOST) or device
+ *    (EB_DEVICE, allocated on the context's GPU) pointers. Host calls copy in,
+ *    compute, copy out, and return when the result is in host memory.
+ *  - Every function returns an eb_status; the library never calls exit().
+ *    eb_last_error() describes the last failure of the calling thread.
+ */
+#ifndef EB_GB300_H
+#define EB_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EB_GB300_VERSION 1
+
+/* Status codes. The reference prints and STOPs on FMM/GMRES errors
+ * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
+ * here every condition is returned to the caller. */
+enum eb_status {
+  EB_OK = 0,
+  EB_ERR_ARG = 1,          /* invalid argument (size mismatch, null pointer, ...) */
+  EB_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  EB_ERR_NOGEOM = 3,       /* no geometry installed in the context */
+  EB_ERR_WORKSPACE = 4,    /* a size exceeds a fixed capacity */
+  EB_ERR_TOL = 5,          /* requested tolerance needs more expansion terms than supported */
+  EB_ERR_NAN = 6,          /* non-finite value detected in an input or a residual */
+  EB_ERR_NOT_CONVERGED = 7,/* GMRES did not reach the tolerance (DGMRES IERR = 1 or 2) */
+  EB_ERR_NODEVICE = 8,     /* no CUDA device available */
+  EB_ERR_TIMEOUT = 9       /* a bounded device-side wait gave up */
+};
+
+enum eb_memspace { EB_HOST = 0, EB_DEVICE = 1 };
+
+/* Arithmetic of a layer-potential sum: plain FP64, or FP32 expansions and near
+ * field (compensated) for the inner operator of the refined solver. */
+enum eb_precision { EB_FP64 = 0, EB_FP32 = 1 };
+
+/* Solver mode: plain FP64 GMRES, or FP32-inner GMRES with FP64 iterative
+ * refinement (outer residual, Arnoldi and least squares in FP64). */
+enum eb_solve_mode { EB_SOLVE_FP64 = 0, EB_SOLVE_FP32_REFINED = 1 };
+
+typedef struct eb_opts {
+  int p64;          /* FP64 expansion order (0: default 44)                    */
+  int p32;          /* FP32 expansion order (0: default 20)                    */
+  int leaf64;       /* target mean points per occupied leaf, FP64 (0: 32)      */
+  int leaf32;       /* target mean points per occupied leaf, FP32 (0: 32)      */
+  double tol64;     /* M2L per-offset truncation tolerance, FP64 (0: 1e-15)    */
+  double tol32;     /* M2L per-offset truncation tolerance, FP32 (0: 1e-7)     */
+  int maxl;         /* GMRES Krylov dimension, MAXL (0: 100, electric.f:1011)  */
+  double gmres_tol; /* GMRES relative residual tolerance (0: 1e-10)            */
+  double inner_tol; /* refined mode: inner FP32 GMRES relative tolerance (0: 1e-5) */
+  int max_outer;    /* refined mode: maximum refinement steps (0: 8)           */
+  int device;       /* CUDA device ordinal                                     */
+} eb_opts;
+
+typedef struct eb_solve_info {
+  int iters;        /* total Krylov iterations (inner iterations in refined mode) */
+  int outer;        /* refinement steps (1 in plain mode)                     */
+  int matvecs64;    /* FP64 operator applies                                  */
+  int matvecs32;    /* FP32 operator applies                                  */
+  double err;       /* final ||b - A x|| / ||b|| estimate (DGMRES ERR)        */
+  int ierr;         /* DGMRES IERR convention: 0 converged, 1 MAXL reached, 2 stalled */
+} eb_solve_info;
+
+typedef struct eb_tree_info {
+  int npoints;      /* points in the tree                                     */
+  int levels;       /* leaf level L (root is level 0)                         */
+  int nboxes;       /* occupied boxes over all levels                         */
+  int nleaves;      /* occupied leaves                                        */
+  long long v_pairs;/* M2L (source box, target box) pairs                     */
+  long long u_pairs;/* near-field (target point, source point) pairs          */
+  int p;            /* expansion order of the last apply                      */
+} eb_tree_info;
+
+typedef struct eb_ctx eb_ctx;
+
+int eb_version(void);
+const char* eb_status_string(int status);
+const char* eb_last_error(void);
+void eb_opts_default(eb_opts* opts);
+
+int eb_ctx_create(eb_ctx** out, const eb_opts* opts);
+int eb_ctx_destroy(eb_ctx* ctx);
+/* Run the context's work on an existing CUDA stream (a cudaStream_t passed as void*);
+ * NULL restores the context's own stream. */
+int eb_ctx_set_stream(eb_ctx* ctx, void* cuda_stream);
+int eb_ctx_sync(eb_ctx* ctx);
+/* Kernel launches issued by this context so far. */
+long long eb_ctx_launch_count(eb_ctx* ctx);
+/* When enabled, the dominant near-field and M2L kernels are bracketed by CUDA
+ * events on the context's stream; eb_ctx_kernel_time reports launches and total
+ * milliseconds per kernel class (0: near field P2P+L2P, 1: M2L). */
+int eb_ctx_set_profiling(eb_ctx* ctx, int enable);
+int eb_ctx_kernel_time(eb_ctx* ctx, int kernel_class, long long* launches, double* total_ms);
+int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
+
+/* Install the geometry of k drops: the data EXTRACTDAT (electric.f:636-716) leaves
+ * in COMMON /inteqn/ dsdth, rkappa, z, dz and /problem/ zk, nd, k, nbk
+ * (electric.f:1022-1023). z, dz, zk are complex; dsda, kappa real. Builds the
+ * quadtree and interaction lists once; they stay valid until the next call. */
+int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const double* dz,
+                    const double* dsda, const double* kappa, const double* zk, int mem);
+
+/* EXTRACTDAT (electric.f:636-716) on the GPU: from the RK state rku (interleaved
+ * x, y of all nodes) compute z, zk, dz, dsda, kappa, ckern, tha and the drop areas,
+ * and install the geometry. Outputs may be NULL. zbond enters only zc. */
+int eb_extractdat(eb_ctx* ctx, int k, const int* nd, const double* rku, double* zk,
+                  double* dz, double* dsda, double* kappa, double* ckern, double* tha,
+                  double* area, int mem);
+
+/* Stokes operator FASMVP (stokesbubb.f:496-614), the body of MATVEC
+ * (stokesbubb.f:419-465): x, y interleaved real vectors of length n = 2 nbk. */
+int eb_stokes_matvec(eb_ctx* ctx, int n, const double* x, double* y, int precision, int mem);
+
+/* Laplace operator FASMVP_LAP (laplace.f:159-262), the body of MATVEC_LAPL
+ * (laplace.f:429-465): x, y of length n = nbk. The reference additionally writes k
+ * constraint sums past y(n) (laplace.f:252-259); eb_laplace_constraints returns them. */
+int eb_laplace_matvec(eb_ctx* ctx, int n, const double* x, double* y, int precision, int mem);
+int eb_laplace_constraints(eb_ctx* ctx, int n, const double* x, double* sums, int mem);
+
+/* The sum CADAPDR (sign = -1, cadapdrop.f:3-387, used by FASMVP) or CADAPMOD
+ * (sign = +1, cadapmod.f:3-386, used by INTERFACENEW) evaluates at the installed
+ * nodes, self excluded: dens complex density (n = nbk complex values), gradw out. */
+int eb_stokes_sum(eb_ctx* ctx, int n, const double* dens, int sign, double* gradw,
+                  int precision, int mem);
+
+/* The Cauchy sum DAPIF2 returns for IFLAG7 = 3 (dapif1.f:458-1077):
+ * field_i = sum_{j != i} q_j / (z_i - z_j), on n arbitrary points (own tree). */
+int eb_cauchy_sum(eb_ctx* ctx, int n, const double* z, const double* q, double* field,
+                  int precision, int mem);
+
+/* GMRES solves with the settings of SOLVEI (stokesbubb.f:294-415) and SOLVE_LAPL
+ * (laplace.f:335-425): x0 = rhs, MAXL Krylov vectors, no restart, stop when
+ * ||b - A x|| / ||b|| <= gmres_tol (DGMRES ITOL = 0). soln receives the solution. */
+int eb_stokes_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                    eb_solve_info* info, int mem);
+int eb_laplace_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                     eb_solve_info* info, int mem);
+
+/* FDIFFF (dcfft.f:1371-1428) per drop on the installed drop sizes: complex f -> df. */
+int eb_fdiff(eb_ctx* ctx, const double* f, double* df, int mem);
+
+/* PVINTEV (pv_integral.f:53-204) on the installed geometry: ucmplx -> phicmplx. */
+int eb_pvintev(eb_ctx* ctx, const double* ucmplx, double* phicmplx, int precision, int mem);
+
+/* DIRICH_NEU_MAP (laplace.f:266-331): Laplace density u -> phi, psi, dphi_dn. */
+int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi,
+                      double* dphi_dn, int precision, int mem);
+
+/* INTERFACENEW (electric.f:791-912), free space: Stokes density u (complex, nbk) ->
+ * interface normal velocity un and the FLUX diagnostic. zc: per-drop C_k (complex). */
+int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap,
+                          double* un, double* flux, int precision, int mem);
+
+/* gfortran-callable shims with the exact DGMRES MATVEC signature
+ * (dpigmr.f:316-318, stokesbubb.f:419, laplace.f:429). They use the context set with
+ * eb_set_default_ctx and host memory, and abort the process on error, as the
+ * reference's STOP would. */
+int eb_set_default_ctx(eb_ctx* ctx);
+void matvec_(const int* n, const double* xx, double* yy, const int* nelt, const int* ia,
+             const int* ja, const double* a, const int* isym);
+void matvec_lapl_(const int* n, const double* xx, double* yy, const int* nelt,
+                  const int* ia, const int* ja, const double* a, const int* isym);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
