@@ -163,7 +163,8 @@ __global__ void k_parent_fill(unsigned long long* __restrict__ bkey, int offc, i
                               int* __restrict__ parent, int* __restrict__ child0) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbc) return;
-  int P = offp + scan[b];
+  // inclusive count of parent heads up to b, minus one: the parent's index
+  int P = offp + scan[b] + flags[b] - 1;
   parent[offc + b] = P;
   if (flags[b]) {
     bkey[P] = bkey[offc + b] >> 2;
