@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the boundary-integral hot path: GMRES solves/s of the Stokes system
+(SOLVEI, stokesbubb.f:294-415) on the 64-drop workload, FP32-refined vs plain FP64.
+
+Workload: 64 seeded drops, radii U[0.5, 1], r(theta) = r (1 + 0.05 cos 2 theta) at equal
+arclength, centres in [-20, 20]^2 with gaps > 0.2, 512 nodes each (N = 32,768 nodes,
+65,536 unknowns). One step = one Stokes GMRES solve to ||b - A x|| / ||b|| <= 1e-10 with
+x0 = b (the reference's settings), geometry and right-hand side resident in HBM.
+The right-hand side is SETVELF's surface-tension term -dz/(2 |dz|) (stokesbubb.f:55-57),
+computed from the geometry EXTRACTDAT produced on the GPU.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs N independent replicas (one per GPU; the path has no data exchange), and
+value is the aggregate over ranks. `--impl reference` times the reference algorithm
+(the per-level CADAPDR FMM and SLATEC GMRES, restated in C) on the host cores.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GMRES solves/s and FMM Mpts/s, FP32-refined vs FP64 on GPU at 1e-10 rel err"
+WORKLOAD = "many_drops_64x512"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload():
+    from electricbubbles_gb300 import configs
+    return configs.many_drops()
+
+
+# ---------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------
+# reference arm / CPU baseline: the reference algorithm restated in C, on host cores
+# ---------------------------------------------------------------------------------
+def cpu_reference_solves(cfg, nsolves, nthreads):
+    """Times `nsolves` Stokes solves of the reference algorithm (CADAPDR per-level FMM,
+    LEVMAX = 7, TOL = 1e-13, and SLATEC GMRES) with nthreads OpenMP threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle as O
+    ex = O.extractdat(cfg.nd, cfg.rku())
+    g = O.Geometry.from_extract(cfg.nd, ex)
+    rhs = surface_tension_rhs(ex["dz"], ex["dsda"])
+    times, infos = [], []
+    for _ in range(nsolves):
+        t0 = time.perf_counter()
+        x, info = O.solvei(g, rhs, mode=1, nthreads=nthreads)  # 1: CADAPDR restatement
+        times.append(time.perf_counter() - t0)
+        infos.append(info)
+    return times, infos, x
+
+
+def surface_tension_rhs(dz, dsda):
+    import numpy as np
+    zn = -0.5 * dz / dsda
+    return np.ascontiguousarray(zn).view(np.float64).copy()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = workload()
+    nthreads = O.max_threads()
+    if args.warmup > 0:
+        cpu_reference_solves(cfg, 1, nthreads)
+    times, infos, _ = cpu_reference_solves(cfg, args.steps, nthreads)
+    total = sum(times)
+    value = args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded drops)",
+        "config": {"workload": WORKLOAD, "nodes": cfg.nbk, "unknowns": 2 * cfg.nbk,
+                   "solver": "CADAPDR per-level FMM (LEVMAX=7, TOL=1e-13) + SLATEC GMRES, C restatement",
+                   "gmres_tol": 1e-10, "threads": nthreads},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d full Stokes solves of the 64x512 workload" % args.steps},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gmres_iters": [i["iters"] for i in infos],
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+    from electricbubbles_gb300.api import Context
+
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    cfg = workload()
+    ctx = Context(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    geo = ctx.extractdat(cfg.nd, cfg.rku())          # EXTRACTDAT on the GPU (set-up)
+    rhs_h = surface_tension_rhs(geo["dz"], geo["dsda"])
+    n = rhs_h.shape[0]
+    rhs = torch.from_numpy(rhs_h).to(dev)
+    x = torch.empty_like(rhs)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(max(args.steps, 1))]
+
+    def timed(mode, steps, warmup):
+        for _ in range(warmup):
+            ctx.solvei(rhs, mode, out=x)
+        torch.cuda.synchronize()
+        if dist:
+            td.barrier()
+        infos = []
+        t0 = time.perf_counter()
+        l0 = ctx.launch_count()
+        for s in range(steps):
+            flush.zero_()
+            ev[s][0].record(stream)
+            _, info = ctx.solvei(rhs, mode, out=x)
+            ev[s][1].record(stream)
+            infos.append(info)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        timed.launches = ctx.launch_count() - l0
+        dev_ms = sum(a.elapsed_time(b) for a, b in ev[:steps])
+        if dist:
+            t = torch.tensor([dev_ms], device=dev)
+            td.all_reduce(t, op=td.ReduceOp.MAX)
+            dev_ms = float(t.item())
+        return dev_ms, wall, infos
+
+    # plain FP64 and refined solves (the refined one is the headline)
+    ms64, _, inf64 = timed("fp64", args.steps, args.warmup)
+    x64 = x.clone()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms32, wall32, inf32 = timed("fp32_refined", args.steps, args.warmup)
+    clk = clocks.stop()
+    launches = timed.launches
+    rel_diff = float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
+
+    # FMM Mpts/s: single Stokes operator applies, FP64 and FP32
+    u = torch.randn(n, dtype=torch.float64, device=dev)
+    y = torch.empty_like(u)
+    mpts = {}
+    for prec in ("fp64", "fp32"):
+        for _ in range(3):
+            ctx.fasmvp(u, prec, out=y)
+        reps = 10
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            e0.record(stream)
+            ctx.fasmvp(u, prec, out=y)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        mpts[prec] = cfg.nbk / (tot / reps * 1e-3) / 1e6
+
+    # dominant kernel: FP64 near field (P2P + L2P), live CUDA-event timing
+    tree = ctx.tree_info()
+    ctx.set_profiling(True)
+    for _ in range(10):
+        ctx.fasmvp(u, "fp64", out=y)
+    nl, near_ms = ctx.kernel_time(0)
+    nm, m2l_ms = ctx.kernel_time(1)
+    ctx.set_profiling(False)
+    p64 = 44
+    near_flops = 40.0 * tree["u_pairs"] + 24.0 * p64 * tree["npoints"]
+    near_avg_ms = near_ms / nl
+    fp64_peak = ctx.measure_fp64_peak()
+    achieved = near_flops / (near_avg_ms * 1e-3) / 1e12
+
+    # end to end through the C ABI with host buffers: geometry + rhs in, solution out
+    zh = torch.from_numpy(np.ascontiguousarray(geo["z"]).view(np.float64).copy()).pin_memory()
+    dzh = torch.from_numpy(np.ascontiguousarray(geo["dz"]).view(np.float64).copy()).pin_memory()
+    dsh = torch.from_numpy(geo["dsda"].copy()).pin_memory()
+    kah = torch.from_numpy(geo["kappa"].copy()).pin_memory()
+    zkh = torch.from_numpy(np.ascontiguousarray(geo["zk"]).view(np.float64).copy()).pin_memory()
+    rhh = torch.from_numpy(rhs_h.copy()).pin_memory()
+    xh = torch.empty_like(rhh).pin_memory()
+    lib, h = ctx._lib, ctx._h
+    nd = np.ascontiguousarray(cfg.nd, dtype=np.int32)
+    import ctypes
+    from electricbubbles_gb300._lib import SolveInfo, check
+
+    def e2e_step():
+        check("eb_set_geometry", lib.eb_set_geometry(h, cfg.k, nd.ctypes.data, zh.data_ptr(), dzh.data_ptr(),
+                                                      dsh.data_ptr(), kah.data_ptr(), zkh.data_ptr(), 0))
+        info = SolveInfo()
+        check("eb_stokes_solve", lib.eb_stokes_solve(h, n, rhh.data_ptr(), xh.data_ptr(), 1,
+                                                      ctypes.byref(info), 0))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = 0.0
+    for s in range(args.steps):
+        flush.zero_()
+        ev[s][0].record(stream)
+        e2e_step()  # returns with the solution in host memory
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in ev[:args.steps])
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = 8 * (zh.numel() + dzh.numel() + dsh.numel() + kah.numel() + zkh.numel() + rhh.numel()) + 4 * cfg.k
+    d2h = 8 * xh.numel()
+
+    cpu = None
+    if rank == 0:
+        ncores = os.cpu_count() or 1
+        try:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle as O
+            ncores = O.max_threads()
+            times, _, xr = cpu_reference_solves(cfg, 2, ncores)
+            cpu = {"value": 2 / sum(times), "unit": "solves/s", "cores": ncores, "kind": "port",
+                   "sample": "2 full Stokes solves of the 64x512 workload with the restated "
+                             "CADAPDR FMM + SLATEC GMRES",
+                   "gpu_vs_cpu_solution_rel": float(np.linalg.norm(x.cpu().numpy() - xr) / np.linalg.norm(xr))}
+        except Exception as exc:  # the baseline must not hide the GPU result
+            cpu = {"value": None, "unit": "solves/s", "cores": ncores, "kind": "port",
+                   "sample": "failed: %s" % exc}
+
+    value = world * args.steps / (ms32 * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 inner operator, f64 residual/Arnoldi (refined)",
+        "data": "synthetic (seeded drops; surface-tension right-hand side)",
+        "config": {"workload": WORKLOAD, "nodes": cfg.nbk, "unknowns": n, "drops": cfg.k,
+                   "solve": "fp32_refined GMRES-IR, tol 1e-10, x0 = b", "parallelism": "replicas",
+                   "l2": "256 MiB write between timed steps (outside the step's CUDA events)"},
+        "fp64_solves_per_s": world * args.steps / (ms64 * 1e-3),
+        "refined_speedup_vs_fp64": ms64 / ms32,
+        "fmm_mpts_per_s": mpts,
+        "solve_info": {"fp64": inf64[-1], "fp32_refined": inf32[-1]},
+        "accuracy": {"refined_vs_fp64_rel_l2": rel_diff, "refined_true_residual": inf32[-1]["err"]},
+        "tree": tree,
+        "roofline": {"kernel": "k_leaf64<2> (FP64 near field P2P + L2P)", "bound": "fp64",
+                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp64_peak, "traffic": None,
+                     "peak_source": "measured in-run FP64 FMA chain (MEASURED_PEAKS.json has no FP64 figure)",
+                     "flops_per_launch": near_flops, "avg_launch_ms": near_avg_ms,
+                     "m2l_avg_launch_ms": m2l_ms / nm},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "solves/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "includes": "eb_set_geometry (copy + tree build) and eb_stokes_solve from pinned host buffers"},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        td.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    from electricbubbles_gb300 import build
+    build.build()
+    run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -38,7 +38,7 @@ def _is_device(a):
 def _ptr(a):
     if a is None:
         return None
-    if _is_device(a):
+    if hasattr(a, "data_ptr"):  # CUDA tensor, or a (pinned) host tensor
         return ctypes.c_void_p(a.data_ptr())
     if not (isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]):
         raise TypeError("expected a C-contiguous numpy array or a CUDA tensor")
@@ -118,6 +118,11 @@ class Context:
         check("eb_ctx_kernel_time", self._lib.eb_ctx_kernel_time(self._h, cls, ctypes.byref(n),
                                                                  ctypes.byref(ms)))
         return n.value, ms.value
+
+    def measure_fp64_peak(self):
+        v = ctypes.c_double()
+        check("eb_measure_fp64_peak", self._lib.eb_measure_fp64_peak(self._h, ctypes.byref(v)))
+        return v.value
 
     def tree_info(self):
         t = TreeInfo()

@@ -386,3 +386,42 @@ int eb_laplace_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mo
   cudaSetDevice(ctx->device);
   return solve(ctx, n, eb_laplace_matvec_dev, rhs, soln, mode, info, mem);
 }
+
+// ---------------------------------------------------------------------------------
+// FP64 FMA throughput calibration: the roofline denominator of the FP64 kernels
+// (the FMM apply is bound by the FP64 pipe, not by HBM or the tensor cores).
+// ---------------------------------------------------------------------------------
+namespace {
+__global__ void k_dfma_chain(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+
+int eb_measure_fp64_peak(eb_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int sms = 0;
+  EB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int blocks = sms * 8, threads = 256, iters = 2000;
+  DevBuf out;
+  EB_TRY(out.ensure(sizeof(double) * (size_t)blocks * threads));
+  cudaStream_t s = ctx->stream;
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+    k_dfma_chain<<<blocks, threads, 0, s>>>(out.as<double>(), iters, 0.999, 1e-3);
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+    EB_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    EB_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (ms < best) best = ms;
+  }
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return eb_check_launch(ctx, "fp64 peak");
+}

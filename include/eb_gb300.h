@@ -107,6 +107,9 @@ long long eb_ctx_launch_count(eb_ctx* ctx);
 int eb_ctx_set_profiling(eb_ctx* ctx, int enable);
 int eb_ctx_kernel_time(eb_ctx* ctx, int kernel_class, long long* launches, double* total_ms);
 int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
+/* FP64 FMA throughput of the context's GPU in TFLOP/s (a short calibration kernel):
+ * the roofline denominator of the FP64 FMM kernels. No counterpart in the reference. */
+int eb_measure_fp64_peak(eb_ctx* ctx, double* tflops);
 
 /* Install the geometry of k drops: the data EXTRACTDAT (electric.f:636-716) leaves
  * in COMMON /inteqn/ dsdth, rkappa, z, dz and /problem/ zk, nd, k, nbk
