@@ -81,6 +81,7 @@ SIGNATURES = {
     "eb_laplace_constraints": (_I, [_P, _I, _P, _P, _I]),
     "eb_stokes_sum": (_I, [_P, _I, _P, _I, _P, _I, _I]),
     "eb_cauchy_sum": (_I, [_P, _I, _P, _P, _P, _I, _I]),
+    "eb_stokes_sum_noalloc": (_I, [_I, _P, _P, _P, _P, _I, _P, _P]),
     "eb_stokes_solve": (_I, [_P, _I, _P, _P, _I, ctypes.POINTER(SolveInfo), _I]),
     "eb_laplace_solve": (_I, [_P, _I, _P, _P, _I, ctypes.POINTER(SolveInfo), _I]),
     "eb_fdiff": (_I, [_P, _P, _P, _I]),

@@ -141,6 +141,24 @@ int eb_laplace_constraints(eb_ctx* ctx, int n, const double* x, double* sums, in
 int eb_stokes_sum(eb_ctx* ctx, int n, const double* dens, int sign, double* gradw,
                   int precision, int mem);
 
+/* For callers that cannot allocate GPU memory; no counterpart in the reference.
+ * Hosts that own every device buffer themselves, code running inside an allocator or
+ * memory-pool callback, and loops that forbid allocation after start-up cannot use the
+ * context-based entry points, which draw working memory from cudaMalloc. This one needs
+ * no eb_ctx and allocates nothing: it evaluates the sum of eb_stokes_sum (CADAPDR for
+ * sign = -1, CADAPMOD for sign = +1, self excluded) by direct FP64 summation for
+ * n <= EB_NOALLOC_MAX_POINTS nodes, larger n returns EB_ERR_WORKSPACE. All arrays are
+ * device pointers: z, dz, dens, gradw complex (n values), h real (the per-node weight
+ * 2 pi / nd of the node's drop). Its scratch is a fixed 768 KiB array in the library's
+ * device memory, held by every GPU that loads the library until exit and shared by all
+ * calls: calls that overlap on the GPU race, so order them on one stream. The first call
+ * on each device looks up that array's address; make it before any stream capture.
+ * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream); the result
+ * is ready when the stream reaches it. */
+#define EB_NOALLOC_MAX_POINTS 16384
+int eb_stokes_sum_noalloc(int n, const double* z, const double* dz, const double* h,
+                          const double* dens, int sign, double* gradw, void* stream);
+
 /* The Cauchy sum DAPIF2 returns for IFLAG7 = 3 (dapif1.f:458-1077):
  * field_i = sum_{j != i} q_j / (z_i - z_j), on n arbitrary points (own tree). */
 int eb_cauchy_sum(eb_ctx* ctx, int n, const double* z, const double* q, double* field,
