@@ -85,180 +85,256 @@ __global__ void k_charges_cauchy(int n, const int* __restrict__ perm,
 }
 
 // ---------------------------------------------------------------------------------
-// P2M at the leaves: one warp per leaf, lanes over the leaf's points, one warp
-// reduction per coefficient (SLMKXP, cadap2.f:412-468, with scaled coefficients
-// and psi relative to the box centre).
+// 1/x in FP64 for the near field: the hardware reciprocal approximation refined by two
+// Newton-Raphson steps r <- r + r (1 - x r), each of which squares the relative error.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+
+template <typename T>
+__device__ __forceinline__ c_t<T> cpow_int(c_t<T> u, int n) {
+  c_t<T> r = cmk<T>(1, 0), b = u;
+  while (n > 0) {
+    if (n & 1) r = cmul<T>(r, b);
+    b = cmul<T>(b, b);
+    n >>= 1;
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------------
+// P2M at the leaves (SLMKXP, cadap2.f:412-468, with scaled coefficients and psi
+// relative to the box centre). One block per leaf: the leaf's points (32 at a time)
+// write their powers w^j to shared memory, then thread j forms the power sums
+//   A_j = sum a w^j,  B_j = sum b w^j,  C_j = sum conj(w) a w^j   (a = qa/r, b = qb/r)
+// and M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 // ---------------------------------------------------------------------------------
 template <typename T, int E>
-__global__ void k_p2m(int off, int nleaf, const unsigned long long* __restrict__ bkey,
-                      const int* __restrict__ pt0, const int* __restrict__ pt1,
-                      const double2* __restrict__ zs, const c_t<T>* __restrict__ qa,
-                      const c_t<T>* __restrict__ qb, double x0, double y0, double r, int p,
-                      c_t<T>* __restrict__ mpole) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= nleaf) return;
-  int b = off + warp;
+__global__ void __launch_bounds__(64) k_p2m(int off, const unsigned long long* __restrict__ bkey,
+                                            const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                            const double2* __restrict__ zs,
+                                            const c_t<T>* __restrict__ qa,
+                                            const c_t<T>* __restrict__ qb, double x0, double y0,
+                                            double r, int p, c_t<T>* __restrict__ mpole) {
+  extern __shared__ unsigned char smem_raw[];
+  const int ps = p + 1;  // odd row stride: conflict-free rows
+  c_t<T>* pw = reinterpret_cast<c_t<T>*>(smem_raw);
+  c_t<T>* sc = pw + 32 * ps;
+  int b = off + blockIdx.x;
+  int tid = threadIdx.x;
   double2 c = box_center(bkey[b], x0, y0, r);
   const T rinv = (T)(1.0 / r);
-  c_t<T> acc[2][2];
-#pragma unroll
-  for (int e = 0; e < 2; ++e)
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) acc[e][sl] = cmk<T>(0, 0);
+  c_t<T> A = cmk<T>(0, 0), B = cmk<T>(0, 0), C = cmk<T>(0, 0);
   int i0 = pt0[b], i1 = pt1[b];
   for (int base = i0; base < i1; base += 32) {
-    int i = base + lane;
-    c_t<T> w = cmk<T>(0, 0), ah = cmk<T>(0, 0), bh = cmk<T>(0, 0);
-    if (i < i1) {
+    int cnt = min(32, i1 - base);
+    __syncthreads();
+    if (tid < cnt) {
+      int i = base + tid;
       double2 zi = zs[i];
-      w = cmk<T>((T)((zi.x - c.x) / r), (T)((zi.y - c.y) / r));
-      ah = cscale<T>(qa[i], rinv);
-      if (E == 2) bh = cscale<T>(qb[i], rinv);
-    }
-    c_t<T> cw = cconj<T>(w);
-    c_t<T> cwa = cmul<T>(cw, ah);  // conj(w) a / r
-    c_t<T> pw = cmk<T>(1, 0), pwm = cmk<T>(0, 0);
-    for (int k = 1; k <= p; ++k) {
-      c_t<T> tphi = cmul<T>(ah, pw);
-      T s0 = warp_sum<T>(-tphi.x), s1 = warp_sum<T>(-tphi.y);
-      int slot = (k - 1) >> 5;
-      bool own = ((k - 1) & 31) == lane;
-      if (own) {
-        if (slot == 0) { acc[0][0].x += s0; acc[0][0].y += s1; }
-        else { acc[0][1].x += s0; acc[0][1].y += s1; }
-      }
+      c_t<T> w = cmk<T>((T)((zi.x - c.x) / r), (T)((zi.y - c.y) / r));
+      c_t<T> ah = cscale<T>(qa[i], rinv);
+      sc[tid] = ah;
       if (E == 2) {
-        c_t<T> tpsi = cmul<T>(bh, pw);
-        cfma<T>(tpsi, cscale<T>(cwa, (T)(k - 1)), pwm);
-        T s2 = warp_sum<T>(-tpsi.x), s3 = warp_sum<T>(-tpsi.y);
-        if (own) {
-          if (slot == 0) { acc[1][0].x += s2; acc[1][0].y += s3; }
-          else { acc[1][1].x += s2; acc[1][1].y += s3; }
+        sc[32 + tid] = cscale<T>(qb[i], rinv);
+        sc[64 + tid] = cmul<T>(cconj<T>(w), ah);
+      }
+      c_t<T> pwr = cmk<T>(1, 0);
+      c_t<T>* row = pw + tid * ps;
+      for (int j = 0; j < p; ++j) {
+        row[j] = pwr;
+        pwr = cmul<T>(pwr, w);
+      }
+    }
+    __syncthreads();
+    if (tid < p) {
+      for (int s = 0; s < cnt; ++s) {
+        c_t<T> v = pw[s * ps + tid];
+        cfma<T>(A, sc[s], v);
+        if (E == 2) {
+          cfma<T>(B, sc[32 + s], v);
+          cfma<T>(C, sc[64 + s], v);
         }
       }
-      pwm = pw;
-      pw = cmul<T>(pw, w);
     }
   }
-#pragma unroll
-  for (int sl = 0; sl < 2; ++sl) {
-    int kk = lane + 32 * sl;
-    if (kk < p) {
-#pragma unroll
-      for (int e = 0; e < E; ++e) mpole[((size_t)b * E + e) * p + kk] = acc[e][sl];
+  __syncthreads();
+  if (tid < p) pw[tid] = C;
+  __syncthreads();
+  if (tid < p) {
+    c_t<T>* mp = mpole + (size_t)b * E * p;
+    mp[tid] = cmk<T>(-A.x, -A.y);
+    if (E == 2) {
+      c_t<T> v = B;
+      if (tid >= 1) crfma<T>(v, (T)tid, pw[tid - 1]);
+      mp[p + tid] = cmk<T>(-v.x, -v.y);
     }
   }
 }
 
 // ---------------------------------------------------------------------------------
-// M2M: one warp per parent box, children processed in turn. With e the child centre
-// offset in child units and a_k = e^-k M_k:   M'_n = (e/2)^n sum_{k<=n} C(n-1,k-1) a_k.
+// M2M: one block per parent, one thread per output coefficient (e, n). With e the child
+// centre offset in child units and a_k = e^-k M_k:  M'_n = (e/2)^n sum_{k<=n} C(n-1,k-1) a_k.
 // psi is first moved to the parent centre: psi_k += conj(e) (k-1) phi_{k-1}.
 // ---------------------------------------------------------------------------------
 template <typename T, int E>
-__global__ void k_m2m(int offp, int nbp, const unsigned long long* __restrict__ bkey,
+__global__ void k_m2m(int offp, const unsigned long long* __restrict__ bkey,
                       const int* __restrict__ child0, const int* __restrict__ nchild, int p,
                       const T* __restrict__ binom, int ldb, const c_t<T>* __restrict__ epow2,
                       const c_t<T>* __restrict__ einv, c_t<T>* __restrict__ mpole) {
   extern __shared__ unsigned char smem_raw[];
-  c_t<T>* sa = reinterpret_cast<c_t<T>*>(smem_raw);
-  int wib = threadIdx.x >> 5;
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= nbp) return;
-  c_t<T>* a = sa + (size_t)wib * E * p;
-  int P = offp + warp;
-  const int ld = p + 2;
-  c_t<T> acc[2][2];
-#pragma unroll
-  for (int e = 0; e < 2; ++e)
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) acc[e][sl] = cmk<T>(0, 0);
+  c_t<T>* a = reinterpret_cast<c_t<T>*>(smem_raw);
+  const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
+  const int e = tid / p, nn = tid - e * p;
+  const bool active = tid < nout;
+  c_t<T> acc = cmk<T>(0, 0);
   int c0 = child0[P], nc = nchild[P];
   for (int ci = 0; ci < nc; ++ci) {
     int c = c0 + ci;
     int q = quadrant(bkey[c]);
-    c_t<T> ec = epow2[q * ld + 1];
-    ec = cscale<T>(ec, (T)2);  // e = 2 (e/2)
+    c_t<T> ec = cscale<T>(epow2[q * ld + 1], (T)2);
     const c_t<T>* mc = mpole + (size_t)c * E * p;
-    for (int kk = lane; kk < p; kk += 32) {
-      int k = kk + 1;
-      c_t<T> sc = einv[q * ld + k];
-      a[kk] = cmul<T>(mc[kk], sc);
-      if (E == 2) {
-        c_t<T> mpsi = mc[p + kk];
-        if (k >= 2) cfma<T>(mpsi, cscale<T>(cconj<T>(ec), (T)(k - 1)), mc[kk - 1]);
-        a[p + kk] = cmul<T>(mpsi, sc);
-      }
+    __syncthreads();
+    for (int idx = tid; idx < nout; idx += blockDim.x) {
+      int e2 = idx / p, kk = idx - e2 * p, k = kk + 1;
+      c_t<T> v = mc[idx];
+      if (e2 == 1 && k >= 2) cfma<T>(v, cscale<T>(cconj<T>(ec), (T)(k - 1)), mc[kk - 1]);
+      a[idx] = cmul<T>(v, einv[q * ld + k]);
     }
-    __syncwarp();
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) {
-      int nn = lane + 32 * sl;
-      if (nn < p) {
-        int n = nn + 1;
-        c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
-        const T* brow = binom + (size_t)(n - 1) * ldb;
-        for (int k = 1; k <= n; ++k) {
-          T cb = brow[k - 1];
-          crfma<T>(s0, cb, a[k - 1]);
-          if (E == 2) crfma<T>(s1, cb, a[p + k - 1]);
-        }
-        c_t<T> post = epow2[q * ld + n];
-        cfma<T>(acc[0][sl], post, s0);
-        if (E == 2) cfma<T>(acc[1][sl], post, s1);
+    __syncthreads();
+    if (active) {
+      int n = nn + 1;
+      const T* brow = binom + (size_t)(n - 1) * ldb;
+      const c_t<T>* ae = a + e * p;
+      c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
+      int k = 0;
+      for (; k + 1 < n; k += 2) {
+        crfma<T>(s0, brow[k], ae[k]);
+        crfma<T>(s1, brow[k + 1], ae[k + 1]);
       }
+      if (k < n) crfma<T>(s0, brow[k], ae[k]);
+      cfma<T>(acc, epow2[q * ld + n], cadd<T>(s0, s1));
     }
-    __syncwarp();
   }
-#pragma unroll
-  for (int sl = 0; sl < 2; ++sl) {
-    int nn = lane + 32 * sl;
-    if (nn < p) {
-#pragma unroll
-      for (int e = 0; e < E; ++e) mpole[((size_t)P * E + e) * p + nn] = acc[e][sl];
+  if (active) mpole[(size_t)P * E * p + tid] = acc;
+}
+
+// ---------------------------------------------------------------------------------
+// L2L: one block per child box, one thread per output (e, j). With e the child offset
+// in child units and a_m = (e/2)^m L_m:  L'_j += e^-j sum_{m>=j} C(m, j) a_m.
+// psi is first moved to the child centre: psi_m += conj(e/2) (m+1) phi_{m+1}.
+// ---------------------------------------------------------------------------------
+template <typename T, int E>
+__global__ void k_l2l(int offc, const unsigned long long* __restrict__ bkey,
+                      const int* __restrict__ parent, int p, const T* __restrict__ binom,
+                      int ldb, const c_t<T>* __restrict__ epow2, const c_t<T>* __restrict__ einv,
+                      c_t<T>* __restrict__ local) {
+  extern __shared__ unsigned char smem_raw[];
+  c_t<T>* a = reinterpret_cast<c_t<T>*>(smem_raw);
+  const int ldl = p + 1, ld = p + 2, nout = E * ldl, tid = threadIdx.x;
+  const int c = offc + blockIdx.x;
+  const int P = parent[c];
+  const int q = quadrant(bkey[c]);
+  c_t<T> eh = epow2[q * ld + 1];
+  const c_t<T>* lp = local + (size_t)P * nout;
+  for (int idx = tid; idx < nout; idx += blockDim.x) {
+    int e2 = idx / ldl, m = idx - e2 * ldl;
+    c_t<T> v = lp[idx];
+    if (e2 == 1 && m < p) cfma<T>(v, cscale<T>(cconj<T>(eh), (T)(m + 1)), lp[m + 1]);
+    a[idx] = cmul<T>(v, epow2[q * ld + m]);
+  }
+  __syncthreads();
+  if (tid < nout) {
+    int e = tid / ldl, j = tid - e * ldl;
+    const c_t<T>* ae = a + e * ldl;
+    c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
+    int m = j;
+    for (; m + 1 <= p; m += 2) {
+      crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
+      crfma<T>(s1, binom[(size_t)(m + 1) * ldb + j], ae[m + 1]);
     }
+    if (m <= p) crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
+    c_t<T>* lc = local + (size_t)c * nout;
+    c_t<T> v = lc[tid];
+    cfma<T>(v, einv[q * ld + j], cadd<T>(s0, s1));
+    lc[tid] = v;
   }
 }
 
 // ---------------------------------------------------------------------------------
 // M2L over the interaction lists of every box of levels >= 2 (one launch for all
-// levels): one warp per target box. For offset d = (c_t - c_s)/r,
-//   a_k = M_k d^-k,  L_m += (-1)^m d^-m sum_k C(m+k-1, m) a_k,
-// with k, m <= pd(d). psi is first moved to the target centre:
-//   psi_k -= conj(d) (k-1) phi_{k-1}.
+// levels). One block per target box; its 4 warps take every 4th entry of the V list
+// and accumulate in shared memory, and the 4 partial expansions are added in a fixed
+// order at the end. For offset d = (c_t - c_s)/r and a_k = M_k d^-k,
+//   L_m += (-1)^m d^-m sum_{k <= pd} C(m+k-1, m) a_k,   m <= pd(d),
+// after moving psi to the target centre: psi_k -= conj(d) (k-1) phi_{k-1}.
+// The E (pd+1) outputs of a pair are spread over the lanes, up to 3 per lane.
 // ---------------------------------------------------------------------------------
+template <typename T, int NS>
+__device__ __forceinline__ void m2l_slots(int ob, int lane, int nout, int ldo, int pd, int p,
+                                          int ldc, const T* C2, const c_t<T>* a,
+                                          const c_t<T>* dv, c_t<T>* acc, int ldl) {
+  int o[NS], m[NS], e[NS];
+  bool v[NS];
+  c_t<T> bsum[NS];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    o[sl] = ob + lane + 32 * sl;
+    v[sl] = o[sl] < nout;
+    e[sl] = v[sl] ? o[sl] / ldo : 0;
+    m[sl] = v[sl] ? o[sl] - e[sl] * ldo : 0;
+    bsum[sl] = cmk<T>(0, 0);
+  }
+  for (int k = 0; k < pd; ++k) {
+#pragma unroll
+    for (int sl = 0; sl < NS; ++sl) crfma<T>(bsum[sl], C2[k * ldc + m[sl]], a[e[sl] * p + k]);
+  }
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    if (v[sl]) {
+      c_t<T> post = dv[m[sl]];
+      if (m[sl] & 1) post = cmk<T>(-post.x, -post.y);
+      c_t<T>* ap = acc + e[sl] * ldl + m[sl];
+      c_t<T> t = *ap;
+      cfma<T>(t, post, bsum[sl]);
+      *ap = t;
+    }
+  }
+}
+
 template <typename T, int E>
-__global__ void __launch_bounds__(128) k_m2l(int first, int ntarget, const int* __restrict__ vlist,
-                      const unsigned char* __restrict__ vcode, const int* __restrict__ vcount,
-                      int p, const T* __restrict__ binom, int ldb,
-                      const c_t<T>* __restrict__ dinv, const int* __restrict__ pdv,
-                      const c_t<T>* __restrict__ mpole, c_t<T>* __restrict__ local) {
+__global__ void __launch_bounds__(128) k_m2l(int first, const int* __restrict__ vlist,
+                                             const unsigned char* __restrict__ vcode,
+                                             const int* __restrict__ vcount, int p,
+                                             const T* __restrict__ binom, int ldb,
+                                             const c_t<T>* __restrict__ dinv,
+                                             const int* __restrict__ pdv,
+                                             const c_t<T>* __restrict__ mpole,
+                                             c_t<T>* __restrict__ local) {
   extern __shared__ unsigned char smem_raw[];
+  const int ldc = p + 1, ldl = p + 1, ldd = p + 2;
   // C2[(k-1)*(p+1) + m] = C(m+k-1, m), k = 1..p, m = 0..p
   T* C2 = reinterpret_cast<T*>(smem_raw);
-  const int ldc = p + 1;
   c_t<T>* sa = reinterpret_cast<c_t<T>*>(smem_raw + ((sizeof(T) * (size_t)p * ldc + 15) & ~(size_t)15));
+  c_t<T>* sacc = sa + 4 * E * p;
   for (int idx = threadIdx.x; idx < p * ldc; idx += blockDim.x) {
     int k = idx / ldc + 1, m = idx % ldc;
     C2[idx] = binom[(size_t)(m + k - 1) * ldb + m];
   }
+  for (int idx = threadIdx.x; idx < 4 * E * ldl; idx += blockDim.x) sacc[idx] = cmk<T>(0, 0);
   __syncthreads();
-  int wib = threadIdx.x >> 5;
-  int lane = threadIdx.x & 31;
-  int t = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (t >= ntarget) return;
-  int gid = first + t;
-  c_t<T>* a = sa + (size_t)wib * E * p;
-  const int ldd = p + 2;
-  c_t<T> acc[2][2];
-#pragma unroll
-  for (int e = 0; e < 2; ++e)
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) acc[e][sl] = cmk<T>(0, 0);
-  int nv = vcount[gid];
-  for (int j = 0; j < nv; ++j) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = first + blockIdx.x;
+  c_t<T>* a = sa + w * E * p;
+  c_t<T>* acc = sacc + w * E * ldl;
+  const int nv = vcount[gid];
+  for (int j = w; j < nv; j += 4) {
     int s = vlist[(size_t)gid * EB_VMAX + j];
     int code = vcode[(size_t)gid * EB_VMAX + j];
     int pd = pdv[code];
@@ -271,184 +347,333 @@ __global__ void __launch_bounds__(128) k_m2l(int first, int ntarget, const int* 
       a[kk] = cmul<T>(ms[kk], sc);
       if (E == 2) {
         c_t<T> mpsi = ms[p + kk];
-        // psi_k -= conj(d) (k-1) phi_{k-1}
         if (k >= 2) cfma<T>(mpsi, cmk<T>(-dxr * (T)(k - 1), dyr * (T)(k - 1)), ms[kk - 1]);
         a[p + kk] = cmul<T>(mpsi, sc);
       }
     }
     __syncwarp();
-#pragma unroll
-    for (int sl = 0; sl < 2; ++sl) {
-      int m = lane + 32 * sl;
-      if (m <= pd) {
-        c_t<T> b0 = cmk<T>(0, 0), b1 = cmk<T>(0, 0);
-        const T* col = C2 + m;
-#pragma unroll 4
-        for (int k = 1; k <= pd; ++k) {
-          T cb = col[(k - 1) * ldc];
-          crfma<T>(b0, cb, a[k - 1]);
-          if (E == 2) crfma<T>(b1, cb, a[p + k - 1]);
-        }
-        c_t<T> post = dv[m];
-        if (m & 1) post = cmk<T>(-post.x, -post.y);
-        cfma<T>(acc[0][sl], post, b0);
-        if (E == 2) cfma<T>(acc[1][sl], post, b1);
-      }
+    const int ldo = pd + 1, nout = E * ldo;
+    for (int ob = 0; ob < nout; ob += 96) {
+      int rem = nout - ob;
+      if (rem > 64) m2l_slots<T, 3>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
+      else if (rem > 32) m2l_slots<T, 2>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
+      else m2l_slots<T, 1>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
     }
     __syncwarp();
   }
-  const int ldl = p + 1;
-#pragma unroll
-  for (int sl = 0; sl < 2; ++sl) {
-    int m = lane + 32 * sl;
-    if (m <= p) {
-#pragma unroll
-      for (int e = 0; e < E; ++e) local[((size_t)gid * E + e) * ldl + m] = acc[e][sl];
-    }
+  __syncthreads();
+  const int tot = E * ldl;
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    c_t<T> v = cadd<T>(cadd<T>(sacc[idx], sacc[tot + idx]), cadd<T>(sacc[2 * tot + idx], sacc[3 * tot + idx]));
+    local[(size_t)gid * tot + idx] = v;
   }
 }
 
 // ---------------------------------------------------------------------------------
-// L2L: one warp per child box. With e the child offset in child units and
-// a_m = (e/2)^m L_m:   L'_j += e^-j sum_{m>=j} C(m, j) a_m.
-// psi is first moved to the child centre: psi_m += conj(e/2) (m+1) phi_{m+1}.
+// Upward pass in one launch: one block per leaf forms the leaf's multipole (P2M), then
+// climbs: after writing a box's multipole it increments the parent's arrival counter,
+// and the block that delivers the last child forms the parent's multipole (M2M) from
+// all children in their fixed order. The counters are cleared before each launch.
+// M2M: with e the child centre offset in child units and a_k = e^-k M_k,
+//   M'_n = (e/2)^n sum_{k<=n} C(n-1,k-1) a_k, after psi_k += conj(e) (k-1) phi_{k-1}.
+// P2M (SLMKXP, cadap2.f:412-468, scaled and centre-relative): the leaf's points, 32 at
+// a time, write their powers w^j to shared memory; thread j forms the power sums
+//   A_j = sum a w^j, B_j = sum b w^j, C_j = sum conj(w) a w^j (a = qa/r, b = qb/r),
+// and M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 // ---------------------------------------------------------------------------------
 template <typename T, int E>
-__global__ void k_l2l(int offc, int nbc, const unsigned long long* __restrict__ bkey,
-                      const int* __restrict__ parent, int p, const T* __restrict__ binom,
-                      int ldb, const c_t<T>* __restrict__ epow2, const c_t<T>* __restrict__ einv,
-                      c_t<T>* __restrict__ local) {
-  extern __shared__ unsigned char smem_raw[];
-  c_t<T>* sa = reinterpret_cast<c_t<T>*>(smem_raw);
-  int wib = threadIdx.x >> 5;
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= nbc) return;
-  const int ldl = p + 1, ld = p + 2;
-  c_t<T>* a = sa + (size_t)wib * E * ldl;
-  int c = offc + warp;
-  int P = parent[c];
-  int q = quadrant(bkey[c]);
-  c_t<T> eh = epow2[q * ld + 1];  // e/2
-  const c_t<T>* lp = local + (size_t)P * E * ldl;
-  for (int m = lane; m <= p; m += 32) {
-    c_t<T> sc = epow2[q * ld + m];
-    a[m] = cmul<T>(lp[m], sc);
-    if (E == 2) {
-      c_t<T> lpsi = lp[ldl + m];
-      if (m < p) cfma<T>(lpsi, cscale<T>(cconj<T>(eh), (T)(m + 1)), lp[m + 1]);
-      a[ldl + m] = cmul<T>(lpsi, sc);
-    }
-  }
-  __syncwarp();
-  c_t<T>* lc = local + (size_t)c * E * ldl;
-  for (int j = lane; j <= p; j += 32) {
-    c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
-    for (int m = j; m <= p; ++m) {
-      T cb = binom[(size_t)m * ldb + j];
-      crfma<T>(s0, cb, a[m]);
-      if (E == 2) crfma<T>(s1, cb, a[ldl + m]);
-    }
-    c_t<T> post = einv[q * ld + j];
-    c_t<T> v0 = lc[j];
-    cfma<T>(v0, post, s0);
-    lc[j] = v0;
-    if (E == 2) {
-      c_t<T> v1 = lc[ldl + j];
-      cfma<T>(v1, post, s1);
-      lc[ldl + j] = v1;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------------
-// Leaf evaluation, FP64: L2P plus the near field over the U list (SLSELFDR/SLDIRDR,
-// cadapdrop2.f:564-620, 724-769; DABARR's pair loop, dapif3.f:460-545).
-// One warp per leaf, one lane per target point; source data are broadcast loads.
-// ---------------------------------------------------------------------------------
-template <int E>
-__global__ void __launch_bounds__(128) k_leaf64(int off, int nleaf, int has_far,
-                         const unsigned long long* __restrict__ bkey,
-                         const int* __restrict__ pt0, const int* __restrict__ pt1,
-                         const int* __restrict__ ulist, const int* __restrict__ ucount,
-                         const int* __restrict__ perm, const double2* __restrict__ zs,
-                         const double2* __restrict__ pq, const double2* __restrict__ aa,
-                         const double2* __restrict__ qa, double x0, double y0, double r,
-                         int p, double s, const double2* __restrict__ local,
-                         double2* __restrict__ out) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= nleaf) return;
-  int b = off + warp;
+__device__ void p2m_block(int b, const unsigned long long* __restrict__ bkey,
+                          const int* __restrict__ pt0, const int* __restrict__ pt1,
+                          const double2* __restrict__ zs, const c_t<T>* __restrict__ qa,
+                          const c_t<T>* __restrict__ qb, double x0, double y0, double r, int p,
+                          c_t<T>* __restrict__ mpole, c_t<T>* smem) {
+  const int ps = p + 1;  // odd row stride: conflict-free rows
+  c_t<T>* pw = smem;
+  c_t<T>* sc = pw + 32 * ps;
+  const int tid = threadIdx.x;
   double2 c = box_center(bkey[b], x0, y0, r);
+  const T rinv = (T)(1.0 / r);
+  c_t<T> A = cmk<T>(0, 0), B = cmk<T>(0, 0), C = cmk<T>(0, 0);
   int i0 = pt0[b], i1 = pt1[b];
-  int nu = ucount[warp];
-  const int ldl = p + 1;
-  const double2* lb = local + (size_t)b * E * ldl;
   for (int base = i0; base < i1; base += 32) {
-    int i = base + lane;
-    bool act = i < i1;
-    int ii = act ? i : i0;
-    double2 zi = zs[ii];
-    double gx = 0.0, gy = 0.0;
-    if (has_far) {
-      double2 u = make_double2((zi.x - c.x) / r, (zi.y - c.y) / r);
-      double2 phi = lb[p], dphi = make_double2(0.0, 0.0);
-      for (int m = p - 1; m >= 0; --m) {
-        dphi = cmul<double>(dphi, u);
-        dphi = cadd<double>(dphi, phi);
-        phi = cmul<double>(phi, u);
-        phi = cadd<double>(phi, lb[m]);
-      }
+    int cnt = min(32, i1 - base);
+    __syncthreads();
+    if (tid < cnt) {
+      int i = base + tid;
+      double2 zi = zs[i];
+      c_t<T> w = cmk<T>((T)((zi.x - c.x) / r), (T)((zi.y - c.y) / r));
+      c_t<T> ah = cscale<T>(qa[i], rinv);
+      sc[tid] = ah;
       if (E == 2) {
-        double2 psi = lb[ldl + p];
-        for (int m = p - 1; m >= 0; --m) {
-          psi = cmul<double>(psi, u);
-          psi = cadd<double>(psi, lb[ldl + m]);
-        }
-        // GW = phi + s [ u conj(dphi) + conj(psi) ]
-        double2 t = cmulc<double>(u, dphi);
-        gx = phi.x + s * (t.x + psi.x);
-        gy = phi.y + s * (t.y - psi.y);
-      } else {
-        gx = -phi.x;
-        gy = -phi.y;
+        sc[32 + tid] = cscale<T>(qb[i], rinv);
+        sc[64 + tid] = cmul<T>(cconj<T>(w), ah);
+      }
+      c_t<T> pwr = cmk<T>(1, 0);
+      c_t<T>* row = pw + tid * ps;
+      for (int j = 0; j < p; ++j) {
+        row[j] = pwr;
+        pwr = cmul<T>(pwr, w);
       }
     }
-    for (int jl = 0; jl < nu; ++jl) {
-      int sb = ulist[(size_t)warp * EB_UMAX + jl];
-      int j0 = pt0[sb], j1 = pt1[sb];
-      for (int j = j0; j < j1; ++j) {
-        double2 zj = zs[j];
-        double dx = zj.x - zi.x, dy = zj.y - zi.y;
-        double d2 = fma(dx, dx, dy * dy);
-        if (j == ii) continue;
-        double rr = 1.0 / d2;
-        double ix = dx * rr, iy = -dy * rr;  // 1/D
+    __syncthreads();
+    if (tid < p) {
+      for (int s = 0; s < cnt; ++s) {
+        c_t<T> v = pw[s * ps + tid];
+        cfma<T>(A, sc[s], v);
         if (E == 2) {
-          double2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
-          // qa/D + s conj(qb/D)
-          gx = fma(P.x, ix, fma(-P.y, iy, gx));
-          gy = fma(Q.x, iy, fma(Q.y, ix, gy));
-          // - s D conj(qa) conj(1/D)^2 = A * D * w^2, w = conj(1/D)
-          double w2x = fma(ix, ix, -iy * iy), w2y = -2.0 * ix * iy;
-          double tx = fma(dx, w2x, -dy * w2y), ty = fma(dx, w2y, dy * w2x);
-          gx = fma(A.x, tx, fma(-A.y, ty, gx));
-          gy = fma(A.x, ty, fma(A.y, tx, gy));
-        } else {
-          double2 q = qa[j];
-          // F += q/(z_i - z_j) = -q/D
-          gx = fma(-q.x, ix, fma(q.y, iy, gx));
-          gy = fma(-q.x, iy, fma(-q.y, ix, gy));
+          cfma<T>(B, sc[32 + s], v);
+          cfma<T>(C, sc[64 + s], v);
         }
       }
     }
-    if (act) out[perm[i]] = make_double2(gx, gy);
+  }
+  __syncthreads();
+  if (tid < p) pw[tid] = C;
+  __syncthreads();
+  if (tid < p) {
+    c_t<T>* mp = mpole + (size_t)b * E * p;
+    mp[tid] = cmk<T>(-A.x, -A.y);
+    if (E == 2) {
+      c_t<T> v = B;
+      if (tid >= 1) crfma<T>(v, (T)tid, pw[tid - 1]);
+      mp[p + tid] = cmk<T>(-v.x, -v.y);
+    }
   }
 }
 
-// Leaf evaluation, FP32: positions as float hi + lo so that differences are exact to
-// float precision, Kahan-compensated accumulation of the near-field sum.
+template <typename T>
+__device__ __forceinline__ c_t<T> ldcg_c(const c_t<T>* p);
+template <>
+__device__ __forceinline__ double2 ldcg_c<double>(const double2* p) {
+  return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ float2 ldcg_c<float>(const float2* p) {
+  return __ldcg(p);
+}
+
+template <typename T, int E>
+__global__ void k_upward(int offL, int L, const unsigned long long* __restrict__ bkey,
+                         const int* __restrict__ pt0, const int* __restrict__ pt1,
+                         const int* __restrict__ parent, const int* __restrict__ child0,
+                         const int* __restrict__ nchild, const double2* __restrict__ zs,
+                         const c_t<T>* __restrict__ qa, const c_t<T>* __restrict__ qb, double x0,
+                         double y0, double rleaf, int p, const T* __restrict__ binom, int ldb,
+                         const c_t<T>* __restrict__ epow2, const c_t<T>* __restrict__ einv,
+                         int* __restrict__ arrivals, c_t<T>* mpole) {
+  extern __shared__ unsigned char smem_raw[];
+  c_t<T>* smem = reinterpret_cast<c_t<T>*>(smem_raw);
+  __shared__ int s_last;
+  const int tid = threadIdx.x, ld = p + 2, nout = E * p;
+  int cur = offL + blockIdx.x;
+  p2m_block<T, E>(cur, bkey, pt0, pt1, zs, qa, qb, x0, y0, rleaf, p, mpole, smem);
+  const int e = tid / p, nn = tid - e * p;
+  for (int lev = L; lev > 2; --lev) {
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      int P = parent[cur];
+      s_last = (atomicAdd(&arrivals[P], 1) == nchild[P] - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    cur = parent[cur];
+    // M2M into box `cur` from its children
+    c_t<T>* a = smem;
+    c_t<T> acc = cmk<T>(0, 0);
+    int c0 = child0[cur], nc = nchild[cur];
+    for (int ci = 0; ci < nc; ++ci) {
+      int c = c0 + ci;
+      int q = quadrant(bkey[c]);
+      c_t<T> ec = cscale<T>(epow2[q * ld + 1], (T)2);
+      const c_t<T>* mc = mpole + (size_t)c * E * p;
+      __syncthreads();
+      for (int idx = tid; idx < nout; idx += blockDim.x) {
+        int e2 = idx / p, kk = idx - e2 * p, k = kk + 1;
+        c_t<T> v = ldcg_c<T>(mc + idx);
+        if (e2 == 1 && k >= 2) cfma<T>(v, cscale<T>(cconj<T>(ec), (T)(k - 1)), ldcg_c<T>(mc + kk - 1));
+        a[idx] = cmul<T>(v, einv[q * ld + k]);
+      }
+      __syncthreads();
+      if (tid < nout) {
+        int n = nn + 1;
+        const T* brow = binom + (size_t)(n - 1) * ldb;
+        const c_t<T>* ae = a + e * p;
+        c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
+        int k = 0;
+        for (; k + 1 < n; k += 2) {
+          crfma<T>(s0, brow[k], ae[k]);
+          crfma<T>(s1, brow[k + 1], ae[k + 1]);
+        }
+        if (k < n) crfma<T>(s0, brow[k], ae[k]);
+        cfma<T>(acc, epow2[q * ld + n], cadd<T>(s0, s1));
+      }
+    }
+    if (tid < nout) mpole[(size_t)cur * E * p + tid] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Downward pass in one launch: one block per leaf adds to its own M2L expansion the
+// M2L expansion of every ancestor (levels L-1 .. 2) shifted directly to the leaf centre
+// (a polynomial shift is exact, so this equals the level-by-level L2L chain). For an
+// ancestor of side r_a, with d = (c_leaf - c_a)/r_leaf and g = d r_leaf/r_a:
+//   a_m = g^m L_m,  L_leaf[j] += d^-j sum_{m>=j} C(m, j) a_m,
+// after moving psi to the leaf centre: psi_m += conj(g) (m+1) phi_{m+1}.
+// ---------------------------------------------------------------------------------
+template <typename T, int E>
+__global__ void k_downward(int offL, int L, const unsigned long long* __restrict__ bkey,
+                           const int* __restrict__ parent, int p, const T* __restrict__ binom,
+                           int ldb, c_t<T>* __restrict__ local) {
+  extern __shared__ unsigned char smem_raw[];
+  c_t<T>* as = reinterpret_cast<c_t<T>*>(smem_raw);
+  const int tid = threadIdx.x, ldl = p + 1, nout = E * ldl;
+  const int b = offL + blockIdx.x;
+  const unsigned long long kb = bkey[b];
+  const double lx = (double)compact2d(kb) + 0.5, ly = (double)compact2d(kb >> 1) + 0.5;
+  const int e = tid / ldl, j = tid - e * ldl;
+  c_t<T> acc = cmk<T>(0, 0);
+  int a = parent[b];
+  for (int lev = L - 1; lev >= 2; --lev, a = parent[a]) {
+    const int shift = L - lev;
+    const unsigned long long ka = bkey[a];
+    const double sc = (double)(1u << shift);
+    const double dx = lx - ((double)compact2d(ka) + 0.5) * sc, dy = ly - ((double)compact2d(ka >> 1) + 0.5) * sc;
+    const c_t<T> d = cmk<T>((T)dx, (T)dy);
+    const c_t<T> g = cmk<T>((T)(dx / sc), (T)(dy / sc));
+    const c_t<T>* la = local + (size_t)a * nout;
+    __syncthreads();
+    for (int idx = tid; idx < nout; idx += blockDim.x) {
+      int e2 = idx / ldl, m = idx - e2 * ldl;
+      c_t<T> v = la[idx];
+      if (e2 == 1 && m < p) cfma<T>(v, cscale<T>(cconj<T>(g), (T)(m + 1)), la[m + 1]);
+      as[idx] = cmul<T>(v, cpow_int<T>(g, m));
+    }
+    __syncthreads();
+    if (tid < nout) {
+      const c_t<T>* ae = as + e * ldl;
+      c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
+      int m = j;
+      for (; m + 1 <= p; m += 2) {
+        crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
+        crfma<T>(s1, binom[(size_t)(m + 1) * ldb + j], ae[m + 1]);
+      }
+      if (m <= p) crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
+      cfma<T>(acc, cpow_int<T>(cinv<T>(d), j), cadd<T>(s0, s1));
+    }
+  }
+  if (tid < nout) {
+    c_t<T>* lb = local + (size_t)b * nout;
+    lb[tid] = cadd<T>(lb[tid], acc);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Leaf evaluation: L2P plus the near field over the U list (SLSELFDR/SLDIRDR,
+// cadapdrop2.f:564-620, 724-769; DABARR's pair loop, dapif3.f:460-545), self excluded.
+// One warp per group of up to 8 targets of a leaf; 4 lanes per target split the
+// sources (and the terms of the local expansion), and their partial sums are added
+// with two shuffles in a fixed order.
+// ---------------------------------------------------------------------------------
+// Partial far field of lane sl: terms m0 <= m < m1 of the local expansions at u.
+template <typename T, int E>
+__device__ __forceinline__ void l2p_part(const c_t<T>* lb, int p, int sl, c_t<T> u, T s, T& gx,
+                                         T& gy) {
+  const int ldl = p + 1, q = (ldl + 3) / 4;
+  int m0 = sl * q, m1 = min(ldl, m0 + q);
+  if (m0 >= m1) return;
+  c_t<T> ph = lb[m1 - 1], dph = cmk<T>(0, 0);
+  for (int m = m1 - 2; m >= m0; --m) {
+    dph = cadd<T>(cmul<T>(dph, u), ph);
+    ph = cadd<T>(cmul<T>(ph, u), lb[m]);
+  }
+  c_t<T> ps = cmk<T>(0, 0);
+  if (E == 2) {
+    ps = lb[ldl + m1 - 1];
+    for (int m = m1 - 2; m >= m0; --m) ps = cadd<T>(cmul<T>(ps, u), lb[ldl + m]);
+  }
+  if (m0 > 0) {
+    c_t<T> um1 = cpow_int<T>(u, m0 - 1);  // u^(m0-1)
+    // d/du (u^m0 H) = u^(m0-1) (u H' + m0 H)
+    dph = cmul<T>(um1, cadd<T>(cmul<T>(u, dph), cscale<T>(ph, (T)m0)));
+    c_t<T> um = cmul<T>(um1, u);
+    ph = cmul<T>(um, ph);
+    if (E == 2) ps = cmul<T>(um, ps);
+  }
+  if (E == 2) {
+    c_t<T> t = cmulc<T>(u, dph);
+    gx += ph.x + s * (t.x + ps.x);
+    gy += ph.y + s * (t.y - ps.y);
+  } else {
+    gx -= ph.x;
+    gy -= ph.y;
+  }
+}
+
+template <int E>
+__global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restrict__ gleaf,
+                                                const int* __restrict__ gfirst, int off, int has_far,
+                                                const unsigned long long* __restrict__ bkey,
+                                                const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                const int* __restrict__ ulist,
+                                                const int* __restrict__ ucount,
+                                                const int* __restrict__ perm,
+                                                const double2* __restrict__ zs,
+                                                const double2* __restrict__ pq,
+                                                const double2* __restrict__ aa,
+                                                const double2* __restrict__ qa, double x0, double y0,
+                                                double r, int p, double s,
+                                                const double2* __restrict__ local,
+                                                double2* __restrict__ out) {
+  int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= ngroup) return;
+  const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
+  const int leaf = gleaf[g], b = off + leaf;
+  const int i = gfirst[g] + tg;
+  const bool act = i < pt1[b];
+  const int ii = act ? i : gfirst[g];
+  const double2 zi = zs[ii];
+  double gx = 0.0, gy = 0.0;
+  if (has_far) {
+    double2 c = box_center(bkey[b], x0, y0, r);
+    double2 u = make_double2((zi.x - c.x) / r, (zi.y - c.y) / r);
+    l2p_part<double, E>(local + (size_t)b * E * (p + 1), p, sl, u, s, gx, gy);
+  }
+  const int nu = ucount[leaf];
+  for (int jl = 0; jl < nu; ++jl) {
+    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
+    const int j1 = pt1[sb];
+    for (int j = pt0[sb] + sl; j < j1; j += 4) {
+      if (j == ii) continue;
+      double2 zj = zs[j];
+      double dx = zj.x - zi.x, dy = zj.y - zi.y;
+      double rr = rcp_nr(fma(dx, dx, dy * dy));
+      double ix = dx * rr, iy = -dy * rr;  // 1/D
+      if (E == 2) {
+        double2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
+        gx = fma(P.x, ix, fma(-P.y, iy, gx));  // qa/D + s conj(qb/D)
+        gy = fma(Q.x, iy, fma(Q.y, ix, gy));
+        double w2x = fma(ix, ix, -iy * iy), w2y = -2.0 * ix * iy;  // conj(1/D)^2
+        double tx = fma(dx, w2x, -dy * w2y), ty = fma(dx, w2y, dy * w2x);
+        gx = fma(A.x, tx, fma(-A.y, ty, gx));  // - s D conj(qa) conj(1/D)^2
+        gy = fma(A.x, ty, fma(A.y, tx, gy));
+      } else {
+        double2 q = qa[j];
+        gx = fma(-q.x, ix, fma(q.y, iy, gx));  // q/(z_i - z_j) = -q/D
+        gy = fma(-q.x, iy, fma(-q.y, ix, gy));
+      }
+    }
+  }
+  gx += __shfl_xor_sync(0xffffffffu, gx, 1);
+  gy += __shfl_xor_sync(0xffffffffu, gy, 1);
+  gx += __shfl_xor_sync(0xffffffffu, gx, 2);
+  gy += __shfl_xor_sync(0xffffffffu, gy, 2);
+  if (sl == 0 && act) out[perm[i]] = make_double2(gx, gy);
+}
+
+// FP32 leaf evaluation: node positions as float hi + lo so that differences are exact
+// to float precision, Kahan-compensated per-lane sums.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   float y = v - c;
   float t = s + y;
@@ -457,83 +682,76 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 }
 
 template <int E>
-__global__ void __launch_bounds__(128) k_leaf32(int off, int nleaf, int has_far,
-                         const unsigned long long* __restrict__ bkey,
-                         const int* __restrict__ pt0, const int* __restrict__ pt1,
-                         const int* __restrict__ ulist, const int* __restrict__ ucount,
-                         const int* __restrict__ perm, const double2* __restrict__ zs,
-                         const float2* __restrict__ zhi, const float2* __restrict__ zlo,
-                         const float2* __restrict__ pq, const float2* __restrict__ aa,
-                         const float2* __restrict__ qa, double x0, double y0, double r,
-                         int p, float s, const float2* __restrict__ local,
-                         double2* __restrict__ out) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (warp >= nleaf) return;
-  int b = off + warp;
-  double2 c = box_center(bkey[b], x0, y0, r);
-  int i0 = pt0[b], i1 = pt1[b];
-  int nu = ucount[warp];
-  const int ldl = p + 1;
-  const float2* lb = local + (size_t)b * E * ldl;
-  for (int base = i0; base < i1; base += 32) {
-    int i = base + lane;
-    bool act = i < i1;
-    int ii = act ? i : i0;
-    float2 hi = zhi[ii], lo = zlo[ii];
-    float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
-    if (has_far) {
-      double2 zi = zs[ii];
-      float2 u = make_float2((float)((zi.x - c.x) / r), (float)((zi.y - c.y) / r));
-      float2 phi = lb[p], dphi = make_float2(0.f, 0.f);
-      for (int m = p - 1; m >= 0; --m) {
-        dphi = cadd<float>(cmul<float>(dphi, u), phi);
-        phi = cadd<float>(cmul<float>(phi, u), lb[m]);
-      }
-      if (E == 2) {
-        float2 psi = lb[ldl + p];
-        for (int m = p - 1; m >= 0; --m) psi = cadd<float>(cmul<float>(psi, u), lb[ldl + m]);
-        float2 t = cmulc<float>(u, dphi);
-        gx = phi.x + s * (t.x + psi.x);
-        gy = phi.y + s * (t.y - psi.y);
-      } else {
-        gx = -phi.x;
-        gy = -phi.y;
-      }
-    }
-    for (int jl = 0; jl < nu; ++jl) {
-      int sb = ulist[(size_t)warp * EB_UMAX + jl];
-      int j0 = pt0[sb], j1 = pt1[sb];
-      for (int j = j0; j < j1; ++j) {
-        float2 hj = zhi[j], lj = zlo[j];
-        float dx = (hj.x - hi.x) + (lj.x - lo.x);
-        float dy = (hj.y - hi.y) + (lj.y - lo.y);
-        if (j == ii) continue;
-        float d2 = fmaf(dx, dx, dy * dy);
-        float rr = __fdividef(1.0f, d2);
-        float ix = dx * rr, iy = -dy * rr;
-        float tx_, ty_;
-        if (E == 2) {
-          float2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
-          float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
-          float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
-          tx_ = fmaf(P.x, ix, fmaf(-P.y, iy, fmaf(A.x, tx, -A.y * ty)));
-          ty_ = fmaf(Q.x, iy, fmaf(Q.y, ix, fmaf(A.x, ty, A.y * tx)));
-        } else {
-          float2 q = qa[j];
-          tx_ = fmaf(-q.x, ix, q.y * iy);
-          ty_ = fmaf(-q.x, iy, -q.y * ix);
-        }
-        kahan_add(gx, cx, tx_);
-        kahan_add(gy, cy, ty_);
-      }
-    }
-    if (act) out[perm[i]] = make_double2((double)gx, (double)gy);
+__global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restrict__ gleaf,
+                                                const int* __restrict__ gfirst, int off, int has_far,
+                                                const unsigned long long* __restrict__ bkey,
+                                                const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                const int* __restrict__ ulist,
+                                                const int* __restrict__ ucount,
+                                                const int* __restrict__ perm,
+                                                const double2* __restrict__ zs,
+                                                const float2* __restrict__ zhi,
+                                                const float2* __restrict__ zlo,
+                                                const float2* __restrict__ pq,
+                                                const float2* __restrict__ aa,
+                                                const float2* __restrict__ qa, double x0, double y0,
+                                                double r, int p, float s,
+                                                const float2* __restrict__ local,
+                                                double2* __restrict__ out) {
+  int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= ngroup) return;
+  const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
+  const int leaf = gleaf[g], b = off + leaf;
+  const int i = gfirst[g] + tg;
+  const bool act = i < pt1[b];
+  const int ii = act ? i : gfirst[g];
+  const float2 hi = zhi[ii], lo = zlo[ii];
+  float fx = 0.f, fy = 0.f;
+  if (has_far) {
+    double2 zi = zs[ii];
+    double2 c = box_center(bkey[b], x0, y0, r);
+    float2 u = make_float2((float)((zi.x - c.x) / r), (float)((zi.y - c.y) / r));
+    l2p_part<float, E>(local + (size_t)b * E * (p + 1), p, sl, u, s, fx, fy);
   }
+  float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
+  const int nu = ucount[leaf];
+  for (int jl = 0; jl < nu; ++jl) {
+    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
+    const int j1 = pt1[sb];
+    for (int j = pt0[sb] + sl; j < j1; j += 4) {
+      if (j == ii) continue;
+      float2 hj = zhi[j], lj = zlo[j];
+      float dx = (hj.x - hi.x) + (lj.x - lo.x);
+      float dy = (hj.y - hi.y) + (lj.y - lo.y);
+      float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
+      float ix = dx * rr, iy = -dy * rr;
+      float tx_, ty_;
+      if (E == 2) {
+        float2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
+        float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
+        float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
+        tx_ = fmaf(P.x, ix, fmaf(-P.y, iy, fmaf(A.x, tx, -A.y * ty)));
+        ty_ = fmaf(Q.x, iy, fmaf(Q.y, ix, fmaf(A.x, ty, A.y * tx)));
+      } else {
+        float2 q = qa[j];
+        tx_ = fmaf(-q.x, ix, q.y * iy);
+        ty_ = fmaf(-q.x, iy, -q.y * ix);
+      }
+      kahan_add(gx, cx, tx_);
+      kahan_add(gy, cy, ty_);
+    }
+  }
+  gx = (gx - cx) + fx;
+  gy = (gy - cy) + fy;
+  gx += __shfl_xor_sync(0xffffffffu, gx, 1);
+  gy += __shfl_xor_sync(0xffffffffu, gy, 1);
+  gx += __shfl_xor_sync(0xffffffffu, gx, 2);
+  gy += __shfl_xor_sync(0xffffffffu, gy, 2);
+  if (sl == 0 && act) out[perm[i]] = make_double2((double)gx, (double)gy);
 }
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
-
+inline int round32(int n) { return (n + 31) & ~31; }
 template <typename T>
 int tables_build(EbTables& tb, int p, double tol) {
   tb.p = p;
@@ -620,42 +838,74 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   const int ldb = 2 * p + 2;
   EB_TRY(w.mpole.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * p));
   EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * (p + 1)));
+  EB_TRY(t.arrive.ensure(sizeof(int) * (size_t)t.nbox));
   double rleaf = t.W / (double)(1 << L);
   int offL = t.lev_off[L];
-  k_p2m<T, E><<<nblk((long long)t.nleaf * 32, 128), 128, 0, st>>>(
-      offL, t.nleaf, t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
-      t.zs.as<double2>(), w.qa.as<c_t<T>>(), w.qb.as<c_t<T>>(), t.x0, t.y0, rleaf, p,
-      w.mpole.as<c_t<T>>());
-  eb_count_launch(ctx);
-  for (int l = L - 1; l >= 2; --l) {
-    int nb = t.lev_off[l + 1] - t.lev_off[l];
-    size_t sm = sizeof(c_t<T>) * 4 * E * p;
-    k_m2m<T, E><<<nblk((long long)nb * 32, 128), 128, sm, st>>>(
-        t.lev_off[l], nb, t.bkey.as<unsigned long long>(), t.child0.as<int>(), t.nchild.as<int>(), p,
-        tb.binom.as<T>(), ldb, tb.epow.as<c_t<T>>(), tb.einv.as<c_t<T>>(), w.mpole.as<c_t<T>>());
+  // Upward pass. FP32: one launch (P2M plus climbing M2M), whose short chain of
+  // dependent steps matters more than its extra arithmetic. FP64: P2M and one M2M launch
+  // per level, which keep the slow FP64 pipe busier.
+  if (sizeof(T) == 4) {
+    EB_CUDA_TRY(cudaMemsetAsync(t.arrive.p, 0, sizeof(int) * (size_t)t.nbox, st));
+    size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
+    int bs = std::max(64, round32(E * p));
+    k_upward<T, E><<<t.nleaf, bs, sm, st>>>(offL, L, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                            t.pt1.as<int>(), t.parent.as<int>(), t.child0.as<int>(),
+                                            t.nchild.as<int>(), t.zs.as<double2>(), w.qa.as<c_t<T>>(),
+                                            w.qb.as<c_t<T>>(), t.x0, t.y0, rleaf, p, tb.binom.as<T>(),
+                                            ldb, tb.epow.as<c_t<T>>(), tb.einv.as<c_t<T>>(),
+                                            t.arrive.as<int>(), w.mpole.as<c_t<T>>());
     eb_count_launch(ctx);
+  } else {
+    size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
+    k_p2m<T, E><<<t.nleaf, 64, sm, st>>>(offL, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                          t.pt1.as<int>(), t.zs.as<double2>(), w.qa.as<c_t<T>>(),
+                                          w.qb.as<c_t<T>>(), t.x0, t.y0, rleaf, p,
+                                          w.mpole.as<c_t<T>>());
+    eb_count_launch(ctx);
+    for (int l = L - 1; l >= 2; --l) {
+      int nb = t.lev_off[l + 1] - t.lev_off[l];
+      size_t sm2 = sizeof(c_t<T>) * E * p;
+      k_m2m<T, E><<<nb, round32(E * p), sm2, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
+                                                   t.child0.as<int>(), t.nchild.as<int>(), p,
+                                                   tb.binom.as<T>(), ldb, tb.epow.as<c_t<T>>(),
+                                                   tb.einv.as<c_t<T>>(), w.mpole.as<c_t<T>>());
+      eb_count_launch(ctx);
+    }
   }
   {
     int first = t.lev_off[2], nt = t.nbox - first;
     size_t c2 = (sizeof(T) * (size_t)p * (p + 1) + 15) & ~(size_t)15;
-    size_t sm = c2 + sizeof(c_t<T>) * 4 * E * p;
+    size_t sm = c2 + sizeof(c_t<T>) * 4 * E * (size_t)(2 * p + 1);
     if (sm > 48 * 1024)
       EB_CUDA_TRY(cudaFuncSetAttribute(k_m2l<T, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     ProfScope ps(ctx, 1, st);
-    k_m2l<T, E><<<nblk(nt, 4), 128, sm, st>>>(first, nt, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
-                                              t.vcount.as<int>(), p, tb.binom.as<T>(), ldb,
-                                              tb.dinv.as<c_t<T>>(), tb.pd.as<int>(),
-                                              w.mpole.as<c_t<T>>(), w.local.as<c_t<T>>());
-    eb_count_launch(ctx);
+    if (nt > 0) {
+      k_m2l<T, E><<<nt, 128, sm, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
+                                       t.vcount.as<int>(), p, tb.binom.as<T>(), ldb,
+                                       tb.dinv.as<c_t<T>>(), tb.pd.as<int>(), w.mpole.as<c_t<T>>(),
+                                       w.local.as<c_t<T>>());
+      eb_count_launch(ctx);
+    }
     ps.done();
   }
-  for (int l = 3; l <= L; ++l) {
-    int nb = t.lev_off[l + 1] - t.lev_off[l];
-    size_t sm = sizeof(c_t<T>) * 4 * E * (p + 1);
-    k_l2l<T, E><<<nblk((long long)nb * 32, 128), 128, sm, st>>>(
-        t.lev_off[l], nb, t.bkey.as<unsigned long long>(), t.parent.as<int>(), p, tb.binom.as<T>(),
-        ldb, tb.epow.as<c_t<T>>(), tb.einv.as<c_t<T>>(), w.local.as<c_t<T>>());
+  // Downward pass: FP32 gathers every ancestor's expansion in one launch; FP64 shifts
+  // level by level.
+  if (L >= 3 && sizeof(T) == 4) {
+    size_t sm = sizeof(c_t<T>) * E * (p + 1);
+    k_downward<T, E><<<t.nleaf, round32(E * (p + 1)), sm, st>>>(offL, L, t.bkey.as<unsigned long long>(),
+                                                                t.parent.as<int>(), p, tb.binom.as<T>(),
+                                                                ldb, w.local.as<c_t<T>>());
     eb_count_launch(ctx);
+  } else {
+    for (int l = 3; l <= L; ++l) {
+      int nb = t.lev_off[l + 1] - t.lev_off[l];
+      size_t sm = sizeof(c_t<T>) * E * (p + 1);
+      k_l2l<T, E><<<nb, round32(E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
+                                                       t.parent.as<int>(), p, tb.binom.as<T>(), ldb,
+                                                       tb.epow.as<c_t<T>>(), tb.einv.as<c_t<T>>(),
+                                                       w.local.as<c_t<T>>());
+      eb_count_launch(ctx);
+    }
   }
   return EB_OK;
 }
@@ -685,19 +935,21 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   else EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
   double rleaf = t.W / (double)(1 << t.L);
   int offL = t.lev_off[t.L];
+  int blocks = nblk((long long)t.ngroup * 32, 128);
   ProfScope ps(ctx, 0, st);
   if (f64) {
-    k_leaf64<E><<<nblk((long long)t.nleaf * 32, 128), 128, 0, st>>>(
-        offL, t.nleaf, has_far, t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
-        t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(), t.zs.as<double2>(),
-        w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0, rleaf, tb.p,
-        (double)sign, w.local.as<double2>(), out);
+    k_leaf64<E><<<blocks, 128, 0, st>>>(
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
+        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
+        rleaf, tb.p, (double)sign, w.local.as<double2>(), out);
   } else {
-    k_leaf32<E><<<nblk((long long)t.nleaf * 32, 128), 128, 0, st>>>(
-        offL, t.nleaf, has_far, t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
-        t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(), t.zs.as<double2>(),
-        t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(), w.aa.as<float2>(),
-        w.qa.as<float2>(), t.x0, t.y0, rleaf, tb.p, (float)sign, w.local.as<float2>(), out);
+    k_leaf32<E><<<blocks, 128, 0, st>>>(
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
+        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.zs.as<double2>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+        w.aa.as<float2>(), w.qa.as<float2>(), t.x0, t.y0, rleaf, tb.p, (float)sign,
+        w.local.as<float2>(), out);
   }
   eb_count_launch(ctx);
   ps.done();

@@ -15,6 +15,7 @@
 #define EB_VMAX 27
 #define EB_UMAX 9
 #define EB_NCODE 49
+#define EB_GROUP 8
 
 // ---------------------------------------------------------------------------------
 // Device buffer that grows on demand (never shrinks) and frees itself.
@@ -54,6 +55,11 @@ struct EbTree {
   DevBuf vcount;   // int[nbox]
   DevBuf ulist;    // int[nleaf*EB_UMAX] (global box ids)
   DevBuf ucount;   // int[nleaf]
+  // near-field work items: groups of up to EB_GROUP targets of one leaf
+  int ngroup = 0;
+  DevBuf arrive;   // int[nbox]: children delivered in the upward pass (cleared per apply)
+  DevBuf gleaf;    // int[ngroup]: leaf index (0-based within the leaf level)
+  DevBuf gfirst;   // int[ngroup]: first sorted target of the group
   DevBuf flags, scan, hist, bbox, partial, cubtmp;
 };
 
@@ -110,7 +116,7 @@ struct eb_ctx {
   DevBuf fftbuf, fftbuf2;          // spectral scratch
 
   // GMRES workspace
-  DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ;
+  DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ, gTicket;
   std::vector<double> hH;
 };
 

@@ -11,8 +11,9 @@
 // (MAXL+1) x MAXL Hessenberg matrix, its Givens rotations (DHEQR, dheqr.f:82-176) and
 // the triangular solve (DHELS, dhels.f:77-96) are O(MAXL^2) and run on the host.
 //
-// Refined mode (FP32 inner operator): iterative refinement with FP64 residuals,
-//   r = b - A64 x;  solve A32 d = r to inner_tol with the same GMRES;  x += d,
+// Refined mode (FP32 inner operator): iterative refinement with FP64 residuals from
+// x = 0 (so r = b needs no apply),
+//   solve A32 d = r to inner_tol with the same GMRES;  x += d;  r = b - A64 x,
 // until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual.
 #include <cmath>
 #include <vector>
@@ -39,33 +40,51 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return r;
 }
 
-// part[blk * ncol + j] = partial sum over this block's rows of V[:, j] . w
-__global__ void k_vtw_partial(int n, int ncol, const double* __restrict__ V, size_t ldv,
-                              const double* __restrict__ w, double* __restrict__ part) {
-  __shared__ double red[32];
-  for (int j = 0; j < ncol; ++j) {
+// Sums part[blk * ncol + j] over the blocks into out[j] (one warp per column, fixed
+// order); run by the last block of a kernel to finish, which also resets the ticket.
+__device__ void finish_columns(int nb, int ncol, const double* part, double* out,
+                               unsigned int* ticket) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int j = w; j < ncol; j += nw) {
     double s = 0.0;
-    const double* v = V + (size_t)j * ldv;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-      s = fma(v[i], w[i], s);
-    s = block_sum(s, red);
-    if (threadIdx.x == 0) part[(size_t)blockIdx.x * ncol + j] = s;
+    for (int b = lane; b < nb; b += 32) s += __ldcg(part + (size_t)b * ncol + j);
+    s = warp_sum<double>(s);
+    if (lane == 0) out[j] = s;
   }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
-__global__ void k_partial_final(int nb, int ncol, const double* __restrict__ part,
-                                double* __restrict__ out) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= ncol) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += part[(size_t)b * ncol + j];
-  out[j] = s;
+// out[j] = V[:, j] . w for j < ncol. Each block takes a contiguous range of rows and
+// each of its warps a subset of the columns; partial sums per block go to `part` and
+// the last block to finish adds them in block order.
+__global__ void k_vtw(int n, int ncol, const double* __restrict__ V, size_t ldv,
+                      const double* __restrict__ w, double* __restrict__ part,
+                      double* __restrict__ out, unsigned int* __restrict__ ticket) {
+  const int rows = (n + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int j = wi; j < ncol; j += nw) {
+    const double* v = V + (size_t)j * ldv;
+    double s = 0.0;
+    for (int i = r0 + lane; i < r1; i += 32) s = fma(v[i], w[i], s);
+    s = warp_sum<double>(s);
+    if (lane == 0) part[(size_t)blockIdx.x * ncol + j] = s;
+  }
+  finish_columns(gridDim.x, ncol, part, out, ticket);
 }
 
-// w -= V[:, 0:ncol] h; if part != nullptr also partial sums of the new w^2.
+// w -= V[:, 0:ncol] h; if part != nullptr also ||w||^2 of the new w into *out.
 __global__ void k_gemv_sub(int n, int ncol, const double* __restrict__ V, size_t ldv,
                            const double* __restrict__ h, double* __restrict__ w,
-                           double* __restrict__ part) {
+                           double* __restrict__ part, double* __restrict__ out,
+                           unsigned int* __restrict__ ticket) {
   __shared__ double hs[128];
   __shared__ double red[32];
   for (int j = threadIdx.x; j < ncol; j += blockDim.x) hs[j] = h[j];
@@ -81,6 +100,7 @@ __global__ void k_gemv_sub(int n, int ncol, const double* __restrict__ V, size_t
   if (part) {
     sq = block_sum(sq, red);
     if (threadIdx.x == 0) part[blockIdx.x] = sq;
+    finish_columns(gridDim.x, 1, part, out, ticket);
   }
 }
 
@@ -97,9 +117,10 @@ __global__ void k_gemv_add(int n, int ncol, const double* __restrict__ V, size_t
   }
 }
 
-// out = a - out (residual), with partial sums of out^2.
+// out = a - out (residual), with ||out||^2 into *nrm2.
 __global__ void k_resid(int n, const double* __restrict__ a, double* __restrict__ out,
-                        double* __restrict__ part) {
+                        double* __restrict__ part, double* __restrict__ nrm2,
+                        unsigned int* __restrict__ ticket) {
   __shared__ double red[32];
   double sq = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -109,14 +130,11 @@ __global__ void k_resid(int n, const double* __restrict__ a, double* __restrict_
   }
   sq = block_sum(sq, red);
   if (threadIdx.x == 0) part[blockIdx.x] = sq;
+  finish_columns(gridDim.x, 1, part, nrm2, ticket);
 }
 
 __global__ void k_scale(int n, double s, double* __restrict__ v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] *= s;
-}
-
-__global__ void k_scale_copy(int n, double s, const double* __restrict__ a, double* __restrict__ v) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = s * a[i];
 }
 
 __global__ void k_axpy(int n, double s, const double* __restrict__ a, double* __restrict__ v) {
@@ -130,15 +148,14 @@ struct Gm {
   int n;
   int nb;  // reduction blocks
   cudaStream_t s;
+  unsigned int* ticket;  // last-block counter of the reduction kernels
 };
 
 // ||v||^2 into host
 int dev_sumsq(Gm& g, const double* v, double* out) {
   eb_ctx* ctx = g.ctx;
   double* part = ctx->gPart.as<double>();
-  k_vtw_partial<<<g.nb, RBS, 0, g.s>>>(g.n, 1, v, (size_t)g.n, v, part);
-  eb_count_launch(ctx);
-  k_partial_final<<<1, 32, 0, g.s>>>(g.nb, 1, part, ctx->gH.as<double>());
+  k_vtw<<<g.nb, RBS, 0, g.s>>>(g.n, 1, v, (size_t)g.n, v, part, ctx->gH.as<double>(), g.ticket);
   eb_count_launch(ctx);
   EB_CUDA_TRY(cudaMemcpyAsync(out, ctx->gH.p, sizeof(double), cudaMemcpyDeviceToHost, g.s));
   EB_CUDA_TRY(cudaStreamSynchronize(g.s));
@@ -218,15 +235,13 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
   } else {
     EB_TRY(op(ctx, x, V, prec));
     (*nmv)++;
-    k_resid<<<g.nb, RBS, 0, g.s>>>(n, b, V, part);
+    k_resid<<<g.nb, RBS, 0, g.s>>>(n, b, V, part, hdev, g.ticket);
     eb_count_launch(ctx);
   }
   double ss;
   if (x0_zero) {
     EB_TRY(dev_sumsq(g, V, &ss));
   } else {
-    k_partial_final<<<1, 32, 0, g.s>>>(g.nb, 1, part, hdev);
-    eb_count_launch(ctx);
     EB_CUDA_TRY(cudaMemcpyAsync(&ss, hdev, sizeof(double), cudaMemcpyDeviceToHost, g.s));
     EB_CUDA_TRY(cudaStreamSynchronize(g.s));
   }
@@ -247,15 +262,13 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     EB_TRY(op(ctx, V + (size_t)(ll - 1) * ldv, w, prec));
     (*nmv)++;
     // pass 1: h1 = V^T w; w -= V h1
-    k_vtw_partial<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part);
-    k_partial_final<<<nblk(ll, 128), 128, 0, g.s>>>(g.nb, ll, part, hdev);
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev, w, nullptr);
+    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part, hdev, g.ticket);
+    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev, w, nullptr, nullptr, nullptr);
     // pass 2: h2 = V^T w; w -= V h2 with ||w||^2
-    k_vtw_partial<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part);
-    k_partial_final<<<nblk(ll, 128), 128, 0, g.s>>>(g.nb, ll, part, hdev + (maxl + 2));
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev + (maxl + 2), w, part);
-    k_partial_final<<<1, 32, 0, g.s>>>(g.nb, 1, part, hdev + 2 * (maxl + 2));
-    ctx->launches += 7;
+    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part, hdev + (maxl + 2), g.ticket);
+    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev + (maxl + 2), w, part,
+                                      hdev + 2 * (maxl + 2), g.ticket);
+    ctx->launches += 4;
     EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
                                 cudaMemcpyDeviceToHost, g.s));
     EB_CUDA_TRY(cudaStreamSynchronize(g.s));
@@ -294,7 +307,7 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
 int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mode,
           eb_solve_info* info, int mem) {
   cudaStream_t s = ctx->stream;
-  Gm g{ctx, n, std::min(nblk(n, RBS), RMAXB), s};
+  Gm g{ctx, n, std::min(nblk(n, RBS), RMAXB), s, nullptr};
   const int maxl = ctx->opts.maxl;
   if (maxl > 126) {
     eb_set_last_error_msg("maxl above 126 is not supported");
@@ -302,6 +315,9 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
   }
   EB_TRY(ctx->gPart.ensure(sizeof(double) * (size_t)RMAXB * (maxl + 2)));
   EB_TRY(ctx->gH.ensure(sizeof(double) * 3 * (maxl + 2)));
+  EB_TRY(ctx->gTicket.ensure(sizeof(unsigned int)));
+  EB_CUDA_TRY(cudaMemsetAsync(ctx->gTicket.p, 0, sizeof(unsigned int), s));
+  g.ticket = ctx->gTicket.as<unsigned int>();
   EB_TRY(ctx->gR.ensure(sizeof(double) * n));
   EB_TRY(ctx->gX.ensure(sizeof(double) * n));
   double* b = ctx->gR.as<double>();
@@ -323,37 +339,43 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
     EB_TRY(ctx->gZ.ensure(sizeof(double) * n));
     double* r = ctx->gZ.as<double>();
     double* d = ctx->gD.as<double>();
+    // Refinement starts from x = 0, so the first residual is b itself and costs no
+    // FP64 apply; every step is one inner FP32 solve plus one FP64 residual.
     double bss;
     EB_TRY(dev_sumsq(g, b, &bss));
-    double bnrm = std::sqrt(bss);
+    double bnrm = std::sqrt(bss), rnrm = bnrm;
+    EB_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    EB_CUDA_TRY(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     inf.ierr = 1;
-    for (int outer = 1; outer <= ctx->opts.max_outer; ++outer) {
+    inf.err = bnrm > 0 ? 1.0 : 0.0;
+    if (!(bnrm > 0)) inf.ierr = 0;
+    for (int outer = 1; outer <= ctx->opts.max_outer && inf.ierr != 0; ++outer) {
       inf.outer = outer;
-      EB_TRY(op(ctx, x, r, EB_FP64));
-      inf.matvecs64++;
-      double* part = ctx->gPart.as<double>();
-      k_resid<<<g.nb, RBS, 0, s>>>(n, b, r, part);
-      k_partial_final<<<1, 32, 0, s>>>(g.nb, 1, part, ctx->gH.as<double>());
-      ctx->launches += 2;
-      double rss;
-      EB_CUDA_TRY(cudaMemcpyAsync(&rss, ctx->gH.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-      EB_CUDA_TRY(cudaStreamSynchronize(s));
-      inf.err = bnrm > 0 ? std::sqrt(rss) / bnrm : 0.0;
-      if (!std::isfinite(inf.err)) {
-        eb_set_last_error_msg("non-finite residual");
-        st = EB_ERR_NAN;
-        break;
-      }
-      if (inf.err <= ctx->opts.gmres_tol) { inf.ierr = 0; break; }
       int it = 0, ie = 0, nmv = 0;
       double e2 = 0;
       st = gmres_cycle(g, op, EB_FP32, r, d, true, ctx->opts.inner_tol, maxl, &it, &e2, &ie, &nmv,
-                       std::sqrt(rss));
+                       rnrm);
       inf.iters += it;
       inf.matvecs32 += nmv;
       if (st != EB_OK) break;
       k_axpy<<<g.nb, RBS, 0, s>>>(n, 1.0, d, x);
       eb_count_launch(ctx);
+      EB_TRY(op(ctx, x, r, EB_FP64));
+      inf.matvecs64++;
+      double* part = ctx->gPart.as<double>();
+      k_resid<<<g.nb, RBS, 0, s>>>(n, b, r, part, ctx->gH.as<double>(), g.ticket);
+      ctx->launches += 1;
+      double rss;
+      EB_CUDA_TRY(cudaMemcpyAsync(&rss, ctx->gH.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+      EB_CUDA_TRY(cudaStreamSynchronize(s));
+      rnrm = std::sqrt(rss);
+      inf.err = rnrm / bnrm;
+      if (!std::isfinite(inf.err)) {
+        eb_set_last_error_msg("non-finite residual");
+        st = EB_ERR_NAN;
+        break;
+      }
+      if (inf.err <= ctx->opts.gmres_tol) inf.ierr = 0;
     }
   }
   if (st == EB_OK) {

@@ -272,6 +272,25 @@ __global__ void k_pair_counts(int off, int nleaf, const int* __restrict__ pt0,
   }
 }
 
+__global__ void k_group_count(int off, int nleaf, const int* __restrict__ pt0,
+                              const int* __restrict__ pt1, int* __restrict__ cnt) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nleaf) return;
+  cnt[b] = (pt1[off + b] - pt0[off + b] + EB_GROUP - 1) / EB_GROUP;
+}
+
+__global__ void k_group_fill(int off, int nleaf, const int* __restrict__ pt0,
+                             const int* __restrict__ cnt, const int* __restrict__ start,
+                             int* __restrict__ gleaf, int* __restrict__ gfirst) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nleaf) return;
+  int g0 = start[b];
+  for (int g = 0; g < cnt[b]; ++g) {
+    gleaf[g0 + g] = b;
+    gfirst[g0 + g] = pt0[off + b] + g * EB_GROUP;
+  }
+}
+
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -434,7 +453,27 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   k_ulist<<<nblk(t.nleaf, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[L], t.nleaf, L,
                                              t.ulist.as<int>(), t.ucount.as<int>());
   eb_count_launch(ctx);
-  // 8. pair counts (the algorithmic work of the near field and M2L)
+  // 8. near-field work items: groups of EB_GROUP targets
+  {
+    int nl = t.nleaf;
+    k_group_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                               t.flags.as<int>());
+    eb_count_launch(ctx);
+    tb = t.cubtmp.bytes;
+    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
+    eb_count_launch(ctx);
+    int last[2];
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaStreamSynchronize(st));
+    t.ngroup = last[0] + last[1];
+    EB_TRY(t.gleaf.ensure(sizeof(int) * (size_t)t.ngroup));
+    EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
+    k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
+                                              t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
+    eb_count_launch(ctx);
+  }
+  // 9. pair counts (the algorithmic work of the near field and M2L)
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(t.partial.p);
   EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
   int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
