@@ -55,6 +55,21 @@ class TreeInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Model(ctypes.Structure):
+    _fields_ = [("cap", ctypes.c_double), ("e0", ctypes.c_double),
+                ("zbond", ctypes.c_double * 2), ("mode", ctypes.c_int)]
+
+
+class StageInfo(ctypes.Structure):
+    _fields_ = [("lap_iters", ctypes.c_int), ("stokes_iters", ctypes.c_int),
+                ("lap_err", ctypes.c_double), ("stokes_err", ctypes.c_double),
+                ("flux", ctypes.c_double), ("lap_ierr", ctypes.c_int),
+                ("stokes_ierr", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -88,6 +103,10 @@ SIGNATURES = {
     "eb_pvintev": (_I, [_P, _P, _P, _I, _I]),
     "eb_dirich_neu_map": (_I, [_P, _P, _P, _P, _P, _I, _I]),
     "eb_interface_velocity": (_I, [_P, _P, _P, _D, _P, _P, _I, _I]),
+    "eb_setvelf": (_I, [_P, _P, _D, _D, _P, _I]),
+    "eb_rk_f": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo), _I]),
+    "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
+                         _I]),
     "eb_set_default_ctx": (_I, [_P]),
     "matvec_": (None, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "matvec_lapl_": (None, [_P, _P, _P, _P, _P, _P, _P, _P]),

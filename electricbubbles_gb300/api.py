@@ -13,6 +13,8 @@ same operations under the reference's names:
     pvintev, dirich_neu_map    PV integral, DtN map     (pv_integral.f:53-204, laplace.f:266-331)
     interfacenew               interface velocity       (electric.f:791-912)
     extractdat                 geometry from the RK state (electric.f:636-716)
+    setvelf                    Stokes right-hand side   (stokesbubb.f:4-135)
+    f / rk2                    RK right-hand side and step (electric.f:968-1109, 762-786)
 
 Arrays may be numpy arrays (host memory; copied in and out) or CUDA tensors exposing
 `data_ptr()` and `is_cuda` (device memory; used in place). Errors raise `EbError`,
@@ -25,7 +27,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (EB_DEVICE, EB_FP32, EB_FP64, EB_HOST, EB_SOLVE_FP32_REFINED, EB_SOLVE_FP64,
-                   EbError, Opts, SolveInfo, TreeInfo, check)
+                   EbError, Model, Opts, SolveInfo, StageInfo, TreeInfo, check)
 
 PRECISION = {"fp64": EB_FP64, "fp32": EB_FP32}
 SOLVE_MODE = {"fp64": EB_SOLVE_FP64, "fp32_refined": EB_SOLVE_FP32_REFINED}
@@ -290,6 +292,61 @@ class Context:
             self._h, _ptr(u), _ptr(zc), float(cap), _ptr(un), ctypes.byref(flux),
             PRECISION[precision], EB_HOST))
         return un, flux.value
+
+    def setvelf(self, dphi_dn, cap=0.0, e0=0.0):
+        """SETVELF (free space): the Stokes right-hand side, 2 nbk reals."""
+        d = _host(dphi_dn, np.float64)
+        rhs = np.empty(2 * self.nbk)
+        check("eb_setvelf", self._lib.eb_setvelf(self._h, _ptr(d), float(cap), float(e0),
+                                                 _ptr(rhs), EB_HOST))
+        return rhs
+
+    # ---- RK stage ------------------------------------------------------------
+    @staticmethod
+    def _model(cap, e0, zbond, mode):
+        m = Model()
+        m.cap = float(cap)
+        m.e0 = float(e0)
+        m.zbond[0] = float(np.real(zbond))
+        m.zbond[1] = float(np.imag(zbond))
+        m.mode = SOLVE_MODE[mode]
+        return m
+
+    def _set_drops(self, nd):
+        self.k = int(nd.shape[0])
+        self.nbk = int(nd.sum())
+        self.nd = nd
+
+    def f(self, nd, rku, cap=0.0, e0=0.0, zbond=0.0, mode="fp64", out=None):
+        """F: the node velocities rkup of the RK state rku (both interleaved x, y, length
+        2 nbk). Returns (rkup, info); installs the geometry of rku."""
+        nd = _host(nd, np.int32)
+        if not _is_device(rku):
+            rku = _host(rku, np.float64)
+        rkup = out if out is not None else self._out(rku, 2 * int(nd.sum()), np.float64)
+        info = StageInfo()
+        m = self._model(cap, e0, zbond, mode)
+        check("eb_rk_f", self._lib.eb_rk_f(self._h, int(nd.shape[0]), _ptr(nd), _ptr(rku),
+                                           _ptr(rkup), ctypes.byref(m), ctypes.byref(info),
+                                           _mem(rku, rkup)))
+        self._set_drops(nd)
+        return rkup, info.as_dict()
+
+    def rk2(self, nd, dt, ybar, cap=0.0, e0=0.0, zbond=0.0, mode="fp64"):
+        """RK2: one modified-Euler step of size dt; ybar (float64 numpy array or CUDA
+        tensor, length 2 nbk) is updated in place. Returns the stage diagnostics."""
+        nd = _host(nd, np.int32)
+        if not _is_device(ybar):
+            if not (isinstance(ybar, np.ndarray) and ybar.dtype == np.float64
+                    and ybar.flags["C_CONTIGUOUS"]):
+                raise TypeError("ybar must be a C-contiguous float64 array (updated in place)")
+        info = StageInfo()
+        m = self._model(cap, e0, zbond, mode)
+        check("eb_rk2_step", self._lib.eb_rk2_step(self._h, int(nd.shape[0]), _ptr(nd),
+                                                   float(dt), _ptr(ybar), ctypes.byref(m),
+                                                   ctypes.byref(info), _mem(ybar)))
+        self._set_drops(nd)
+        return info.as_dict()
 
 
 def geometry_from_extract(ctx, cfg):

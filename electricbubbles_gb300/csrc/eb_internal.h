@@ -114,6 +114,12 @@ struct eb_ctx {
   DevBuf stress;                   // double2[nbk]
   DevBuf pvz, pvq, pvout;          // PVINTEV fine grid
   DevBuf fftbuf, fftbuf2;          // spectral scratch
+  DevBuf ex_zk, ex_dz, ex_ds, ex_ka, ex_area;  // EXTRACTDAT outputs before install
+
+  // RK stage F and the RK2 step
+  DevBuf st_lap;                   // double[5*nbk]: Laplace rhs/Un, density, phi, psi, dphi/dn
+  DevBuf st_rhs, st_u, st_zc;      // Stokes rhs and density (double2[nbk]), C_k (double2[k])
+  DevBuf rk_y, rk_y1, rk_d0, rk_phi;  // RK state, predictor, derivative, dt * F(y)
 
   // GMRES workspace
   DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ, gTicket;

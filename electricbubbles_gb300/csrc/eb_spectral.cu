@@ -384,8 +384,12 @@ int eb_extractdat(eb_ctx* ctx, int k, const int* nd, const double* rku, double* 
   EB_TRY(ctx->fftbuf.ensure(sizeof(double2) * nbk));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->fftbuf.p, rku, sizeof(double2) * nbk,
                               mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-  // geometry buffers of the context receive the results
-  DevBuf zk_d, dz_d, ds_d, ka_d, area_d;
+  // staging buffers of the context receive the results before the install copies them
+  DevBuf& zk_d = ctx->ex_zk;
+  DevBuf& dz_d = ctx->ex_dz;
+  DevBuf& ds_d = ctx->ex_ds;
+  DevBuf& ka_d = ctx->ex_ka;
+  DevBuf& area_d = ctx->ex_area;
   EB_TRY(zk_d.ensure(sizeof(double2) * k));
   EB_TRY(dz_d.ensure(sizeof(double2) * nbk));
   EB_TRY(ds_d.ensure(sizeof(double) * nbk));
@@ -544,5 +548,302 @@ int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double
   EB_CUDA_TRY(cudaMemcpyAsync(&fl, ctx->redpart.as<double>() + 2047, sizeof(double), cudaMemcpyDeviceToHost, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   if (flux) *flux = fl;
+  return EB_OK;
+}
+
+// =================================================================================
+// One RK stage F (electric.f:968-1109) and the RK2 step (electric.f:762-786), free
+// space (zbond = 0), with everything resident on the GPU.
+// =================================================================================
+namespace {
+
+// Antiderivative in Fourier space (FOURINT, electric.f:1307-1331): c_k -> c_k/(i k),
+// mean and Nyquist dropped.
+__device__ void spectral_int(double2* a, int n) {
+  for (int m = threadIdx.x; m < n; m += blockDim.x) {
+    if (m == 0 || m == n / 2) {
+      a[m] = make_double2(0.0, 0.0);
+    } else {
+      double k = (double)((m <= n / 2) ? m : m - n);
+      double2 c = a[m];
+      a[m] = make_double2(c.y / k, -c.x / k);  // c / (i k)
+    }
+  }
+  __syncthreads();
+}
+
+// SETVELF (stokesbubb.f:4-135) for zbond = 0: surface tension -dz/(2|dz|), the far
+// field -conj(psi) with psi = -i cap z/2, and the electric stress i E0/4 times the
+// antiderivative of dz (dphi/dn)^2 (:110-128). As in the reference, the electric term
+// uses the `alpha` left from the previous loops, 2 pi (nd_k - 1)/nd_k of the last drop.
+__global__ void k_setvelf(const int* __restrict__ start, const double2* __restrict__ z,
+                          const double2* __restrict__ dz, const double* __restrict__ dsda,
+                          const double* __restrict__ dphi, double cap, double e0,
+                          double alpha_stale, double2* __restrict__ rhs, int nmax) {
+  extern __shared__ double2 sm[];
+  __shared__ double2 s_c0, s_f0;
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0;
+  double2* a = sm;
+  double2* tw = sm + nmax;
+  make_twiddles(tw, n);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double d = dphi[i0 + i];
+    a[i] = make_double2(dz[i0 + i].x * d * d, dz[i0 + i].y * d * d);
+  }
+  smem_fft(a, n, tw, n, -1);
+  double inv = 1.0 / (double)n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(a[i].x * inv, a[i].y * inv);
+  __syncthreads();
+  if (threadIdx.x == 0) s_c0 = a[0];
+  __syncthreads();
+  spectral_int(a, n);
+  smem_fft(a, n, tw, n, +1);
+  if (threadIdx.x == 0) s_f0 = a[0];
+  __syncthreads();
+  const double2 c0 = s_c0, f0 = s_f0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int t = i0 + i;
+    double s = dsda[t];
+    double2 r = make_double2(-0.5 * dz[t].x / s, -0.5 * dz[t].y / s);
+    // - zstr, zstr = -conj(-i cap z/2) = -i cap conj(z)/2
+    r.x += 0.5 * cap * z[t].y;
+    r.y += 0.5 * cap * z[t].x;
+    double2 zs = make_double2(alpha_stale * c0.x + a[i].x - f0.x, alpha_stale * c0.y + a[i].y - f0.y);
+    r.x += -0.25 * e0 * zs.y;  // (i E0/4) zs
+    r.y += 0.25 * e0 * zs.x;
+    rhs[t] = r;
+  }
+}
+
+int setvelf_dev(eb_ctx* ctx, const double* dphi, double cap, double e0, double2* rhs) {
+  int nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  const int nlast = ctx->nd_host[ctx->k - 1];
+  const double alpha_stale = 2.0 * EB_PI * (double)(nlast - 1) / (double)nlast;
+  size_t sm = sizeof(double2) * ((size_t)nmax + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_setvelf, sm));
+  k_setvelf<<<ctx->k, SBS, sm, ctx->stream>>>(ctx->start.as<int>(), ctx->z.as<double2>(),
+                                              ctx->dz.as<double2>(), ctx->dsda.as<double>(), dphi,
+                                              cap, e0, alpha_stale, rhs, nmax);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "setvelf");
+}
+
+__device__ __forceinline__ double powi25(double x) {
+  double r = 1.0;
+  int e = 25;
+  while (e > 0) {
+    if (e & 1) r *= x;
+    x *= x;
+    e >>= 1;
+  }
+  return r;
+}
+
+// EQUIT (electric.f:1270-1302), then the velocity of the nodes
+// (-Un i dz - T dz)/|dz|, Fourier filtered (FILTER, electric.f:1152-1187, with k/n
+// formed in single precision as the reference does) and transformed back
+// (electric.f:1076-1103).
+__global__ void k_equit_rkup(const int* __restrict__ start, const double* __restrict__ tha,
+                             const double* __restrict__ un, const double2* __restrict__ dz,
+                             const double* __restrict__ dsda, double2* __restrict__ rkup, int nmax) {
+  extern __shared__ double2 sm[];
+  __shared__ double2 s_c0;
+  int b = blockIdx.x;
+  int i0 = start[b], n = start[b + 1] - i0;
+  double2* a = sm;
+  double2* c = sm + nmax;
+  double2* tw = c + nmax;
+  make_twiddles(tw, n);
+  const double inv = 1.0 / (double)n, dal = 2.0 * EB_PI / (double)n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(-tha[i0 + i] * un[i0 + i], 0.0);
+  smem_fft(a, n, tw, n, -1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(a[i].x * inv, a[i].y * inv);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a[n / 2] = make_double2(0.0, 0.0);
+    s_c0 = a[0];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) c[i] = a[i];
+  __syncthreads();
+  spectral_int(c, n);
+  smem_fft(c, n, tw, n, +1);
+  const double2 zf0 = s_c0;
+  const double dadt = zf0.x;
+  // node velocity samples (reuse a)
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int t = i0 + i;
+    double alpha = dal * (double)i;
+    double T = -(zf0.x * alpha + c[i].x) + alpha * dadt;
+    double u = un[t], s = dsda[t];
+    double2 d = dz[t];
+    a[i] = make_double2((u * d.y - T * d.x) / s, (-u * d.x - T * d.y) / s);
+  }
+  smem_fft(a, n, tw, n, -1);
+  const int h = n / 2;
+  for (int m = threadIdx.x; m < n; m += blockDim.x) {
+    double2 v = make_double2(a[m].x * inv, a[m].y * inv);
+    int i = (m <= h) ? m : n - m;
+    double ratio = (double)__fdiv_rn((float)i, (float)h);
+    double f = exp(-10.0 * powi25(ratio));
+    v = make_double2(f * v.x, f * v.y);
+    if (fabs(v.x) < 1e-13) v.x = 0.0;
+    if (fabs(v.y) < 1e-13) v.y = 0.0;
+    if (m == h) v = make_double2(0.0, 0.0);
+    a[m] = v;
+  }
+  smem_fft(a, n, tw, n, +1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) rkup[i0 + i] = a[i];
+}
+
+__global__ void k_lap_bc(int nbk, const double2* __restrict__ z, double* __restrict__ rhs) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nbk) rhs[i] = -2.0 * z[i].x;  // GETBCs, laplace.f:14-18
+}
+
+__global__ void k_rk_first(int n, double dt, const double* __restrict__ y, const double* __restrict__ d,
+                           double* __restrict__ phi0, double* __restrict__ y1) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double p = dt * d[i];
+  phi0[i] = p;
+  y1[i] = y[i] + p;
+}
+
+__global__ void k_rk_second(int n, double dt, const double* __restrict__ phi0,
+                            const double* __restrict__ d, double* __restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  y[i] = y[i] + 0.5 * phi0[i] + 0.5 * (dt * d[i]);
+}
+
+int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
+            eb_stage_info* info) {
+  EB_TRY(eb_extractdat(ctx, k, nd, rku, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       EB_DEVICE));
+  int nbk = ctx->nbk, nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->st_lap.ensure(sizeof(double) * 5 * (size_t)nbk));
+  EB_TRY(ctx->st_rhs.ensure(sizeof(double2) * (size_t)nbk));
+  EB_TRY(ctx->st_u.ensure(sizeof(double2) * (size_t)nbk));
+  EB_TRY(ctx->st_zc.ensure(sizeof(double2) * (size_t)k));
+  double* rl = ctx->st_lap.as<double>();
+  double* ul = rl + nbk;
+  double* phi = ul + nbk;
+  double* psi = phi + nbk;
+  double* dphi = psi + nbk;
+  eb_solve_info li{}, si{};
+  k_lap_bc<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->z.as<double2>(), rl);
+  eb_count_launch(ctx);
+  EB_TRY(eb_laplace_solve(ctx, nbk, rl, ul, m->mode, &li, EB_DEVICE));
+  EB_TRY(eb_dirich_neu_map(ctx, ul, phi, psi, dphi, EB_FP64, EB_DEVICE));
+  EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, ctx->st_rhs.as<double2>()));
+  EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
+                         EB_DEVICE));
+  EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
+  double* un = rl;  // the Laplace right-hand side is no longer needed
+  double flux = 0.0;
+  EB_TRY(eb_interface_velocity(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, &flux,
+                               EB_FP64, EB_DEVICE));
+  size_t sm2 = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_equit_rkup, sm2));
+  k_equit_rkup<<<k, SBS, sm2, s>>>(ctx->start.as<int>(), ctx->tha.as<double>(), un, ctx->dz.as<double2>(),
+                                   ctx->dsda.as<double>(), reinterpret_cast<double2*>(rkup), nmax);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "stage F"));
+  if (info) {
+    info->lap_iters += li.iters;
+    info->stokes_iters += si.iters;
+    info->lap_err = li.err;
+    info->stokes_err = si.err;
+    info->flux = flux;
+    info->lap_ierr = li.ierr;
+    info->stokes_ierr = si.ierr;
+  }
+  return EB_OK;
+}
+
+int check_model(const eb_model* m) {
+  if (!m) return EB_ERR_ARG;
+  if (m->zbond[0] != 0.0 || m->zbond[1] != 0.0) {
+    eb_set_last_error_msg("wall-bounded flow (zbond != 0) is not supported");
+    return EB_ERR_ARG;
+  }
+  if (m->mode != EB_SOLVE_FP64 && m->mode != EB_SOLVE_FP32_REFINED) return EB_ERR_ARG;
+  return EB_OK;
+}
+
+}  // namespace
+
+int eb_setvelf(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, double* rhs, int mem) {
+  if (!ctx || !dphi_dn || !rhs) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  cudaSetDevice(ctx->device);
+  if (mem == EB_DEVICE)
+    return setvelf_dev(ctx, dphi_dn, cap, e0, reinterpret_cast<double2*>(rhs));
+  int nbk = ctx->nbk;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->vin.ensure(sizeof(double) * (size_t)nbk));
+  EB_TRY(ctx->vout.ensure(sizeof(double2) * (size_t)nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, dphi_dn, sizeof(double) * nbk, cudaMemcpyHostToDevice, s));
+  EB_TRY(setvelf_dev(ctx, ctx->vin.as<double>(), cap, e0, ctx->vout.as<double2>()));
+  EB_CUDA_TRY(cudaMemcpyAsync(rhs, ctx->vout.p, sizeof(double2) * nbk, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* model,
+            eb_stage_info* info, int mem) {
+  if (!ctx || k <= 0 || !nd || !rku || !rkup) return EB_ERR_ARG;
+  EB_TRY(check_model(model));
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = 0;
+  for (int b = 0; b < k; ++b) nbk += nd[b];
+  cudaStream_t s = ctx->stream;
+  if (info) *info = eb_stage_info{};
+  if (mem == EB_DEVICE) return stage_f(ctx, k, nd, rku, rkup, model, info);
+  EB_TRY(ctx->rk_y.ensure(sizeof(double) * 2 * (size_t)nbk));
+  EB_TRY(ctx->rk_d0.ensure(sizeof(double) * 2 * (size_t)nbk));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->rk_y.p, rku, sizeof(double) * 2 * nbk, cudaMemcpyHostToDevice, s));
+  EB_TRY(stage_f(ctx, k, nd, ctx->rk_y.as<double>(), ctx->rk_d0.as<double>(), model, info));
+  EB_CUDA_TRY(cudaMemcpyAsync(rkup, ctx->rk_d0.p, sizeof(double) * 2 * nbk, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar, const eb_model* model,
+                eb_stage_info* info, int mem) {
+  if (!ctx || k <= 0 || !nd || !ybar) return EB_ERR_ARG;
+  EB_TRY(check_model(model));
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int nbk = 0;
+  for (int b = 0; b < k; ++b) nbk += nd[b];
+  const int neq = 2 * nbk;
+  cudaStream_t s = ctx->stream;
+  if (info) *info = eb_stage_info{};
+  EB_TRY(ctx->rk_y.ensure(sizeof(double) * (size_t)neq));
+  EB_TRY(ctx->rk_y1.ensure(sizeof(double) * (size_t)neq));
+  EB_TRY(ctx->rk_d0.ensure(sizeof(double) * (size_t)neq));
+  EB_TRY(ctx->rk_phi.ensure(sizeof(double) * (size_t)neq));
+  double* y = ctx->rk_y.as<double>();
+  EB_CUDA_TRY(cudaMemcpyAsync(y, ybar, sizeof(double) * neq,
+                              mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+  EB_TRY(stage_f(ctx, k, nd, y, ctx->rk_d0.as<double>(), model, info));
+  k_rk_first<<<nblk(neq, 256), 256, 0, s>>>(neq, dt, y, ctx->rk_d0.as<double>(), ctx->rk_phi.as<double>(),
+                                            ctx->rk_y1.as<double>());
+  eb_count_launch(ctx);
+  EB_TRY(stage_f(ctx, k, nd, ctx->rk_y1.as<double>(), ctx->rk_d0.as<double>(), model, info));
+  k_rk_second<<<nblk(neq, 256), 256, 0, s>>>(neq, dt, ctx->rk_phi.as<double>(), ctx->rk_d0.as<double>(), y);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "rk2 step"));
+  EB_CUDA_TRY(cudaMemcpyAsync(ybar, y, sizeof(double) * neq,
+                              mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
   return EB_OK;
 }

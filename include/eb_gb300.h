@@ -86,6 +86,29 @@ typedef struct eb_tree_info {
   int p;            /* expansion order of the last apply                      */
 } eb_tree_info;
 
+/* Physical parameters of the RK right-hand side F (electric.f:968-1109), the values the
+ * reference keeps in COMMON: cap (strain rate of the far field psi = -i cap z / 2,
+ * stokesbubb.f:64-68), e0 (electric field strength, the E0 of the electric stress,
+ * stokesbubb.f:110-128) and zbond (complex Bond number; only 0, free space, is
+ * supported). mode selects the solver of both GMRES solves. */
+typedef struct eb_model {
+  double cap;
+  double e0;
+  double zbond[2];
+  int mode;         /* eb_solve_mode */
+} eb_model;
+
+/* Diagnostics of eb_rk_f / eb_rk2_step (summed over the stages of a step). */
+typedef struct eb_stage_info {
+  int lap_iters;    /* Krylov iterations of the Laplace solves (SOLVE_LAPL)   */
+  int stokes_iters; /* Krylov iterations of the Stokes solves (SOLVEI)        */
+  double lap_err;   /* last Laplace relative residual                         */
+  double stokes_err;/* last Stokes relative residual                          */
+  double flux;      /* FLUX of the last stage (electric.f:848-882)            */
+  int lap_ierr;     /* DGMRES IERR of the last Laplace solve                  */
+  int stokes_ierr;  /* DGMRES IERR of the last Stokes solve                   */
+} eb_stage_info;
+
 typedef struct eb_ctx eb_ctx;
 
 int eb_version(void);
@@ -186,6 +209,28 @@ int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi,
  * interface normal velocity un and the FLUX diagnostic. zc: per-drop C_k (complex). */
 int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap,
                           double* un, double* flux, int precision, int mem);
+
+/* SETVELF (stokesbubb.f:4-135), free space: the right-hand side of the Stokes solve
+ * (rhs, 2 nbk doubles, interleaved) from dphi_dn (nbk) on the installed geometry:
+ * surface tension, the far field of strain rate cap and the electric stress of
+ * strength e0. As in the reference, the electric term's `alpha` is the value left by
+ * the previous loop, 2 pi (nd_k - 1) / nd_k of the last drop (stokesbubb.f:125). */
+int eb_setvelf(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, double* rhs,
+               int mem);
+
+/* F (electric.f:968-1109), free space: the RK right-hand side of the interface
+ * positions. rku (interleaved x, y of all nodes, 2 nbk doubles) -> rkup (the node
+ * velocities, same layout): EXTRACTDAT, Laplace solve, DIRICH_NEU_MAP, SETVELF, Stokes
+ * solve, INTERFACENEW, EQUIT and the filtered node velocity, all on the GPU. Installs
+ * the geometry of rku in the context. */
+int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup,
+            const eb_model* model, eb_stage_info* info, int mem);
+
+/* RK2 (electric.f:762-786): one modified-Euler step of size dt on ybar (2 nbk
+ * doubles, updated in place). Both stages run on the GPU; with mem = EB_DEVICE the
+ * state never leaves device memory. */
+int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar,
+                const eb_model* model, eb_stage_info* info, int mem);
 
 /* gfortran-callable shims with the exact DGMRES MATVEC signature
  * (dpigmr.f:316-318, stokesbubb.f:419, laplace.f:429). They use the context set with
