@@ -166,6 +166,7 @@ def run_reference(args, rank, world):
 def run_gpu(args, rank, world, local):
     import numpy as np
     import torch
+    from electricbubbles_gb300 import configs
     from electricbubbles_gb300.api import Context
 
     dist = world > 1
@@ -295,6 +296,55 @@ def run_gpu(args, rank, world, local):
     h2d = 8 * (zh.numel() + dzh.numel() + dsh.numel() + kah.numel() + zkh.numel() + rhh.numel()) + 4 * cfg.k
     d2h = 8 * xh.numel()
 
+    # RK2 steps (F twice: EXTRACTDAT, Laplace solve, DtN, SETVELF, Stokes solve,
+    # INTERFACENEW, EQUIT/FILTER) with the state resident on the GPU
+    def rk_rate(c, mode, steps, e0=0.5):
+        y0 = torch.from_numpy(c.rku()).to(dev)
+        y = y0.clone()
+        ctx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
+        torch.cuda.synchronize()
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record(stream)
+        for _ in range(steps):
+            info = ctx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
+        e1_.record(stream)
+        torch.cuda.synchronize()
+        return steps / (e0_.elapsed_time(e1_) * 1e-3), info
+
+    rk = {}
+    for mode in ("fp64", "fp32_refined"):
+        r, info = rk_rate(cfg, mode, 3)
+        rk[WORKLOAD + "/" + mode] = {"steps_per_s": r, "last_step": info}
+    single = configs.single_drop(256)
+    r, info = rk_rate(single, "fp64", 20)
+    rk["single_drop_n256/fp64"] = {"steps_per_s": r, "last_step": info}
+
+    # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
+    big = configs.large_drops()
+    gb = ctx.extractdat(big.nd, big.rku())
+    ub = torch.randn(2 * big.nbk, dtype=torch.float64, device=dev)
+    yb = torch.empty_like(ub)
+    large = {"workload": "large_drops_1024x1024", "nodes": big.nbk, "tree": ctx.tree_info()}
+    ea, eb_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for prec in ("fp64", "fp32"):
+        ctx.fasmvp(ub, prec, out=yb)
+        torch.cuda.synchronize()
+        ea.record(stream)
+        for _ in range(3):
+            ctx.fasmvp(ub, prec, out=yb)
+        eb_.record(stream)
+        torch.cuda.synchronize()
+        large["fmm_mpts_per_s_" + prec] = big.nbk / (ea.elapsed_time(eb_) / 3 * 1e-3) / 1e6
+    rb = torch.from_numpy(surface_tension_rhs(gb["dz"], gb["dsda"])).to(dev)
+    xb = torch.empty_like(rb)
+    for mode in ("fp64", "fp32_refined"):
+        ea.record(stream)
+        _, info = ctx.solvei(rb, mode, out=xb)
+        eb_.record(stream)
+        torch.cuda.synchronize()
+        large["solve_ms_" + mode] = ea.elapsed_time(eb_)
+        large["solve_info_" + mode] = info
+
     cpu = None
     if rank == 0:
         ncores = os.cpu_count() or 1
@@ -339,6 +389,8 @@ def run_gpu(args, rank, world, local):
                 "includes": "eb_set_geometry (copy + tree build) and eb_stokes_solve from pinned host buffers"},
         "clocks": clk,
         "gpu_launches": launches,
+        "rk2": rk,
+        "large": large,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

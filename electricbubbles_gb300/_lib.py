@@ -35,12 +35,13 @@ class Opts(ctypes.Structure):
                 ("leaf32", ctypes.c_int), ("tol64", ctypes.c_double), ("tol32", ctypes.c_double),
                 ("maxl", ctypes.c_int), ("gmres_tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("graphs", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int), ("outer", ctypes.c_int), ("matvecs64", ctypes.c_int),
-                ("matvecs32", ctypes.c_int), ("err", ctypes.c_double), ("ierr", ctypes.c_int)]
+                ("matvecs32", ctypes.c_int), ("err", ctypes.c_double), ("ierr", ctypes.c_int),
+                ("graph", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -203,6 +203,7 @@ void eb_opts_default(eb_opts* o) {
   o->inner_tol = 1e-5;
   o->max_outer = 8;
   o->device = 0;
+  o->graphs = 1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -230,6 +231,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.gmres_tol <= 0) o.gmres_tol = d.gmres_tol;
     if (o.inner_tol <= 0) o.inner_tol = d.inner_tol;
     if (o.max_outer <= 0) o.max_outer = d.max_outer;
+    if (o.graphs == 0) o.graphs = d.graphs;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {
@@ -240,6 +242,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   c->device = c->opts.device;
   e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e != cudaSuccess) {
@@ -263,8 +266,11 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (GmGraph& g : ctx->gcache) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   delete ctx;
+  eb_devbuf_collect();
   return EB_OK;
 }
 
@@ -350,6 +356,8 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
   ctx->tree_pv.valid = false;
   ctx->geom_valid = true;
+  ctx->geom_version++;
+  eb_devbuf_collect();
   return EB_OK;
 }
 

@@ -479,27 +479,31 @@ __global__ void k_upward(int offL, int L, const unsigned long long* __restrict__
     if (!s_last) return;
     __threadfence();
     cur = parent[cur];
-    // M2M into box `cur` from its children
+    // M2M into box `cur`: all children's shifted coefficients are staged in one round
+    // of loads, then each output sums over the children in their fixed order.
     c_t<T>* a = smem;
-    c_t<T> acc = cmk<T>(0, 0);
-    int c0 = child0[cur], nc = nchild[cur];
-    for (int ci = 0; ci < nc; ++ci) {
+    const int c0 = child0[cur], nc = nchild[cur];
+    for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
+      int ci = idx / nout, o = idx - ci * nout;
       int c = c0 + ci;
       int q = quadrant(bkey[c]);
-      c_t<T> ec = cscale<T>(epow2[q * ld + 1], (T)2);
-      const c_t<T>* mc = mpole + (size_t)c * E * p;
-      __syncthreads();
-      for (int idx = tid; idx < nout; idx += blockDim.x) {
-        int e2 = idx / p, kk = idx - e2 * p, k = kk + 1;
-        c_t<T> v = ldcg_c<T>(mc + idx);
-        if (e2 == 1 && k >= 2) cfma<T>(v, cscale<T>(cconj<T>(ec), (T)(k - 1)), ldcg_c<T>(mc + kk - 1));
-        a[idx] = cmul<T>(v, einv[q * ld + k]);
+      int e2 = o / p, kk = o - e2 * p, k = kk + 1;
+      const c_t<T>* mc = mpole + (size_t)c * nout;
+      c_t<T> v = ldcg_c<T>(mc + o);
+      if (e2 == 1 && k >= 2) {
+        c_t<T> ec = cscale<T>(epow2[q * ld + 1], (T)2);
+        cfma<T>(v, cscale<T>(cconj<T>(ec), (T)(k - 1)), ldcg_c<T>(mc + kk - 1));
       }
-      __syncthreads();
-      if (tid < nout) {
-        int n = nn + 1;
-        const T* brow = binom + (size_t)(n - 1) * ldb;
-        const c_t<T>* ae = a + e * p;
+      a[idx] = cmul<T>(v, einv[q * ld + k]);
+    }
+    __syncthreads();
+    if (tid < nout) {
+      const int n = nn + 1;
+      const T* brow = binom + (size_t)(n - 1) * ldb;
+      c_t<T> acc = cmk<T>(0, 0);
+      for (int ci = 0; ci < nc; ++ci) {
+        const int q = quadrant(bkey[c0 + ci]);
+        const c_t<T>* ae = a + ci * nout + e * p;
         c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
         int k = 0;
         for (; k + 1 < n; k += 2) {
@@ -509,63 +513,8 @@ __global__ void k_upward(int offL, int L, const unsigned long long* __restrict__
         if (k < n) crfma<T>(s0, brow[k], ae[k]);
         cfma<T>(acc, epow2[q * ld + n], cadd<T>(s0, s1));
       }
+      mpole[(size_t)cur * nout + tid] = acc;
     }
-    if (tid < nout) mpole[(size_t)cur * E * p + tid] = acc;
-  }
-}
-
-// ---------------------------------------------------------------------------------
-// Downward pass in one launch: one block per leaf adds to its own M2L expansion the
-// M2L expansion of every ancestor (levels L-1 .. 2) shifted directly to the leaf centre
-// (a polynomial shift is exact, so this equals the level-by-level L2L chain). For an
-// ancestor of side r_a, with d = (c_leaf - c_a)/r_leaf and g = d r_leaf/r_a:
-//   a_m = g^m L_m,  L_leaf[j] += d^-j sum_{m>=j} C(m, j) a_m,
-// after moving psi to the leaf centre: psi_m += conj(g) (m+1) phi_{m+1}.
-// ---------------------------------------------------------------------------------
-template <typename T, int E>
-__global__ void k_downward(int offL, int L, const unsigned long long* __restrict__ bkey,
-                           const int* __restrict__ parent, int p, const T* __restrict__ binom,
-                           int ldb, c_t<T>* __restrict__ local) {
-  extern __shared__ unsigned char smem_raw[];
-  c_t<T>* as = reinterpret_cast<c_t<T>*>(smem_raw);
-  const int tid = threadIdx.x, ldl = p + 1, nout = E * ldl;
-  const int b = offL + blockIdx.x;
-  const unsigned long long kb = bkey[b];
-  const double lx = (double)compact2d(kb) + 0.5, ly = (double)compact2d(kb >> 1) + 0.5;
-  const int e = tid / ldl, j = tid - e * ldl;
-  c_t<T> acc = cmk<T>(0, 0);
-  int a = parent[b];
-  for (int lev = L - 1; lev >= 2; --lev, a = parent[a]) {
-    const int shift = L - lev;
-    const unsigned long long ka = bkey[a];
-    const double sc = (double)(1u << shift);
-    const double dx = lx - ((double)compact2d(ka) + 0.5) * sc, dy = ly - ((double)compact2d(ka >> 1) + 0.5) * sc;
-    const c_t<T> d = cmk<T>((T)dx, (T)dy);
-    const c_t<T> g = cmk<T>((T)(dx / sc), (T)(dy / sc));
-    const c_t<T>* la = local + (size_t)a * nout;
-    __syncthreads();
-    for (int idx = tid; idx < nout; idx += blockDim.x) {
-      int e2 = idx / ldl, m = idx - e2 * ldl;
-      c_t<T> v = la[idx];
-      if (e2 == 1 && m < p) cfma<T>(v, cscale<T>(cconj<T>(g), (T)(m + 1)), la[m + 1]);
-      as[idx] = cmul<T>(v, cpow_int<T>(g, m));
-    }
-    __syncthreads();
-    if (tid < nout) {
-      const c_t<T>* ae = as + e * ldl;
-      c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
-      int m = j;
-      for (; m + 1 <= p; m += 2) {
-        crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
-        crfma<T>(s1, binom[(size_t)(m + 1) * ldb + j], ae[m + 1]);
-      }
-      if (m <= p) crfma<T>(s0, binom[(size_t)m * ldb + j], ae[m]);
-      cfma<T>(acc, cpow_int<T>(cinv<T>(d), j), cadd<T>(s0, s1));
-    }
-  }
-  if (tid < nout) {
-    c_t<T>* lb = local + (size_t)b * nout;
-    lb[tid] = cadd<T>(lb[tid], acc);
   }
 }
 
@@ -695,8 +644,8 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
                                                 const float2* __restrict__ pq,
                                                 const float2* __restrict__ aa,
                                                 const float2* __restrict__ qa, double x0, double y0,
-                                                double r, int p, float s,
-                                                const float2* __restrict__ local,
+                                                double r, int L, const int* __restrict__ parent,
+                                                int p, float s, const float2* __restrict__ local,
                                                 double2* __restrict__ out) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
@@ -708,10 +657,25 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   const float2 hi = zhi[ii], lo = zlo[ii];
   float fx = 0.f, fy = 0.f;
   if (has_far) {
-    double2 zi = zs[ii];
-    double2 c = box_center(bkey[b], x0, y0, r);
-    float2 u = make_float2((float)((zi.x - c.x) / r), (float)((zi.y - c.y) / r));
-    l2p_part<float, E>(local + (size_t)b * E * (p + 1), p, sl, u, s, fx, fy);
+    // The M2L expansion of the leaf and of each ancestor (levels L .. 2), each evaluated
+    // about its own centre: the sum equals L2P of the L2L-accumulated leaf expansion.
+    // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
+    //   u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2   (i the leaf's grid index),
+    // whose constant part is exact in FP32 (i < 2^20).
+    const double2 zi = zs[ii];
+    const unsigned long long kb = bkey[b];
+    const unsigned int ix = compact2d(kb), iy = compact2d(kb >> 1);
+    const double2 c = box_center(kb, x0, y0, r);
+    const float ux = (float)((zi.x - c.x) / r), uy = (float)((zi.y - c.y) / r);
+    int a = b;
+    for (int sh = 0; sh <= L - 2; ++sh) {
+      const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
+      const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
+      const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
+      const float2 u = make_float2(fmaf(ux, f, gx), fmaf(uy, f, gy));
+      l2p_part<float, E>(local + (size_t)a * E * (p + 1), p, sl, u, s, fx, fy);
+      a = parent[a];
+    }
   }
   float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
   const int nu = ucount[leaf];
@@ -847,7 +811,8 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   if (sizeof(T) == 4) {
     EB_CUDA_TRY(cudaMemsetAsync(t.arrive.p, 0, sizeof(int) * (size_t)t.nbox, st));
     size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
-    int bs = std::max(64, round32(E * p));
+    // enough threads to stage all four children of a box in one round for p <= 20
+    int bs = std::max(160, round32(E * p));
     k_upward<T, E><<<t.nleaf, bs, sm, st>>>(offL, L, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
                                             t.pt1.as<int>(), t.parent.as<int>(), t.child0.as<int>(),
                                             t.nchild.as<int>(), t.zs.as<double2>(), w.qa.as<c_t<T>>(),
@@ -888,15 +853,10 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     }
     ps.done();
   }
-  // Downward pass: FP32 gathers every ancestor's expansion in one launch; FP64 shifts
-  // level by level.
-  if (L >= 3 && sizeof(T) == 4) {
-    size_t sm = sizeof(c_t<T>) * E * (p + 1);
-    k_downward<T, E><<<t.nleaf, round32(E * (p + 1)), sm, st>>>(offL, L, t.bkey.as<unsigned long long>(),
-                                                                t.parent.as<int>(), p, tb.binom.as<T>(),
-                                                                ldb, w.local.as<c_t<T>>());
-    eb_count_launch(ctx);
-  } else {
+  // Downward pass. FP64: L2L level by level. FP32: none; the leaf kernel evaluates
+  // every ancestor's M2L expansion directly (cheap FP32 work instead of a dependent
+  // chain of shifts).
+  if (sizeof(T) == 8) {
     for (int l = 3; l <= L; ++l) {
       int nb = t.lev_off[l + 1] - t.lev_off[l];
       size_t sm = sizeof(c_t<T>) * E * (p + 1);
@@ -948,8 +908,8 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.zs.as<double2>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
-        w.aa.as<float2>(), w.qa.as<float2>(), t.x0, t.y0, rleaf, tb.p, (float)sign,
-        w.local.as<float2>(), out);
+        w.aa.as<float2>(), w.qa.as<float2>(), t.x0, t.y0, rleaf, t.L, t.parent.as<int>(), tb.p,
+        (float)sign, w.local.as<float2>(), out);
   }
   eb_count_launch(ctx);
   ps.done();

@@ -18,8 +18,16 @@
 #define EB_GROUP 8
 
 // ---------------------------------------------------------------------------------
-// Device buffer that grows on demand (never shrinks) and frees itself.
+// Device buffer that grows on demand (never shrinks) and frees itself. Every
+// reallocation or release advances a process-wide epoch, which invalidates the cached
+// CUDA graphs that captured the old addresses. While a stream capture is in progress
+// on the calling thread, a buffer that must grow keeps its old allocation alive (freed
+// by eb_devbuf_collect) instead of freeing it, since cudaFree synchronises the device.
 // ---------------------------------------------------------------------------------
+unsigned long long eb_devbuf_epoch();
+void eb_devbuf_set_capturing(bool on);
+void eb_devbuf_collect();
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -80,6 +88,18 @@ struct EbFmmWork {
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
 };
 
+// A GMRES cycle (or refinement step) captured as one CUDA graph: the Arnoldi steps run
+// inside a conditional WHILE node whose condition a device kernel sets.
+struct GmGraph {
+  bool valid = false;
+  unsigned long long key[8] = {0};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long n_pre = 0, n_body = 0, n_post = 0;  // kernel launches per part
+  void destroy();
+};
+#define EB_GRAPH_CACHE 4
+
 struct eb_ctx {
   eb_opts opts;
   int device = 0;
@@ -123,7 +143,12 @@ struct eb_ctx {
 
   // GMRES workspace
   DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ, gTicket;
+  DevBuf gCtl, gXin, gWbuf;        // graph mode: control block, operator input and output
   std::vector<double> hH;
+  unsigned long long geom_version = 0;  // advanced by every geometry install
+  cudaStream_t cap_stream = nullptr;    // private stream for graph capture
+  GmGraph gcache[EB_GRAPH_CACHE];
+  int gcache_next = 0;
 };
 
 // tree.cu

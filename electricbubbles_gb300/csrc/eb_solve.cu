@@ -15,7 +15,10 @@
 // x = 0 (so r = b needs no apply),
 //   solve A32 d = r to inner_tol with the same GMRES;  x += d;  r = b - A64 x,
 // until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual.
+#include <algorithm>
 #include <cmath>
+#include <cstddef>
+#include <cstring>
 #include <vector>
 
 #include "eb_internal.h"
@@ -64,9 +67,10 @@ __device__ void finish_columns(int nb, int ncol, const double* part, double* out
 // out[j] = V[:, j] . w for j < ncol. Each block takes a contiguous range of rows and
 // each of its warps a subset of the columns; partial sums per block go to `part` and
 // the last block to finish adds them in block order.
-__global__ void k_vtw(int n, int ncol, const double* __restrict__ V, size_t ldv,
-                      const double* __restrict__ w, double* __restrict__ part,
+__global__ void k_vtw(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                      size_t ldv, const double* __restrict__ w, double* __restrict__ part,
                       double* __restrict__ out, unsigned int* __restrict__ ticket) {
+  if (ncol_dev) ncol = *ncol_dev;
   const int rows = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -81,11 +85,12 @@ __global__ void k_vtw(int n, int ncol, const double* __restrict__ V, size_t ldv,
 }
 
 // w -= V[:, 0:ncol] h; if part != nullptr also ||w||^2 of the new w into *out.
-__global__ void k_gemv_sub(int n, int ncol, const double* __restrict__ V, size_t ldv,
-                           const double* __restrict__ h, double* __restrict__ w,
+__global__ void k_gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                           size_t ldv, const double* __restrict__ h, double* __restrict__ w,
                            double* __restrict__ part, double* __restrict__ out,
                            unsigned int* __restrict__ ticket) {
   __shared__ double hs[128];
+  if (ncol_dev) ncol = *ncol_dev;
   __shared__ double red[32];
   for (int j = threadIdx.x; j < ncol; j += blockDim.x) hs[j] = h[j];
   __syncthreads();
@@ -117,14 +122,14 @@ __global__ void k_gemv_add(int n, int ncol, const double* __restrict__ V, size_t
   }
 }
 
-// out = a - out (residual), with ||out||^2 into *nrm2.
-__global__ void k_resid(int n, const double* __restrict__ a, double* __restrict__ out,
+// out = a - y (residual; y may be out), with ||out||^2 into *nrm2.
+__global__ void k_resid(int n, const double* __restrict__ a, const double* y, double* out,
                         double* __restrict__ part, double* __restrict__ nrm2,
                         unsigned int* __restrict__ ticket) {
   __shared__ double red[32];
   double sq = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double v = a[i] - out[i];
+    double v = a[i] - y[i];
     out[i] = v;
     sq = fma(v, v, sq);
   }
@@ -155,7 +160,7 @@ struct Gm {
 int dev_sumsq(Gm& g, const double* v, double* out) {
   eb_ctx* ctx = g.ctx;
   double* part = ctx->gPart.as<double>();
-  k_vtw<<<g.nb, RBS, 0, g.s>>>(g.n, 1, v, (size_t)g.n, v, part, ctx->gH.as<double>(), g.ticket);
+  k_vtw<<<g.nb, RBS, 0, g.s>>>(g.n, 1, nullptr, v, (size_t)g.n, v, part, ctx->gH.as<double>(), g.ticket);
   eb_count_launch(ctx);
   EB_CUDA_TRY(cudaMemcpyAsync(out, ctx->gH.p, sizeof(double), cudaMemcpyDeviceToHost, g.s));
   EB_CUDA_TRY(cudaStreamSynchronize(g.s));
@@ -163,7 +168,8 @@ int dev_sumsq(Gm& g, const double* v, double* out) {
 }
 
 // DHEQR column update (IJOB > 1 form; identical to IJOB = 1 for the first column).
-int dheqr_col(double* hes, int ldh, int ll, double* q) {
+// Runs on the host (host-driven loop) and in the device Arnoldi kernel (graph mode).
+__host__ __device__ inline int dheqr_col(double* hes, int ldh, int ll, double* q) {
   double* a = hes + (size_t)(ll - 1) * ldh;
   for (int k = 0; k < ll - 1; ++k) {
     double c = q[2 * k], s = q[2 * k + 1], t1 = a[k], t2 = a[k + 1];
@@ -172,8 +178,8 @@ int dheqr_col(double* hes, int ldh, int ll, double* q) {
   }
   double t1 = a[ll - 1], t2 = a[ll], c, s;
   if (t2 == 0.0) { c = 1.0; s = 0.0; }
-  else if (std::fabs(t2) >= std::fabs(t1)) { double t = t1 / t2; s = -1.0 / std::sqrt(1.0 + t * t); c = -s * t; }
-  else { double t = t2 / t1; c = 1.0 / std::sqrt(1.0 + t * t); s = -c * t; }
+  else if (fabs(t2) >= fabs(t1)) { double t = t1 / t2; s = -1.0 / sqrt(1.0 + t * t); c = -s * t; }
+  else { double t = t2 / t1; c = 1.0 / sqrt(1.0 + t * t); s = -c * t; }
   q[2 * (ll - 1)] = c;
   q[2 * (ll - 1) + 1] = s;
   a[ll - 1] = c * t1 - s * t2;
@@ -235,7 +241,7 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
   } else {
     EB_TRY(op(ctx, x, V, prec));
     (*nmv)++;
-    k_resid<<<g.nb, RBS, 0, g.s>>>(n, b, V, part, hdev, g.ticket);
+    k_resid<<<g.nb, RBS, 0, g.s>>>(n, b, V, V, part, hdev, g.ticket);
     eb_count_launch(ctx);
   }
   double ss;
@@ -262,11 +268,11 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     EB_TRY(op(ctx, V + (size_t)(ll - 1) * ldv, w, prec));
     (*nmv)++;
     // pass 1: h1 = V^T w; w -= V h1
-    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part, hdev, g.ticket);
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev, w, nullptr, nullptr, nullptr);
+    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket);
+    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, nullptr, nullptr, nullptr);
     // pass 2: h2 = V^T w; w -= V h2 with ||w||^2
-    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, w, part, hdev + (maxl + 2), g.ticket);
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev + (maxl + 2), w, part,
+    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev + (maxl + 2), g.ticket);
+    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev + (maxl + 2), w, part,
                                       hdev + 2 * (maxl + 2), g.ticket);
     ctx->launches += 4;
     EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
@@ -304,6 +310,424 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
   return eb_check_launch(ctx, "gmres");
 }
 
+
+// =================================================================================
+// Graph mode. One GMRES cycle (plain mode) or one refinement step (refined mode) is a
+// single CUDA graph launch: the Arnoldi steps run inside a conditional WHILE node whose
+// condition the device-side Arnoldi kernel sets after its DHEQR update, and DHELS and
+// the solution update run on the device too. The host waits once per launch instead
+// of once per Krylov step. Operator launches depend only on the installed geometry,
+// so a captured graph is reused until the geometry or a work buffer changes.
+// =================================================================================
+#define EB_GM_MAXL 126
+
+struct GmCtl {
+  int ll;         // Krylov column the next Arnoldi step produces (DPIGMR's LL)
+  int maxl;
+  int iters;
+  int iflag;      // DGMRES IERR convention
+  int lgmr;       // columns of the least-squares problem (= Arnoldi steps taken)
+  int cont;       // the WHILE node iterates while this is 1
+  int status;     // EB_OK or EB_ERR_NAN
+  int store_col;  // column k_gm_store writes
+  int nadd;       // columns k_gm_add adds to x
+  int zero_x;     // b = 0: the solution is x = 0
+  int pad[2];
+  double tol, bnrm, r0nrm, prod, rho, err, scale, rnrm2;  // rnrm2: refinement ||r||^2
+  double q[2 * EB_GM_MAXL];
+  double hes[(EB_GM_MAXL + 1) * EB_GM_MAXL];
+};
+constexpr size_t GM_HEAD = offsetof(GmCtl, q);
+
+// slots of the reduction output buffer (gH)
+constexpr int GM_H1 = 0, GM_H2 = EB_GM_MAXL + 2, GM_NW = 2 * (EB_GM_MAXL + 2), GM_BN = GM_NW + 1,
+              GM_R0 = GM_NW + 2, GM_Y = GM_NW + 4, GM_HSIZE = GM_Y + EB_GM_MAXL + 2;
+
+__global__ void k_gm_init(GmCtl* c, const double* __restrict__ hdev, cudaGraphConditionalHandle h,
+                          double tol, int maxl, int r0_is_b) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->tol = tol;
+  c->maxl = maxl;
+  c->iters = 0;
+  c->iflag = 0;
+  c->lgmr = 0;
+  c->cont = 0;
+  c->status = EB_OK;
+  c->store_col = 0;
+  c->nadd = 0;
+  c->zero_x = 0;
+  c->ll = 1;
+  c->err = 0.0;
+  const double bnrm = sqrt(hdev[GM_BN]);
+  c->bnrm = bnrm;
+  if (!isfinite(bnrm)) {
+    c->status = EB_ERR_NAN;
+  } else if (!(bnrm > 0.0)) {
+    c->zero_x = 1;  // b = 0 (DGMRES would divide by zero)
+  } else {
+    const double r0 = r0_is_b ? bnrm : sqrt(hdev[GM_R0]);
+    c->r0nrm = r0;
+    c->err = r0 / bnrm;
+    if (!isfinite(r0)) {
+      c->status = EB_ERR_NAN;
+    } else if (c->err > tol) {
+      c->scale = 1.0 / r0;
+      c->prod = 1.0;
+      c->rho = r0;
+      c->iflag = 1;
+      c->cont = 1;
+    }
+  }
+  cudaGraphSetConditional(h, c->cont ? 1u : 0u);
+}
+
+// V[:, store_col] = xin = scale * src while the iteration continues (src may alias V).
+__global__ void k_gm_store(int n, const GmCtl* __restrict__ c, const double* src, double* V, size_t ldv,
+                           double* __restrict__ xin) {
+  if (!c->cont) return;
+  const double sc = c->scale;
+  double* dst = V + (size_t)c->store_col * ldv;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = src[i] * sc;
+    dst[i] = v;
+    xin[i] = v;
+  }
+}
+
+// End of an Arnoldi step (DPIGMR, dpigmr.f:333-380): the Hessenberg column from the two
+// Gram-Schmidt passes, its Givens update (DHEQR), the residual estimate and the decision.
+__global__ void k_gm_arnoldi(GmCtl* c, const double* __restrict__ hdev, cudaGraphConditionalHandle h) {
+  const int lane = threadIdx.x;
+  const int ll = c->ll, ldh = c->maxl + 1;
+  double* col = c->hes + (size_t)(ll - 1) * ldh;
+  for (int i = lane; i < ll; i += 32) col[i] = hdev[GM_H1 + i] + hdev[GM_H2 + i];
+  __syncwarp();
+  if (lane != 0) return;
+  const double snormw = sqrt(fmax(hdev[GM_NW], 0.0));
+  col[ll] = snormw;
+  int cont = 0;
+  c->lgmr = ll;
+  if (!isfinite(snormw)) {
+    c->status = EB_ERR_NAN;
+  } else if (dheqr_col(c->hes, ldh, ll, c->q) == ll) {
+    c->iflag = 2;
+  } else {
+    c->prod *= c->q[2 * (ll - 1) + 1];
+    c->rho = fabs(c->prod * c->r0nrm);
+    c->iters = ll;
+    c->err = c->rho / c->bnrm;
+    if (c->err <= c->tol) {
+      c->iflag = 0;
+    } else if (ll >= c->maxl) {
+      // MAXL reached; IERR is resolved by k_gm_finish
+    } else if (snormw == 0.0) {
+      c->iflag = 2;
+    } else {
+      c->scale = 1.0 / snormw;
+      c->store_col = ll;
+      c->ll = ll + 1;
+      cont = 1;
+    }
+  }
+  c->cont = cont;
+  cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+// DHELS (dhels.f:77-96) on the device: y = R^-1 Q^T (r0nrm e1), into ydev.
+__global__ void k_gm_finish(GmCtl* c, double* __restrict__ ydev) {
+  __shared__ double y[EB_GM_MAXL + 1];
+  __shared__ int s_n;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    int n = 0;
+    if (c->status == EB_OK && !c->zero_x && c->lgmr > 0) {
+      if (c->iflag != 0 && c->iflag != 2) c->iflag = (c->rho < c->r0nrm) ? 1 : 2;
+      if (c->iflag != 2) n = c->lgmr;
+    }
+    c->nadd = n;
+    s_n = n;
+    if (n > 0) {
+      for (int i = 0; i <= n; ++i) y[i] = 0.0;
+      y[0] = c->r0nrm;
+      for (int k = 0; k < n; ++k) {
+        double cc = c->q[2 * k], ss = c->q[2 * k + 1], t1 = y[k], t2 = y[k + 1];
+        y[k] = cc * t1 - ss * t2;
+        y[k + 1] = ss * t1 + cc * t2;
+      }
+    }
+  }
+  __syncthreads();
+  const int n = s_n;
+  if (n == 0) return;
+  const int ldh = c->maxl + 1;
+  for (int kb = 0; kb < n; ++kb) {
+    const int k = n - 1 - kb;
+    if (tid == 0) y[k] /= c->hes[(size_t)k * ldh + k];
+    __syncthreads();
+    const double t = -y[k];
+    for (int r = tid; r < k; r += blockDim.x) y[r] += t * c->hes[(size_t)k * ldh + r];
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += blockDim.x) ydev[i] = y[i];
+}
+
+// x += V[:, 0:nadd] y, or x = 0 when b = 0.
+__global__ void k_gm_add(int n, const GmCtl* __restrict__ c, const double* __restrict__ V, size_t ldv,
+                         const double* __restrict__ y, double* __restrict__ x) {
+  __shared__ double ys[EB_GM_MAXL + 1];
+  const int stride = gridDim.x * blockDim.x;
+  if (c->zero_x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) x[i] = 0.0;
+    return;
+  }
+  const int ncol = c->nadd;
+  if (ncol == 0) return;
+  for (int j = threadIdx.x; j < ncol; j += blockDim.x) ys[j] = y[j];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double acc = 0.0;
+    for (int j = 0; j < ncol; ++j) acc = fma(V[(size_t)j * ldv + i], ys[j], acc);
+    x[i] += acc;
+  }
+}
+
+// refinement: x += d unless the inner solve failed
+__global__ void k_gm_axpy(int n, const GmCtl* __restrict__ c, const double* __restrict__ d,
+                          double* __restrict__ x) {
+  if (c->status != EB_OK) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += d[i];
+}
+
+enum { GM_PLAIN = 0, GM_REFINE = 1 };
+constexpr int GM_BUILD_FAILED = -100;  // internal: fall back to the host-driven loop
+
+// Enqueues `f` on the capture stream into graph `gr` after `deps`; records the sink
+// nodes of the capture and the kernel launches it issued.
+template <typename F>
+int capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* deps, size_t ndeps,
+                 std::vector<cudaGraphNode_t>* sinks, long long* nlaunch, F f) {
+  cudaStream_t saved = ctx->stream;
+  const long long l0 = ctx->launches;
+  ctx->stream = ctx->cap_stream;
+  eb_devbuf_set_capturing(true);
+  int st = EB_OK;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(ctx->cap_stream, gr, deps, nullptr, ndeps,
+                                                cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    eb_set_last_cuda_error(e, "cudaStreamBeginCaptureToGraph", __FILE__, __LINE__);
+    st = EB_ERR_CUDA;
+  } else {
+    st = f();
+    if (sinks) {
+      cudaStreamCaptureStatus cs;
+      const cudaGraphNode_t* d = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(ctx->cap_stream, &cs, nullptr, nullptr, &d, nullptr, &nd);
+      if (e == cudaSuccess && d) sinks->assign(d, d + nd);
+      else if (st == EB_OK) {
+        eb_set_last_cuda_error(e, "cudaStreamGetCaptureInfo", __FILE__, __LINE__);
+        st = EB_ERR_CUDA;
+      }
+    }
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(ctx->cap_stream, &out);
+    if (e != cudaSuccess && st == EB_OK) {
+      eb_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+      st = EB_ERR_CUDA;
+    }
+  }
+  eb_devbuf_set_capturing(false);
+  ctx->stream = saved;
+  *nlaunch = ctx->launches - l0;
+  ctx->launches = l0;
+  return st;
+}
+
+// Builds the graph of one plain GMRES cycle (x0 = x, tolerance gmres_tol) or of one
+// refinement step (inner FP32 cycle on r from x0 = 0 to inner_tol, x += d, r = b - A x).
+int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
+  G.destroy();
+  EB_CUDA_TRY(cudaGraphCreate(&G.graph, 0));
+  cudaGraphConditionalHandle h;
+  EB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, G.graph, 0, cudaGraphCondAssignDefault));
+  const int nb = std::min(nblk(n, RBS), RMAXB);
+  const size_t ldv = (size_t)n;
+  double* V = ctx->gV.as<double>();
+  double* part = ctx->gPart.as<double>();
+  double* hdev = ctx->gH.as<double>();
+  GmCtl* ctl = ctx->gCtl.as<GmCtl>();
+  double* xin = ctx->gXin.as<double>();
+  double* wbuf = ctx->gWbuf.as<double>();
+  unsigned int* ticket = ctx->gTicket.as<unsigned int>();
+  const bool refine = kind == GM_REFINE;
+  const int prec = refine ? EB_FP32 : EB_FP64;
+  const double tol = refine ? ctx->opts.inner_tol : ctx->opts.gmres_tol;
+  double* bb = refine ? ctx->gZ.as<double>() : ctx->gR.as<double>();  // right-hand side of the cycle
+  double* xx = refine ? ctx->gD.as<double>() : ctx->gX.as<double>();  // its solution
+  std::vector<cudaGraphNode_t> sinks;
+  // pre: norms, r0, V[:, 0]
+  EB_TRY(capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, [&]() -> int {
+    cudaStream_t s = ctx->stream;
+    k_vtw<<<nb, RBS, 0, s>>>(n, 1, nullptr, bb, ldv, bb, part, hdev + GM_BN, ticket);
+    eb_count_launch(ctx);
+    if (refine) {
+      EB_CUDA_TRY(cudaMemsetAsync(xx, 0, sizeof(double) * n, s));
+      EB_CUDA_TRY(cudaMemcpyAsync(V, bb, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    } else {
+      EB_CUDA_TRY(cudaMemcpyAsync(xin, xx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      EB_TRY(op(ctx, xin, wbuf, prec));
+      k_resid<<<nb, RBS, 0, s>>>(n, bb, wbuf, V, part, hdev + GM_R0, ticket);
+      eb_count_launch(ctx);
+    }
+    k_gm_init<<<1, 32, 0, s>>>(ctl, hdev, h, tol, maxl, refine ? 1 : 0);
+    k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, V, V, ldv, xin);
+    ctx->launches += 2;
+    return eb_check_launch(ctx, "gmres graph (pre)");
+  }));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t ncond;
+  EB_CUDA_TRY(cudaGraphAddNode(&ncond, G.graph, sinks.data(), nullptr, sinks.size(), &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  // body: one Arnoldi step
+  const int* lld = &ctl->ll;
+  EB_TRY(capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, [&]() -> int {
+    cudaStream_t s = ctx->stream;
+    EB_TRY(op(ctx, xin, wbuf, prec));
+    k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
+    k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, nullptr, nullptr, nullptr);
+    k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H2, ticket);
+    k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev + GM_NW, ticket);
+    k_gm_arnoldi<<<1, 32, 0, s>>>(ctl, hdev, h);
+    k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
+    ctx->launches += 6;
+    return eb_check_launch(ctx, "gmres graph (body)");
+  }));
+  // post: DHELS, x update; refined: x += d, r = b - A64 x with ||r||^2
+  EB_TRY(capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, [&]() -> int {
+    cudaStream_t s = ctx->stream;
+    k_gm_finish<<<1, 128, 0, s>>>(ctl, hdev + GM_Y);
+    k_gm_add<<<nb, RBS, 0, s>>>(n, ctl, V, ldv, hdev + GM_Y, xx);
+    ctx->launches += 2;
+    if (refine) {
+      double* x = ctx->gX.as<double>();
+      k_gm_axpy<<<nb, RBS, 0, s>>>(n, ctl, xx, x);
+      eb_count_launch(ctx);
+      EB_TRY(op(ctx, x, bb, EB_FP64));
+      k_resid<<<nb, RBS, 0, s>>>(n, ctx->gR.as<double>(), bb, bb, part, &ctl->rnrm2, ticket);
+      eb_count_launch(ctx);
+    }
+    return eb_check_launch(ctx, "gmres graph (post)");
+  }));
+  EB_CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, 0));
+  G.valid = true;
+  return EB_OK;
+}
+
+GmGraph* find_graph(eb_ctx* ctx, const unsigned long long* key) {
+  for (GmGraph& g : ctx->gcache)
+    if (g.valid && std::equal(key, key + 8, g.key)) return &g;
+  return nullptr;
+}
+
+// Runs one graph launch (building it on first use) and reads the control block back.
+int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
+  unsigned long long key[8];
+  auto fill_key = [&](unsigned long long epoch) {
+    double t1 = ctx->opts.gmres_tol, t2 = ctx->opts.inner_tol;
+    key[0] = (unsigned long long)kind;
+    key[1] = (unsigned long long)(uintptr_t)op;
+    key[2] = (unsigned long long)n;
+    key[3] = (unsigned long long)maxl;
+    key[4] = ctx->geom_version;
+    key[5] = epoch;
+    memcpy(&key[6], &t1, 8);
+    memcpy(&key[7], &t2, 8);
+  };
+  fill_key(eb_devbuf_epoch());
+  GmGraph* G = find_graph(ctx, key);
+  if (!G) {
+    G = &ctx->gcache[ctx->gcache_next];
+    ctx->gcache_next = (ctx->gcache_next + 1) % EB_GRAPH_CACHE;
+    int st = build_graph(ctx, *G, kind, op, n, maxl);
+    if (st != EB_OK) {
+      G->destroy();
+      cudaGetLastError();
+      return GM_BUILD_FAILED;
+    }
+    fill_key(eb_devbuf_epoch());  // buffers first allocated during capture stay in place
+    memcpy(G->key, key, sizeof(key));
+  }
+  cudaStream_t s = ctx->stream;
+  EB_CUDA_TRY(cudaGraphLaunch(G->exec, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(head, ctx->gCtl.p, GM_HEAD, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  ctx->launches += G->n_pre + G->n_post + G->n_body * (long long)head->lgmr;
+  return EB_OK;
+}
+
+int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info* inf) {
+  cudaStream_t s = ctx->stream;
+  if (maxl > n) maxl = n;
+  EB_TRY(ctx->gCtl.ensure(sizeof(GmCtl)));
+  EB_TRY(ctx->gXin.ensure(sizeof(double) * n));
+  EB_TRY(ctx->gWbuf.ensure(sizeof(double) * n));
+  EB_TRY(ctx->gV.ensure(sizeof(double) * (size_t)n * (maxl + 1)));
+  EB_TRY(ctx->gD.ensure(sizeof(double) * n));
+  EB_TRY(ctx->gZ.ensure(sizeof(double) * n));
+  GmCtl head;
+  if (mode == EB_SOLVE_FP64) {
+    EB_TRY(run_graph(ctx, GM_PLAIN, op, n, maxl, &head));
+    if (head.status != EB_OK) {
+      eb_set_last_error_msg("non-finite value in GMRES");
+      return head.status;
+    }
+    inf->iters = head.iters;
+    inf->err = head.err;
+    inf->ierr = head.lgmr > 0 ? head.iflag : 0;
+    inf->outer = 1;
+    inf->matvecs64 = 1 + head.lgmr;
+    return EB_OK;
+  }
+  double* x = ctx->gX.as<double>();
+  EB_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->gZ.p, ctx->gR.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  inf->ierr = 1;
+  double bnrm = 0.0;
+  for (int outer = 1; outer <= ctx->opts.max_outer; ++outer) {
+    inf->outer = outer;
+    EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, &head));
+    if (head.status != EB_OK) {
+      eb_set_last_error_msg("non-finite value in GMRES");
+      return head.status;
+    }
+    inf->iters += head.iters;
+    inf->matvecs32 += head.lgmr;
+    inf->matvecs64 += 1;
+    if (outer == 1) {
+      bnrm = head.bnrm;  // the first inner right-hand side is b itself
+      if (head.zero_x) {
+        inf->err = 0.0;
+        inf->ierr = 0;
+        break;
+      }
+    }
+    inf->err = std::sqrt(std::max(head.rnrm2, 0.0)) / bnrm;
+    if (!std::isfinite(inf->err)) {
+      eb_set_last_error_msg("non-finite residual");
+      return EB_ERR_NAN;
+    }
+    if (inf->err <= ctx->opts.gmres_tol) {
+      inf->ierr = 0;
+      break;
+    }
+  }
+  return EB_OK;
+}
+
 int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mode,
           eb_solve_info* info, int mem) {
   cudaStream_t s = ctx->stream;
@@ -314,7 +738,7 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
     return EB_ERR_WORKSPACE;
   }
   EB_TRY(ctx->gPart.ensure(sizeof(double) * (size_t)RMAXB * (maxl + 2)));
-  EB_TRY(ctx->gH.ensure(sizeof(double) * 3 * (maxl + 2)));
+  EB_TRY(ctx->gH.ensure(sizeof(double) * std::max(3 * (maxl + 2), (int)GM_HSIZE)));
   EB_TRY(ctx->gTicket.ensure(sizeof(unsigned int)));
   EB_CUDA_TRY(cudaMemsetAsync(ctx->gTicket.p, 0, sizeof(unsigned int), s));
   g.ticket = ctx->gTicket.as<unsigned int>();
@@ -328,13 +752,27 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
   EB_CUDA_TRY(cudaMemcpyAsync(x, rhs, sizeof(double) * n, kin, s));
   eb_solve_info inf{};
   int st = EB_OK;
-  if (mode == EB_SOLVE_FP64) {
+  bool eager = true;
+  if (ctx->opts.graphs > 0 && !ctx->profiling) {
+    st = solve_graph(ctx, n, op, mode, maxl, &inf);
+    if (st == GM_BUILD_FAILED) {
+      // graphs with conditional nodes are unavailable: use the host-driven loop from now on
+      ctx->opts.graphs = -1;
+      inf = eb_solve_info{};
+      st = EB_OK;
+      EB_CUDA_TRY(cudaMemcpyAsync(x, rhs, sizeof(double) * n, kin, s));
+    } else {
+      inf.graph = 1;
+      eager = false;
+    }
+  }
+  if (eager && mode == EB_SOLVE_FP64) {
     int nmv = 0;
     st = gmres_cycle(g, op, EB_FP64, b, x, false, ctx->opts.gmres_tol, maxl, &inf.iters, &inf.err,
                      &inf.ierr, &nmv, -1.0);
     inf.outer = 1;
     inf.matvecs64 = nmv;
-  } else {
+  } else if (eager) {
     EB_TRY(ctx->gD.ensure(sizeof(double) * n));
     EB_TRY(ctx->gZ.ensure(sizeof(double) * n));
     double* r = ctx->gZ.as<double>();
@@ -363,7 +801,7 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
       EB_TRY(op(ctx, x, r, EB_FP64));
       inf.matvecs64++;
       double* part = ctx->gPart.as<double>();
-      k_resid<<<g.nb, RBS, 0, s>>>(n, b, r, part, ctx->gH.as<double>(), g.ticket);
+      k_resid<<<g.nb, RBS, 0, s>>>(n, b, r, r, part, ctx->gH.as<double>(), g.ticket);
       ctx->launches += 1;
       double rss;
       EB_CUDA_TRY(cudaMemcpyAsync(&rss, ctx->gH.p, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -388,6 +826,14 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
 }
 
 }  // namespace
+
+void GmGraph::destroy() {
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  exec = nullptr;
+  graph = nullptr;
+  valid = false;
+}
 
 int eb_stokes_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
                     eb_solve_info* info, int mem) {

@@ -14,6 +14,9 @@
 #include <algorithm>
 #include <cmath>
 
+#include <atomic>
+#include <mutex>
+
 #include "eb_internal.h"
 
 namespace {
@@ -295,8 +298,33 @@ inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 }  // namespace
 
+namespace {
+std::atomic<unsigned long long> g_epoch{1};
+thread_local bool t_capturing = false;
+std::mutex g_deferred_mu;
+std::vector<void*> g_deferred;
+}  // namespace
+
+unsigned long long eb_devbuf_epoch() { return g_epoch.load(); }
+void eb_devbuf_set_capturing(bool on) { t_capturing = on; }
+void eb_devbuf_collect() {
+  std::vector<void*> v;
+  {
+    std::lock_guard<std::mutex> lk(g_deferred_mu);
+    v.swap(g_deferred);
+  }
+  for (void* q : v) cudaFree(q);
+}
+
 int DevBuf::ensure(size_t nbytes) {
   if (nbytes <= bytes && p) return EB_OK;
+  if (p && t_capturing) {
+    std::lock_guard<std::mutex> lk(g_deferred_mu);
+    g_deferred.push_back(p);
+    p = nullptr;
+    bytes = 0;
+    g_epoch++;
+  }
   release();
   size_t want = nbytes < 256 ? 256 : nbytes;
   cudaError_t e = cudaMalloc(&p, want);
@@ -311,7 +339,10 @@ int DevBuf::ensure(size_t nbytes) {
 }
 
 void DevBuf::release() {
-  if (p) cudaFree(p);
+  if (p) {
+    cudaFree(p);
+    g_epoch++;
+  }
   p = nullptr;
   bytes = 0;
 }

@@ -65,6 +65,8 @@ typedef struct eb_opts {
   double inner_tol; /* refined mode: inner FP32 GMRES relative tolerance (0: 1e-5) */
   int max_outer;    /* refined mode: maximum refinement steps (0: 8)           */
   int device;       /* CUDA device ordinal                                     */
+  int graphs;       /* GMRES as CUDA graphs with a device-side Arnoldi loop:
+                       0 default (on), 1 on, -1 off (host-driven loop)          */
 } eb_opts;
 
 typedef struct eb_solve_info {
@@ -74,6 +76,7 @@ typedef struct eb_solve_info {
   int matvecs32;    /* FP32 operator applies                                  */
   double err;       /* final ||b - A x|| / ||b|| estimate (DGMRES ERR)        */
   int ierr;         /* DGMRES IERR convention: 0 converged, 1 MAXL reached, 2 stalled */
+  int graph;        /* 1 if the solve ran as CUDA graphs with the device-side loop */
 } eb_solve_info;
 
 typedef struct eb_tree_info {

@@ -274,6 +274,35 @@ void eb_or_stokes_direct(int n, const cplx* z, const cplx* dz, const double* hpt
   free(qb);
 }
 
+/* The same direct sum evaluated only at the nodes tidx[0..nt) (self excluded); used to
+ * check large layer-potential sums on a sample of targets. */
+void eb_or_stokes_direct_at(int n, const cplx* z, const cplx* dz, const double* hpt,
+                            const cplx* dens, int sign, int nt_, const int* tidx, cplx* out,
+                            int nthreads) {
+  cplx* qa = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+  cplx* qb = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+  stokes_charges(n, dz, hpt, dens, qa, qb);
+  const double s = (double)sign;
+  int nt = clamp_threads(nthreads);
+  (void)nt;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 4)
+  for (int ii = 0; ii < nt_; ++ii) {
+    int t = tidx[ii];
+    cplx acc = 0;
+    cplx zt = z[t];
+    for (int j = 0; j < n; ++j) {
+      if (j == t) continue;
+      cplx d = z[j] - zt;
+      cplx zinv = 1.0 / d;
+      cplx zinv2c = conj(zinv * zinv);
+      acc += qa[j] * zinv + s * (conj(qb[j] * zinv) - d * conj(qa[j]) * zinv2c);
+    }
+    out[ii] = acc;
+  }
+  free(qa);
+  free(qb);
+}
+
 /* ---- restatement of the per-level uniform-grid FMM CADAPDR/CADAPMOD ---- */
 
 /* SLMKXP, cadap2.f:412-468 (P2M, 1-based coefficients m1[1..p], m2[1..p]). */

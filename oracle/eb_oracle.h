@@ -57,6 +57,9 @@ void eb_or_extractdat(int k, const int* nd, const double* rku, eb_or_cplx* z,
 void eb_or_stokes_direct(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
                          const double* hpt, const eb_or_cplx* dens, int sign,
                          eb_or_cplx* gradw, int nthreads);
+void eb_or_stokes_direct_at(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
+                            const double* hpt, const eb_or_cplx* dens, int sign, int nt,
+                            const int* tidx, eb_or_cplx* out, int nthreads);
 int eb_or_cadap_fmm(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
                     const double* hpt, const eb_or_cplx* dens, int sign, int levmax,
                     double tol, eb_or_cplx* gradw, int nthreads);

@@ -53,6 +53,7 @@ def lib():
             "eb_or_finter": (None, [_I, _P, _P]),
             "eb_or_extractdat": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "eb_or_stokes_direct": (None, [_I, _P, _P, _P, _P, _I, _P, _I]),
+            "eb_or_stokes_direct_at": (None, [_I, _P, _P, _P, _P, _I, _I, _P, _P, _I]),
             "eb_or_cadap_fmm": (_I, [_I, _P, _P, _P, _P, _I, _I, _D, _P, _I]),
             "eb_or_cauchy_direct": (None, [_I, _P, _I, _P, _P, _I, _P, _I]),
             "eb_or_fasmvp": (None, [ctypes.POINTER(Geom), _P, _P, _I, _I]),
@@ -163,6 +164,17 @@ def stokes_direct(z, dz, hpt, dens, sign, nthreads=0):
     lib().eb_or_stokes_direct(z.shape[0], _p(z), _p(dz), _p(hpt), _p(dens), int(sign), _p(g),
                               int(nthreads))
     return g
+
+
+def stokes_direct_at(z, dz, hpt, dens, sign, tidx, nthreads=0):
+    """The direct Stokes sum at the nodes tidx only (self excluded)."""
+    z, dz, dens = _c(z), _c(dz), _c(dens)
+    hpt = _r(hpt)
+    tidx = _i(tidx)
+    out = np.empty(tidx.shape[0], np.complex128)
+    lib().eb_or_stokes_direct_at(z.shape[0], _p(z), _p(dz), _p(hpt), _p(dens), int(sign),
+                                 tidx.shape[0], _p(tidx), _p(out), int(nthreads))
+    return out
 
 
 def cadap_fmm(z, dz, hpt, dens, sign, levmax=7, tol=1e-13, nthreads=0):
