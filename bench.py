@@ -218,6 +218,20 @@ def run_gpu(args, rank, world, local):
     # plain FP64 and refined solves (the refined one is the headline)
     ms64, _, inf64 = timed("fp64", args.steps, args.warmup)
     x64 = x.clone()
+    # the same FP64 solves with the native FP64 near-field kernels (df64 = -1)
+    ctx_native = Context(device=local, df64=-1)
+    ctx_native.set_stream(stream.cuda_stream)
+    ctx_native.extractdat(cfg.nd, cfg.rku())
+    for _ in range(args.warmup):
+        ctx_native.solvei(rhs, "fp64", out=x)
+    torch.cuda.synchronize()
+    ev[0][0].record(stream)
+    for _ in range(args.steps):
+        ctx_native.solvei(rhs, "fp64", out=x)
+    ev[0][1].record(stream)
+    torch.cuda.synchronize()
+    ms64_native = ev[0][0].elapsed_time(ev[0][1])
+    ctx_native.close()
     clocks = ClockSampler(local)
     clocks.start()
     ms32, wall32, inf32 = timed("fp32_refined", args.steps, args.warmup)
@@ -372,6 +386,7 @@ def run_gpu(args, rank, world, local):
                    "solve": "fp32_refined GMRES-IR, tol 1e-10, x0 = b", "parallelism": "replicas",
                    "l2": "256 MiB write between timed steps (outside the step's CUDA events)"},
         "fp64_solves_per_s": world * args.steps / (ms64 * 1e-3),
+        "fp64_native_solves_per_s": world * args.steps / (ms64_native * 1e-3),
         "refined_speedup_vs_fp64": ms64 / ms32,
         "fmm_mpts_per_s": mpts,
         "solve_info": {"fp64": inf64[-1], "fp32_refined": inf32[-1]},

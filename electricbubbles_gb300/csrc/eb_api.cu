@@ -204,6 +204,7 @@ void eb_opts_default(eb_opts* o) {
   o->max_outer = 8;
   o->device = 0;
   o->graphs = 1;
+  o->df64 = 1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -232,6 +233,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.inner_tol <= 0) o.inner_tol = d.inner_tol;
     if (o.max_outer <= 0) o.max_outer = d.max_outer;
     if (o.graphs == 0) o.graphs = d.graphs;
+    if (o.df64 == 0) o.df64 = d.df64;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <vector>
 
+#include "eb_df.cuh"
 #include "eb_internal.h"
 
 namespace {
@@ -73,6 +74,43 @@ __global__ void k_charges_stokes(int n, const int* __restrict__ perm,
   pq[2 * i] = cmk<T>((T)(a.x + s * b.x), (T)(a.y + s * b.y));
   pq[2 * i + 1] = cmk<T>((T)(a.x - s * b.x), (T)(a.y - s * b.y));
   aa[i] = cmk<T>((T)(-s * a.x), (T)(s * a.y));
+}
+
+__device__ __forceinline__ float4 df4(double2 v) {
+  float hx = __double2float_rn(v.x), hy = __double2float_rn(v.y);
+  return make_float4(hx, __double2float_rn(v.x - (double)hx), hy, __double2float_rn(v.y - (double)hy));
+}
+
+// FP64 charges plus the double-float near-field data P, Q, A scaled by 1/r_leaf (the
+// near field works in leaf units).
+__global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const double2* __restrict__ dens,
+                                    const double2* __restrict__ dz, const double* __restrict__ hpt,
+                                    double s, double rinv, double2* __restrict__ qa,
+                                    double2* __restrict__ qb, float4* __restrict__ pq,
+                                    float4* __restrict__ aa) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int o = perm[i];
+  double2 u = dens[o], d = dz[o];
+  double h = hpt[o] * (1.0 / (2.0 * EB_PI));
+  double2 w = cmul<double>(u, d);
+  double2 a = make_double2(w.y * h, -w.x * h);
+  double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
+  double2 b = make_double2(v.y * h, -v.x * h);
+  qa[i] = a;
+  qb[i] = b;
+  pq[2 * i] = df4(make_double2((a.x + s * b.x) * rinv, (a.y + s * b.y) * rinv));
+  pq[2 * i + 1] = df4(make_double2((a.x - s * b.x) * rinv, (a.y - s * b.y) * rinv));
+  aa[i] = df4(make_double2(-s * a.x * rinv, s * a.y * rinv));
+}
+
+__global__ void k_charges_cauchy_df(int n, const int* __restrict__ perm, const double2* __restrict__ q,
+                                    double rinv, double2* __restrict__ qa, float4* __restrict__ qdf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 v = q[perm[i]];
+  qa[i] = v;
+  qdf[i] = df4(make_double2(v.x * rinv, v.y * rinv));
 }
 
 template <typename T>
@@ -621,6 +659,173 @@ __global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restric
   if (sl == 0 && act) out[perm[i]] = make_double2(gx, gy);
 }
 
+// ---------------------------------------------------------------------------------
+// FP64-accurate leaf evaluation in double-float arithmetic (the same sums as k_leaf64,
+// about 2^-47 relative per operation, several times faster on GB300's FP32 pipes).
+// Offsets are leaf-relative: for target i in leaf b and source j in neighbour b',
+// (z_j - z_i)/r = w_j - (w_i - (b' - b)), exact up to the double-float rounding of w;
+// the charges carry the factor 1/r. The leaf's local expansion is converted to
+// double-float once per warp into shared memory.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ cdf cdf_pow(cdf u, int n) {
+  cdf r = cdf{{1.f, 0.f}, {0.f, 0.f}}, b = u;
+  while (n > 0) {
+    if (n & 1) r = cdf_mul(r, b);
+    b = cdf_mul(b, b);
+    n >>= 1;
+  }
+  return r;
+}
+
+// (hi, mid, lo) - d for a small integer d, renormalised into three floats
+__device__ __forceinline__ float3 tf_shift(float hi, float mid, float lo, float d) {
+  dfl a = two_sum(hi, -d);
+  dfl b = two_sum(mid, a.lo);
+  return make_float3(a.hi, b.hi, __fadd_rn(lo, b.lo));
+}
+
+// (ah + am + al) - (b.x + b.y + b.z) as a double-float; the hi and mid differences are
+// formed exactly, so the result carries the full precision of the three-float inputs.
+__device__ __forceinline__ dfl tf_diff(float ah, float am, float al, float3 b) {
+  dfl s = two_sum(ah, -b.x);
+  dfl t = two_sum(am, -b.y);
+  float u = __fadd_rn(__fadd_rn(__fsub_rn(al, b.z), s.lo), t.lo);
+  dfl h = two_sum(s.hi, t.hi);
+  return fast_two_sum(h.hi, __fadd_rn(h.lo, u));
+}
+
+template <int E>
+__device__ __forceinline__ void l2p_part_df(const float4* L, int p, int sl, cdf u, bool neg, dfacc& gx,
+                                            dfacc& gy) {
+  const int ldl = p + 1, q = (ldl + 3) / 4;
+  int m0 = sl * q, m1 = min(ldl, m0 + q);
+  if (m0 >= m1) return;
+  cdf ph = cdf_from_float4(L[m1 - 1]), dph = cdf{{0.f, 0.f}, {0.f, 0.f}};
+  for (int m = m1 - 2; m >= m0; --m) {
+    dph = cdf_add(cdf_mul(dph, u), ph);
+    ph = cdf_add(cdf_mul(ph, u), cdf_from_float4(L[m]));
+  }
+  cdf ps = cdf{{0.f, 0.f}, {0.f, 0.f}};
+  if (E == 2) {
+    ps = cdf_from_float4(L[ldl + m1 - 1]);
+    for (int m = m1 - 2; m >= m0; --m) ps = cdf_add(cdf_mul(ps, u), cdf_from_float4(L[ldl + m]));
+  }
+  if (m0 > 0) {
+    cdf um1 = cdf_pow(u, m0 - 1);
+    cdf t = cdf_add(cdf_mul(u, dph), cdf{dfl_mul_f(ph.x, (float)m0), dfl_mul_f(ph.y, (float)m0)});
+    dph = cdf_mul(um1, t);
+    cdf um = cdf_mul(um1, u);
+    ph = cdf_mul(um, ph);
+    if (E == 2) ps = cdf_mul(um, ps);
+  }
+  if (E == 2) {
+    // phi + s (u conj(phi') + conj(psi))
+    dfl tx = dfl_add(dfl_mul(u.x, dph.x), dfl_mul(u.y, dph.y));
+    dfl ty = dfl_sub(dfl_mul(u.y, dph.x), dfl_mul(u.x, dph.y));
+    dfl sx = dfl_add(tx, ps.x), sy = dfl_sub(ty, ps.y);
+    if (neg) {
+      sx = dfl_neg(sx);
+      sy = dfl_neg(sy);
+    }
+    acc_dfl(gx, ph.x);
+    acc_dfl(gx, sx);
+    acc_dfl(gy, ph.y);
+    acc_dfl(gy, sy);
+  } else {
+    acc_dfl(gx, dfl_neg(ph.x));
+    acc_dfl(gy, dfl_neg(ph.y));
+  }
+}
+
+template <int E>
+__global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restrict__ gleaf,
+                                                 const int* __restrict__ gfirst, int off, int has_far,
+                                                 const unsigned long long* __restrict__ bkey,
+                                                 const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                 const int* __restrict__ ulist,
+                                                 const int* __restrict__ ucount,
+                                                 const int* __restrict__ perm,
+                                                 const float4* __restrict__ wa,
+                                                 const float2* __restrict__ wb,
+                                                 const float4* __restrict__ pq,
+                                                 const float4* __restrict__ aa, int p, double s,
+                                                 const double2* __restrict__ local,
+                                                 double2* __restrict__ out) {
+  extern __shared__ float4 sloc[];
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g >= ngroup) return;
+  const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
+  const int leaf = gleaf[g], b = off + leaf;
+  const int i = gfirst[g] + tg;
+  const bool act = i < pt1[b];
+  const int ii = act ? i : gfirst[g];
+  const float4 wia = wa[ii];
+  const float2 wib = wb[ii];
+  const cdf wi = cdf{{wia.x, wia.z}, {wia.y, wia.w}};
+  const bool neg = s < 0.0;
+  dfacc gx{0.f, 0.f}, gy{0.f, 0.f};
+  if (has_far) {
+    const int nl = E * (p + 1);
+    float4* L = sloc + (threadIdx.x >> 5) * nl;
+    const double2* lb = local + (size_t)b * nl;
+    for (int idx = lane; idx < nl; idx += 32) L[idx] = df4(lb[idx]);
+    __syncwarp();
+    l2p_part_df<E>(L, p, sl, wi, neg, gx, gy);
+  }
+  const unsigned long long kb = bkey[b];
+  const int bx = (int)compact2d(kb), by = (int)compact2d(kb >> 1);
+  const int nu = ucount[leaf];
+  for (int jl = 0; jl < nu; ++jl) {
+    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
+    const unsigned long long ks = bkey[sb];
+    // the target relative to the source leaf's centre, in leaf units (three floats)
+    const float3 tx = tf_shift(wia.x, wia.z, wib.x, (float)((int)compact2d(ks) - bx));
+    const float3 ty = tf_shift(wia.y, wia.w, wib.y, (float)((int)compact2d(ks >> 1) - by));
+    const int j1 = pt1[sb];
+    for (int j = pt0[sb] + sl; j < j1; j += 4) {
+      if (j == ii) continue;
+      const float4 ja = wa[j];
+      const float2 jb = wb[j];
+      // D / r = w_j - (w_i - offset): hi and mid parts subtracted exactly
+      const dfl dx = tf_diff(ja.x, ja.z, jb.x, tx), dy = tf_diff(ja.y, ja.w, jb.y, ty);
+      const dfl rr = dfl_rcp(dfl_add(dfl_sqr(dx), dfl_sqr(dy)));
+      const dfl ix = dfl_mul(dx, rr), iy = dfl_neg(dfl_mul(dy, rr));  // 1/D
+      if (E == 2) {
+        const cdf P = cdf_from_float4(pq[2 * j]), Q = cdf_from_float4(pq[2 * j + 1]);
+        const cdf A = cdf_from_float4(aa[j]);
+        acc_prod(gx, P.x, ix);  // qa/D + s conj(qb/D)
+        acc_prod(gx, dfl_neg(P.y), iy);
+        acc_prod(gy, Q.x, iy);
+        acc_prod(gy, Q.y, ix);
+        const dfl w2x = dfl_mul(dfl_add(ix, iy), dfl_sub(ix, iy));  // conj(1/D)^2
+        const dfl ixy = dfl_mul(ix, iy);
+        const dfl w2y = dfl{-2.f * ixy.hi, -2.f * ixy.lo};
+        const dfl t2x = dfl_sub(dfl_mul(dx, w2x), dfl_mul(dy, w2y));
+        const dfl t2y = dfl_add(dfl_mul(dx, w2y), dfl_mul(dy, w2x));
+        acc_prod(gx, A.x, t2x);  // - s D conj(qa) conj(1/D)^2
+        acc_prod(gx, dfl_neg(A.y), t2y);
+        acc_prod(gy, A.x, t2y);
+        acc_prod(gy, A.y, t2x);
+      } else {
+        const cdf q = cdf_from_float4(pq[j]);  // q/(z_i - z_j) = -q/D
+        acc_prod(gx, dfl_neg(q.x), ix);
+        acc_prod(gx, q.y, iy);
+        acc_prod(gy, dfl_neg(q.x), iy);
+        acc_prod(gy, dfl_neg(q.y), ix);
+      }
+    }
+  }
+  dfl vx = acc_value(gx), vy = acc_value(gy);
+#pragma unroll
+  for (int o = 1; o <= 2; o <<= 1) {
+    dfl ox{__shfl_xor_sync(0xffffffffu, vx.hi, o), __shfl_xor_sync(0xffffffffu, vx.lo, o)};
+    dfl oy{__shfl_xor_sync(0xffffffffu, vy.hi, o), __shfl_xor_sync(0xffffffffu, vy.lo, o)};
+    vx = (sl & o) ? dfl_add(ox, vx) : dfl_add(vx, ox);
+    vy = (sl & o) ? dfl_add(oy, vy) : dfl_add(vy, oy);
+  }
+  if (sl == 0 && act) out[perm[i]] = make_double2(dfl_to_double(vx), dfl_to_double(vy));
+}
+
 // FP32 leaf evaluation: node positions as float hi + lo so that differences are exact
 // to float precision, Kahan-compensated per-lane sums.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
@@ -878,11 +1083,25 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   EbTables& tb = f64 ? ctx->tab64 : ctx->tab32;
   EbFmmWork& w = f64 ? ctx->work64 : ctx->work32;
   const int n = t.n;
+  const bool df = f64 && ctx->opts.df64 > 0;
+  double rleaf = t.W / (double)(1 << t.L);
   EB_TRY(w.qa.ensure(sizeof(c_t<T>) * (size_t)n));
   EB_TRY(w.qb.ensure(sizeof(c_t<T>) * (size_t)n));
-  EB_TRY(w.pq.ensure(sizeof(c_t<T>) * 2 * (size_t)n));
-  EB_TRY(w.aa.ensure(sizeof(c_t<T>) * (size_t)n));
-  if (E == 2) {
+  if (df) {
+    EB_TRY(w.pqdf.ensure(sizeof(float4) * 2 * (size_t)n));
+    EB_TRY(w.aadf.ensure(sizeof(float4) * (size_t)n));
+  } else {
+    EB_TRY(w.pq.ensure(sizeof(c_t<T>) * 2 * (size_t)n));
+    EB_TRY(w.aa.ensure(sizeof(c_t<T>) * (size_t)n));
+  }
+  if (df && E == 2) {
+    k_charges_stokes_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
+                                                      1.0 / rleaf, w.qa.as<double2>(), w.qb.as<double2>(),
+                                                      w.pqdf.as<float4>(), w.aadf.as<float4>());
+  } else if (df) {
+    k_charges_cauchy_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, 1.0 / rleaf,
+                                                      w.qa.as<double2>(), w.pqdf.as<float4>());
+  } else if (E == 2) {
     k_charges_stokes<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
                                                       w.qa.as<c_t<T>>(), w.qb.as<c_t<T>>(),
                                                       w.pq.as<c_t<T>>(), w.aa.as<c_t<T>>());
@@ -893,11 +1112,18 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   const int has_far = t.L >= 2;
   if (has_far) EB_TRY((fmm_expansions<T, E>(ctx, t, tb, w)));
   else EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
-  double rleaf = t.W / (double)(1 << t.L);
   int offL = t.lev_off[t.L];
   int blocks = nblk((long long)t.ngroup * 32, 128);
   ProfScope ps(ctx, 0, st);
-  if (f64) {
+  if (df) {
+    size_t sm = sizeof(float4) * 4 * E * (size_t)(tb.p + 1);
+    k_leaf_df<E><<<blocks, 128, sm, st>>>(
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
+        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
+        (double)sign,
+        w.local.as<double2>(), out);
+  } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),

@@ -53,6 +53,8 @@ struct EbTree {
   DevBuf perm;     // int[n]: sorted index -> original index
   DevBuf zs;       // double2[n]: sorted positions
   DevBuf zhi, zlo; // float2[n]: sorted positions as float hi + lo
+  DevBuf wdf;      // float4[n]: offset from the leaf centre in leaf units, (x.hi, y.hi, x.mid, y.mid)
+  DevBuf wdf_lo;   // float2[n]: (x.lo, y.lo) of the same offset
   DevBuf keys, keys_alt, idx_alt;  // sort buffers
   DevBuf bkey;     // unsigned long long[nbox]: Morton key of the box at its level
   DevBuf pt0, pt1; // int[nbox]: point range
@@ -84,6 +86,7 @@ struct EbTables {
 struct EbFmmWork {
   DevBuf qa, qb;     // c_t<T>[n] sorted charges (P2M)
   DevBuf pq, aa;     // near-field source data (P2P)
+  DevBuf pqdf, aadf; // double-float near-field source data, scaled by 1/r_leaf (float4)
   DevBuf mpole;      // c_t<T>[nbox*E*p]
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
 };

@@ -347,6 +347,50 @@ void DevBuf::release() {
   bytes = 0;
 }
 
+// (z - x0 - (i + 1/2) r) / r, the offset of a coordinate from the centre of its leaf in
+// leaf units, with both subtractions carried exactly (two-sum, two-product), so that
+// for two nodes the offsets differ by exactly (z_j - z_i)/r minus the integer index
+// offset of their leaves, up to the final rounding (about 2^-53 of a leaf side).
+__device__ __forceinline__ double leaf_offset(double z, double x0, unsigned int i, double r) {
+  double s = __dsub_rn(z, x0);
+  double bb = __dsub_rn(s, z);
+  double e1 = __dadd_rn(__dsub_rn(z, __dsub_rn(s, bb)), __dsub_rn(-x0, bb));
+  double ci = (double)i + 0.5;
+  double c = __dmul_rn(ci, r);
+  double e2 = __fma_rn(ci, r, -c);
+  double u = __dsub_rn(s, c);
+  double bb2 = __dsub_rn(u, s);
+  double e3 = __dadd_rn(__dsub_rn(s, __dsub_rn(u, bb2)), __dsub_rn(-c, bb2));
+  return __ddiv_rn(__dadd_rn(u, __dadd_rn(__dsub_rn(e1, e2), e3)), r);
+}
+
+// Leaf-relative node coordinates as three floats hi + mid + lo (all 53 bits of the
+// double offset), for the double-float near field: wa = (x.hi, y.hi, x.mid, y.mid),
+// wb = (x.lo, y.lo). (hi, mid) alone is a double-float. One block per leaf.
+__device__ __forceinline__ void split3(double w, float& hi, float& mid, float& lo) {
+  hi = __double2float_rn(w);
+  double r1 = w - (double)hi;
+  mid = __double2float_rn(r1);
+  lo = __double2float_rn(r1 - (double)mid);
+}
+
+__global__ void k_leaf_coords(int offL, const unsigned long long* __restrict__ bkey,
+                              const int* __restrict__ pt0, const int* __restrict__ pt1,
+                              const double2* __restrict__ zs, double x0, double y0, double r,
+                              float4* __restrict__ wa, float2* __restrict__ wb) {
+  const int b = offL + blockIdx.x;
+  const unsigned long long k = bkey[b];
+  const unsigned int ix = compact2(k), iy = compact2(k >> 1);
+  for (int i = pt0[b] + threadIdx.x; i < pt1[b]; i += blockDim.x) {
+    double2 z = zs[i];
+    float xh, xm, xl, yh, ym, yl;
+    split3(leaf_offset(z.x, x0, ix, r), xh, xm, xl);
+    split3(leaf_offset(z.y, y0, iy, r), yh, ym, yl);
+    wa[i] = make_float4(xh, yh, xm, ym);
+    wb[i] = make_float2(xl, yl);
+  }
+}
+
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target) {
   cudaStream_t st = eb_stream(ctx);
   t.valid = false;
@@ -504,7 +548,15 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
                                               t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
     eb_count_launch(ctx);
   }
-  // 9. pair counts (the algorithmic work of the near field and M2L)
+  // 9. leaf-relative coordinates for the double-float near field
+  EB_TRY(t.wdf.ensure(sizeof(float4) * (size_t)n));
+  EB_TRY(t.wdf_lo.ensure(sizeof(float2) * (size_t)n));
+  k_leaf_coords<<<t.nleaf, 64, 0, st>>>(t.lev_off[L], t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                        t.pt1.as<int>(), t.zs.as<double2>(), t.x0, t.y0,
+                                        t.W / (double)(1u << L), t.wdf.as<float4>(),
+                                        t.wdf_lo.as<float2>());
+  eb_count_launch(ctx);
+  // 10. pair counts (the algorithmic work of the near field and M2L)
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(t.partial.p);
   EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
   int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;

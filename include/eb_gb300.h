@@ -67,6 +67,8 @@ typedef struct eb_opts {
   int device;       /* CUDA device ordinal                                     */
   int graphs;       /* GMRES as CUDA graphs with a device-side Arnoldi loop:
                        0 default (on), 1 on, -1 off (host-driven loop)          */
+  int df64;         /* FP64 near field (P2P + L2P) in double-float arithmetic on the
+                       FP32 pipes: 0 default (on), 1 on, -1 off (native FP64)   */
 } eb_opts;
 
 typedef struct eb_solve_info {
