@@ -190,24 +190,25 @@ def run_gpu(args, rank, world, local):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(max(args.steps, 1))]
 
-    def timed(mode, steps, warmup):
+    def timed(mode, steps, warmup, c=None):
+        c = c or ctx
         for _ in range(warmup):
-            ctx.solvei(rhs, mode, out=x)
+            c.solvei(rhs, mode, out=x)
         torch.cuda.synchronize()
         if dist:
             td.barrier()
         infos = []
         t0 = time.perf_counter()
-        l0 = ctx.launch_count()
+        l0 = c.launch_count()
         for s in range(steps):
             flush.zero_()
             ev[s][0].record(stream)
-            _, info = ctx.solvei(rhs, mode, out=x)
+            _, info = c.solvei(rhs, mode, out=x)
             ev[s][1].record(stream)
             infos.append(info)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        timed.launches = ctx.launch_count() - l0
+        timed.launches = c.launch_count() - l0
         dev_ms = sum(a.elapsed_time(b) for a, b in ev[:steps])
         if dist:
             t = torch.tensor([dev_ms], device=dev)
@@ -222,15 +223,7 @@ def run_gpu(args, rank, world, local):
     ctx_native = Context(device=local, df64=-1)
     ctx_native.set_stream(stream.cuda_stream)
     ctx_native.extractdat(cfg.nd, cfg.rku())
-    for _ in range(args.warmup):
-        ctx_native.solvei(rhs, "fp64", out=x)
-    torch.cuda.synchronize()
-    ev[0][0].record(stream)
-    for _ in range(args.steps):
-        ctx_native.solvei(rhs, "fp64", out=x)
-    ev[0][1].record(stream)
-    torch.cuda.synchronize()
-    ms64_native = ev[0][0].elapsed_time(ev[0][1])
+    ms64_native, _, _ = timed("fp64", args.steps, args.warmup, ctx_native)
     ctx_native.close()
     clocks = ClockSampler(local)
     clocks.start()

@@ -85,9 +85,8 @@ __device__ __forceinline__ float4 df4(double2 v) {
 // near field works in leaf units).
 __global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const double2* __restrict__ dens,
                                     const double2* __restrict__ dz, const double* __restrict__ hpt,
-                                    double s, double rinv, double2* __restrict__ qa,
-                                    double2* __restrict__ qb, float4* __restrict__ pq,
-                                    float4* __restrict__ aa) {
+                                    double s, double rinv, float4* __restrict__ qdf,
+                                    float4* __restrict__ pq, float4* __restrict__ aa) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int o = perm[i];
@@ -97,19 +96,18 @@ __global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const d
   double2 a = make_double2(w.y * h, -w.x * h);
   double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
   double2 b = make_double2(v.y * h, -v.x * h);
-  qa[i] = a;
-  qb[i] = b;
+  qdf[2 * i] = df4(make_double2(a.x * rinv, a.y * rinv));
+  qdf[2 * i + 1] = df4(make_double2(b.x * rinv, b.y * rinv));
   pq[2 * i] = df4(make_double2((a.x + s * b.x) * rinv, (a.y + s * b.y) * rinv));
   pq[2 * i + 1] = df4(make_double2((a.x - s * b.x) * rinv, (a.y - s * b.y) * rinv));
   aa[i] = df4(make_double2(-s * a.x * rinv, s * a.y * rinv));
 }
 
 __global__ void k_charges_cauchy_df(int n, const int* __restrict__ perm, const double2* __restrict__ q,
-                                    double rinv, double2* __restrict__ qa, float4* __restrict__ qdf) {
+                                    double rinv, float4* __restrict__ qdf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double2 v = q[perm[i]];
-  qa[i] = v;
   qdf[i] = df4(make_double2(v.x * rinv, v.y * rinv));
 }
 
@@ -408,6 +406,279 @@ __global__ void __launch_bounds__(128) k_m2l(int first, const int* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------------
+// The same M2L in double-float arithmetic (FP64-class accuracy on the FP32 pipes): the
+// multipoles, d^-j and binomial tables are double-float; each output's binomial sum is
+// accumulated with compensation; the four warps' partial expansions are added in a
+// fixed order and written as FP64.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ cdf cdf_ld(const float4* p) { return cdf_from_float4(*p); }
+__device__ __forceinline__ float4 cdf_f4(cdf v) { return make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo); }
+
+template <int NS>
+__device__ __forceinline__ void m2l_slots_df(int ob, int lane, int nout, int ldo, int pd, int p, int ldc,
+                                             const float2* C2, const float4* a, const float4* dv,
+                                             float4* acc, int ldl) {
+  int o[NS], m[NS], e[NS];
+  bool v[NS];
+  dfacc bx[NS], by[NS];
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    o[sl] = ob + lane + 32 * sl;
+    v[sl] = o[sl] < nout;
+    e[sl] = v[sl] ? o[sl] / ldo : 0;
+    m[sl] = v[sl] ? o[sl] - e[sl] * ldo : 0;
+    bx[sl] = dfacc{0.f, 0.f};
+    by[sl] = dfacc{0.f, 0.f};
+  }
+  for (int k = 0; k < pd; ++k) {
+#pragma unroll
+    for (int sl = 0; sl < NS; ++sl) {
+      const float2 c = C2[k * ldc + m[sl]];
+      const float4 av = a[e[sl] * p + k];
+      acc_prod(bx[sl], dfl{c.x, c.y}, dfl{av.x, av.y});
+      acc_prod(by[sl], dfl{c.x, c.y}, dfl{av.z, av.w});
+    }
+  }
+#pragma unroll
+  for (int sl = 0; sl < NS; ++sl) {
+    if (v[sl]) {
+      cdf post = cdf_ld(dv + m[sl]);
+      if (m[sl] & 1) post = cdf{dfl_neg(post.x), dfl_neg(post.y)};
+      float4* ap = acc + e[sl] * ldl + m[sl];
+      *ap = cdf_f4(cdf_add(cdf_from_float4(*ap), cdf_mul(post, cdf{acc_value(bx[sl]), acc_value(by[sl])})));
+    }
+  }
+}
+
+template <int E>
+__global__ void __launch_bounds__(128) k_m2l_df(int first, const int* __restrict__ vlist,
+                                                const unsigned char* __restrict__ vcode,
+                                                const int* __restrict__ vcount, int p,
+                                                const float2* __restrict__ binom, int ldb,
+                                                const float4* __restrict__ dinv,
+                                                const int* __restrict__ pdv,
+                                                const float4* __restrict__ mpole,
+                                                float4* __restrict__ local) {
+  extern __shared__ float4 smem_f4[];
+  const int ldc = p + 1, ldl = p + 1, ldd = p + 2;
+  float2* C2 = reinterpret_cast<float2*>(smem_f4);
+  float4* sa = smem_f4 + (p * ldc + 1) / 2;
+  float4* sacc = sa + 4 * E * p;
+  for (int idx = threadIdx.x; idx < p * ldc; idx += blockDim.x) {
+    int k = idx / ldc + 1, m = idx % ldc;
+    C2[idx] = binom[(size_t)(m + k - 1) * ldb + m];
+  }
+  for (int idx = threadIdx.x; idx < 4 * E * ldl; idx += blockDim.x) sacc[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = first + blockIdx.x;
+  float4* a = sa + w * E * p;
+  float4* acc = sacc + w * E * ldl;
+  const int nv = vcount[gid];
+  for (int j = w; j < nv; j += 4) {
+    const int s = vlist[(size_t)gid * EB_VMAX + j];
+    const int code = vcode[(size_t)gid * EB_VMAX + j];
+    const int pd = pdv[code];
+    const float4* dv = dinv + (size_t)code * ldd;
+    const float4* ms = mpole + (size_t)s * E * p;
+    const float dxr = (float)(code % 7 - 3), dyr = (float)(code / 7 - 3);
+    for (int kk = lane; kk < pd; kk += 32) {
+      const int k = kk + 1;
+      const cdf sc = cdf_ld(dv + k);
+      a[kk] = cdf_f4(cdf_mul(cdf_ld(ms + kk), sc));
+      if (E == 2) {
+        cdf mpsi = cdf_ld(ms + p + kk);
+        if (k >= 2) {
+          const cdf f = cdf{{-dxr * (float)(k - 1), 0.f}, {dyr * (float)(k - 1), 0.f}};
+          mpsi = cdf_add(mpsi, cdf_mul(f, cdf_ld(ms + kk - 1)));
+        }
+        a[p + kk] = cdf_f4(cdf_mul(mpsi, sc));
+      }
+    }
+    __syncwarp();
+    const int ldo = pd + 1, nout = E * ldo;
+    for (int ob = 0; ob < nout; ob += 96) {
+      int rem = nout - ob;
+      if (rem > 64) m2l_slots_df<3>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
+      else if (rem > 32) m2l_slots_df<2>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
+      else m2l_slots_df<1>(ob, lane, nout, ldo, pd, p, ldc, C2, a, dv, acc, ldl);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  const int tot = E * ldl;
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    cdf v01 = cdf_add(cdf_from_float4(sacc[idx]), cdf_from_float4(sacc[tot + idx]));
+    cdf v23 = cdf_add(cdf_from_float4(sacc[2 * tot + idx]), cdf_from_float4(sacc[3 * tot + idx]));
+    local[(size_t)gid * tot + idx] = cdf_f4(cdf_add(v01, v23));
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Upward and downward passes of the double-float pipeline: the P2M, M2M and L2L of the
+// FP64 kernels above with double-float operands and compensated sums.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ cdf cdf_zero() { return cdf{{0.f, 0.f}, {0.f, 0.f}}; }
+__device__ __forceinline__ cdf cdf_conj(cdf a) { return cdf{a.x, dfl_neg(a.y)}; }
+__device__ __forceinline__ cdf cdf_scale(cdf a, float f) { return cdf{dfl_mul_f(a.x, f), dfl_mul_f(a.y, f)}; }
+
+// acc += a * b (complex) with compensated real and imaginary sums
+__device__ __forceinline__ void cacc_mul(dfacc& rx, dfacc& ry, cdf a, cdf b) {
+  acc_prod(rx, a.x, b.x);
+  acc_prod(rx, dfl_neg(a.y), b.y);
+  acc_prod(ry, a.x, b.y);
+  acc_prod(ry, a.y, b.x);
+}
+
+// acc += c * a (c real)
+__device__ __forceinline__ void cacc_rmul(dfacc& rx, dfacc& ry, dfl c, cdf a) {
+  acc_prod(rx, c, a.x);
+  acc_prod(ry, c, a.y);
+}
+
+__device__ __forceinline__ cdf cacc_value(const dfacc& rx, const dfacc& ry) {
+  return cdf{acc_value(rx), acc_value(ry)};
+}
+
+// P2M at the leaves from the leaf-relative offsets w (units of the leaf side) and the
+// charges qa/r, qb/r: M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
+template <int E>
+__global__ void __launch_bounds__(64) k_p2m_df(int off, const int* __restrict__ pt0,
+                                               const int* __restrict__ pt1, const float4* __restrict__ wa,
+                                               const float4* __restrict__ q, int p,
+                                               float4* __restrict__ mpole) {
+  extern __shared__ float4 sm4[];
+  const int ps = p + 1;
+  float4* pw = sm4;
+  float4* sc = pw + 32 * ps;
+  const int b = off + blockIdx.x, tid = threadIdx.x;
+  dfacc Ax{0.f, 0.f}, Ay{0.f, 0.f}, Bx{0.f, 0.f}, By{0.f, 0.f}, Cx{0.f, 0.f}, Cy{0.f, 0.f};
+  const int i0 = pt0[b], i1 = pt1[b];
+  for (int base = i0; base < i1; base += 32) {
+    const int cnt = min(32, i1 - base);
+    __syncthreads();
+    if (tid < cnt) {
+      const int i = base + tid;
+      const float4 wv = wa[i];
+      const cdf w = cdf{{wv.x, wv.z}, {wv.y, wv.w}};
+      const cdf ah = cdf_from_float4(q[(size_t)E * i]);
+      sc[tid] = cdf_f4(ah);
+      if (E == 2) {
+        sc[32 + tid] = q[2 * (size_t)i + 1];
+        sc[64 + tid] = cdf_f4(cdf_mul(cdf_conj(w), ah));
+      }
+      cdf pwr = cdf{{1.f, 0.f}, {0.f, 0.f}};
+      float4* row = pw + tid * ps;
+      for (int j = 0; j < p; ++j) {
+        row[j] = cdf_f4(pwr);
+        pwr = cdf_mul(pwr, w);
+      }
+    }
+    __syncthreads();
+    if (tid < p) {
+      for (int s = 0; s < cnt; ++s) {
+        const cdf v = cdf_from_float4(pw[s * ps + tid]);
+        cacc_mul(Ax, Ay, cdf_from_float4(sc[s]), v);
+        if (E == 2) {
+          cacc_mul(Bx, By, cdf_from_float4(sc[32 + s]), v);
+          cacc_mul(Cx, Cy, cdf_from_float4(sc[64 + s]), v);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < p) pw[tid] = cdf_f4(cacc_value(Cx, Cy));
+  __syncthreads();
+  if (tid < p) {
+    float4* mp = mpole + (size_t)b * E * p;
+    const cdf A = cacc_value(Ax, Ay);
+    mp[tid] = cdf_f4(cdf{dfl_neg(A.x), dfl_neg(A.y)});
+    if (E == 2) {
+      cdf v = cacc_value(Bx, By);
+      if (tid >= 1) v = cdf_add(v, cdf_scale(cdf_from_float4(pw[tid - 1]), (float)tid));
+      mp[p + tid] = cdf_f4(cdf{dfl_neg(v.x), dfl_neg(v.y)});
+    }
+  }
+}
+
+template <int E>
+__global__ void k_m2m_df(int offp, const unsigned long long* __restrict__ bkey,
+                         const int* __restrict__ child0, const int* __restrict__ nchild, int p,
+                         const float2* __restrict__ binom, int ldb, const float4* __restrict__ epow2,
+                         const float4* __restrict__ einv, float4* __restrict__ mpole) {
+  extern __shared__ float4 sm4[];
+  float4* a = sm4;  // [child][E*p]
+  const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
+  const int e = tid / p, nn = tid - e * p;
+  const int c0 = child0[P], nc = nchild[P];
+  for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
+    const int ci = idx / nout, o = idx - ci * nout;
+    const int c = c0 + ci, q = quadrant(bkey[c]);
+    const int e2 = o / p, kk = o - e2 * p, k = kk + 1;
+    const float4* mc = mpole + (size_t)c * nout;
+    cdf v = cdf_from_float4(mc[o]);
+    if (e2 == 1 && k >= 2) {
+      const cdf ec = cdf_scale(cdf_from_float4(epow2[q * ld + 1]), 2.f);
+      v = cdf_add(v, cdf_mul(cdf_scale(cdf_conj(ec), (float)(k - 1)), cdf_from_float4(mc[kk - 1])));
+    }
+    a[idx] = cdf_f4(cdf_mul(v, cdf_from_float4(einv[q * ld + k])));
+  }
+  __syncthreads();
+  if (tid < nout) {
+    const int n = nn + 1;
+    const float2* brow = binom + (size_t)(n - 1) * ldb;
+    dfacc rx{0.f, 0.f}, ry{0.f, 0.f};
+    for (int ci = 0; ci < nc; ++ci) {
+      const int q = quadrant(bkey[c0 + ci]);
+      const float4* ae = a + ci * nout + e * p;
+      dfacc sx{0.f, 0.f}, sy{0.f, 0.f};
+      for (int k = 0; k < n; ++k) cacc_rmul(sx, sy, dfl{brow[k].x, brow[k].y}, cdf_from_float4(ae[k]));
+      cacc_mul(rx, ry, cdf_from_float4(epow2[q * ld + n]), cacc_value(sx, sy));
+    }
+    mpole[(size_t)P * nout + tid] = cdf_f4(cacc_value(rx, ry));
+  }
+}
+
+template <int E>
+__global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
+                         const int* __restrict__ parent, int p, const float2* __restrict__ binom,
+                         int ldb, const float4* __restrict__ epow2, const float4* __restrict__ einv,
+                         float4* __restrict__ local) {
+  extern __shared__ float4 sm4[];
+  float4* a = sm4;
+  const int ldl = p + 1, ld = p + 2, nout = E * ldl, tid = threadIdx.x;
+  const int c = offc + blockIdx.x;
+  const int P = parent[c];
+  const int q = quadrant(bkey[c]);
+  const cdf eh = cdf_from_float4(epow2[q * ld + 1]);
+  const float4* lp = local + (size_t)P * nout;
+  for (int idx = tid; idx < nout; idx += blockDim.x) {
+    const int e2 = idx / ldl, m = idx - e2 * ldl;
+    cdf v = cdf_from_float4(lp[idx]);
+    if (e2 == 1 && m < p)
+      v = cdf_add(v, cdf_mul(cdf_scale(cdf_conj(eh), (float)(m + 1)), cdf_from_float4(lp[m + 1])));
+    a[idx] = cdf_f4(cdf_mul(v, cdf_from_float4(epow2[q * ld + m])));
+  }
+  __syncthreads();
+  if (tid < nout) {
+    const int e = tid / ldl, j = tid - e * ldl;
+    const float4* ae = a + e * ldl;
+    dfacc sx{0.f, 0.f}, sy{0.f, 0.f};
+    for (int m = j; m <= p; ++m) {
+      const float2 bm = binom[(size_t)m * ldb + j];
+      cacc_rmul(sx, sy, dfl{bm.x, bm.y}, cdf_from_float4(ae[m]));
+    }
+    float4* lc = local + (size_t)c * nout;
+    dfacc rx{0.f, 0.f}, ry{0.f, 0.f};
+    const cdf old = cdf_from_float4(lc[tid]);
+    acc_dfl(rx, old.x);
+    acc_dfl(ry, old.y);
+    cacc_mul(rx, ry, cdf_from_float4(einv[q * ld + j]), cacc_value(sx, sy));
+    lc[tid] = cdf_f4(cacc_value(rx, ry));
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // Upward pass in one launch: one block per leaf forms the leaf's multipole (P2M), then
 // climbs: after writing a box's multipole it increments the parent's arrival counter,
 // and the block that delivers the last child forms the parent's multipole (M2M) from
@@ -664,8 +935,7 @@ __global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restric
 // about 2^-47 relative per operation, several times faster on GB300's FP32 pipes).
 // Offsets are leaf-relative: for target i in leaf b and source j in neighbour b',
 // (z_j - z_i)/r = w_j - (w_i - (b' - b)), exact up to the double-float rounding of w;
-// the charges carry the factor 1/r. The leaf's local expansion is converted to
-// double-float once per warp into shared memory.
+// the charges carry the factor 1/r. The local expansions are double-float already.
 // ---------------------------------------------------------------------------------
 __device__ __forceinline__ cdf cdf_pow(cdf u, int n) {
   cdf r = cdf{{1.f, 0.f}, {0.f, 0.f}}, b = u;
@@ -749,9 +1019,8 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
                                                  const float2* __restrict__ wb,
                                                  const float4* __restrict__ pq,
                                                  const float4* __restrict__ aa, int p, double s,
-                                                 const double2* __restrict__ local,
+                                                 const float4* __restrict__ local,
                                                  double2* __restrict__ out) {
-  extern __shared__ float4 sloc[];
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -764,14 +1033,7 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   const cdf wi = cdf{{wia.x, wia.z}, {wia.y, wia.w}};
   const bool neg = s < 0.0;
   dfacc gx{0.f, 0.f}, gy{0.f, 0.f};
-  if (has_far) {
-    const int nl = E * (p + 1);
-    float4* L = sloc + (threadIdx.x >> 5) * nl;
-    const double2* lb = local + (size_t)b * nl;
-    for (int idx = lane; idx < nl; idx += 32) L[idx] = df4(lb[idx]);
-    __syncwarp();
-    l2p_part_df<E>(L, p, sl, wi, neg, gx, gy);
-  }
+  if (has_far) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
   const unsigned long long kb = bkey[b];
   const int bx = (int)compact2d(kb), by = (int)compact2d(kb >> 1);
   const int nu = ucount[leaf];
@@ -977,6 +1239,31 @@ int tables_build(EbTables& tb, int p, double tol) {
   EB_CUDA_TRY(cudaMemcpy(tb.pd.p, pd.data(), sizeof(int) * pd.size(), cudaMemcpyHostToDevice));
   EB_CUDA_TRY(cudaMemcpy(tb.epow.p, epow2.data(), sizeof(c_t<T>) * epow2.size(), cudaMemcpyHostToDevice));
   EB_CUDA_TRY(cudaMemcpy(tb.einv.p, einv.data(), sizeof(c_t<T>) * einv.size(), cudaMemcpyHostToDevice));
+  if (sizeof(T) == 8) {
+    auto split = [](double v, float& h, float& l) {
+      h = (float)v;
+      l = (float)(v - (double)h);
+    };
+    std::vector<float2> bdf(bd.size());
+    for (size_t i = 0; i < bd.size(); ++i) split(bd[i], bdf[i].x, bdf[i].y);
+    auto to_df = [&](const std::vector<c_t<T>>& v) {
+      std::vector<float4> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        split((double)v[i].x, o[i].x, o[i].y);
+        split((double)v[i].y, o[i].z, o[i].w);
+      }
+      return o;
+    };
+    std::vector<float4> ddf = to_df(dinv), edf = to_df(epow2), idf = to_df(einv);
+    EB_TRY(tb.binom_df.ensure(sizeof(float2) * bdf.size()));
+    EB_TRY(tb.dinv_df.ensure(sizeof(float4) * ddf.size()));
+    EB_TRY(tb.epow_df.ensure(sizeof(float4) * edf.size()));
+    EB_TRY(tb.einv_df.ensure(sizeof(float4) * idf.size()));
+    EB_CUDA_TRY(cudaMemcpy(tb.binom_df.p, bdf.data(), sizeof(float2) * bdf.size(), cudaMemcpyHostToDevice));
+    EB_CUDA_TRY(cudaMemcpy(tb.dinv_df.p, ddf.data(), sizeof(float4) * ddf.size(), cudaMemcpyHostToDevice));
+    EB_CUDA_TRY(cudaMemcpy(tb.epow_df.p, edf.data(), sizeof(float4) * edf.size(), cudaMemcpyHostToDevice));
+    EB_CUDA_TRY(cudaMemcpy(tb.einv_df.p, idf.data(), sizeof(float4) * idf.size(), cudaMemcpyHostToDevice));
+  }
   return EB_OK;
 }
 
@@ -1000,6 +1287,57 @@ struct ProfScope {
 
 // Upward pass, M2L and downward pass, shared by both kernels. Leaves the local
 // expansions of every box in w.local.
+// Expansions of the double-float pipeline (FP64-class accuracy on the FP32 pipes):
+// P2M, M2M per level, M2L, L2L per level; multipoles and locals stay double-float.
+template <int E>
+int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
+  cudaStream_t st = eb_stream(ctx);
+  const int p = tb.p, L = t.L;
+  const int ldb = 2 * p + 2;
+  EB_TRY(w.mpole_df.ensure(sizeof(float4) * (size_t)t.nbox * E * p));
+  EB_TRY(w.local_df.ensure(sizeof(float4) * (size_t)t.nbox * E * (p + 1)));
+  float4* mp = w.mpole_df.as<float4>();
+  float4* lo = w.local_df.as<float4>();
+  {
+    size_t sm = sizeof(float4) * (32 * (size_t)(p + 1) + 96);
+    if (sm > 48 * 1024) EB_CUDA_TRY(cudaFuncSetAttribute(k_p2m_df<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_p2m_df<E><<<t.nleaf, 64, sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
+                                          E == 2 ? w.qdf.as<float4>() : w.pqdf.as<float4>(), p, mp);
+    eb_count_launch(ctx);
+  }
+  for (int l = L - 1; l >= 2; --l) {
+    int nb = t.lev_off[l + 1] - t.lev_off[l];
+    size_t sm = sizeof(float4) * 4 * E * p;
+    k_m2m_df<E><<<nb, round32(E * p), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(), t.child0.as<int>(),
+                                                t.nchild.as<int>(), p, tb.binom_df.as<float2>(), ldb,
+                                                tb.epow_df.as<float4>(), tb.einv_df.as<float4>(), mp);
+    eb_count_launch(ctx);
+  }
+  {
+    int first = t.lev_off[2], nt = t.nbox - first;
+    size_t sm = sizeof(float4) * ((size_t)(p * (p + 1) + 1) / 2 + 4 * E * (size_t)(2 * p + 1));
+    if (sm > 48 * 1024)
+      EB_CUDA_TRY(cudaFuncSetAttribute(k_m2l_df<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    ProfScope ps(ctx, 1, st);
+    if (nt > 0) {
+      k_m2l_df<E><<<nt, 128, sm, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(), t.vcount.as<int>(),
+                                       p, tb.binom_df.as<float2>(), ldb, tb.dinv_df.as<float4>(), tb.pd.as<int>(),
+                                       mp, lo);
+      eb_count_launch(ctx);
+    }
+    ps.done();
+  }
+  for (int l = 3; l <= L; ++l) {
+    int nb = t.lev_off[l + 1] - t.lev_off[l];
+    size_t sm = sizeof(float4) * E * (p + 1);
+    k_l2l_df<E><<<nb, round32(E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
+                                                     t.parent.as<int>(), p, tb.binom_df.as<float2>(), ldb,
+                                                     tb.epow_df.as<float4>(), tb.einv_df.as<float4>(), lo);
+    eb_count_launch(ctx);
+  }
+  return EB_OK;
+}
+
 template <typename T, int E>
 int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   cudaStream_t st = eb_stream(ctx);
@@ -1085,22 +1423,23 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   const int n = t.n;
   const bool df = f64 && ctx->opts.df64 > 0;
   double rleaf = t.W / (double)(1 << t.L);
-  EB_TRY(w.qa.ensure(sizeof(c_t<T>) * (size_t)n));
-  EB_TRY(w.qb.ensure(sizeof(c_t<T>) * (size_t)n));
   if (df) {
     EB_TRY(w.pqdf.ensure(sizeof(float4) * 2 * (size_t)n));
     EB_TRY(w.aadf.ensure(sizeof(float4) * (size_t)n));
+    EB_TRY(w.qdf.ensure(sizeof(float4) * 2 * (size_t)n));
   } else {
+    EB_TRY(w.qa.ensure(sizeof(c_t<T>) * (size_t)n));
+    EB_TRY(w.qb.ensure(sizeof(c_t<T>) * (size_t)n));
     EB_TRY(w.pq.ensure(sizeof(c_t<T>) * 2 * (size_t)n));
     EB_TRY(w.aa.ensure(sizeof(c_t<T>) * (size_t)n));
   }
   if (df && E == 2) {
     k_charges_stokes_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
-                                                      1.0 / rleaf, w.qa.as<double2>(), w.qb.as<double2>(),
-                                                      w.pqdf.as<float4>(), w.aadf.as<float4>());
+                                                      1.0 / rleaf, w.qdf.as<float4>(), w.pqdf.as<float4>(),
+                                                      w.aadf.as<float4>());
   } else if (df) {
     k_charges_cauchy_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, 1.0 / rleaf,
-                                                      w.qa.as<double2>(), w.pqdf.as<float4>());
+                                                      w.pqdf.as<float4>());
   } else if (E == 2) {
     k_charges_stokes<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
                                                       w.qa.as<c_t<T>>(), w.qb.as<c_t<T>>(),
@@ -1110,19 +1449,22 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   }
   eb_count_launch(ctx);
   const int has_far = t.L >= 2;
-  if (has_far) EB_TRY((fmm_expansions<T, E>(ctx, t, tb, w)));
-  else EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
+  if (has_far && df) EB_TRY(fmm_expansions_df<E>(ctx, t, tb, w));
+  else if (has_far) EB_TRY((fmm_expansions<T, E>(ctx, t, tb, w)));
+  if (!has_far) {
+    EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
+    EB_TRY(w.local_df.ensure(sizeof(float4) * (size_t)(E * (tb.p + 1))));
+  }
   int offL = t.lev_off[t.L];
   int blocks = nblk((long long)t.ngroup * 32, 128);
   ProfScope ps(ctx, 0, st);
   if (df) {
-    size_t sm = sizeof(float4) * 4 * E * (size_t)(tb.p + 1);
-    k_leaf_df<E><<<blocks, 128, sm, st>>>(
+    k_leaf_df<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign,
-        w.local.as<double2>(), out);
+        w.local_df.as<float4>(), out);
   } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),

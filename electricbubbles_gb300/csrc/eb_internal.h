@@ -81,12 +81,20 @@ struct EbTables {
   DevBuf pd;      // int[EB_NCODE]: per-offset truncation order
   DevBuf epow;    // c_t<T>[4*(p+2)]: e_q^j for the 4 child offsets (child units)
   DevBuf einv;    // c_t<T>[4*(p+2)]: e_q^-j
+  // double-float copies (FP64 tables only) for the double-float M2L
+  DevBuf binom_df;  // float2[(2p+2)*(2p+2)]
+  DevBuf dinv_df;   // float4[EB_NCODE*(p+2)]
+  DevBuf epow_df;   // float4[4*(p+2)]
+  DevBuf einv_df;   // float4[4*(p+2)]
 };
 
 struct EbFmmWork {
   DevBuf qa, qb;     // c_t<T>[n] sorted charges (P2M)
   DevBuf pq, aa;     // near-field source data (P2P)
   DevBuf pqdf, aadf; // double-float near-field source data, scaled by 1/r_leaf (float4)
+  DevBuf mpole_df;   // float4[nbox*E*p]: multipoles, double-float pipeline
+  DevBuf local_df;   // float4[nbox*E*(p+1)]: local expansions, double-float pipeline
+  DevBuf qdf;        // float4[2n]: qa/r, qb/r as double-float (P2M)
   DevBuf mpole;      // c_t<T>[nbox*E*p]
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
 };
