@@ -679,59 +679,74 @@ __global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
 }
 
 // ---------------------------------------------------------------------------------
-// Upward pass in one launch: one block per leaf forms the leaf's multipole (P2M), then
-// climbs: after writing a box's multipole it increments the parent's arrival counter,
-// and the block that delivers the last child forms the parent's multipole (M2M) from
-// all children in their fixed order. The counters are cleared before each launch.
-// M2M: with e the child centre offset in child units and a_k = e^-k M_k,
-//   M'_n = (e/2)^n sum_{k<=n} C(n-1,k-1) a_k, after psi_k += conj(e) (k-1) phi_{k-1}.
-// P2M (SLMKXP, cadap2.f:412-468, scaled and centre-relative): the leaf's points, 32 at
-// a time, write their powers w^j to shared memory; thread j forms the power sums
-//   A_j = sum a w^j, B_j = sum b w^j, C_j = sum conj(w) a w^j (a = qa/r, b = qb/r),
-// and M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
+// FP32 multipoles of every box of levels 2..L directly from its points, in parallel
+// over all levels (no dependent M2M chain): one block per chunk of at most EB_CHUNK
+// points forms that chunk's contribution (the P2M sums of SLMKXP, cadap2.f:412-468,
+// scaled by the box side and relative to the box centre), and k_chunk_sum adds the
+// chunks of each box in order. The offset of a point from an ancestor's centre in the
+// ancestor's units is u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2 from its leaf offset
+// u and leaf grid index i, exact apart from the rounding of u.
 // ---------------------------------------------------------------------------------
-template <typename T, int E>
-__device__ void p2m_block(int b, const unsigned long long* __restrict__ bkey,
-                          const int* __restrict__ pt0, const int* __restrict__ pt1,
-                          const double2* __restrict__ zs, const c_t<T>* __restrict__ qa,
-                          const c_t<T>* __restrict__ qb, double x0, double y0, double r, int p,
-                          c_t<T>* __restrict__ mpole, c_t<T>* smem) {
-  const int ps = p + 1;  // odd row stride: conflict-free rows
-  c_t<T>* pw = smem;
-  c_t<T>* sc = pw + 32 * ps;
-  const int tid = threadIdx.x;
-  double2 c = box_center(bkey[b], x0, y0, r);
-  const T rinv = (T)(1.0 / r);
-  c_t<T> A = cmk<T>(0, 0), B = cmk<T>(0, 0), C = cmk<T>(0, 0);
-  int i0 = pt0[b], i1 = pt1[b];
+struct LevOff {
+  int v[EB_KEY_LEVELS + 2];
+};
+
+template <int E>
+__global__ void __launch_bounds__(64) k_p2m_chunks(int L, int lmin, LevOff lo, int first2,
+                                                   const int* __restrict__ chunk_box,
+                                                   const int* __restrict__ cstart,
+                                                   const unsigned long long* __restrict__ keys,
+                                                   const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                   const float4* __restrict__ wa, const float2* __restrict__ qa,
+                                                   const float2* __restrict__ qb, double W, int p,
+                                                   float2* __restrict__ mpart) {
+  extern __shared__ float2 sm2[];
+  const int ps = p + 1;
+  float2* pw = sm2;
+  float2* sc = pw + 32 * ps;
+  const int c = blockIdx.x, tid = threadIdx.x;
+  const int b = chunk_box[c];
+  int l = lmin;
+  while (l < L && b >= lo.v[l + 1]) ++l;
+  const int sh = L - l;
+  const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
+  const float rinv = (float)((double)(1u << l) / W);
+  const int i0 = pt0[b] + (c - cstart[b - first2]) * EB_CHUNK;
+  const int i1 = min(pt1[b], i0 + EB_CHUNK);
+  const int lshift = 2 * (EB_KEY_LEVELS - L);
+  float2 A = make_float2(0.f, 0.f), B = A, C = A;
   for (int base = i0; base < i1; base += 32) {
-    int cnt = min(32, i1 - base);
+    const int cnt = min(32, i1 - base);
     __syncthreads();
     if (tid < cnt) {
-      int i = base + tid;
-      double2 zi = zs[i];
-      c_t<T> w = cmk<T>((T)((zi.x - c.x) / r), (T)((zi.y - c.y) / r));
-      c_t<T> ah = cscale<T>(qa[i], rinv);
+      const int i = base + tid;
+      const unsigned long long kl = keys[i] >> lshift;
+      const unsigned int ix = compact2d(kl), iy = compact2d(kl >> 1);
+      const float4 wv = wa[i];
+      const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
+      const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
+      const float2 w = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
+      const float2 ah = cscale<float>(qa[i], rinv);
       sc[tid] = ah;
       if (E == 2) {
-        sc[32 + tid] = cscale<T>(qb[i], rinv);
-        sc[64 + tid] = cmul<T>(cconj<T>(w), ah);
+        sc[32 + tid] = cscale<float>(qb[i], rinv);
+        sc[64 + tid] = cmul<float>(cconj<float>(w), ah);
       }
-      c_t<T> pwr = cmk<T>(1, 0);
-      c_t<T>* row = pw + tid * ps;
+      float2 pwr = make_float2(1.f, 0.f);
+      float2* row = pw + tid * ps;
       for (int j = 0; j < p; ++j) {
         row[j] = pwr;
-        pwr = cmul<T>(pwr, w);
+        pwr = cmul<float>(pwr, w);
       }
     }
     __syncthreads();
     if (tid < p) {
       for (int s = 0; s < cnt; ++s) {
-        c_t<T> v = pw[s * ps + tid];
-        cfma<T>(A, sc[s], v);
+        const float2 v = pw[s * ps + tid];
+        cfma<float>(A, sc[s], v);
         if (E == 2) {
-          cfma<T>(B, sc[32 + s], v);
-          cfma<T>(C, sc[64 + s], v);
+          cfma<float>(B, sc[32 + s], v);
+          cfma<float>(C, sc[64 + s], v);
         }
       }
     }
@@ -740,90 +755,70 @@ __device__ void p2m_block(int b, const unsigned long long* __restrict__ bkey,
   if (tid < p) pw[tid] = C;
   __syncthreads();
   if (tid < p) {
-    c_t<T>* mp = mpole + (size_t)b * E * p;
-    mp[tid] = cmk<T>(-A.x, -A.y);
+    float2* mp = mpart + (size_t)c * E * p;
+    mp[tid] = make_float2(-A.x, -A.y);
     if (E == 2) {
-      c_t<T> v = B;
-      if (tid >= 1) crfma<T>(v, (T)tid, pw[tid - 1]);
-      mp[p + tid] = cmk<T>(-v.x, -v.y);
+      float2 v = B;
+      if (tid >= 1) crfma<float>(v, (float)tid, pw[tid - 1]);
+      mp[p + tid] = make_float2(-v.x, -v.y);
     }
   }
 }
 
-template <typename T>
-__device__ __forceinline__ c_t<T> ldcg_c(const c_t<T>* p);
-template <>
-__device__ __forceinline__ double2 ldcg_c<double>(const double2* p) {
-  return __ldcg(p);
-}
-template <>
-__device__ __forceinline__ float2 ldcg_c<float>(const float2* p) {
-  return __ldcg(p);
+// M2M into the boxes of one level from their children (FP32 coarse levels): all
+// children's shifted coefficients are staged in one round of loads, then each output
+// sums over the children in their fixed order.
+template <int E>
+__global__ void k_m2m_f32(int offp, const unsigned long long* __restrict__ bkey,
+                          const int* __restrict__ child0, const int* __restrict__ nchild, int p,
+                          const float* __restrict__ binom, int ldb, const float2* __restrict__ epow2,
+                          const float2* __restrict__ einv, float2* __restrict__ mpole) {
+  extern __shared__ float2 sm2[];
+  float2* a = sm2;
+  const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
+  const int c0 = child0[P], nc = nchild[P];
+  for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
+    const int ci = idx / nout, o = idx - ci * nout;
+    const int c = c0 + ci, q = quadrant(bkey[c]);
+    const int e2 = o / p, kk = o - e2 * p, k = kk + 1;
+    const float2* mc = mpole + (size_t)c * nout;
+    float2 v = mc[o];
+    if (e2 == 1 && k >= 2) {
+      const float2 ec = cscale<float>(epow2[q * ld + 1], 2.f);
+      cfma<float>(v, cscale<float>(cconj<float>(ec), (float)(k - 1)), mc[kk - 1]);
+    }
+    a[idx] = cmul<float>(v, einv[q * ld + k]);
+  }
+  __syncthreads();
+  if (tid < nout) {
+    const int e = tid / p, n = tid - e * p + 1;
+    const float* brow = binom + (size_t)(n - 1) * ldb;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int ci = 0; ci < nc; ++ci) {
+      const int q = quadrant(bkey[c0 + ci]);
+      const float2* ae = a + ci * nout + e * p;
+      float2 s0 = make_float2(0.f, 0.f), s1 = s0;
+      int k = 0;
+      for (; k + 1 < n; k += 2) {
+        crfma<float>(s0, brow[k], ae[k]);
+        crfma<float>(s1, brow[k + 1], ae[k + 1]);
+      }
+      if (k < n) crfma<float>(s0, brow[k], ae[k]);
+      cfma<float>(acc, epow2[q * ld + n], cadd<float>(s0, s1));
+    }
+    mpole[(size_t)P * nout + tid] = acc;
+  }
 }
 
-template <typename T, int E>
-__global__ void k_upward(int offL, int L, const unsigned long long* __restrict__ bkey,
-                         const int* __restrict__ pt0, const int* __restrict__ pt1,
-                         const int* __restrict__ parent, const int* __restrict__ child0,
-                         const int* __restrict__ nchild, const double2* __restrict__ zs,
-                         const c_t<T>* __restrict__ qa, const c_t<T>* __restrict__ qb, double x0,
-                         double y0, double rleaf, int p, const T* __restrict__ binom, int ldb,
-                         const c_t<T>* __restrict__ epow2, const c_t<T>* __restrict__ einv,
-                         int* __restrict__ arrivals, c_t<T>* mpole) {
-  extern __shared__ unsigned char smem_raw[];
-  c_t<T>* smem = reinterpret_cast<c_t<T>*>(smem_raw);
-  __shared__ int s_last;
-  const int tid = threadIdx.x, ld = p + 2, nout = E * p;
-  int cur = offL + blockIdx.x;
-  p2m_block<T, E>(cur, bkey, pt0, pt1, zs, qa, qb, x0, y0, rleaf, p, mpole, smem);
-  const int e = tid / p, nn = tid - e * p;
-  for (int lev = L; lev > 2; --lev) {
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-      int P = parent[cur];
-      s_last = (atomicAdd(&arrivals[P], 1) == nchild[P] - 1);
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    cur = parent[cur];
-    // M2M into box `cur`: all children's shifted coefficients are staged in one round
-    // of loads, then each output sums over the children in their fixed order.
-    c_t<T>* a = smem;
-    const int c0 = child0[cur], nc = nchild[cur];
-    for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
-      int ci = idx / nout, o = idx - ci * nout;
-      int c = c0 + ci;
-      int q = quadrant(bkey[c]);
-      int e2 = o / p, kk = o - e2 * p, k = kk + 1;
-      const c_t<T>* mc = mpole + (size_t)c * nout;
-      c_t<T> v = ldcg_c<T>(mc + o);
-      if (e2 == 1 && k >= 2) {
-        c_t<T> ec = cscale<T>(epow2[q * ld + 1], (T)2);
-        cfma<T>(v, cscale<T>(cconj<T>(ec), (T)(k - 1)), ldcg_c<T>(mc + kk - 1));
-      }
-      a[idx] = cmul<T>(v, einv[q * ld + k]);
-    }
-    __syncthreads();
-    if (tid < nout) {
-      const int n = nn + 1;
-      const T* brow = binom + (size_t)(n - 1) * ldb;
-      c_t<T> acc = cmk<T>(0, 0);
-      for (int ci = 0; ci < nc; ++ci) {
-        const int q = quadrant(bkey[c0 + ci]);
-        const c_t<T>* ae = a + ci * nout + e * p;
-        c_t<T> s0 = cmk<T>(0, 0), s1 = cmk<T>(0, 0);
-        int k = 0;
-        for (; k + 1 < n; k += 2) {
-          crfma<T>(s0, brow[k], ae[k]);
-          crfma<T>(s1, brow[k + 1], ae[k + 1]);
-        }
-        if (k < n) crfma<T>(s0, brow[k], ae[k]);
-        cfma<T>(acc, epow2[q * ld + n], cadd<T>(s0, s1));
-      }
-      mpole[(size_t)cur * nout + tid] = acc;
-    }
+// mpole[b] = sum of the chunk partials of box b, in chunk order
+__global__ void k_chunk_sum(int first2, int nout, const int* __restrict__ cstart,
+                            const float2* __restrict__ mpart, float2* __restrict__ mpole) {
+  const int bb = blockIdx.x;
+  const int c0 = cstart[bb], c1 = cstart[bb + 1];
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+    float2 s = mpart[(size_t)c0 * nout + o];
+    for (int c = c0 + 1; c < c1; ++c) s = cadd<float>(s, mpart[(size_t)c * nout + o]);
+    mpole[(size_t)(first2 + bb) * nout + o] = s;
   }
 }
 
@@ -1345,24 +1340,34 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   const int ldb = 2 * p + 2;
   EB_TRY(w.mpole.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * p));
   EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * (p + 1)));
-  EB_TRY(t.arrive.ensure(sizeof(int) * (size_t)t.nbox));
   double rleaf = t.W / (double)(1 << L);
   int offL = t.lev_off[L];
-  // Upward pass. FP32: one launch (P2M plus climbing M2M), whose short chain of
-  // dependent steps matters more than its extra arithmetic. FP64: P2M and one M2M launch
-  // per level, which keep the slow FP64 pipe busier.
+  // Upward pass. FP32: direct P2M for every box of levels 2..L (chunks, then their
+  // sum), no dependent chain of M2M steps. FP64: P2M and one M2M launch per level.
   if (sizeof(T) == 4) {
-    EB_CUDA_TRY(cudaMemsetAsync(t.arrive.p, 0, sizeof(int) * (size_t)t.nbox, st));
-    size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
-    // enough threads to stage all four children of a box in one round for p <= 20
-    int bs = std::max(160, round32(E * p));
-    k_upward<T, E><<<t.nleaf, bs, sm, st>>>(offL, L, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
-                                            t.pt1.as<int>(), t.parent.as<int>(), t.child0.as<int>(),
-                                            t.nchild.as<int>(), t.zs.as<double2>(), w.qa.as<c_t<T>>(),
-                                            w.qb.as<c_t<T>>(), t.x0, t.y0, rleaf, p, tb.binom.as<T>(),
-                                            ldb, tb.epow.as<c_t<T>>(), tb.einv.as<c_t<T>>(),
-                                            t.arrive.as<int>(), w.mpole.as<c_t<T>>());
-    eb_count_launch(ctx);
+    const int lmin = t.chunk_lmin;
+    const int first2 = t.lev_off[lmin], nb2 = t.nbox - first2, nout = E * p;
+    EB_TRY(w.mpart.ensure(sizeof(float2) * (size_t)t.nchunk * nout));
+    LevOff lo;
+    for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) lo.v[l] = t.lev_off[l];
+    size_t sm = sizeof(float2) * (32 * (size_t)(p + 1) + 96);
+    k_p2m_chunks<E><<<t.nchunk, 64, sm, st>>>(L, lmin, lo, first2, t.chunk_box.as<int>(), t.cstart.as<int>(),
+                                             t.keys.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                             t.wdf.as<float4>(), reinterpret_cast<const float2*>(w.qa.p),
+                                             reinterpret_cast<const float2*>(w.qb.p), t.W, p,
+                                             w.mpart.as<float2>());
+    k_chunk_sum<<<nb2, round32(nout), 0, st>>>(first2, nout, t.cstart.as<int>(), w.mpart.as<float2>(),
+                                               reinterpret_cast<float2*>(w.mpole.p));
+    ctx->launches += 2;
+    for (int l = lmin - 1; l >= 2; --l) {
+      int nb = t.lev_off[l + 1] - t.lev_off[l];
+      size_t sm2 = sizeof(float2) * 4 * (size_t)nout;
+      k_m2m_f32<E><<<nb, std::max(128, round32(nout)), sm2, st>>>(
+          t.lev_off[l], t.bkey.as<unsigned long long>(), t.child0.as<int>(), t.nchild.as<int>(), p,
+          reinterpret_cast<const float*>(tb.binom.p), ldb, reinterpret_cast<const float2*>(tb.epow.p),
+          reinterpret_cast<const float2*>(tb.einv.p), reinterpret_cast<float2*>(w.mpole.p));
+      eb_count_launch(ctx);
+    }
   } else {
     size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
     k_p2m<T, E><<<t.nleaf, 64, sm, st>>>(offL, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),

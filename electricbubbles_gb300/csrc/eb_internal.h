@@ -67,11 +67,19 @@ struct EbTree {
   DevBuf ucount;   // int[nleaf]
   // near-field work items: groups of up to EB_GROUP targets of one leaf
   int ngroup = 0;
-  DevBuf arrive;   // int[nbox]: children delivered in the upward pass (cleared per apply)
   DevBuf gleaf;    // int[ngroup]: leaf index (0-based within the leaf level)
   DevBuf gfirst;   // int[ngroup]: first sorted target of the group
   DevBuf flags, scan, hist, bbox, partial, cubtmp;
+  // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
+  // EB_CHUNK points (coarser levels by M2M)
+  int nchunk = 0;
+  int chunk_lmin = 2;
+  DevBuf ccount;     // int[nbox - lev_off[chunk_lmin]]: chunks per box
+  DevBuf cstart;     // int[nbox - lev_off[chunk_lmin] + 1]: first chunk of each box
+  DevBuf chunk_box;  // int[nchunk]: the box of each chunk
 };
+#define EB_CHUNK 64
+#define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
 
 // Per-precision constant tables for the translation operators.
 struct EbTables {
@@ -96,6 +104,7 @@ struct EbFmmWork {
   DevBuf local_df;   // float4[nbox*E*(p+1)]: local expansions, double-float pipeline
   DevBuf qdf;        // float4[2n]: qa/r, qb/r as double-float (P2M)
   DevBuf mpole;      // c_t<T>[nbox*E*p]
+  DevBuf mpart;      // c_t<T>[nchunk*E*p]: per-chunk partial multipoles (FP32 direct P2M)
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
 };
 

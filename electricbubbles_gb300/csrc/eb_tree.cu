@@ -294,6 +294,20 @@ __global__ void k_group_fill(int off, int nleaf, const int* __restrict__ pt0,
   }
 }
 
+__global__ void k_chunk_count(int first, int nb, const int* __restrict__ pt0, const int* __restrict__ pt1,
+                              int* __restrict__ cnt) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  cnt[b] = (pt1[first + b] - pt0[first + b] + EB_CHUNK - 1) / EB_CHUNK;
+}
+
+__global__ void k_chunk_fill(int first, int nb, const int* __restrict__ cnt, const int* __restrict__ start,
+                             int* __restrict__ chunk_box) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  for (int c = 0; c < cnt[b]; ++c) chunk_box[start[b] + c] = first + b;
+}
+
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -546,6 +560,33 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
     k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
                                               t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
+    eb_count_launch(ctx);
+  }
+  // 8b. chunks of at most EB_CHUNK points of every box of the EB_DIRECT_LEVELS finest
+  // levels (FP32 direct P2M)
+  t.nchunk = 0;
+  t.chunk_lmin = std::max(2, L - EB_DIRECT_LEVELS + 1);
+  if (L >= 2) {
+    const int first = t.lev_off[t.chunk_lmin], nb2 = t.nbox - first;
+    EB_TRY(t.ccount.ensure(sizeof(int) * (size_t)nb2));
+    EB_TRY(t.cstart.ensure(sizeof(int) * (size_t)(nb2 + 1)));
+    k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(first, nb2, t.pt0.as<int>(), t.pt1.as<int>(), t.ccount.as<int>());
+    eb_count_launch(ctx);
+    size_t need = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, need, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st);
+    if (need > t.cubtmp.bytes) EB_TRY(t.cubtmp.ensure(need));
+    tb = t.cubtmp.bytes;
+    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st));
+    eb_count_launch(ctx);
+    int last[2];
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.ccount.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.cstart.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaStreamSynchronize(st));
+    t.nchunk = last[0] + last[1];
+    EB_CUDA_TRY(cudaMemcpyAsync(t.cstart.as<int>() + nb2, &t.nchunk, sizeof(int), cudaMemcpyHostToDevice, st));
+    EB_TRY(t.chunk_box.ensure(sizeof(int) * (size_t)t.nchunk));
+    k_chunk_fill<<<nblk(nb2, BS), BS, 0, st>>>(first, nb2, t.ccount.as<int>(), t.cstart.as<int>(),
+                                               t.chunk_box.as<int>());
     eb_count_launch(ctx);
   }
   // 9. leaf-relative coordinates for the double-float near field
