@@ -254,19 +254,37 @@ def run_gpu(args, rank, world, local):
             tot += e0.elapsed_time(e1)
         mpts[prec] = cfg.nbk / (tot / reps * 1e-3) / 1e6
 
-    # dominant kernel: FP64 near field (P2P + L2P), live CUDA-event timing
+    # per-kernel live CUDA-event timing of the near-field (P2P + L2P) and M2L kernels of
+    # both operator precisions; algorithmic flops per launch from the tree actually built:
+    # 40 per near-field pair, 8 p e per point per level of L2P, 2 * 8 p^2 per M2L pair
     tree = ctx.tree_info()
-    ctx.set_profiling(True)
-    for _ in range(10):
-        ctx.fasmvp(u, "fp64", out=y)
-    nl, near_ms = ctx.kernel_time(0)
-    nm, m2l_ms = ctx.kernel_time(1)
-    ctx.set_profiling(False)
-    p64 = 44
-    near_flops = 40.0 * tree["u_pairs"] + 24.0 * p64 * tree["npoints"]
-    near_avg_ms = near_ms / nl
     fp64_peak = ctx.measure_fp64_peak()
-    achieved = near_flops / (near_avg_ms * 1e-3) / 1e12
+    fp32_peak = ctx.measure_fp32_peak()
+    levels_l2p = max(tree["levels"] - 1, 1)
+    kern = {}
+    for prec, p_ord, near_name, m2l_name, l2p_levels in (
+            ("fp32", 20, "k_leaf32<2>", "k_m2l<float, 2>", levels_l2p),
+            ("fp64", 44, "k_leaf_df<2>", "k_m2l_df<2>", 1)):
+        ctx.set_profiling(True)
+        for _ in range(10):
+            ctx.fasmvp(u, prec, out=y)
+        nl, near_ms = ctx.kernel_time(0)
+        nm, m2l_ms = ctx.kernel_time(1)
+        ctx.set_profiling(False)
+        near_flops = 40.0 * tree["u_pairs"] + 8.0 * p_ord * 2 * tree["npoints"] * l2p_levels
+        m2l_flops = 2 * 8.0 * p_ord * p_ord * tree["v_pairs"]
+        kern[near_name] = {"avg_launch_ms": near_ms / nl, "flops_per_launch": near_flops,
+                           "achieved_tflops": near_flops / (near_ms / nl * 1e-3) / 1e12}
+        kern[m2l_name] = {"avg_launch_ms": m2l_ms / nm, "flops_per_launch": m2l_flops,
+                          "achieved_tflops": m2l_flops / (m2l_ms / nm * 1e-3) / 1e12}
+    for name, k in kern.items():
+        peak = fp32_peak
+        k["peak_tflops"] = peak
+        k["frac_of_fp32_peak"] = k["achieved_tflops"] / peak
+        if "df" in name:
+            # double-float kernels do FP64-class arithmetic on the FP32 pipes
+            k["frac_of_fp64_peak"] = k["achieved_tflops"] / fp64_peak
+    dom = kern["k_leaf32<2>"]
 
     # end to end through the C ABI with host buffers: geometry + rhs in, solution out
     zh = torch.from_numpy(np.ascontiguousarray(geo["z"]).view(np.float64).copy()).pin_memory()
@@ -388,12 +406,15 @@ def run_gpu(args, rank, world, local):
         "solve_info": {"fp64": inf64[-1], "fp32_refined": inf32[-1]},
         "accuracy": {"refined_vs_fp64_rel_l2": rel_diff, "refined_true_residual": inf32[-1]["err"]},
         "tree": tree,
-        "roofline": {"kernel": "k_leaf64<2> (FP64 near field P2P + L2P)", "bound": "fp64",
-                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp64_peak, "traffic": None,
-                     "peak_source": "measured in-run FP64 FMA chain (MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_launch": near_flops, "avg_launch_ms": near_avg_ms,
-                     "m2l_avg_launch_ms": m2l_ms / nm},
+        "roofline": {"kernel": "k_leaf32<2> (FP32 near field P2P + L2P of every level; the largest "
+                               "kernel of the refined solve)", "bound": "fp32",
+                     "achieved": dom["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": dom["achieved_tflops"] / fp32_peak, "traffic": None,
+                     "peak_source": "measured in-run FP32 FMA chain (MEASURED_PEAKS.json has no FP32 "
+                                    "CUDA-core figure)",
+                     "flops_per_launch": dom["flops_per_launch"], "avg_launch_ms": dom["avg_launch_ms"]},
+        "kernels": kern,
+        "peaks_measured_in_run": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
         "cpu_baseline": cpu,
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -90,6 +90,7 @@ SIGNATURES = {
     "eb_ctx_kernel_time": (_I, [_P, _I, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_D)]),
     "eb_ctx_tree_info": (_I, [_P, ctypes.POINTER(TreeInfo)]),
     "eb_measure_fp64_peak": (_I, [_P, ctypes.POINTER(_D)]),
+    "eb_measure_fp32_peak": (_I, [_P, ctypes.POINTER(_D)]),
     "eb_set_geometry": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I]),
     "eb_extractdat": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I]),
     "eb_stokes_matvec": (_I, [_P, _I, _P, _P, _I, _I]),

@@ -126,6 +126,11 @@ class Context:
         check("eb_measure_fp64_peak", self._lib.eb_measure_fp64_peak(self._h, ctypes.byref(v)))
         return v.value
 
+    def measure_fp32_peak(self):
+        v = ctypes.c_double()
+        check("eb_measure_fp32_peak", self._lib.eb_measure_fp32_peak(self._h, ctypes.byref(v)))
+        return v.value
+
     def tree_info(self):
         t = TreeInfo()
         check("eb_ctx_tree_info", self._lib.eb_ctx_tree_info(self._h, ctypes.byref(t)))

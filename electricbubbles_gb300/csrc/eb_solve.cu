@@ -860,6 +860,16 @@ int eb_laplace_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mo
 // (the FMM apply is bound by the FP64 pipe, not by HBM or the tensor cores).
 // ---------------------------------------------------------------------------------
 namespace {
+__global__ void k_ffma_chain(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 __global__ void k_dfma_chain(double* out, int iters, double a, double b) {
   double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
   double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
@@ -892,4 +902,28 @@ int eb_measure_fp64_peak(eb_ctx* ctx, double* tflops) {
   }
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return eb_check_launch(ctx, "fp64 peak");
+}
+
+// FP32 FMA throughput: the roofline denominator of the FP32 and double-float kernels.
+int eb_measure_fp32_peak(eb_ctx* ctx, double* tflops) {
+  if (!ctx || !tflops) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  int sms = 0;
+  EB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+  const int blocks = sms * 8, threads = 256, iters = 20000;
+  DevBuf out;
+  EB_TRY(out.ensure(sizeof(float) * (size_t)blocks * threads));
+  cudaStream_t s = ctx->stream;
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+    k_ffma_chain<<<blocks, threads, 0, s>>>(out.as<float>(), iters, 0.9999f, 1e-4f);
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+    EB_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    EB_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (ms < best) best = ms;
+  }
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return eb_check_launch(ctx, "fp32 peak");
 }

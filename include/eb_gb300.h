@@ -138,6 +138,8 @@ int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
 /* FP64 FMA throughput of the context's GPU in TFLOP/s (a short calibration kernel):
  * the roofline denominator of the FP64 FMM kernels. No counterpart in the reference. */
 int eb_measure_fp64_peak(eb_ctx* ctx, double* tflops);
+/* FP32 FMA throughput in TFLOP/s: the denominator of the FP32 and double-float kernels. */
+int eb_measure_fp32_peak(eb_ctx* ctx, double* tflops);
 
 /* Install the geometry of k drops: the data EXTRACTDAT (electric.f:636-716) leaves
  * in COMMON /inteqn/ dsdth, rkappa, z, dz and /problem/ zk, nd, k, nbk
