@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "eb_internal.h"
+#include "eb_post.cuh"
 
 // ---------------------------------------------------------------------------------
 // Errors
@@ -71,58 +72,6 @@ __global__ void k_drop_reduce_stokes(const int* __restrict__ start, const double
     za[b] = make_double2(h * s[0][0], h * s[1][0]);
     pk[b] = s[2][0];
   }
-}
-
-// Identity, self and singular terms of FASMVP (stokesbubb.f:585-612).
-__global__ void k_fasmvp_post(int nbk, const int* __restrict__ drop_of, const double2* __restrict__ dens,
-                              const double2* __restrict__ z, const double2* __restrict__ dz,
-                              const double* __restrict__ dsda, const double* __restrict__ kappa,
-                              const double* __restrict__ hpt, const double2* __restrict__ za,
-                              const double* __restrict__ pk, const double2* __restrict__ stress,
-                              double2* __restrict__ w) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nbk) return;
-  int b = drop_of[t];
-  double2 u = dens[t];
-  double qwi = hpt[t], s = dsda[t], kap = kappa[t];
-  double2 zn = make_double2(dz[t].y / s, -dz[t].x / s);  // -i dz / s'
-  double c1 = qwi * s * 0.5 * kap / EB_PI;
-  double2 zn2 = cmul<double>(zn, zn);
-  double2 zself = cscale<double>(u, c1);
-  zself = csub<double>(zself, cscale<double>(cmul<double>(cconj<double>(u), zn2), c1));
-  double pinf = -pk[0];
-  double pkb = pk[b] + pinf;
-  double f = -0.5 * (pinf - pkb);  // times i z
-  double2 zz = z[t];
-  double2 st = stress[t];
-  st.x += zself.x - f * zz.y;
-  st.y += zself.y + f * zz.x;
-  double2 zab = za[b];
-  w[t] = make_double2(u.x + zab.x + st.x, u.y + zab.y + st.y);
-}
-
-// Charges of FASMVP_LAP (laplace.f:190-200): q = u dz h.
-__global__ void k_lap_charges(int nbk, const double* __restrict__ u, const double2* __restrict__ dz,
-                              const double* __restrict__ hpt, double2* __restrict__ q) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nbk) return;
-  double f = u[t] * hpt[t];
-  q[t] = make_double2(f * dz[t].x, f * dz[t].y);
-}
-
-// Discrete operator of FASMVP_LAP (laplace.f:225-243).
-__global__ void k_lap_post(int nbk, const double* __restrict__ u, const double* __restrict__ dsda,
-                           const double* __restrict__ kappa, const double* __restrict__ hpt,
-                           const double2* __restrict__ cf, double* __restrict__ w) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nbk) return;
-  double hs = hpt[t];
-  double self = 0.25 * hs * kappa[t] * dsda[t] / EB_PI;
-  // Re(cf / (2 pi i)) = Im(cf) / (2 pi)
-  double zc = self * u[t] - cf[t].y / (2.0 * EB_PI);
-  double wt = u[t] + 2.0 * zc;
-  double du = hs * u[t] * dsda[t];
-  w[t] = wt - 2.0 * du;
 }
 
 // Constraint sums the reference writes past YY(N) (laplace.f:252-259): h s' u per drop.
@@ -245,6 +194,9 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e != cudaSuccess) {
@@ -271,6 +223,9 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   for (GmGraph& g : ctx->gcache) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+  if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   delete ctx;
   eb_devbuf_collect();
   return EB_OK;
@@ -379,34 +334,31 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   const double2* dens = reinterpret_cast<const double2*>(x);
   EB_TRY(ctx->za.ensure(sizeof(double2) * k));
   EB_TRY(ctx->pk.ensure(sizeof(double) * k));
-  EB_TRY(ctx->stress.ensure(sizeof(double2) * nbk));
-  k_drop_reduce_stokes<<<k, 256, 0, s>>>(ctx->start.as<int>(), dens, ctx->dz.as<double2>(),
-                                         ctx->z.as<double2>(), ctx->zk.as<double2>(),
-                                         ctx->za.as<double2>(), ctx->pk.as<double>());
+  // the per-drop sums run on the side stream, overlapping the FMM; the leaf kernel, whose
+  // fused post-processing reads them, waits for them
+  EB_CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
+  EB_CUDA_TRY(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
+  k_drop_reduce_stokes<<<k, 256, 0, ctx->side_stream>>>(ctx->start.as<int>(), dens, ctx->dz.as<double2>(),
+                                                       ctx->z.as<double2>(), ctx->zk.as<double2>(),
+                                                       ctx->za.as<double2>(), ctx->pk.as<double>());
   eb_count_launch(ctx);
-  EB_TRY(eb_stokes_sum_dev(ctx, dens, -1, ctx->stress.as<double2>(), prec));
-  k_fasmvp_post<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->drop_of.as<int>(), dens, ctx->z.as<double2>(),
-                                               ctx->dz.as<double2>(), ctx->dsda.as<double>(),
-                                               ctx->kappa.as<double>(), ctx->hpt.as<double>(),
-                                               ctx->za.as<double2>(), ctx->pk.as<double>(),
-                                               ctx->stress.as<double2>(), reinterpret_cast<double2*>(y));
-  eb_count_launch(ctx);
+  EB_CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side_stream));
+  EbPost post{1, dens, nullptr, ctx->z.as<double2>(), ctx->dz.as<double2>(), ctx->dsda.as<double>(),
+               ctx->kappa.as<double>(), ctx->hpt.as<double>(), ctx->drop_of.as<int>(),
+               ctx->za.as<double2>(), ctx->pk.as<double>(), y};
+  EB_TRY(eb_fmm_apply(ctx, ctx->tree, 0, -1, prec, dens, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
+                      nullptr, &post, ctx->ev_join));
   return eb_check_launch(ctx, "stokes matvec");
 }
 
 int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   if (!ctx->geom_valid) return EB_ERR_NOGEOM;
   cudaStream_t s = ctx->stream;
-  int nbk = ctx->nbk;
-  EB_TRY(ctx->vtmp.ensure(sizeof(double2) * nbk));
-  EB_TRY(ctx->stress.ensure(sizeof(double2) * nbk));
-  k_lap_charges<<<nblk(nbk, 256), 256, 0, s>>>(nbk, x, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
-                                               ctx->vtmp.as<double2>());
-  eb_count_launch(ctx);
-  EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, ctx->vtmp.as<double2>(), ctx->stress.as<double2>()));
-  k_lap_post<<<nblk(nbk, 256), 256, 0, s>>>(nbk, x, ctx->dsda.as<double>(), ctx->kappa.as<double>(),
-                                            ctx->hpt.as<double>(), ctx->stress.as<double2>(), y);
-  eb_count_launch(ctx);
+  // the Cauchy charges q = u dz h of FASMVP_LAP (laplace.f:190-200) are formed by the
+  // FMM's charge kernel from u (EbPost::u)
+  EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
+               ctx->kappa.as<double>(), ctx->hpt.as<double>(), nullptr, nullptr, nullptr, y};
+  EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, nullptr, nullptr, &post));
   return eb_check_launch(ctx, "laplace matvec");
 }
 

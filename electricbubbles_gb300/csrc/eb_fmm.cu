@@ -26,6 +26,7 @@
 
 #include "eb_df.cuh"
 #include "eb_internal.h"
+#include "eb_post.cuh"
 
 namespace {
 
@@ -103,20 +104,33 @@ __global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const d
   aa[i] = df4(make_double2(-s * a.x * rinv, s * a.y * rinv));
 }
 
+// Cauchy charge of node o: q[o], or u_o dz_o h_o (FASMVP_LAP, laplace.f:190-200) when
+// q is null.
+__device__ __forceinline__ double2 cauchy_charge(int o, const double2* q, const double* lu,
+                                                 const double2* dz, const double* hpt) {
+  if (q) return q[o];
+  const double f = lu[o] * hpt[o];
+  return make_double2(f * dz[o].x, f * dz[o].y);
+}
+
 __global__ void k_charges_cauchy_df(int n, const int* __restrict__ perm, const double2* __restrict__ q,
-                                    double rinv, float4* __restrict__ qdf) {
+                                    const double* __restrict__ lu, const double2* __restrict__ dz,
+                                    const double* __restrict__ hpt, double rinv,
+                                    float4* __restrict__ qdf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double2 v = q[perm[i]];
+  double2 v = cauchy_charge(perm[i], q, lu, dz, hpt);
   qdf[i] = df4(make_double2(v.x * rinv, v.y * rinv));
 }
 
 template <typename T>
 __global__ void k_charges_cauchy(int n, const int* __restrict__ perm,
-                                 const double2* __restrict__ q, c_t<T>* __restrict__ qa) {
+                                 const double2* __restrict__ q, const double* __restrict__ lu,
+                                 const double2* __restrict__ dz, const double* __restrict__ hpt,
+                                 c_t<T>* __restrict__ qa) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double2 v = q[perm[i]];
+  double2 v = cauchy_charge(perm[i], q, lu, dz, hpt);
   qa[i] = cmk<T>((T)v.x, (T)v.y);
 }
 
@@ -878,7 +892,7 @@ __global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restric
                                                 const double2* __restrict__ qa, double x0, double y0,
                                                 double r, int p, double s,
                                                 const double2* __restrict__ local,
-                                                double2* __restrict__ out) {
+                                                double2* __restrict__ out, EbPost post) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -922,7 +936,7 @@ __global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restric
   gy += __shfl_xor_sync(0xffffffffu, gy, 1);
   gx += __shfl_xor_sync(0xffffffffu, gx, 2);
   gy += __shfl_xor_sync(0xffffffffu, gy, 2);
-  if (sl == 0 && act) out[perm[i]] = make_double2(gx, gy);
+  if (sl == 0 && act) eb_post_store(post, perm[i], make_double2(gx, gy), out);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1015,7 +1029,7 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
                                                  const float4* __restrict__ pq,
                                                  const float4* __restrict__ aa, int p, double s,
                                                  const float4* __restrict__ local,
-                                                 double2* __restrict__ out) {
+                                                 double2* __restrict__ out, EbPost post) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -1080,7 +1094,7 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
     vx = (sl & o) ? dfl_add(ox, vx) : dfl_add(vx, ox);
     vy = (sl & o) ? dfl_add(oy, vy) : dfl_add(vy, oy);
   }
-  if (sl == 0 && act) out[perm[i]] = make_double2(dfl_to_double(vx), dfl_to_double(vy));
+  if (sl == 0 && act) eb_post_store(post, perm[i], make_double2(dfl_to_double(vx), dfl_to_double(vy)), out);
 }
 
 // FP32 leaf evaluation: node positions as float hi + lo so that differences are exact
@@ -1108,7 +1122,7 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
                                                 const float2* __restrict__ qa, double x0, double y0,
                                                 double r, int L, const int* __restrict__ parent,
                                                 int p, float s, const float2* __restrict__ local,
-                                                double2* __restrict__ out) {
+                                                double2* __restrict__ out, EbPost post) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -1173,7 +1187,7 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   gy += __shfl_xor_sync(0xffffffffu, gy, 1);
   gx += __shfl_xor_sync(0xffffffffu, gx, 2);
   gy += __shfl_xor_sync(0xffffffffu, gy, 2);
-  if (sl == 0 && act) out[perm[i]] = make_double2((double)gx, (double)gy);
+  if (sl == 0 && act) eb_post_store(post, perm[i], make_double2((double)gx, (double)gy), out);
 }
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
@@ -1420,7 +1434,10 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
 
 template <typename T, int E>
 int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2* dz,
-            const double* hpt, const double2* q, double2* out) {
+            const double* hpt, const double2* q, double2* out, const EbPost* postp,
+            cudaEvent_t join) {
+  EbPost post{};
+  if (postp) post = *postp;
   cudaStream_t st = eb_stream(ctx);
   const bool f64 = sizeof(T) == 8;
   EbTables& tb = f64 ? ctx->tab64 : ctx->tab32;
@@ -1443,14 +1460,15 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                                       1.0 / rleaf, w.qdf.as<float4>(), w.pqdf.as<float4>(),
                                                       w.aadf.as<float4>());
   } else if (df) {
-    k_charges_cauchy_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, 1.0 / rleaf,
-                                                      w.pqdf.as<float4>());
+    k_charges_cauchy_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, post.u, post.dz, post.hpt,
+                                                      1.0 / rleaf, w.pqdf.as<float4>());
   } else if (E == 2) {
     k_charges_stokes<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
                                                       w.qa.as<c_t<T>>(), w.qb.as<c_t<T>>(),
                                                       w.pq.as<c_t<T>>(), w.aa.as<c_t<T>>());
   } else {
-    k_charges_cauchy<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, w.qa.as<c_t<T>>());
+    k_charges_cauchy<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, post.u, post.dz, post.hpt,
+                                                      w.qa.as<c_t<T>>());
   }
   eb_count_launch(ctx);
   const int has_far = t.L >= 2;
@@ -1462,6 +1480,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   }
   int offL = t.lev_off[t.L];
   int blocks = nblk((long long)t.ngroup * 32, 128);
+  if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
   ProfScope ps(ctx, 0, st);
   if (df) {
     k_leaf_df<E><<<blocks, 128, 0, st>>>(
@@ -1469,20 +1488,20 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign,
-        w.local_df.as<float4>(), out);
+        w.local_df.as<float4>(), out, post);
   } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
-        rleaf, tb.p, (double)sign, w.local.as<double2>(), out);
+        rleaf, tb.p, (double)sign, w.local.as<double2>(), out, post);
   } else {
     k_leaf32<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.zs.as<double2>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
         w.aa.as<float2>(), w.qa.as<float2>(), t.x0, t.y0, rleaf, t.L, t.parent.as<int>(), tb.p,
-        (float)sign, w.local.as<float2>(), out);
+        (float)sign, w.local.as<float2>(), out, post);
   }
   eb_count_launch(ctx);
   ps.done();
@@ -1504,15 +1523,17 @@ int eb_tables_init(eb_ctx* ctx) {
 }
 
 int eb_fmm_apply(eb_ctx* ctx, EbTree& t, int kernel, int sign, int precision,
-                 const double2* dens, const double2* dz, const double* hpt, double2* out) {
+                 const double2* dens, const double2* dz, const double* hpt, double2* out,
+                 const EbPost* post, cudaEvent_t join) {
   if (!t.valid) return EB_ERR_NOGEOM;
   if (kernel != 0) return EB_ERR_ARG;
-  if (precision == EB_FP64) return fmm_run<double, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out);
-  return fmm_run<float, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out);
+  if (precision == EB_FP64) return fmm_run<double, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join);
+  return fmm_run<float, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join);
 }
 
-int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q, double2* out) {
+int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q, double2* out,
+                        const EbPost* post) {
   if (!t.valid) return EB_ERR_NOGEOM;
-  if (precision == EB_FP64) return fmm_run<double, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out);
-  return fmm_run<float, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out);
+  if (precision == EB_FP64) return fmm_run<double, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr);
+  return fmm_run<float, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr);
 }

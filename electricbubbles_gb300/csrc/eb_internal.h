@@ -151,7 +151,6 @@ struct eb_ctx {
   // operator scratch
   DevBuf za, pk, redpart;          // per-drop reductions
   DevBuf vin, vout, vtmp, vtmp2;   // host-path staging and temporaries
-  DevBuf stress;                   // double2[nbk]
   DevBuf pvz, pvq, pvout;          // PVINTEV fine grid
   DevBuf fftbuf, fftbuf2;          // spectral scratch
   DevBuf ex_zk, ex_dz, ex_ds, ex_ka, ex_area;  // EXTRACTDAT outputs before install
@@ -167,6 +166,8 @@ struct eb_ctx {
   std::vector<double> hH;
   unsigned long long geom_version = 0;  // advanced by every geometry install
   cudaStream_t cap_stream = nullptr;    // private stream for graph capture
+  cudaStream_t side_stream = nullptr;   // second stream for work that overlaps the FMM
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   GmGraph gcache[EB_GRAPH_CACHE];
   int gcache_next = 0;
 };
@@ -175,12 +176,17 @@ struct eb_ctx {
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target);
 
 // fmm.cu
+struct EbPost;
 int eb_tables_init(eb_ctx* ctx);
-// kernel: 0 = Stokes (sign from `sign`), 1 = Cauchy
+// kernel: 0 = Stokes (sign from `sign`). `post` (may be null: store the sum into out)
+// fuses an operator's post-processing into the leaf kernels.
+// `join` (may be null): an event the leaf kernel waits for (work the caller forked onto
+// another stream whose results the post-processing reads).
 int eb_fmm_apply(eb_ctx* ctx, EbTree& t, int kernel, int sign, int precision,
-                 const double2* dens, const double2* dz, const double* hpt, double2* out);
+                 const double2* dens, const double2* dz, const double* hpt, double2* out,
+                 const EbPost* post = nullptr, cudaEvent_t join = nullptr);
 int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q,
-                        double2* out);
+                        double2* out, const EbPost* post = nullptr);
 
 // api.cu: operators on device vectors (x, y device pointers)
 int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw, int prec);
