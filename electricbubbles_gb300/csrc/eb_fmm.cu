@@ -1114,14 +1114,14 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
                                                 const int* __restrict__ ulist,
                                                 const int* __restrict__ ucount,
                                                 const int* __restrict__ perm,
-                                                const double2* __restrict__ zs,
+                                                const float4* __restrict__ wa,
                                                 const float2* __restrict__ zhi,
                                                 const float2* __restrict__ zlo,
                                                 const float2* __restrict__ pq,
                                                 const float2* __restrict__ aa,
-                                                const float2* __restrict__ qa, double x0, double y0,
-                                                double r, int L, const int* __restrict__ parent,
-                                                int p, float s, const float2* __restrict__ local,
+                                                const float2* __restrict__ qa, int L,
+                                                const int* __restrict__ parent, int p, float s,
+                                                const float2* __restrict__ local,
                                                 double2* __restrict__ out, EbPost post) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
@@ -1138,17 +1138,15 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
     // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
     //   u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2   (i the leaf's grid index),
     // whose constant part is exact in FP32 (i < 2^20).
-    const double2 zi = zs[ii];
     const unsigned long long kb = bkey[b];
     const unsigned int ix = compact2d(kb), iy = compact2d(kb >> 1);
-    const double2 c = box_center(kb, x0, y0, r);
-    const float ux = (float)((zi.x - c.x) / r), uy = (float)((zi.y - c.y) / r);
+    const float4 wv = wa[ii];
     int a = b;
     for (int sh = 0; sh <= L - 2; ++sh) {
       const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
       const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
       const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
-      const float2 u = make_float2(fmaf(ux, f, gx), fmaf(uy, f, gy));
+      const float2 u = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
       l2p_part<float, E>(local + (size_t)a * E * (p + 1), p, sl, u, s, fx, fy);
       a = parent[a];
     }
@@ -1499,8 +1497,8 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     k_leaf32<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-        t.zs.as<double2>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
-        w.aa.as<float2>(), w.qa.as<float2>(), t.x0, t.y0, rleaf, t.L, t.parent.as<int>(), tb.p,
+        t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+        w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
         (float)sign, w.local.as<float2>(), out, post);
   }
   eb_count_launch(ctx);

@@ -84,6 +84,37 @@ __global__ void k_vtw(int n, int ncol, const int* __restrict__ ncol_dev, const d
   finish_columns(gridDim.x, ncol, part, out, ticket);
 }
 
+// Pass-1 update fused with the pass-2 projection of classical Gram-Schmidt: each block
+// updates its contiguous range of rows, w -= V[:, 0:ncol] hin, and then forms the
+// block's partial V^T w for those rows exactly as k_vtw does (warps over columns, lanes
+// over rows); the last block adds the partials in block order.
+__global__ void k_update_vtw(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                             size_t ldv, const double* __restrict__ hin, double* w,
+                             double* __restrict__ part, double* __restrict__ out,
+                             unsigned int* __restrict__ ticket) {
+  __shared__ double hs[128];
+  if (ncol_dev) ncol = *ncol_dev;
+  for (int j = threadIdx.x; j < ncol; j += blockDim.x) hs[j] = hin[j];
+  __syncthreads();
+  const int rows = (n + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < ncol; ++j) acc = fma(V[(size_t)j * ldv + i], hs[j], acc);
+    w[i] -= acc;
+  }
+  __syncthreads();
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int j = wi; j < ncol; j += nw) {
+    const double* v = V + (size_t)j * ldv;
+    double sum = 0.0;
+    for (int i = r0 + lane; i < r1; i += 32) sum = fma(v[i], w[i], sum);
+    sum = warp_sum<double>(sum);
+    if (lane == 0) part[(size_t)blockIdx.x * ncol + j] = sum;
+  }
+  finish_columns(gridDim.x, ncol, part, out, ticket);
+}
+
 // w -= V[:, 0:ncol] h; if part != nullptr also ||w||^2 of the new w into *out.
 __global__ void k_gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
                            size_t ldv, const double* __restrict__ h, double* __restrict__ w,
@@ -269,12 +300,11 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     (*nmv)++;
     // pass 1: h1 = V^T w; w -= V h1
     k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket);
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, nullptr, nullptr, nullptr);
-    // pass 2: h2 = V^T w; w -= V h2 with ||w||^2
-    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev + (maxl + 2), g.ticket);
+    // w -= V h1; pass 2: h2 = V^T w; w -= V h2 with ||w||^2
+    k_update_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + (maxl + 2), g.ticket);
     k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev + (maxl + 2), w, part,
                                       hdev + 2 * (maxl + 2), g.ticket);
-    ctx->launches += 4;
+    ctx->launches += 3;
     EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
                                 cudaMemcpyDeviceToHost, g.s));
     EB_CUDA_TRY(cudaStreamSynchronize(g.s));
@@ -598,12 +628,11 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
-    k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, nullptr, nullptr, nullptr);
-    k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H2, ticket);
+    k_update_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_H2, ticket);
     k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev + GM_NW, ticket);
     k_gm_arnoldi<<<1, 32, 0, s>>>(ctl, hdev, h);
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
-    ctx->launches += 6;
+    ctx->launches += 5;
     return eb_check_launch(ctx, "gmres graph (body)");
   }));
   // post: DHELS, x update; refined: x += d, r = b - A64 x with ||r||^2
