@@ -197,6 +197,8 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_p2p, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e != cudaSuccess) {
@@ -226,6 +228,8 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->ev_c) cudaEventDestroy(ctx->ev_c);
+  if (ctx->ev_p2p) cudaEventDestroy(ctx->ev_p2p);
   delete ctx;
   eb_devbuf_collect();
   return EB_OK;

@@ -557,7 +557,7 @@ __device__ __forceinline__ cdf cacc_value(const dfacc& rx, const dfacc& ry) {
 // P2M at the leaves from the leaf-relative offsets w (units of the leaf side) and the
 // charges qa/r, qb/r: M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 template <int E>
-__global__ void __launch_bounds__(64) k_p2m_df(int off, const int* __restrict__ pt0,
+__global__ void __launch_bounds__(128) k_p2m_df(int off, const int* __restrict__ pt0,
                                                const int* __restrict__ pt1, const float4* __restrict__ wa,
                                                const float4* __restrict__ q, int p,
                                                float4* __restrict__ mpole) {
@@ -581,14 +581,22 @@ __global__ void __launch_bounds__(64) k_p2m_df(int off, const int* __restrict__ 
         sc[32 + tid] = q[2 * (size_t)i + 1];
         sc[64 + tid] = cdf_f4(cdf_mul(cdf_conj(w), ah));
       }
-      cdf pwr = cdf{{1.f, 0.f}, {0.f, 0.f}};
       float4* row = pw + tid * ps;
-      for (int j = 0; j < p; ++j) {
-        row[j] = cdf_f4(pwr);
-        pwr = cdf_mul(pwr, w);
-      }
+      row[0] = make_float4(1.f, 0.f, 0.f, 0.f);
+      row[1] = cdf_f4(w);
     }
     __syncthreads();
+    // powers w^j, j < p, by doubling: w^j = w^(j-len) w^len for len < j <= 2 len, all
+    // (point, j) pairs of a step in parallel
+    for (int len = 1; len + 1 < p; len <<= 1) {
+      const int span = min(len, p - 1 - len);
+      for (int pr = tid; pr < cnt * span; pr += blockDim.x) {
+        const int sp = pr / span, jj = len + 1 + (pr - sp * span);
+        float4* row = pw + sp * ps;
+        row[jj] = cdf_f4(cdf_mul(cdf_from_float4(row[jj - len]), cdf_from_float4(row[len])));
+      }
+      __syncthreads();
+    }
     if (tid < p) {
       for (int s = 0; s < cnt; ++s) {
         const cdf v = cdf_from_float4(pw[s * ps + tid]);
@@ -615,6 +623,21 @@ __global__ void __launch_bounds__(64) k_p2m_df(int off, const int* __restrict__ 
   }
 }
 
+// merge the compensated complex sums of the 4 lanes of an output (lanes 4o .. 4o+3),
+// in a fixed order; every lane ends with the total
+__device__ __forceinline__ cdf quad_merge(dfacc rx, dfacc ry) {
+  cdf v = cacc_value(rx, ry);
+#pragma unroll
+  for (int o = 1; o <= 2; o <<= 1) {
+    cdf u{{__shfl_xor_sync(0xffffffffu, v.x.hi, o), __shfl_xor_sync(0xffffffffu, v.x.lo, o)},
+          {__shfl_xor_sync(0xffffffffu, v.y.hi, o), __shfl_xor_sync(0xffffffffu, v.y.lo, o)}};
+    v = (threadIdx.x & o) ? cdf_add(u, v) : cdf_add(v, u);
+  }
+  return v;
+}
+
+// M2M: 4 lanes per output coefficient, each summing every 4th term, so the dependent
+// chain of compensated products is a quarter as long.
 template <int E>
 __global__ void k_m2m_df(int offp, const unsigned long long* __restrict__ bkey,
                          const int* __restrict__ child0, const int* __restrict__ nchild, int p,
@@ -623,7 +646,6 @@ __global__ void k_m2m_df(int offp, const unsigned long long* __restrict__ bkey,
   extern __shared__ float4 sm4[];
   float4* a = sm4;  // [child][E*p]
   const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
-  const int e = tid / p, nn = tid - e * p;
   const int c0 = child0[P], nc = nchild[P];
   for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
     const int ci = idx / nout, o = idx - ci * nout;
@@ -638,19 +660,23 @@ __global__ void k_m2m_df(int offp, const unsigned long long* __restrict__ bkey,
     a[idx] = cdf_f4(cdf_mul(v, cdf_from_float4(einv[q * ld + k])));
   }
   __syncthreads();
-  if (tid < nout) {
-    const int n = nn + 1;
-    const float2* brow = binom + (size_t)(n - 1) * ldb;
-    dfacc rx{0.f, 0.f}, ry{0.f, 0.f};
+  const int o = tid >> 2, part = tid & 3;
+  const bool act = o < nout;
+  const int oo = act ? o : 0;
+  const int e = oo / p, n = oo - e * p + 1;
+  const float2* brow = binom + (size_t)(n - 1) * ldb;
+  dfacc rx{0.f, 0.f}, ry{0.f, 0.f};
+  if (act) {
     for (int ci = 0; ci < nc; ++ci) {
       const int q = quadrant(bkey[c0 + ci]);
       const float4* ae = a + ci * nout + e * p;
       dfacc sx{0.f, 0.f}, sy{0.f, 0.f};
-      for (int k = 0; k < n; ++k) cacc_rmul(sx, sy, dfl{brow[k].x, brow[k].y}, cdf_from_float4(ae[k]));
+      for (int k = part; k < n; k += 4) cacc_rmul(sx, sy, dfl{brow[k].x, brow[k].y}, cdf_from_float4(ae[k]));
       cacc_mul(rx, ry, cdf_from_float4(epow2[q * ld + n]), cacc_value(sx, sy));
     }
-    mpole[(size_t)P * nout + tid] = cdf_f4(cacc_value(rx, ry));
   }
+  const cdf v = quad_merge(rx, ry);
+  if (act && part == 0) mpole[(size_t)P * nout + o] = cdf_f4(v);
 }
 
 template <int E>
@@ -674,21 +700,28 @@ __global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
     a[idx] = cdf_f4(cdf_mul(v, cdf_from_float4(epow2[q * ld + m])));
   }
   __syncthreads();
-  if (tid < nout) {
-    const int e = tid / ldl, j = tid - e * ldl;
-    const float4* ae = a + e * ldl;
-    dfacc sx{0.f, 0.f}, sy{0.f, 0.f};
-    for (int m = j; m <= p; ++m) {
+  // 4 lanes per output, each summing every 4th term
+  const int o = tid >> 2, part = tid & 3;
+  const bool act = o < nout;
+  const int oo = act ? o : 0;
+  const int e = oo / ldl, j = oo - e * ldl;
+  const float4* ae = a + e * ldl;
+  dfacc sx{0.f, 0.f}, sy{0.f, 0.f};
+  if (act) {
+    for (int m = j + part; m <= p; m += 4) {
       const float2 bm = binom[(size_t)m * ldb + j];
       cacc_rmul(sx, sy, dfl{bm.x, bm.y}, cdf_from_float4(ae[m]));
     }
+  }
+  const cdf ssum = quad_merge(sx, sy);
+  if (act && part == 0) {
     float4* lc = local + (size_t)c * nout;
     dfacc rx{0.f, 0.f}, ry{0.f, 0.f};
-    const cdf old = cdf_from_float4(lc[tid]);
+    const cdf old = cdf_from_float4(lc[o]);
     acc_dfl(rx, old.x);
     acc_dfl(ry, old.y);
-    cacc_mul(rx, ry, cdf_from_float4(einv[q * ld + j]), cacc_value(sx, sy));
-    lc[tid] = cdf_f4(cacc_value(rx, ry));
+    cacc_mul(rx, ry, cdf_from_float4(einv[q * ld + j]), ssum);
+    lc[o] = cdf_f4(cacc_value(rx, ry));
   }
 }
 
@@ -1016,7 +1049,10 @@ __device__ __forceinline__ void l2p_part_df(const float4* L, int p, int sl, cdf 
   }
 }
 
-template <int E>
+// MODE 0: far and near field; 1: near field only, into nearbuf (sorted order);
+// 2: far field only, plus nearbuf, then the post-processing. Modes 1 and 2 let the near
+// field run concurrently with the expansion passes.
+template <int E, int MODE>
 __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restrict__ gleaf,
                                                  const int* __restrict__ gfirst, int off, int has_far,
                                                  const unsigned long long* __restrict__ bkey,
@@ -1029,7 +1065,8 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
                                                  const float4* __restrict__ pq,
                                                  const float4* __restrict__ aa, int p, double s,
                                                  const float4* __restrict__ local,
-                                                 double2* __restrict__ out, EbPost post) {
+                                                 double2* __restrict__ out, EbPost post,
+                                                 double2* __restrict__ nearbuf) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -1042,10 +1079,10 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   const cdf wi = cdf{{wia.x, wia.z}, {wia.y, wia.w}};
   const bool neg = s < 0.0;
   dfacc gx{0.f, 0.f}, gy{0.f, 0.f};
-  if (has_far) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
+  if (MODE != 1 && has_far) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
   const unsigned long long kb = bkey[b];
   const int bx = (int)compact2d(kb), by = (int)compact2d(kb >> 1);
-  const int nu = ucount[leaf];
+  const int nu = MODE == 2 ? 0 : ucount[leaf];
   for (int jl = 0; jl < nu; ++jl) {
     const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
     const unsigned long long ks = bkey[sb];
@@ -1094,7 +1131,18 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
     vx = (sl & o) ? dfl_add(ox, vx) : dfl_add(vx, ox);
     vy = (sl & o) ? dfl_add(oy, vy) : dfl_add(vy, oy);
   }
-  if (sl == 0 && act) eb_post_store(post, perm[i], make_double2(dfl_to_double(vx), dfl_to_double(vy)), out);
+  if (sl == 0 && act) {
+    double2 v = make_double2(dfl_to_double(vx), dfl_to_double(vy));
+    if (MODE == 1) {
+      nearbuf[i] = v;
+    } else {
+      if (MODE == 2) {
+        const double2 nv = nearbuf[i];
+        v = make_double2(v.x + nv.x, v.y + nv.y);
+      }
+      eb_post_store(post, perm[i], v, out);
+    }
+  }
 }
 
 // FP32 leaf evaluation: node positions as float hi + lo so that differences are exact
@@ -1106,7 +1154,8 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-template <int E>
+// MODE as for k_leaf_df.
+template <int E, int MODE>
 __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restrict__ gleaf,
                                                 const int* __restrict__ gfirst, int off, int has_far,
                                                 const unsigned long long* __restrict__ bkey,
@@ -1122,7 +1171,8 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
                                                 const float2* __restrict__ qa, int L,
                                                 const int* __restrict__ parent, int p, float s,
                                                 const float2* __restrict__ local,
-                                                double2* __restrict__ out, EbPost post) {
+                                                double2* __restrict__ out, EbPost post,
+                                                double2* __restrict__ nearbuf) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -1132,7 +1182,7 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   const int ii = act ? i : gfirst[g];
   const float2 hi = zhi[ii], lo = zlo[ii];
   float fx = 0.f, fy = 0.f;
-  if (has_far) {
+  if (MODE != 1 && has_far) {
     // The M2L expansion of the leaf and of each ancestor (levels L .. 2), each evaluated
     // about its own centre: the sum equals L2P of the L2L-accumulated leaf expansion.
     // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
@@ -1152,7 +1202,7 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
     }
   }
   float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
-  const int nu = ucount[leaf];
+  const int nu = MODE == 2 ? 0 : ucount[leaf];
   for (int jl = 0; jl < nu; ++jl) {
     const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
     const int j1 = pt1[sb];
@@ -1185,7 +1235,18 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   gy += __shfl_xor_sync(0xffffffffu, gy, 1);
   gx += __shfl_xor_sync(0xffffffffu, gx, 2);
   gy += __shfl_xor_sync(0xffffffffu, gy, 2);
-  if (sl == 0 && act) eb_post_store(post, perm[i], make_double2((double)gx, (double)gy), out);
+  if (sl == 0 && act) {
+    double2 v = make_double2((double)gx, (double)gy);
+    if (MODE == 1) {
+      nearbuf[i] = v;
+    } else {
+      if (MODE == 2) {
+        const double2 nv = nearbuf[i];
+        v = make_double2(v.x + nv.x, v.y + nv.y);
+      }
+      eb_post_store(post, perm[i], v, out);
+    }
+  }
 }
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
@@ -1308,14 +1369,14 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   {
     size_t sm = sizeof(float4) * (32 * (size_t)(p + 1) + 96);
     if (sm > 48 * 1024) EB_CUDA_TRY(cudaFuncSetAttribute(k_p2m_df<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_p2m_df<E><<<t.nleaf, 64, sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
+    k_p2m_df<E><<<t.nleaf, 128, sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
                                           E == 2 ? w.qdf.as<float4>() : w.pqdf.as<float4>(), p, mp);
     eb_count_launch(ctx);
   }
   for (int l = L - 1; l >= 2; --l) {
     int nb = t.lev_off[l + 1] - t.lev_off[l];
     size_t sm = sizeof(float4) * 4 * E * p;
-    k_m2m_df<E><<<nb, round32(E * p), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(), t.child0.as<int>(),
+    k_m2m_df<E><<<nb, round32(4 * E * p), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(), t.child0.as<int>(),
                                                 t.nchild.as<int>(), p, tb.binom_df.as<float2>(), ldb,
                                                 tb.epow_df.as<float4>(), tb.einv_df.as<float4>(), mp);
     eb_count_launch(ctx);
@@ -1337,7 +1398,7 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   for (int l = 3; l <= L; ++l) {
     int nb = t.lev_off[l + 1] - t.lev_off[l];
     size_t sm = sizeof(float4) * E * (p + 1);
-    k_l2l_df<E><<<nb, round32(E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
+    k_l2l_df<E><<<nb, round32(4 * E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
                                                      t.parent.as<int>(), p, tb.binom_df.as<float2>(), ldb,
                                                      tb.epow_df.as<float4>(), tb.einv_df.as<float4>(), lo);
     eb_count_launch(ctx);
@@ -1470,23 +1531,64 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   }
   eb_count_launch(ctx);
   const int has_far = t.L >= 2;
+  int offL = t.lev_off[t.L];
+  int blocks = nblk((long long)t.ngroup * 32, 128);
+  // FP32 and double-float: the near field runs on the side stream while the expansion
+  // passes run on the main stream, and the far-field kernel adds both. This pays while
+  // the passes are latency-bound (up to ~256K nodes); above that each kernel fills the
+  // GPU by itself. The per-kernel profiling timer times the combined kernel.
+  const bool split = has_far && (df || !f64) && !ctx->profiling && n <= (1 << 18);
+  if (split) {
+    EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev_c, st));
+    EB_CUDA_TRY(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_c, 0));
+    cudaStream_t ss = ctx->side_stream;
+    if (df) {
+      k_leaf_df<E, 1><<<blocks, 128, 0, ss>>>(
+          t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, 0, t.bkey.as<unsigned long long>(),
+          t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+          t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
+          (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
+    } else {
+      k_leaf32<E, 1><<<blocks, 128, 0, ss>>>(
+          t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, 0, t.bkey.as<unsigned long long>(),
+          t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+          t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+          w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
+          (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+    }
+    eb_count_launch(ctx);
+    EB_CUDA_TRY(cudaEventRecord(ctx->ev_p2p, ss));
+  }
   if (has_far && df) EB_TRY(fmm_expansions_df<E>(ctx, t, tb, w));
   else if (has_far) EB_TRY((fmm_expansions<T, E>(ctx, t, tb, w)));
   if (!has_far) {
     EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
     EB_TRY(w.local_df.ensure(sizeof(float4) * (size_t)(E * (tb.p + 1))));
   }
-  int offL = t.lev_off[t.L];
-  int blocks = nblk((long long)t.ngroup * 32, 128);
+  if (split) EB_CUDA_TRY(cudaStreamWaitEvent(st, ctx->ev_p2p, 0));
   if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
   ProfScope ps(ctx, 0, st);
-  if (df) {
-    k_leaf_df<E><<<blocks, 128, 0, st>>>(
+  if (df && split) {
+    k_leaf_df<E, 2><<<blocks, 128, 0, st>>>(
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
+        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
+        (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
+  } else if (split) {
+    k_leaf32<E, 2><<<blocks, 128, 0, st>>>(
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
+        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+        w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
+        (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+  } else if (df) {
+    k_leaf_df<E, 0><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign,
-        w.local_df.as<float4>(), out, post);
+        w.local_df.as<float4>(), out, post, nullptr);
   } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
@@ -1494,12 +1596,12 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
         rleaf, tb.p, (double)sign, w.local.as<double2>(), out, post);
   } else {
-    k_leaf32<E><<<blocks, 128, 0, st>>>(
+    k_leaf32<E, 0><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
         w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
-        (float)sign, w.local.as<float2>(), out, post);
+        (float)sign, w.local.as<float2>(), out, post, nullptr);
   }
   eb_count_launch(ctx);
   ps.done();

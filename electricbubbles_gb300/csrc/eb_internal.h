@@ -103,6 +103,7 @@ struct EbFmmWork {
   DevBuf mpole_df;   // float4[nbox*E*p]: multipoles, double-float pipeline
   DevBuf local_df;   // float4[nbox*E*(p+1)]: local expansions, double-float pipeline
   DevBuf qdf;        // float4[2n]: qa/r, qb/r as double-float (P2M)
+  DevBuf nearbuf;    // double2[n]: near-field sums (sorted order) when split from the far field
   DevBuf mpole;      // c_t<T>[nbox*E*p]
   DevBuf mpart;      // c_t<T>[nchunk*E*p]: per-chunk partial multipoles (FP32 direct P2M)
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
@@ -168,6 +169,7 @@ struct eb_ctx {
   cudaStream_t cap_stream = nullptr;    // private stream for graph capture
   cudaStream_t side_stream = nullptr;   // second stream for work that overlaps the FMM
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_c = nullptr, ev_p2p = nullptr;  // FMM: near field forked after the charges
   GmGraph gcache[EB_GRAPH_CACHE];
   int gcache_next = 0;
 };
