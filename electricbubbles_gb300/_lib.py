@@ -109,6 +109,10 @@ SIGNATURES = {
     "eb_rk_f": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo), _I]),
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
                          _I]),
+    "eb_bubbin_read": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _P]),
+    "eb_geoinit": (_I, [_I, _P, _P, _P, _P, _P, _P]),
+    "eb_dumpdata": (_I, [ctypes.c_char_p, _I, _P, _D, _D, _P, _P, _P]),
+    "eb_readdata": (_I, [ctypes.c_char_p, _I, ctypes.c_long, _P, _P, _P, _P, _P, _P, _P]),
     "eb_set_default_ctx": (_I, [_P]),
     "matvec_": (None, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "matvec_lapl_": (None, [_P, _P, _P, _P, _P, _P, _P, _P]),

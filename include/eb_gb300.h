@@ -239,6 +239,23 @@ int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup,
 int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar,
                 const eb_model* model, eb_stage_info* info, int mem);
 
+/* Input deck and checkpoint files of the reference (host only, no context).
+ * eb_bubbin_read: the first deck of a `bubbin` file as READINI reads it
+ * (electric.f:275-337): k drops (k <= kmax), nd[k], params[7] = {dt, tfinal, nplot, cap,
+ * bondx, bondy, E0}, drops[6k] = per drop {ai, bi, thetax, cx, cy, ncyc}.
+ * eb_geoinit: the initial curves of GEOINIT / INITPARAM (electric.f:340-496) at theta_i =
+ * 2 pi i / nd: z (interleaved x, y), and optionally dsdth, kappa (nbk each) and the
+ * initial areas area0 (k).
+ * eb_dumpdata / eb_readdata: `geometry.data` as DUMPDATA writes and READDATA reads it
+ * (electric.f:1360-1421); z holds the nbk nodes interleaved, nmax bounds nbk on read. */
+int eb_bubbin_read(const char* path, int kmax, int* k, int* nd, double* params, double* drops);
+int eb_geoinit(int k, const int* nd, const double* drops, double* z, double* dsdth, double* kappa,
+               double* area0);
+int eb_dumpdata(const char* path, int k, const int* nd, double dt, double time, const double* area0,
+                const double* arcl0, const double* z);
+int eb_readdata(const char* path, int kmax, long nmax, int* k, int* nd, double* dt, double* time,
+                double* area0, double* arcl0, double* z);
+
 /* gfortran-callable shims with the exact DGMRES MATVEC signature
  * (dpigmr.f:316-318, stokesbubb.f:419, laplace.f:429). They use the context set with
  * eb_set_default_ctx and host memory, and abort the process on error, as the
