@@ -347,6 +347,52 @@ def run_gpu(args, rank, world, local):
     r, info = rk_rate(single, "fp64", 20)
     rk["single_drop_n256/fp64"] = {"steps_per_s": r, "last_step": info}
 
+    # independent single-drop simulations of uneven sizes (N in [128, 4096], E0 U[0.1, 1]),
+    # FP32-refined RK2 steps: a bounded sample (the first 32 of the 256 seeded
+    # simulations, 4 steps each), on one context, then on 8 contexts with their own
+    # streams driven by host threads
+    import threading
+    sims = configs.uneven_simulations()[:32]
+    steps_per_sim = 4
+
+    def run_sims(nctx):
+        ctxs = [Context(device=local) for _ in range(nctx)]
+        strs = [torch.cuda.Stream(device=dev) for _ in range(nctx)]
+        for c, s_ in zip(ctxs, strs):
+            c.set_stream(s_.cuda_stream)
+        states = [torch.from_numpy(sm.rku()).to(dev) for sm in sims]
+        torch.cuda.synchronize()
+        err = []
+
+        def worker(w):
+            try:
+                for j in range(w, len(sims), nctx):
+                    for _ in range(steps_per_sim):
+                        ctxs[w].rk2(sims[j].nd, 1e-3, states[j], e0=sims[j].params["E0"],
+                                    mode="fp32_refined")
+            except Exception as exc:  # reported in the JSON line
+                err.append(repr(exc))
+
+        t0 = time.perf_counter()
+        th = [threading.Thread(target=worker, args=(w,)) for w in range(nctx)]
+        for x_ in th:
+            x_.start()
+        for x_ in th:
+            x_.join()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        for c in ctxs:
+            c.close()
+        return len(sims) * steps_per_sim / wall, err
+
+    run_sims(8)  # warm-up: graph capture and buffers
+    sim_rate1, e1 = run_sims(1)
+    sim_rate8, e8 = run_sims(8)
+    uneven = {"workload": "uneven_simulations (first 32 of 256, seed 4)", "steps_per_sim": steps_per_sim,
+              "nodes": [int(sm.nbk) for sm in sims], "mode": "fp32_refined",
+              "sim_steps_per_s_1ctx": sim_rate1, "sim_steps_per_s_8ctx": sim_rate8,
+              "errors": e1 + e8}
+
     # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
     big = configs.large_drops()
     gb = ctx.extractdat(big.nd, big.rku())
@@ -422,6 +468,7 @@ def run_gpu(args, rank, world, local):
         "clocks": clk,
         "gpu_launches": launches,
         "rk2": rk,
+        "uneven": uneven,
         "large": large,
     }
     if rank == 0:
