@@ -356,7 +356,7 @@ def run_gpu(args, rank, world, local):
     steps_per_sim = 4
 
     def run_sims(nctx):
-        ctxs = [Context(device=local) for _ in range(nctx)]
+        ctxs = [Context(device=local, graphs=graphs) for _ in range(nctx)]
         strs = [torch.cuda.Stream(device=dev) for _ in range(nctx)]
         for c, s_ in zip(ctxs, strs):
             c.set_stream(s_.cuda_stream)

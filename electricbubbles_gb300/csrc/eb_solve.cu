@@ -535,7 +535,7 @@ constexpr int GM_BUILD_FAILED = -100;  // internal: fall back to the host-driven
 // nodes of the capture and the kernel launches it issued.
 template <typename F>
 int capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* deps, size_t ndeps,
-                 std::vector<cudaGraphNode_t>* sinks, long long* nlaunch, F f) {
+                 std::vector<cudaGraphNode_t>* sinks, long long* nlaunch, bool* graph_lost, F f) {
   cudaStream_t saved = ctx->stream;
   const long long l0 = ctx->launches;
   ctx->stream = ctx->cap_stream;
@@ -561,9 +561,13 @@ int capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* deps, size_
     }
     cudaGraph_t out = nullptr;
     e = cudaStreamEndCapture(ctx->cap_stream, &out);
-    if (e != cudaSuccess && st == EB_OK) {
-      eb_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-      st = EB_ERR_CUDA;
+    if (e != cudaSuccess || out == nullptr) {
+      // an invalidated capture: the graph is not ours to destroy any more
+      if (graph_lost) *graph_lost = true;
+      if (st == EB_OK) {
+        eb_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        st = EB_ERR_CUDA;
+      }
     }
   }
   eb_devbuf_set_capturing(false);
@@ -596,7 +600,12 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   double* xx = refine ? ctx->gD.as<double>() : ctx->gX.as<double>();  // its solution
   std::vector<cudaGraphNode_t> sinks;
   // pre: norms, r0, V[:, 0]
-  EB_TRY(capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, [&]() -> int {
+  bool lost = false;
+  auto fail = [&](int st) {
+    if (lost) G.graph = nullptr;  // not destroyed by G.destroy()
+    return st;
+  };
+  int cst = capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, &lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     k_vtw<<<nb, RBS, 0, s>>>(n, 1, nullptr, bb, ldv, bb, part, hdev + GM_BN, ticket);
     eb_count_launch(ctx);
@@ -613,7 +622,8 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, V, V, ldv, xin);
     ctx->launches += 2;
     return eb_check_launch(ctx, "gmres graph (pre)");
-  }));
+  });
+  if (cst != EB_OK) return fail(cst);
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = h;
@@ -624,7 +634,8 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   // body: one Arnoldi step
   const int* lld = &ctl->ll;
-  EB_TRY(capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, [&]() -> int {
+  bool body_lost = false;
+  cst = capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, &body_lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
@@ -634,9 +645,11 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
     ctx->launches += 5;
     return eb_check_launch(ctx, "gmres graph (body)");
-  }));
+  });
+  if (body_lost) lost = true;  // the body belongs to the graph; leave the whole graph alone
+  if (cst != EB_OK) return fail(cst);
   // post: DHELS, x update; refined: x += d, r = b - A64 x with ||r||^2
-  EB_TRY(capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, [&]() -> int {
+  cst = capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, &lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     k_gm_finish<<<1, 128, 0, s>>>(ctl, hdev + GM_Y);
     k_gm_add<<<nb, RBS, 0, s>>>(n, ctl, V, ldv, hdev + GM_Y, xx);
@@ -650,7 +663,8 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
       eb_count_launch(ctx);
     }
     return eb_check_launch(ctx, "gmres graph (post)");
-  }));
+  });
+  if (cst != EB_OK) return fail(cst);
   EB_CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, 0));
   G.valid = true;
   return EB_OK;
