@@ -103,6 +103,13 @@ __global__ void k_fill_drop(int k, const int* __restrict__ start, int* __restric
   }
 }
 
+__global__ void k_post_coefs(int nbk, const double2* __restrict__ dz, const double* __restrict__ dsda,
+                             const double* __restrict__ kappa, const double* __restrict__ hpt,
+                             double* __restrict__ c1, double2* __restrict__ c2, double* __restrict__ d) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nbk) eb_post_coefs(t, dz, dsda, kappa, hpt, c1, c2, d);
+}
+
 int copy_in(eb_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem) {
   EB_TRY(buf.ensure(bytes));
   EB_CUDA_TRY(cudaMemcpyAsync(buf.p, src, bytes,
@@ -314,6 +321,14 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   EB_TRY(copy_in(ctx, ctx->zk, zk, sizeof(double2) * k, mem));
   k_fill_drop<<<k, 256, 0, s>>>(k, ctx->start.as<int>(), ctx->drop_of.as<int>(), ctx->hpt.as<double>());
   eb_count_launch(ctx);
+  EB_TRY(ctx->pc1.ensure(sizeof(double) * nbk));
+  EB_TRY(ctx->pc2.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->plap.ensure(sizeof(double) * nbk));
+  k_post_coefs<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
+                                             ctx->kappa.as<double>(), ctx->hpt.as<double>(),
+                                             ctx->pc1.as<double>(), ctx->pc2.as<double2>(),
+                                             ctx->plap.as<double>());
+  eb_count_launch(ctx);
   EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
   ctx->tree_pv.valid = false;
   ctx->geom_valid = true;
@@ -347,8 +362,8 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
                                                        ctx->za.as<double2>(), ctx->pk.as<double>());
   eb_count_launch(ctx);
   EB_CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side_stream));
-  EbPost post{1, dens, nullptr, ctx->z.as<double2>(), ctx->dz.as<double2>(), ctx->dsda.as<double>(),
-               ctx->kappa.as<double>(), ctx->hpt.as<double>(), ctx->drop_of.as<int>(),
+  EbPost post{1, dens, nullptr, ctx->z.as<double2>(), ctx->dz.as<double2>(), ctx->hpt.as<double>(),
+               ctx->pc1.as<double>(), ctx->pc2.as<double2>(), ctx->drop_of.as<int>(),
                ctx->za.as<double2>(), ctx->pk.as<double>(), y};
   EB_TRY(eb_fmm_apply(ctx, ctx->tree, 0, -1, prec, dens, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                       nullptr, &post, ctx->ev_join));
@@ -360,8 +375,8 @@ int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   cudaStream_t s = ctx->stream;
   // the Cauchy charges q = u dz h of FASMVP_LAP (laplace.f:190-200) are formed by the
   // FMM's charge kernel from u (EbPost::u)
-  EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
-               ctx->kappa.as<double>(), ctx->hpt.as<double>(), nullptr, nullptr, nullptr, y};
+  EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
+               ctx->plap.as<double>(), nullptr, nullptr, nullptr, nullptr, y};
   EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, nullptr, nullptr, &post));
   return eb_check_launch(ctx, "laplace matvec");
 }

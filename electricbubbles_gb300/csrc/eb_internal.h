@@ -140,6 +140,7 @@ struct eb_ctx {
   DevBuf nd, start, drop_of;     // int[k], int[k+1], int[nbk]
   DevBuf z, dz, zk, ckern;       // double2
   DevBuf dsda, kappa, tha, hpt;  // double
+  DevBuf pc1, pc2, plap;         // per-node post-processing coefficients (eb_post_coefs)
   bool geom_valid = false;
   bool ckern_valid = false;       // ckern/tha filled by eb_extractdat
 
