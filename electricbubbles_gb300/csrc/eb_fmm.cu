@@ -1164,8 +1164,7 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
                                                 const int* __restrict__ ucount,
                                                 const int* __restrict__ perm,
                                                 const float4* __restrict__ wa,
-                                                const float2* __restrict__ zhi,
-                                                const float2* __restrict__ zlo,
+                                                const float4* __restrict__ zhl,
                                                 const float2* __restrict__ pq,
                                                 const float2* __restrict__ aa,
                                                 const float2* __restrict__ qa, int L,
@@ -1180,7 +1179,8 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   const int i = gfirst[g] + tg;
   const bool act = i < pt1[b];
   const int ii = act ? i : gfirst[g];
-  const float2 hi = zhi[ii], lo = zlo[ii];
+  const float4 hl = zhl[ii];
+  const float2 hi = make_float2(hl.x, hl.y), lo = make_float2(hl.z, hl.w);
   float fx = 0.f, fy = 0.f;
   if (MODE != 1 && has_far) {
     // The M2L expansion of the leaf and of each ancestor (levels L .. 2), each evaluated
@@ -1208,14 +1208,15 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
     const int j1 = pt1[sb];
     for (int j = pt0[sb] + sl; j < j1; j += 4) {
       if (j == ii) continue;
-      float2 hj = zhi[j], lj = zlo[j];
-      float dx = (hj.x - hi.x) + (lj.x - lo.x);
-      float dy = (hj.y - hi.y) + (lj.y - lo.y);
+      const float4 hlj = zhl[j];
+      float dx = (hlj.x - hi.x) + (hlj.z - lo.x);
+      float dy = (hlj.y - hi.y) + (hlj.w - lo.y);
       float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
       float ix = dx * rr, iy = -dy * rr;
       float tx_, ty_;
       if (E == 2) {
-        float2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
+        const float4 PQ = reinterpret_cast<const float4*>(pq)[j];  // (P, Q)
+        const float2 P = make_float2(PQ.x, PQ.y), Q = make_float2(PQ.z, PQ.w), A = aa[j];
         float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
         float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
         tx_ = fmaf(P.x, ix, fmaf(-P.y, iy, fmaf(A.x, tx, -A.y * ty)));
@@ -1553,7 +1554,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
       k_leaf32<E, 1><<<blocks, 128, 0, ss>>>(
           t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, 0, t.bkey.as<unsigned long long>(),
           t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-          t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+          t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
           w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
           (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
     }
@@ -1579,7 +1580,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     k_leaf32<E, 2><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-        t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+        t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
         w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
         (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
   } else if (df) {
@@ -1599,7 +1600,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     k_leaf32<E, 0><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
         t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-        t.wdf.as<float4>(), t.zhi.as<float2>(), t.zlo.as<float2>(), w.pq.as<float2>(),
+        t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
         w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
         (float)sign, w.local.as<float2>(), out, post, nullptr);
   }

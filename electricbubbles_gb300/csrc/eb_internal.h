@@ -52,7 +52,7 @@ struct EbTree {
 
   DevBuf perm;     // int[n]: sorted index -> original index
   DevBuf zs;       // double2[n]: sorted positions
-  DevBuf zhi, zlo; // float2[n]: sorted positions as float hi + lo
+  DevBuf zhl;      // float4[n]: sorted positions as float hi + lo, (hi.x, hi.y, lo.x, lo.y)
   DevBuf wdf;      // float4[n]: offset from the leaf centre in leaf units, (x.hi, y.hi, x.mid, y.mid)
   DevBuf wdf_lo;   // float2[n]: (x.lo, y.lo) of the same offset
   DevBuf keys, keys_alt, idx_alt;  // sort buffers

@@ -120,16 +120,15 @@ __global__ void k_level_hist(const unsigned long long* __restrict__ keys, int n,
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
+// sorted positions, also as float hi + lo pairs packed (hi.x, hi.y, lo.x, lo.y)
 __global__ void k_gather_points(const double2* __restrict__ z, const int* __restrict__ perm,
-                                int n, double2* __restrict__ zs, float2* __restrict__ zhi,
-                                float2* __restrict__ zlo) {
+                                int n, double2* __restrict__ zs, float4* __restrict__ zhl) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double2 p = z[perm[i]];
   zs[i] = p;
   float hx = (float)p.x, hy = (float)p.y;
-  zhi[i] = make_float2(hx, hy);
-  zlo[i] = make_float2((float)(p.x - (double)hx), (float)(p.y - (double)hy));
+  zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
 }
 
 __global__ void k_heads(const unsigned long long* __restrict__ keys, int n, int shift,
@@ -459,10 +458,9 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   eb_count_launch(ctx);
   // 3. sorted positions
   EB_TRY(t.zs.ensure(sizeof(double2) * (size_t)n));
-  EB_TRY(t.zhi.ensure(sizeof(float2) * (size_t)n));
-  EB_TRY(t.zlo.ensure(sizeof(float2) * (size_t)n));
+  EB_TRY(t.zhl.ensure(sizeof(float4) * (size_t)n));
   k_gather_points<<<nblk(n, BS), BS, 0, st>>>(z, t.perm.as<int>(), n, t.zs.as<double2>(),
-                                              t.zhi.as<float2>(), t.zlo.as<float2>());
+                                              t.zhl.as<float4>());
   eb_count_launch(ctx);
   // 4. occupied boxes per level, leaf level
   EB_TRY(t.hist.ensure(sizeof(int) * (EB_KEY_LEVELS + 1)));
