@@ -105,9 +105,10 @@ __global__ void k_fill_drop(int k, const int* __restrict__ start, int* __restric
 
 __global__ void k_post_coefs(int nbk, const double2* __restrict__ dz, const double* __restrict__ dsda,
                              const double* __restrict__ kappa, const double* __restrict__ hpt,
-                             double* __restrict__ c1, double2* __restrict__ c2, double* __restrict__ d) {
+                             double* __restrict__ c1, double2* __restrict__ c2, double* __restrict__ d,
+                             float* __restrict__ c1f, float2* __restrict__ c2f, float* __restrict__ df) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nbk) eb_post_coefs(t, dz, dsda, kappa, hpt, c1, c2, d);
+  if (t < nbk) eb_post_coefs(t, dz, dsda, kappa, hpt, c1, c2, d, c1f, c2f, df);
 }
 
 int copy_in(eb_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem) {
@@ -324,10 +325,14 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   EB_TRY(ctx->pc1.ensure(sizeof(double) * nbk));
   EB_TRY(ctx->pc2.ensure(sizeof(double2) * nbk));
   EB_TRY(ctx->plap.ensure(sizeof(double) * nbk));
+  EB_TRY(ctx->pc1f.ensure(sizeof(float) * nbk));
+  EB_TRY(ctx->pc2f.ensure(sizeof(float2) * nbk));
+  EB_TRY(ctx->plapf.ensure(sizeof(float) * nbk));
   k_post_coefs<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
                                              ctx->kappa.as<double>(), ctx->hpt.as<double>(),
                                              ctx->pc1.as<double>(), ctx->pc2.as<double2>(),
-                                             ctx->plap.as<double>());
+                                             ctx->plap.as<double>(), ctx->pc1f.as<float>(),
+                                             ctx->pc2f.as<float2>(), ctx->plapf.as<float>());
   eb_count_launch(ctx);
   EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
   ctx->tree_pv.valid = false;
@@ -364,7 +369,8 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   EB_CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side_stream));
   EbPost post{1, dens, nullptr, ctx->z.as<double2>(), ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                ctx->pc1.as<double>(), ctx->pc2.as<double2>(), ctx->drop_of.as<int>(),
-               ctx->za.as<double2>(), ctx->pk.as<double>(), y};
+               ctx->za.as<double2>(), ctx->pk.as<double>(), y, ctx->pc1f.as<float>(),
+               ctx->pc2f.as<float2>()};
   EB_TRY(eb_fmm_apply(ctx, ctx->tree, 0, -1, prec, dens, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                       nullptr, &post, ctx->ev_join));
   return eb_check_launch(ctx, "stokes matvec");
@@ -376,7 +382,8 @@ int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   // the Cauchy charges q = u dz h of FASMVP_LAP (laplace.f:190-200) are formed by the
   // FMM's charge kernel from u (EbPost::u)
   EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
-               ctx->plap.as<double>(), nullptr, nullptr, nullptr, nullptr, y};
+               ctx->plap.as<double>(), nullptr, nullptr, nullptr, nullptr, y, ctx->plapf.as<float>(),
+               nullptr};
   EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, nullptr, nullptr, &post));
   return eb_check_launch(ctx, "laplace matvec");
 }

@@ -1237,15 +1237,15 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   gx += __shfl_xor_sync(0xffffffffu, gx, 2);
   gy += __shfl_xor_sync(0xffffffffu, gy, 2);
   if (sl == 0 && act) {
-    double2 v = make_double2((double)gx, (double)gy);
     if (MODE == 1) {
-      nearbuf[i] = v;
+      nearbuf[i] = make_double2((double)gx, (double)gy);
     } else {
+      float2 v = make_float2(gx, gy);
       if (MODE == 2) {
         const double2 nv = nearbuf[i];
-        v = make_double2(v.x + nv.x, v.y + nv.y);
+        v = make_float2(v.x + (float)nv.x, v.y + (float)nv.y);
       }
-      eb_post_store(post, perm[i], v, out);
+      eb_post_store_f32(post, perm[i], v, out);
     }
   }
 }

@@ -141,6 +141,7 @@ struct eb_ctx {
   DevBuf z, dz, zk, ckern;       // double2
   DevBuf dsda, kappa, tha, hpt;  // double
   DevBuf pc1, pc2, plap;         // per-node post-processing coefficients (eb_post_coefs)
+  DevBuf pc1f, pc2f, plapf;      // their float copies (FP32 operator)
   bool geom_valid = false;
   bool ckern_valid = false;       // ckern/tha filled by eb_extractdat
 
