@@ -209,6 +209,8 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_p2p, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev_near0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev_near1);
   if (e != cudaSuccess) {
     eb_set_last_cuda_error(e, "context setup", __FILE__, __LINE__);
     delete c;
@@ -230,6 +232,8 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev_near0) cudaEventDestroy(ctx->ev_near0);
+  if (ctx->ev_near1) cudaEventDestroy(ctx->ev_near1);
   for (GmGraph& g : ctx->gcache) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
@@ -260,13 +264,15 @@ long long eb_ctx_launch_count(eb_ctx* ctx) { return ctx ? ctx->launches : -1; }
 int eb_ctx_set_profiling(eb_ctx* ctx, int enable) {
   if (!ctx) return EB_ERR_ARG;
   ctx->profiling = enable != 0;
-  ctx->prof_launch[0] = ctx->prof_launch[1] = 0;
-  ctx->prof_ms[0] = ctx->prof_ms[1] = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    ctx->prof_launch[k] = 0;
+    ctx->prof_ms[k] = 0.0;
+  }
   return EB_OK;
 }
 
 int eb_ctx_kernel_time(eb_ctx* ctx, int cls, long long* launches, double* total_ms) {
-  if (!ctx || cls < 0 || cls > 1) return EB_ERR_ARG;
+  if (!ctx || cls < 0 || cls > 2) return EB_ERR_ARG;
   if (launches) *launches = ctx->prof_launch[cls];
   if (total_ms) *total_ms = ctx->prof_ms[cls];
   return EB_OK;

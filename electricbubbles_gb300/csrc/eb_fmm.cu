@@ -1145,8 +1145,6 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   }
 }
 
-// FP32 leaf evaluation: node positions as float hi + lo so that differences are exact
-// to float precision, Kahan-compensated per-lane sums.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   float y = v - c;
   float t = s + y;
@@ -1154,24 +1152,20 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-// MODE as for k_leaf_df.
-template <int E, int MODE>
-__global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restrict__ gleaf,
-                                                const int* __restrict__ gfirst, int off, int has_far,
-                                                const unsigned long long* __restrict__ bkey,
-                                                const int* __restrict__ pt0, const int* __restrict__ pt1,
-                                                const int* __restrict__ ulist,
-                                                const int* __restrict__ ucount,
-                                                const int* __restrict__ perm,
-                                                const float4* __restrict__ wa,
-                                                const float4* __restrict__ zhl,
-                                                const float2* __restrict__ pq,
-                                                const float2* __restrict__ aa,
-                                                const float2* __restrict__ qa, int L,
-                                                const int* __restrict__ parent, int p, float s,
-                                                const float2* __restrict__ local,
-                                                double2* __restrict__ out, EbPost post,
-                                                double2* __restrict__ nearbuf) {
+// FP32 far field: warp per EB_GROUP targets of one leaf, 4 lanes per target each taking
+// a quarter of the expansion orders. Adds the near-field sums of k_near32 and applies the
+// post-processing.
+template <int E>
+__global__ void __launch_bounds__(128) k_far32(int ngroup, const int* __restrict__ gleaf,
+                                               const int* __restrict__ gfirst, int off, int has_far,
+                                               const unsigned long long* __restrict__ bkey,
+                                               const int* __restrict__ pt1,
+                                               const int* __restrict__ perm,
+                                               const float4* __restrict__ wa, int L,
+                                               const int* __restrict__ parent, int p, float s,
+                                               const float2* __restrict__ local,
+                                               double2* __restrict__ out, EbPost post,
+                                               const double2* __restrict__ nearbuf) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
@@ -1179,10 +1173,8 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
   const int i = gfirst[g] + tg;
   const bool act = i < pt1[b];
   const int ii = act ? i : gfirst[g];
-  const float4 hl = zhl[ii];
-  const float2 hi = make_float2(hl.x, hl.y), lo = make_float2(hl.z, hl.w);
   float fx = 0.f, fy = 0.f;
-  if (MODE != 1 && has_far) {
+  if (has_far) {
     // The M2L expansion of the leaf and of each ancestor (levels L .. 2), each evaluated
     // about its own centre: the sum equals L2P of the L2L-accumulated leaf expansion.
     // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
@@ -1201,28 +1193,110 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
       a = parent[a];
     }
   }
+  fx += __shfl_xor_sync(0xffffffffu, fx, 1);
+  fy += __shfl_xor_sync(0xffffffffu, fy, 1);
+  fx += __shfl_xor_sync(0xffffffffu, fx, 2);
+  fy += __shfl_xor_sync(0xffffffffu, fy, 2);
+  if (sl == 0 && act) {
+    const double2 nv = nearbuf[i];
+    eb_post_store_f32(post, perm[i], make_float2(fx + (float)nv.x, fy + (float)nv.y), out);
+  }
+}
+
+// FP32 near field, one block per tile of up to EB_NTILE targets of one leaf: the sources
+// of the leaf's U list are staged through shared memory in slabs of NEAR_SLAB, and each
+// of the 128 / EB_NTILE warps sums one slice of every slab for all targets of the tile
+// (a shared-memory broadcast per source). Per-thread Kahan-compensated sums; the slices
+// are added in a fixed order. Writes the near-field sums in sorted order.
+#define NEAR_SLAB 256
+template <int E>
+__global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tiles, int off,
+                                                   const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                   const int* __restrict__ ulist,
+                                                   const int* __restrict__ ucount,
+                                                   const float4* __restrict__ zhl,
+                                                   const float2* __restrict__ pq,
+                                                   const float2* __restrict__ aa,
+                                                   const float2* __restrict__ qa,
+                                                   double2* __restrict__ nearbuf) {
+  constexpr int T = EB_NTILE, NS = 128 / T;
+  __shared__ float4 sz[NEAR_SLAB];
+  __shared__ float4 sp[E == 2 ? NEAR_SLAB : 1];
+  __shared__ float2 sa[NEAR_SLAB];
+  __shared__ int spre[EB_UMAX + 1], sj0[EB_UMAX], sself;
+  __shared__ float2 sred[NS][T];
+  const int4 tl = tiles[blockIdx.x];
+  const int leaf = tl.x, b = off + leaf;
+  const int tid = threadIdx.x, tt = tid % T, sl = tid / T;
+  const int i = tl.y + tt;
+  const bool act = i < tl.z;
+  const int ii = act ? i : tl.y;
+  if (tid < 32) {
+    const int nu = ucount[leaf];
+    int c = 0, j0 = 0, sb = -1;
+    if (tid < nu) {
+      sb = ulist[(size_t)leaf * EB_UMAX + tid];
+      j0 = pt0[sb];
+      c = pt1[sb] - j0;
+    }
+    int x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (tid >= o) x += y;
+    }
+    if (tid < EB_UMAX) {
+      sj0[tid] = j0;
+      spre[tid + 1] = x;
+    }
+    if (tid == 0) spre[0] = 0;
+    const unsigned int m = __ballot_sync(0xffffffffu, sb == b);
+    if (tid == 0) sself = __ffs(m) - 1;
+  }
+  __syncthreads();
+  const int total = spre[EB_UMAX];
+  const int ks = sself;
+  // staged position of the target itself (its own leaf is in its U list)
+  const int selfpos = ks >= 0 ? spre[ks] + (ii - sj0[ks]) : -1;
+  const float4 hl = zhl[ii];
   float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
-  const int nu = MODE == 2 ? 0 : ucount[leaf];
-  for (int jl = 0; jl < nu; ++jl) {
-    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
-    const int j1 = pt1[sb];
-    for (int j = pt0[sb] + sl; j < j1; j += 4) {
-      if (j == ii) continue;
-      const float4 hlj = zhl[j];
-      float dx = (hlj.x - hi.x) + (hlj.z - lo.x);
-      float dy = (hlj.y - hi.y) + (hlj.w - lo.y);
+  for (int base = 0; base < total; base += NEAR_SLAB) {
+    const int ns = min(NEAR_SLAB, total - base);
+    if (base > 0) __syncthreads();
+    for (int s2 = tid; s2 < ns; s2 += 128) {
+      const int gs = base + s2;
+      int k = 0;
+#pragma unroll
+      for (int q = 1; q < EB_UMAX; ++q) k += gs >= spre[q];
+      const int j = sj0[k] + gs - spre[k];
+      sz[s2] = zhl[j];
+      if (E == 2) {
+        sp[s2] = reinterpret_cast<const float4*>(pq)[j];
+        sa[s2] = aa[j];
+      } else {
+        sa[s2] = qa[j];
+      }
+    }
+    __syncthreads();
+    const int sp0 = selfpos - base;
+#pragma unroll 4
+    for (int jj = sl; jj < ns; jj += NS) {
+      const float4 hlj = sz[jj];
+      const float dx = (hlj.x - hl.x) + (hlj.z - hl.z);
+      const float dy = (hlj.y - hl.y) + (hlj.w - hl.w);
       float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
-      float ix = dx * rr, iy = -dy * rr;
+      rr = jj == sp0 ? 0.f : rr;  // the self pair (dx = dy = 0) contributes nothing
+      const float ix = dx * rr, iy = -dy * rr;
       float tx_, ty_;
       if (E == 2) {
-        const float4 PQ = reinterpret_cast<const float4*>(pq)[j];  // (P, Q)
-        const float2 P = make_float2(PQ.x, PQ.y), Q = make_float2(PQ.z, PQ.w), A = aa[j];
-        float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
-        float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
-        tx_ = fmaf(P.x, ix, fmaf(-P.y, iy, fmaf(A.x, tx, -A.y * ty)));
-        ty_ = fmaf(Q.x, iy, fmaf(Q.y, ix, fmaf(A.x, ty, A.y * tx)));
+        const float4 PQ = sp[jj];
+        const float2 A = sa[jj];
+        const float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
+        const float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
+        tx_ = fmaf(PQ.x, ix, fmaf(-PQ.y, iy, fmaf(A.x, tx, -A.y * ty)));
+        ty_ = fmaf(PQ.z, iy, fmaf(PQ.w, ix, fmaf(A.x, ty, A.y * tx)));
       } else {
-        float2 q = qa[j];
+        const float2 q = sa[jj];
         tx_ = fmaf(-q.x, ix, q.y * iy);
         ty_ = fmaf(-q.x, iy, -q.y * ix);
       }
@@ -1230,23 +1304,16 @@ __global__ void __launch_bounds__(128) k_leaf32(int ngroup, const int* __restric
       kahan_add(gy, cy, ty_);
     }
   }
-  gx = (gx - cx) + fx;
-  gy = (gy - cy) + fy;
-  gx += __shfl_xor_sync(0xffffffffu, gx, 1);
-  gy += __shfl_xor_sync(0xffffffffu, gy, 1);
-  gx += __shfl_xor_sync(0xffffffffu, gx, 2);
-  gy += __shfl_xor_sync(0xffffffffu, gy, 2);
+  sred[sl][tt] = make_float2(gx - cx, gy - cy);
+  __syncthreads();
   if (sl == 0 && act) {
-    if (MODE == 1) {
-      nearbuf[i] = make_double2((double)gx, (double)gy);
-    } else {
-      float2 v = make_float2(gx, gy);
-      if (MODE == 2) {
-        const double2 nv = nearbuf[i];
-        v = make_float2(v.x + (float)nv.x, v.y + (float)nv.y);
-      }
-      eb_post_store_f32(post, perm[i], v, out);
+    float2 v = sred[0][tt];
+#pragma unroll
+    for (int q = 1; q < NS; ++q) {
+      v.x += sred[q][tt].x;
+      v.y += sred[q][tt].y;
     }
+    nearbuf[i] = make_double2((double)v.x, (double)v.y);
   }
 }
 
@@ -1340,15 +1407,18 @@ struct ProfScope {
   eb_ctx* ctx;
   int cls;
   cudaStream_t st;
+  cudaEvent_t e0, e1;
   ProfScope(eb_ctx* c, int k, cudaStream_t s) : ctx(c), cls(k), st(s) {
-    if (ctx->profiling) cudaEventRecord(ctx->ev0, st);
+    e0 = k == 2 ? ctx->ev_near0 : ctx->ev0;
+    e1 = k == 2 ? ctx->ev_near1 : ctx->ev1;
+    if (ctx->profiling) cudaEventRecord(e0, st);
   }
   void done() {
     if (!ctx->profiling) return;
-    cudaEventRecord(ctx->ev1, st);
-    cudaEventSynchronize(ctx->ev1);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ms, e0, e1);
     ctx->prof_launch[cls]++;
     ctx->prof_ms[cls] += ms;
   }
@@ -1551,12 +1621,10 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
           t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
           (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
     } else {
-      k_leaf32<E, 1><<<blocks, 128, 0, ss>>>(
-          t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, 0, t.bkey.as<unsigned long long>(),
-          t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-          t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
-          w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
-          (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+      k_near32<E><<<t.ntile, 128, 0, ss>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
+                                           t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
+                                           w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
+                                           w.nearbuf.as<double2>());
     }
     eb_count_launch(ctx);
     EB_CUDA_TRY(cudaEventRecord(ctx->ev_p2p, ss));
@@ -1577,12 +1645,10 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
   } else if (split) {
-    k_leaf32<E, 2><<<blocks, 128, 0, st>>>(
-        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
-        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-        t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
-        w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
-        (float)sign, w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+    k_far32<E><<<blocks, 128, 0, st>>>(t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far,
+                                        t.bkey.as<unsigned long long>(), t.pt1.as<int>(), t.perm.as<int>(),
+                                        t.wdf.as<float4>(), t.L, t.parent.as<int>(), tb.p, (float)sign,
+                                        w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
   } else if (df) {
     k_leaf_df<E, 0><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
@@ -1597,12 +1663,19 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
         rleaf, tb.p, (double)sign, w.local.as<double2>(), out, post);
   } else {
-    k_leaf32<E, 0><<<blocks, 128, 0, st>>>(
-        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
-        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
-        t.wdf.as<float4>(), t.zhl.as<float4>(), w.pq.as<float2>(),
-        w.aa.as<float2>(), w.qa.as<float2>(), t.L, t.parent.as<int>(), tb.p,
-        (float)sign, w.local.as<float2>(), out, post, nullptr);
+    // FP32 without the split: near-field kernel, then the far field on the same stream
+    EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
+    ProfScope pn(ctx, 2, st);
+    k_near32<E><<<t.ntile, 128, 0, st>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
+                                         t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
+                                         w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
+                                         w.nearbuf.as<double2>());
+    eb_count_launch(ctx);
+    pn.done();
+    k_far32<E><<<blocks, 128, 0, st>>>(t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far,
+                                        t.bkey.as<unsigned long long>(), t.pt1.as<int>(), t.perm.as<int>(),
+                                        t.wdf.as<float4>(), t.L, t.parent.as<int>(), tb.p, (float)sign,
+                                        w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
   ps.done();

@@ -16,6 +16,7 @@
 #define EB_UMAX 9
 #define EB_NCODE 49
 #define EB_GROUP 8
+#define EB_NTILE 32
 
 // ---------------------------------------------------------------------------------
 // Device buffer that grows on demand (never shrinks) and frees itself. Every
@@ -69,6 +70,10 @@ struct EbTree {
   int ngroup = 0;
   DevBuf gleaf;    // int[ngroup]: leaf index (0-based within the leaf level)
   DevBuf gfirst;   // int[ngroup]: first sorted target of the group
+  // shared-memory near-field work items: tiles of up to EB_NTILE targets of one leaf,
+  // a leaf's targets split evenly over its tiles
+  int ntile = 0;
+  DevBuf tiles;    // int4[ntile]: (leaf, first, end, 0)
   DevBuf flags, scan, hist, bbox, partial, cubtmp;
   // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
   // EB_CHUNK points (coarser levels by M2M)
@@ -129,8 +134,9 @@ struct eb_ctx {
   long long launches = 0;
   bool profiling = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  long long prof_launch[2] = {0, 0};
-  double prof_ms[2] = {0, 0};
+  cudaEvent_t ev_near0 = nullptr, ev_near1 = nullptr;  // kernel class 2 (nested in class 0)
+  long long prof_launch[3] = {0, 0, 0};
+  double prof_ms[3] = {0, 0, 0};
   int last_p = 0;
 
   // installed geometry (COMMON /inteqn/ and /problem/)

@@ -293,6 +293,23 @@ __global__ void k_group_fill(int off, int nleaf, const int* __restrict__ pt0,
   }
 }
 
+__global__ void k_tile_count(int off, int nleaf, const int* __restrict__ pt0,
+                             const int* __restrict__ pt1, int* __restrict__ cnt) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nleaf) return;
+  cnt[b] = (pt1[off + b] - pt0[off + b] + EB_NTILE - 1) / EB_NTILE;
+}
+
+__global__ void k_tile_fill(int off, int nleaf, const int* __restrict__ pt0, const int* __restrict__ pt1,
+                            const int* __restrict__ cnt, const int* __restrict__ start,
+                            int4* __restrict__ tiles) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nleaf) return;
+  const int g0 = start[b], c = cnt[b], a = pt0[off + b], nt = pt1[off + b] - a;
+  for (int g = 0; g < c; ++g)
+    tiles[g0 + g] = make_int4(b, a + (int)((long long)g * nt / c), a + (int)((long long)(g + 1) * nt / c), 0);
+}
+
 __global__ void k_chunk_count(int first, int nb, const int* __restrict__ pt0, const int* __restrict__ pt1,
                               int* __restrict__ cnt) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,6 +575,25 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
     k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
                                               t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
+    eb_count_launch(ctx);
+  }
+  // 8a. shared-memory near-field tiles of at most EB_NTILE targets
+  {
+    int nl = t.nleaf;
+    k_tile_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                              t.flags.as<int>());
+    eb_count_launch(ctx);
+    tb = t.cubtmp.bytes;
+    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
+    eb_count_launch(ctx);
+    int last[2];
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaStreamSynchronize(st));
+    t.ntile = last[0] + last[1];
+    EB_TRY(t.tiles.ensure(sizeof(int4) * (size_t)t.ntile));
+    k_tile_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                             t.flags.as<int>(), t.scan.as<int>(), t.tiles.as<int4>());
     eb_count_launch(ctx);
   }
   // 8b. chunks of at most EB_CHUNK points of every box of the EB_DIRECT_LEVELS finest

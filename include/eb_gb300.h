@@ -131,7 +131,8 @@ int eb_ctx_sync(eb_ctx* ctx);
 long long eb_ctx_launch_count(eb_ctx* ctx);
 /* When enabled, the dominant near-field and M2L kernels are bracketed by CUDA
  * events on the context's stream; eb_ctx_kernel_time reports launches and total
- * milliseconds per kernel class (0: near field P2P+L2P, 1: M2L). */
+ * milliseconds per kernel class (0: the leaf evaluation, near field P2P + L2P;
+ * 1: M2L; 2: the near-field kernel alone where it is a launch of its own). */
 int eb_ctx_set_profiling(eb_ctx* ctx, int enable);
 int eb_ctx_kernel_time(eb_ctx* ctx, int kernel_class, long long* launches, double* total_ms);
 int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
