@@ -726,11 +726,11 @@ __global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
 }
 
 // ---------------------------------------------------------------------------------
-// FP32 multipoles of every box of levels 2..L directly from its points, in parallel
-// over all levels (no dependent M2M chain): one block per chunk of at most EB_CHUNK
-// points forms that chunk's contribution (the P2M sums of SLMKXP, cadap2.f:412-468,
-// scaled by the box side and relative to the box centre), and k_chunk_sum adds the
-// chunks of each box in order. The offset of a point from an ancestor's centre in the
+// FP32 multipoles of every box of the finest levels directly from its points, in
+// parallel over those levels (no dependent M2M chain): one block per chunk of at most
+// EB_CHUNK points forms that chunk's contribution (the P2M sums of SLMKXP,
+// cadap2.f:412-468, scaled by the box side and relative to the box centre), and the
+// last chunk of a box to finish adds the chunks of the box in order. The offset of a point from an ancestor's centre in the
 // ancestor's units is u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2 from its leaf offset
 // u and leaf grid index i, exact apart from the rounding of u.
 // ---------------------------------------------------------------------------------
@@ -739,18 +739,24 @@ struct LevOff {
 };
 
 template <int E>
-__global__ void __launch_bounds__(64) k_p2m_chunks(int L, int lmin, LevOff lo, int first2,
-                                                   const int* __restrict__ chunk_box,
-                                                   const int* __restrict__ cstart,
-                                                   const unsigned long long* __restrict__ keys,
-                                                   const int* __restrict__ pt0, const int* __restrict__ pt1,
-                                                   const float4* __restrict__ wa, const float2* __restrict__ qa,
-                                                   const float2* __restrict__ qb, double W, int p,
-                                                   float2* __restrict__ mpart) {
+__global__ void __launch_bounds__(128) k_p2m_chunks(int L, int lmin, LevOff lo, int first2,
+                                                    const int* __restrict__ chunk_box,
+                                                    const int* __restrict__ cstart,
+                                                    const unsigned long long* __restrict__ keys,
+                                                    const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                    const float4* __restrict__ wa, const float2* __restrict__ qa,
+                                                    const float2* __restrict__ qb, double W, int p,
+                                                    float2* __restrict__ mpart, int* __restrict__ cdone,
+                                                    float2* __restrict__ mpole) {
+  // Sums per chunk: A_k = sum a w^k, B_k = sum b w^k, C_k = sum conj(w) a w^k (a, b the
+  // scaled charges), multipole -A_k and -(B_k + k C_(k-1)).
+  constexpr int NA = E == 2 ? 3 : 1;
   extern __shared__ float2 sm2[];
-  const int ps = p + 1;
-  float2* pw = sm2;
-  float2* sc = pw + 32 * ps;
+  const int ps = p + 1, nacc = NA * p, nout = E * p;
+  float2* pw = sm2;                  // [EB_CHUNK][p + 1]: w^k per point
+  float2* sc = pw + EB_CHUNK * ps;   // [NA][EB_CHUNK]: a, b, conj(w) a per point
+  float2* red = sc + NA * EB_CHUNK;  // [2][nacc]: the sums over each half of the points
+  __shared__ int s_last;
   const int c = blockIdx.x, tid = threadIdx.x;
   const int b = chunk_box[c];
   int l = lmin;
@@ -758,58 +764,75 @@ __global__ void __launch_bounds__(64) k_p2m_chunks(int L, int lmin, LevOff lo, i
   const int sh = L - l;
   const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
   const float rinv = (float)((double)(1u << l) / W);
-  const int i0 = pt0[b] + (c - cstart[b - first2]) * EB_CHUNK;
-  const int i1 = min(pt1[b], i0 + EB_CHUNK);
+  const int bb = b - first2, c0 = cstart[bb], nc = cstart[bb + 1] - c0;
+  const int i0 = pt0[b] + (c - c0) * EB_CHUNK;
+  const int cnt = min(pt1[b], i0 + EB_CHUNK) - i0;
   const int lshift = 2 * (EB_KEY_LEVELS - L);
-  float2 A = make_float2(0.f, 0.f), B = A, C = A;
-  for (int base = i0; base < i1; base += 32) {
-    const int cnt = min(32, i1 - base);
-    __syncthreads();
-    if (tid < cnt) {
-      const int i = base + tid;
+  {
+    // two threads per point: even and odd powers
+    const int sp = tid >> 1, h = tid & 1;
+    if (sp < cnt) {
+      const int i = i0 + sp;
       const unsigned long long kl = keys[i] >> lshift;
       const unsigned int ix = compact2d(kl), iy = compact2d(kl >> 1);
       const float4 wv = wa[i];
       const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
       const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
       const float2 w = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
-      const float2 ah = cscale<float>(qa[i], rinv);
-      sc[tid] = ah;
-      if (E == 2) {
-        sc[32 + tid] = cscale<float>(qb[i], rinv);
-        sc[64 + tid] = cmul<float>(cconj<float>(w), ah);
-      }
-      float2 pwr = make_float2(1.f, 0.f);
-      float2* row = pw + tid * ps;
-      for (int j = 0; j < p; ++j) {
-        row[j] = pwr;
-        pwr = cmul<float>(pwr, w);
-      }
-    }
-    __syncthreads();
-    if (tid < p) {
-      for (int s = 0; s < cnt; ++s) {
-        const float2 v = pw[s * ps + tid];
-        cfma<float>(A, sc[s], v);
+      if (h == 0) {
+        const float2 ah = cscale<float>(qa[i], rinv);
+        sc[sp] = ah;
         if (E == 2) {
-          cfma<float>(B, sc[32 + s], v);
-          cfma<float>(C, sc[64 + s], v);
+          sc[EB_CHUNK + sp] = cscale<float>(qb[i], rinv);
+          sc[2 * EB_CHUNK + sp] = cmul<float>(cconj<float>(w), ah);
         }
       }
+      const float2 w2 = cmul<float>(w, w);
+      float2 cur = h ? w : make_float2(1.f, 0.f);
+      float2* row = pw + sp * ps;
+      for (int j = h; j < p; j += 2) {
+        row[j] = cur;
+        cur = cmul<float>(cur, w2);
+      }
     }
   }
   __syncthreads();
-  if (tid < p) pw[tid] = C;
-  __syncthreads();
-  if (tid < p) {
-    float2* mp = mpart + (size_t)c * E * p;
-    mp[tid] = make_float2(-A.x, -A.y);
-    if (E == 2) {
-      float2 v = B;
-      if (tid >= 1) crfma<float>(v, (float)tid, pw[tid - 1]);
-      mp[p + tid] = make_float2(-v.x, -v.y);
+  {
+    const int half = tid >> 6, s0 = half * 32, s1 = min(cnt, s0 + 32);
+    for (int o = tid & 63; o < nacc; o += 64) {
+      const int which = o / p, k = o - which * p;
+      const float2* scw = sc + which * EB_CHUNK;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int s2 = s0; s2 < s1; ++s2) cfma<float>(acc, scw[s2], pw[s2 * ps + k]);
+      red[half * nacc + o] = acc;
     }
   }
+  __syncthreads();
+  // a box of one chunk gets its multipole directly; otherwise the chunk's part goes to
+  // mpart and the box's last chunk to finish adds the parts in chunk order
+  float2* dst = nc == 1 ? mpole + (size_t)b * nout : mpart + (size_t)c * nout;
+  for (int o = tid; o < nout; o += 128) {
+    const int e = o / p, k = o - e * p;
+    float2 v = cadd<float>(red[o], red[nacc + o]);
+    if (E == 2 && e == 1 && k >= 1) {
+      const float2 cm = cadd<float>(red[2 * p + k - 1], red[nacc + 2 * p + k - 1]);
+      crfma<float>(v, (float)k, cm);
+    }
+    dst[o] = make_float2(-v.x, -v.y);
+  }
+  if (nc == 1) return;
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = atomicAdd(&cdone[bb], 1) == nc - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int o = tid; o < nout; o += 128) {
+    float2 acc = __ldcg(&mpart[(size_t)c0 * nout + o]);
+    for (int cc = c0 + 1; cc < c0 + nc; ++cc) acc = cadd<float>(acc, __ldcg(&mpart[(size_t)cc * nout + o]));
+    mpole[(size_t)b * nout + o] = acc;
+  }
+  if (tid == 0) cdone[bb] = 0;
 }
 
 // M2M into the boxes of one level from their children (FP32 coarse levels): all
@@ -857,18 +880,6 @@ __global__ void k_m2m_f32(int offp, const unsigned long long* __restrict__ bkey,
   }
 }
 
-// mpole[b] = sum of the chunk partials of box b, in chunk order
-__global__ void k_chunk_sum(int first2, int nout, const int* __restrict__ cstart,
-                            const float2* __restrict__ mpart, float2* __restrict__ mpole) {
-  const int bb = blockIdx.x;
-  const int c0 = cstart[bb], c1 = cstart[bb + 1];
-  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
-    float2 s = mpart[(size_t)c0 * nout + o];
-    for (int c = c0 + 1; c < c1; ++c) s = cadd<float>(s, mpart[(size_t)c * nout + o]);
-    mpole[(size_t)(first2 + bb) * nout + o] = s;
-  }
-}
-
 // ---------------------------------------------------------------------------------
 // Leaf evaluation: L2P plus the near field over the U list (SLSELFDR/SLDIRDR,
 // cadapdrop2.f:564-620, 724-769; DABARR's pair loop, dapif3.f:460-545), self excluded.
@@ -876,12 +887,11 @@ __global__ void k_chunk_sum(int first2, int nout, const int* __restrict__ cstart
 // sources (and the terms of the local expansion), and their partial sums are added
 // with two shuffles in a fixed order.
 // ---------------------------------------------------------------------------------
-// Partial far field of lane sl: terms m0 <= m < m1 of the local expansions at u.
+// Terms m0 <= m < m1 of the local expansions at u.
 template <typename T, int E>
-__device__ __forceinline__ void l2p_part(const c_t<T>* lb, int p, int sl, c_t<T> u, T s, T& gx,
-                                         T& gy) {
-  const int ldl = p + 1, q = (ldl + 3) / 4;
-  int m0 = sl * q, m1 = min(ldl, m0 + q);
+__device__ __forceinline__ void l2p_range(const c_t<T>* lb, int p, int m0, int m1, c_t<T> u, T s, T& gx,
+                                          T& gy) {
+  const int ldl = p + 1;
   if (m0 >= m1) return;
   c_t<T> ph = lb[m1 - 1], dph = cmk<T>(0, 0);
   for (int m = m1 - 2; m >= m0; --m) {
@@ -909,6 +919,15 @@ __device__ __forceinline__ void l2p_part(const c_t<T>* lb, int p, int sl, c_t<T>
     gx -= ph.x;
     gy -= ph.y;
   }
+}
+
+// Partial far field of lane sl of 4: a quarter of the terms.
+template <typename T, int E>
+__device__ __forceinline__ void l2p_part(const c_t<T>* lb, int p, int sl, c_t<T> u, T s, T& gx,
+                                         T& gy) {
+  const int ldl = p + 1, q = (ldl + 3) / 4;
+  const int m0 = sl * q, m1 = min(ldl, m0 + q);
+  l2p_range<T, E>(lb, p, m0, m1, u, s, gx, gy);
 }
 
 template <int E>
@@ -1145,6 +1164,7 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   }
 }
 
+// Kahan-compensated FP32 sum.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   float y = v - c;
   float t = s + y;
@@ -1152,54 +1172,63 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-// FP32 far field: warp per EB_GROUP targets of one leaf, 4 lanes per target each taking
-// a quarter of the expansion orders. Adds the near-field sums of k_near32 and applies the
-// post-processing.
+// FP32 far field, one block per tile of the near field: the local expansions of the
+// leaf and of its nlev - 1 nearest ancestors are staged in shared memory, and each
+// expansion is evaluated directly about its own centre at every target (the sum equals
+// L2P of the L2L-accumulated leaf expansion; levels above these reach the coarsest of
+// them by L2L). Thread slice sl of 128 / EB_NTILE takes every slice-th level. Adds the
+// near-field sums of k_near32 and applies the post-processing.
 template <int E>
-__global__ void __launch_bounds__(128) k_far32(int ngroup, const int* __restrict__ gleaf,
-                                               const int* __restrict__ gfirst, int off, int has_far,
+__global__ void __launch_bounds__(128) k_far32(const int4* __restrict__ tiles, int off, int nlev, int nanc,
                                                const unsigned long long* __restrict__ bkey,
-                                               const int* __restrict__ pt1,
+                                               const int* __restrict__ anc,
                                                const int* __restrict__ perm,
-                                               const float4* __restrict__ wa, int L,
-                                               const int* __restrict__ parent, int p, float s,
+                                               const float4* __restrict__ wa, int p, float s,
                                                const float2* __restrict__ local,
                                                double2* __restrict__ out, EbPost post,
                                                const double2* __restrict__ nearbuf) {
-  int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (g >= ngroup) return;
-  const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
-  const int leaf = gleaf[g], b = off + leaf;
-  const int i = gfirst[g] + tg;
-  const bool act = i < pt1[b];
-  const int ii = act ? i : gfirst[g];
+  constexpr int T = EB_NTILE, NS = 128 / T;
+  extern __shared__ float2 sloc[];  // [nlev][E][p + 1]
+  __shared__ float2 sred[NS][T];
+  const int4 tl = tiles[blockIdx.x];
+  const int leaf = tl.x, b = off + leaf;
+  const int tid = threadIdx.x, tt = tid % T, sl = tid / T;
+  const int i = tl.y + tt;
+  const bool act = i < tl.z;
+  const int ii = act ? i : tl.y;
+  const int ldl = p + 1, nco = E * ldl;
+  for (int idx = tid; idx < nlev * nco; idx += 128) {
+    const int q = idx / nco, o = idx - q * nco;
+    sloc[idx] = local[(size_t)anc[(size_t)leaf * nanc + q] * nco + o];
+  }
+  __syncthreads();
   float fx = 0.f, fy = 0.f;
-  if (has_far) {
-    // The M2L expansion of the leaf and of each ancestor (levels L .. 2), each evaluated
-    // about its own centre: the sum equals L2P of the L2L-accumulated leaf expansion.
+  if (nlev > 0) {
     // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
     //   u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2   (i the leaf's grid index),
     // whose constant part is exact in FP32 (i < 2^20).
     const unsigned long long kb = bkey[b];
     const unsigned int ix = compact2d(kb), iy = compact2d(kb >> 1);
     const float4 wv = wa[ii];
-    int a = b;
-    for (int sh = 0; sh <= L - 2; ++sh) {
+    for (int sh = sl; sh < nlev; sh += NS) {
       const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
       const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
       const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
       const float2 u = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
-      l2p_part<float, E>(local + (size_t)a * E * (p + 1), p, sl, u, s, fx, fy);
-      a = parent[a];
+      l2p_range<float, E>(sloc + sh * nco, p, 0, ldl, u, s, fx, fy);
     }
   }
-  fx += __shfl_xor_sync(0xffffffffu, fx, 1);
-  fy += __shfl_xor_sync(0xffffffffu, fy, 1);
-  fx += __shfl_xor_sync(0xffffffffu, fx, 2);
-  fy += __shfl_xor_sync(0xffffffffu, fy, 2);
+  sred[sl][tt] = make_float2(fx, fy);
+  __syncthreads();
   if (sl == 0 && act) {
+    float2 v = sred[0][tt];
+#pragma unroll
+    for (int q = 1; q < NS; ++q) {
+      v.x += sred[q][tt].x;
+      v.y += sred[q][tt].y;
+    }
     const double2 nv = nearbuf[i];
-    eb_post_store_f32(post, perm[i], make_float2(fx + (float)nv.x, fy + (float)nv.y), out);
+    eb_post_store_f32(post, perm[i], make_float2(v.x + (float)nv.x, v.y + (float)nv.y), out);
   }
 }
 
@@ -1486,23 +1515,23 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * (p + 1)));
   double rleaf = t.W / (double)(1 << L);
   int offL = t.lev_off[L];
-  // Upward pass. FP32: direct P2M for every box of levels 2..L (chunks, then their
-  // sum), no dependent chain of M2M steps. FP64: P2M and one M2M launch per level.
+  // Upward pass. FP32: direct P2M (in chunks) for every box of the EB_DIRECT_LEVELS
+  // finest levels in one launch, then M2M per coarser level. FP64: P2M and one M2M
+  // launch per level.
   if (sizeof(T) == 4) {
     const int lmin = t.chunk_lmin;
     const int first2 = t.lev_off[lmin], nb2 = t.nbox - first2, nout = E * p;
     EB_TRY(w.mpart.ensure(sizeof(float2) * (size_t)t.nchunk * nout));
     LevOff lo;
     for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) lo.v[l] = t.lev_off[l];
-    size_t sm = sizeof(float2) * (32 * (size_t)(p + 1) + 96);
-    k_p2m_chunks<E><<<t.nchunk, 64, sm, st>>>(L, lmin, lo, first2, t.chunk_box.as<int>(), t.cstart.as<int>(),
-                                             t.keys.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
-                                             t.wdf.as<float4>(), reinterpret_cast<const float2*>(w.qa.p),
-                                             reinterpret_cast<const float2*>(w.qb.p), t.W, p,
-                                             w.mpart.as<float2>());
-    k_chunk_sum<<<nb2, round32(nout), 0, st>>>(first2, nout, t.cstart.as<int>(), w.mpart.as<float2>(),
-                                               reinterpret_cast<float2*>(w.mpole.p));
-    ctx->launches += 2;
+    const size_t sm = sizeof(float2) * ((size_t)EB_CHUNK * (p + 1) + (E == 2 ? 3 : 1) * (EB_CHUNK + 2 * (size_t)p));
+    k_p2m_chunks<E><<<t.nchunk, 128, sm, st>>>(L, lmin, lo, first2, t.chunk_box.as<int>(), t.cstart.as<int>(),
+                                              t.keys.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                              t.wdf.as<float4>(), reinterpret_cast<const float2*>(w.qa.p),
+                                              reinterpret_cast<const float2*>(w.qb.p), t.W, p,
+                                              w.mpart.as<float2>(), t.cdone.as<int>(),
+                                              reinterpret_cast<float2*>(w.mpole.p));
+    eb_count_launch(ctx);
     for (int l = lmin - 1; l >= 2; --l) {
       int nb = t.lev_off[l + 1] - t.lev_off[l];
       size_t sm2 = sizeof(float2) * 4 * (size_t)nout;
@@ -1545,11 +1574,12 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     }
     ps.done();
   }
-  // Downward pass. FP64: L2L level by level. FP32: none; the leaf kernel evaluates
-  // every ancestor's M2L expansion directly (cheap FP32 work instead of a dependent
-  // chain of shifts).
-  if (sizeof(T) == 8) {
-    for (int l = 3; l <= L; ++l) {
+  // Downward pass. FP64: L2L level by level. FP32: L2L only into the coarsest of the
+  // EB_FAR_LEVELS finest levels; the far-field kernel evaluates the M2L expansions of
+  // those levels directly (cheap FP32 work instead of a dependent chain of shifts).
+  {
+    const int lend = sizeof(T) == 8 ? L : L - std::min(L - 1, EB_FAR_LEVELS) + 1;
+    for (int l = 3; l <= lend; ++l) {
       int nb = t.lev_off[l + 1] - t.lev_off[l];
       size_t sm = sizeof(c_t<T>) * E * (p + 1);
       k_l2l<T, E><<<nb, round32(E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
@@ -1635,6 +1665,8 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
     EB_TRY(w.local_df.ensure(sizeof(float4) * (size_t)(E * (tb.p + 1))));
   }
+  const int far_lev = has_far ? std::min(t.L - 1, EB_FAR_LEVELS) : 0;
+  const size_t far_sm = sizeof(float2) * (size_t)far_lev * E * (tb.p + 1);
   if (split) EB_CUDA_TRY(cudaStreamWaitEvent(st, ctx->ev_p2p, 0));
   if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
   ProfScope ps(ctx, 0, st);
@@ -1645,10 +1677,10 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
   } else if (split) {
-    k_far32<E><<<blocks, 128, 0, st>>>(t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far,
-                                        t.bkey.as<unsigned long long>(), t.pt1.as<int>(), t.perm.as<int>(),
-                                        t.wdf.as<float4>(), t.L, t.parent.as<int>(), tb.p, (float)sign,
-                                        w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), offL, far_lev, t.L - 1,
+                                             t.bkey.as<unsigned long long>(), t.anc.as<int>(), t.perm.as<int>(),
+                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(), out,
+                                             post, w.nearbuf.as<double2>());
   } else if (df) {
     k_leaf_df<E, 0><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
@@ -1672,10 +1704,10 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                          w.nearbuf.as<double2>());
     eb_count_launch(ctx);
     pn.done();
-    k_far32<E><<<blocks, 128, 0, st>>>(t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far,
-                                        t.bkey.as<unsigned long long>(), t.pt1.as<int>(), t.perm.as<int>(),
-                                        t.wdf.as<float4>(), t.L, t.parent.as<int>(), tb.p, (float)sign,
-                                        w.local.as<float2>(), out, post, w.nearbuf.as<double2>());
+    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), offL, far_lev, t.L - 1,
+                                             t.bkey.as<unsigned long long>(), t.anc.as<int>(), t.perm.as<int>(),
+                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(), out,
+                                             post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
   ps.done();

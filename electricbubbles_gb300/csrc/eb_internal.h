@@ -74,6 +74,7 @@ struct EbTree {
   // a leaf's targets split evenly over its tiles
   int ntile = 0;
   DevBuf tiles;    // int4[ntile]: (leaf, first, end, 0)
+  DevBuf anc;      // int[nleaf*(L-1)]: each leaf's boxes at levels L, L-1, .., 2 (itself first)
   DevBuf flags, scan, hist, bbox, partial, cubtmp;
   // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
   // EB_CHUNK points (coarser levels by M2M)
@@ -82,9 +83,13 @@ struct EbTree {
   DevBuf ccount;     // int[nbox - lev_off[chunk_lmin]]: chunks per box
   DevBuf cstart;     // int[nbox - lev_off[chunk_lmin] + 1]: first chunk of each box
   DevBuf chunk_box;  // int[nchunk]: the box of each chunk
+  DevBuf cdone;      // int[nbox - lev_off[chunk_lmin]]: chunks of the box finished in the
+                     // current P2M (zero between launches: the box's last chunk resets it)
 };
 #define EB_CHUNK 64
 #define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
+#define EB_FAR_LEVELS 6     // finest levels whose FP32 locals are evaluated at each target
+                            // directly (coarser levels reach them by L2L)
 
 // Per-precision constant tables for the translation operators.
 struct EbTables {

@@ -310,6 +310,16 @@ __global__ void k_tile_fill(int off, int nleaf, const int* __restrict__ pt0, con
     tiles[g0 + g] = make_int4(b, a + (int)((long long)g * nt / c), a + (int)((long long)(g + 1) * nt / c), 0);
 }
 
+__global__ void k_ancestors(int off, int nleaf, int na, const int* __restrict__ parent, int* __restrict__ anc) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nleaf) return;
+  int a = off + b;
+  for (int q = 0; q < na; ++q) {
+    anc[(size_t)b * na + q] = a;
+    if (q + 1 < na) a = parent[a];
+  }
+}
+
 __global__ void k_chunk_count(int first, int nb, const int* __restrict__ pt0, const int* __restrict__ pt1,
                               int* __restrict__ cnt) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -596,6 +606,12 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
                                              t.flags.as<int>(), t.scan.as<int>(), t.tiles.as<int4>());
     eb_count_launch(ctx);
   }
+  if (L >= 2) {
+    EB_TRY(t.anc.ensure(sizeof(int) * (size_t)t.nleaf * (L - 1)));
+    k_ancestors<<<nblk(t.nleaf, BS), BS, 0, st>>>(t.lev_off[L], t.nleaf, L - 1, t.parent.as<int>(),
+                                                  t.anc.as<int>());
+    eb_count_launch(ctx);
+  }
   // 8b. chunks of at most EB_CHUNK points of every box of the EB_DIRECT_LEVELS finest
   // levels (FP32 direct P2M)
   t.nchunk = 0;
@@ -604,6 +620,8 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     const int first = t.lev_off[t.chunk_lmin], nb2 = t.nbox - first;
     EB_TRY(t.ccount.ensure(sizeof(int) * (size_t)nb2));
     EB_TRY(t.cstart.ensure(sizeof(int) * (size_t)(nb2 + 1)));
+    EB_TRY(t.cdone.ensure(sizeof(int) * (size_t)nb2));
+    EB_CUDA_TRY(cudaMemsetAsync(t.cdone.p, 0, sizeof(int) * (size_t)nb2, st));
     k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(first, nb2, t.pt0.as<int>(), t.pt1.as<int>(), t.ccount.as<int>());
     eb_count_launch(ctx);
     size_t need = 0;
