@@ -54,27 +54,31 @@ __device__ __forceinline__ int quadrant(unsigned long long key) {
 // Charges (sorted order). Stokes: qa, qb of cadapdrop.f:214-222 plus the near-field
 // combinations P = qa + s qb, Q = qa - s qb, A = -s conj(qa).
 // ---------------------------------------------------------------------------------
+// Computed in T: the FP32 operator forms its charges in FP32 (GB300's FP64 pipe is ~1/60
+// of its FP32 rate).
 template <typename T>
 __global__ void k_charges_stokes(int n, const int* __restrict__ perm,
                                  const double2* __restrict__ dens, const double2* __restrict__ dz,
-                                 const double* __restrict__ hpt, double s,
+                                 const double* __restrict__ hpt, double sd,
                                  c_t<T>* __restrict__ qa, c_t<T>* __restrict__ qb,
                                  c_t<T>* __restrict__ pq, c_t<T>* __restrict__ aa) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int o = perm[i];
-  double2 u = dens[o], d = dz[o];
-  double h = hpt[o] * (1.0 / (2.0 * EB_PI));
+  const double2 ud = dens[o], dd = dz[o];
+  const c_t<T> u = cmk<T>((T)ud.x, (T)ud.y), d = cmk<T>((T)dd.x, (T)dd.y);
+  const T s = (T)sd;
+  const T h = (T)hpt[o] * (T)(1.0 / (2.0 * EB_PI));
   // 1/(2 pi i) = -i/(2 pi)
-  double2 w = cmul<double>(u, d);
-  double2 a = make_double2(w.y * h, -w.x * h);
-  double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
-  double2 b = make_double2(v.y * h, -v.x * h);
-  qa[i] = cmk<T>((T)a.x, (T)a.y);
-  qb[i] = cmk<T>((T)b.x, (T)b.y);
-  pq[2 * i] = cmk<T>((T)(a.x + s * b.x), (T)(a.y + s * b.y));
-  pq[2 * i + 1] = cmk<T>((T)(a.x - s * b.x), (T)(a.y - s * b.y));
-  aa[i] = cmk<T>((T)(-s * a.x), (T)(s * a.y));
+  c_t<T> w = cmul<T>(u, d);
+  c_t<T> a = cmk<T>(w.y * h, -w.x * h);
+  c_t<T> v = csub<T>(cmul<T>(u, cconj<T>(d)), cmul<T>(cconj<T>(u), d));
+  c_t<T> b = cmk<T>(v.y * h, -v.x * h);
+  qa[i] = a;
+  qb[i] = b;
+  pq[2 * i] = cmk<T>(a.x + s * b.x, a.y + s * b.y);
+  pq[2 * i + 1] = cmk<T>(a.x - s * b.x, a.y - s * b.y);
+  aa[i] = cmk<T>(-s * a.x, s * a.y);
 }
 
 __device__ __forceinline__ float4 df4(double2 v) {
@@ -130,8 +134,13 @@ __global__ void k_charges_cauchy(int n, const int* __restrict__ perm,
                                  c_t<T>* __restrict__ qa) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double2 v = cauchy_charge(perm[i], q, lu, dz, hpt);
-  qa[i] = cmk<T>((T)v.x, (T)v.y);
+  const int o = perm[i];
+  if (q) {
+    qa[i] = cmk<T>((T)q[o].x, (T)q[o].y);
+  } else {
+    const T f = (T)lu[o] * (T)hpt[o];
+    qa[i] = cmk<T>(f * (T)dz[o].x, f * (T)dz[o].y);
+  }
 }
 
 // ---------------------------------------------------------------------------------
@@ -736,6 +745,7 @@ __global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
 // ---------------------------------------------------------------------------------
 struct LevOff {
   int v[EB_KEY_LEVELS + 2];
+  float rinv[EB_KEY_LEVELS + 2];  // 1 / (box side) per level, rounded to float on the host
 };
 
 template <int E>
@@ -763,7 +773,7 @@ __global__ void __launch_bounds__(128) k_p2m_chunks(int L, int lmin, LevOff lo, 
   while (l < L && b >= lo.v[l + 1]) ++l;
   const int sh = L - l;
   const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
-  const float rinv = (float)((double)(1u << l) / W);
+  const float rinv = lo.rinv[l];
   const int bb = b - first2, c0 = cstart[bb], nc = cstart[bb + 1] - c0;
   const int i0 = pt0[b] + (c - c0) * EB_CHUNK;
   const int cnt = min(pt1[b], i0 + EB_CHUNK) - i0;
@@ -1523,7 +1533,10 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     const int first2 = t.lev_off[lmin], nb2 = t.nbox - first2, nout = E * p;
     EB_TRY(w.mpart.ensure(sizeof(float2) * (size_t)t.nchunk * nout));
     LevOff lo;
-    for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) lo.v[l] = t.lev_off[l];
+    for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) {
+      lo.v[l] = t.lev_off[l];
+      lo.rinv[l] = (float)((double)(1u << std::min(l, 30)) / t.W);
+    }
     const size_t sm = sizeof(float2) * ((size_t)EB_CHUNK * (p + 1) + (E == 2 ? 3 : 1) * (EB_CHUNK + 2 * (size_t)p));
     k_p2m_chunks<E><<<t.nchunk, 128, sm, st>>>(L, lmin, lo, first2, t.chunk_box.as<int>(), t.cstart.as<int>(),
                                               t.keys.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),

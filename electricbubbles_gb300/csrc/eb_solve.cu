@@ -241,6 +241,9 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
   if (maxl > n) maxl = n;
   const size_t ldv = (size_t)n;
   const int ldh = maxl + 1;
+  // classical Gram-Schmidt twice for the FP64 solve; once for the inner FP32 cycle of
+  // the refined solve, whose tolerance (1e-5) is far above the loss of orthogonality
+  const bool cgs2 = prec == EB_FP64;
   EB_TRY(ctx->gV.ensure(sizeof(double) * ldv * (maxl + 1)));
   double* V = ctx->gV.as<double>();
   double* part = ctx->gPart.as<double>();
@@ -300,16 +303,21 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     (*nmv)++;
     // pass 1: h1 = V^T w; w -= V h1
     k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket);
-    // w -= V h1; pass 2: h2 = V^T w; w -= V h2 with ||w||^2
-    k_update_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + (maxl + 2), g.ticket);
-    k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev + (maxl + 2), w, part,
-                                      hdev + 2 * (maxl + 2), g.ticket);
-    ctx->launches += 3;
+    if (cgs2) {
+      // w -= V h1; pass 2: h2 = V^T w; w -= V h2 with ||w||^2
+      k_update_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + (maxl + 2), g.ticket);
+      k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev + (maxl + 2), w, part,
+                                        hdev + 2 * (maxl + 2), g.ticket);
+    } else {
+      k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + 2 * (maxl + 2),
+                                        g.ticket);
+    }
+    ctx->launches += cgs2 ? 3 : 2;
     EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
                                 cudaMemcpyDeviceToHost, g.s));
     EB_CUDA_TRY(cudaStreamSynchronize(g.s));
     double* col = hes.data() + (size_t)(ll - 1) * ldh;
-    for (int i = 0; i < ll; ++i) col[i] = hbuf[i] + hbuf[(maxl + 2) + i];
+    for (int i = 0; i < ll; ++i) col[i] = hbuf[i] + (cgs2 ? hbuf[(maxl + 2) + i] : 0.0);
     double snormw = std::sqrt(std::max(hbuf[2 * (maxl + 2)], 0.0));
     col[ll] = snormw;
     if (!std::isfinite(snormw)) {
@@ -618,6 +626,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
       k_resid<<<nb, RBS, 0, s>>>(n, bb, wbuf, V, part, hdev + GM_R0, ticket);
       eb_count_launch(ctx);
     }
+    if (refine) EB_CUDA_TRY(cudaMemsetAsync(hdev + GM_H2, 0, sizeof(double) * (EB_GM_MAXL + 2), s));
     k_gm_init<<<1, 32, 0, s>>>(ctl, hdev, h, tol, maxl, refine ? 1 : 0);
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, V, V, ldv, xin);
     ctx->launches += 2;
@@ -639,11 +648,16 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
-    k_update_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_H2, ticket);
-    k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev + GM_NW, ticket);
+    if (refine) {
+      // one Gram-Schmidt pass for the inner FP32 cycle (the H2 slots stay zero)
+      k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_NW, ticket);
+    } else {
+      k_update_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_H2, ticket);
+      k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev + GM_NW, ticket);
+    }
     k_gm_arnoldi<<<1, 32, 0, s>>>(ctl, hdev, h);
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
-    ctx->launches += 5;
+    ctx->launches += refine ? 4 : 5;
     return eb_check_launch(ctx, "gmres graph (body)");
   });
   if (body_lost) lost = true;  // the body belongs to the graph; leave the whole graph alone
