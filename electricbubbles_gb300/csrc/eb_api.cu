@@ -37,24 +37,19 @@ namespace {
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 // Per-drop reductions of FASMVP (stokesbubb.f:549-565): za_k = h sum dens,
-// pk_k = sum 2 h Re(dens dz/(z - zk)^2) / pi. One block per drop.
+// pk_k = sum 2 h Re(dens dz/(z - zk)^2) / pi = sum Re(dens w) with the per-node weights
+// w = (2 h / pi) dz / (z - zk)^2 of k_pk_weights. One block per drop.
 __global__ void k_drop_reduce_stokes(const int* __restrict__ start, const double2* __restrict__ dens,
-                                     const double2* __restrict__ dz, const double2* __restrict__ z,
-                                     const double2* __restrict__ zk, double2* __restrict__ za,
+                                     const double2* __restrict__ pkw, double2* __restrict__ za,
                                      double* __restrict__ pk) {
   __shared__ double s[3][256];
   int b = blockIdx.x;
   int i0 = start[b], i1 = start[b + 1];
   double h = 2.0 * EB_PI / (double)(i1 - i0);
   double ax = 0.0, ay = 0.0, pp = 0.0;
-  double2 c = zk[b];
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    double2 u = dens[i];
-    double2 d = make_double2(z[i].x - c.x, z[i].y - c.y);
-    double2 d2 = cmul<double>(d, d);
-    double2 num = cmul<double>(u, dz[i]);
-    double2 q = cdiv<double>(num, d2);
-    pp += 2.0 * h * q.x / EB_PI;
+    const double2 u = dens[i], w = pkw[i];
+    pp = fma(u.x, w.x, fma(-u.y, w.y, pp));
     ax += u.x;
     ay += u.y;
   }
@@ -72,6 +67,19 @@ __global__ void k_drop_reduce_stokes(const int* __restrict__ start, const double
     za[b] = make_double2(h * s[0][0], h * s[1][0]);
     pk[b] = s[2][0];
   }
+}
+
+// Per-node weights of the singular-term sums, once per geometry.
+__global__ void k_pk_weights(int nbk, const int* __restrict__ drop_of, const double* __restrict__ hpt,
+                             const double2* __restrict__ z, const double2* __restrict__ dz,
+                             const double2* __restrict__ zk, double2* __restrict__ pkw) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nbk) return;
+  const double2 c = zk[drop_of[i]];
+  const double2 d = make_double2(z[i].x - c.x, z[i].y - c.y);
+  const double2 q = cdiv<double>(dz[i], cmul<double>(d, d));
+  const double f = 2.0 * hpt[i] / EB_PI;
+  pkw[i] = make_double2(f * q.x, f * q.y);
 }
 
 // Constraint sums the reference writes past YY(N) (laplace.f:252-259): h s' u per drop.
@@ -201,8 +209,13 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   c->device = c->opts.device;
   e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
+  // The capture stream runs at the highest priority and the side stream (the near field,
+  // concurrent with the latency-bound expansion chain) at the lowest, so that the
+  // chain's blocks are scheduled first; captured graphs keep the per-node priorities.
+  int prio_least = 0, prio_greatest = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->cap_stream, cudaStreamNonBlocking, prio_greatest);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side_stream, cudaStreamNonBlocking, prio_least);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming);
@@ -334,6 +347,11 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   EB_TRY(ctx->pc1f.ensure(sizeof(float) * nbk));
   EB_TRY(ctx->pc2f.ensure(sizeof(float2) * nbk));
   EB_TRY(ctx->plapf.ensure(sizeof(float) * nbk));
+  EB_TRY(ctx->pkw.ensure(sizeof(double2) * nbk));
+  k_pk_weights<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->drop_of.as<int>(), ctx->hpt.as<double>(),
+                                             ctx->z.as<double2>(), ctx->dz.as<double2>(),
+                                             ctx->zk.as<double2>(), ctx->pkw.as<double2>());
+  eb_count_launch(ctx);
   k_post_coefs<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
                                              ctx->kappa.as<double>(), ctx->hpt.as<double>(),
                                              ctx->pc1.as<double>(), ctx->pc2.as<double2>(),
@@ -368,8 +386,7 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   // fused post-processing reads them, waits for them
   EB_CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
   EB_CUDA_TRY(cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork, 0));
-  k_drop_reduce_stokes<<<k, 256, 0, ctx->side_stream>>>(ctx->start.as<int>(), dens, ctx->dz.as<double2>(),
-                                                       ctx->z.as<double2>(), ctx->zk.as<double2>(),
+  k_drop_reduce_stokes<<<k, 256, 0, ctx->side_stream>>>(ctx->start.as<int>(), dens, ctx->pkw.as<double2>(),
                                                        ctx->za.as<double2>(), ctx->pk.as<double>());
   eb_count_launch(ctx);
   EB_CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->side_stream));

@@ -153,6 +153,7 @@ struct eb_ctx {
   DevBuf dsda, kappa, tha, hpt;  // double
   DevBuf pc1, pc2, plap;         // per-node post-processing coefficients (eb_post_coefs)
   DevBuf pc1f, pc2f, plapf;      // their float copies (FP32 operator)
+  DevBuf pkw;                    // double2: weights of FASMVP's singular-term sums
   bool geom_valid = false;
   bool ckern_valid = false;       // ckern/tha filled by eb_extractdat
 

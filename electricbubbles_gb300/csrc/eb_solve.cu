@@ -679,7 +679,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     return eb_check_launch(ctx, "gmres graph (post)");
   });
   if (cst != EB_OK) return fail(cst);
-  EB_CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, 0));
+  EB_CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, cudaGraphInstantiateFlagUseNodePriority));
   G.valid = true;
   return EB_OK;
 }

@@ -615,7 +615,9 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   // 8b. chunks of at most EB_CHUNK points of every box of the EB_DIRECT_LEVELS finest
   // levels (FP32 direct P2M)
   t.nchunk = 0;
-  t.chunk_lmin = std::max(2, L - EB_DIRECT_LEVELS + 1);
+  // up to 256K points the multipoles of every level come directly from the points (no
+  // dependent M2M launches on the critical path); above, the EB_DIRECT_LEVELS finest
+  t.chunk_lmin = n <= (1 << 18) ? 2 : std::max(2, L - EB_DIRECT_LEVELS + 1);
   if (L >= 2) {
     const int first = t.lev_off[t.chunk_lmin], nb2 = t.nbox - first;
     EB_TRY(t.ccount.ensure(sizeof(int) * (size_t)nb2));
