@@ -262,21 +262,30 @@ def run_gpu(args, rank, world, local):
     fp32_peak = ctx.measure_fp32_peak()
     levels_l2p = max(tree["levels"] - 1, 1)
     kern = {}
-    for prec, p_ord, near_name, m2l_name, l2p_levels in (
-            ("fp32", 20, "k_leaf32<2>", "k_m2l<float, 2>", levels_l2p),
-            ("fp64", 44, "k_leaf_df<2>", "k_m2l_df<2>", 1)):
+
+    def kentry(ms, nl, flops):
+        return {"avg_launch_ms": ms / nl, "flops_per_launch": flops,
+                "achieved_tflops": flops / (ms / nl * 1e-3) / 1e12}
+
+    near_pair_flops = 40.0 * tree["u_pairs"]
+    for prec, p_ord in (("fp32", 20), ("fp64", 44)):
         ctx.set_profiling(True)
         for _ in range(10):
             ctx.fasmvp(u, prec, out=y)
-        nl, near_ms = ctx.kernel_time(0)
+        nl, leaf_ms = ctx.kernel_time(0)
         nm, m2l_ms = ctx.kernel_time(1)
+        nn, near_ms = ctx.kernel_time(2)
         ctx.set_profiling(False)
-        near_flops = 40.0 * tree["u_pairs"] + 8.0 * p_ord * 2 * tree["npoints"] * l2p_levels
         m2l_flops = 2 * 8.0 * p_ord * p_ord * tree["v_pairs"]
-        kern[near_name] = {"avg_launch_ms": near_ms / nl, "flops_per_launch": near_flops,
-                           "achieved_tflops": near_flops / (near_ms / nl * 1e-3) / 1e12}
-        kern[m2l_name] = {"avg_launch_ms": m2l_ms / nm, "flops_per_launch": m2l_flops,
-                          "achieved_tflops": m2l_flops / (m2l_ms / nm * 1e-3) / 1e12}
+        if prec == "fp32":
+            # the far field evaluates the locals of min(levels - 1, 6) levels at every node
+            far_flops = 8.0 * p_ord * 2 * tree["npoints"] * min(levels_l2p, 6)
+            kern["k_near32<2>"] = kentry(near_ms, nn, near_pair_flops)
+            kern["k_far32<2>"] = kentry(leaf_ms, nl, far_flops)
+            kern["k_m2l<float, 2>"] = kentry(m2l_ms, nm, m2l_flops)
+        else:
+            kern["k_leaf_df<2>"] = kentry(leaf_ms, nl, near_pair_flops + 8.0 * p_ord * 2 * tree["npoints"])
+            kern["k_m2l_df<2>"] = kentry(m2l_ms, nm, m2l_flops)
     for name, k in kern.items():
         peak = fp32_peak
         k["peak_tflops"] = peak
@@ -284,7 +293,7 @@ def run_gpu(args, rank, world, local):
         if "df" in name:
             # double-float kernels do FP64-class arithmetic on the FP32 pipes
             k["frac_of_fp64_peak"] = k["achieved_tflops"] / fp64_peak
-    dom = kern["k_leaf32<2>"]
+    dom = kern["k_near32<2>"]
 
     # end to end through the C ABI with host buffers: geometry + rhs in, solution out
     zh = torch.from_numpy(np.ascontiguousarray(geo["z"]).view(np.float64).copy()).pin_memory()
@@ -452,8 +461,9 @@ def run_gpu(args, rank, world, local):
         "solve_info": {"fp64": inf64[-1], "fp32_refined": inf32[-1]},
         "accuracy": {"refined_vs_fp64_rel_l2": rel_diff, "refined_true_residual": inf32[-1]["err"]},
         "tree": tree,
-        "roofline": {"kernel": "k_leaf32<2> (FP32 near field P2P + L2P of every level; the largest "
-                               "kernel of the refined solve)", "bound": "fp32",
+        "roofline": {"kernel": "k_near32<2> (FP32 near field P2P over the U lists, 40 flop per "
+                               "target-source pair; with k_m2l<float, 2> the largest kernel of the "
+                               "refined solve)", "bound": "fp32",
                      "achieved": dom["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": dom["achieved_tflops"] / fp32_peak, "traffic": None,
                      "peak_source": "measured in-run FP32 FMA chain (MEASURED_PEAKS.json has no FP32 "

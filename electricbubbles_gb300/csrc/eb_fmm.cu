@@ -1682,6 +1682,17 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   const size_t far_sm = sizeof(float2) * (size_t)far_lev * E * (tb.p + 1);
   if (split) EB_CUDA_TRY(cudaStreamWaitEvent(st, ctx->ev_p2p, 0));
   if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
+  if (!split && !f64) {
+    // FP32 without the split: the near-field kernel, then the far field on the same stream
+    EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
+    ProfScope pn(ctx, 2, st);
+    k_near32<E><<<t.ntile, 128, 0, st>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
+                                         t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
+                                         w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
+                                         w.nearbuf.as<double2>());
+    eb_count_launch(ctx);
+    pn.done();
+  }
   ProfScope ps(ctx, 0, st);
   if (df && split) {
     k_leaf_df<E, 2><<<blocks, 128, 0, st>>>(
@@ -1708,15 +1719,6 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
         rleaf, tb.p, (double)sign, w.local.as<double2>(), out, post);
   } else {
-    // FP32 without the split: near-field kernel, then the far field on the same stream
-    EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
-    ProfScope pn(ctx, 2, st);
-    k_near32<E><<<t.ntile, 128, 0, st>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
-                                         t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
-                                         w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
-                                         w.nearbuf.as<double2>());
-    eb_count_launch(ctx);
-    pn.done();
     k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), offL, far_lev, t.L - 1,
                                              t.bkey.as<unsigned long long>(), t.anc.as<int>(), t.perm.as<int>(),
                                              t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(), out,

@@ -129,10 +129,11 @@ int eb_ctx_set_stream(eb_ctx* ctx, void* cuda_stream);
 int eb_ctx_sync(eb_ctx* ctx);
 /* Kernel launches issued by this context so far. */
 long long eb_ctx_launch_count(eb_ctx* ctx);
-/* When enabled, the dominant near-field and M2L kernels are bracketed by CUDA
- * events on the context's stream; eb_ctx_kernel_time reports launches and total
- * milliseconds per kernel class (0: the leaf evaluation, near field P2P + L2P;
- * 1: M2L; 2: the near-field kernel alone where it is a launch of its own). */
+/* When enabled, the dominant leaf and M2L kernels are bracketed by CUDA events on
+ * the context's stream (and the near field runs on it, not concurrently);
+ * eb_ctx_kernel_time reports launches and total milliseconds per kernel class
+ * (0: the kernel that ends an apply: far-field L2P and post-processing, for the
+ * FP64-class operators also the near field; 1: M2L; 2: the FP32 near-field kernel). */
 int eb_ctx_set_profiling(eb_ctx* ctx, int enable);
 int eb_ctx_kernel_time(eb_ctx* ctx, int kernel_class, long long* launches, double* total_ms);
 int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
