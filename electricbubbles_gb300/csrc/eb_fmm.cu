@@ -1530,7 +1530,7 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   // launch per level.
   if (sizeof(T) == 4) {
     const int lmin = t.chunk_lmin;
-    const int first2 = t.lev_off[lmin], nb2 = t.nbox - first2, nout = E * p;
+    const int first2 = t.lev_off[lmin], nout = E * p;
     EB_TRY(w.mpart.ensure(sizeof(float2) * (size_t)t.nchunk * nout));
     LevOff lo;
     for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) {

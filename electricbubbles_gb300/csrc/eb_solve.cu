@@ -14,7 +14,9 @@
 // Refined mode (FP32 inner operator): iterative refinement with FP64 residuals from
 // x = 0 (so r = b needs no apply),
 //   solve A32 d = r to inner_tol with the same GMRES;  x += d;  r = b - A64 x,
-// until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual.
+// until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual. Steps after
+// the first tighten the inner tolerance (to at most a tenth) when that is expected to
+// end the solve (inner_tolerance below).
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
@@ -378,12 +380,15 @@ struct GmCtl {
 constexpr size_t GM_HEAD = offsetof(GmCtl, q);
 
 // slots of the reduction output buffer (gH)
+// (GM_TOL: the inner tolerance of the next refinement step, written by the host)
 constexpr int GM_H1 = 0, GM_H2 = EB_GM_MAXL + 2, GM_NW = 2 * (EB_GM_MAXL + 2), GM_BN = GM_NW + 1,
-              GM_R0 = GM_NW + 2, GM_Y = GM_NW + 4, GM_HSIZE = GM_Y + EB_GM_MAXL + 2;
+              GM_R0 = GM_NW + 2, GM_Y = GM_NW + 4, GM_TOL = GM_Y + EB_GM_MAXL + 2, GM_HSIZE = GM_TOL + 1;
 
+// tol_dev (if not null) holds the tolerance instead of `tol`
 __global__ void k_gm_init(GmCtl* c, const double* __restrict__ hdev, cudaGraphConditionalHandle h,
-                          double tol, int maxl, int r0_is_b) {
+                          double tol, const double* __restrict__ tol_dev, int maxl, int r0_is_b) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (tol_dev) tol = *tol_dev;
   c->tol = tol;
   c->maxl = maxl;
   c->iters = 0;
@@ -627,7 +632,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
       eb_count_launch(ctx);
     }
     if (refine) EB_CUDA_TRY(cudaMemsetAsync(hdev + GM_H2, 0, sizeof(double) * (EB_GM_MAXL + 2), s));
-    k_gm_init<<<1, 32, 0, s>>>(ctl, hdev, h, tol, maxl, refine ? 1 : 0);
+    k_gm_init<<<1, 32, 0, s>>>(ctl, hdev, h, tol, refine ? hdev + GM_TOL : nullptr, maxl, refine ? 1 : 0);
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, V, V, ldv, xin);
     ctx->launches += 2;
     return eb_check_launch(ctx, "gmres graph (pre)");
@@ -726,6 +731,17 @@ int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
   return EB_OK;
 }
 
+// Inner tolerance of refinement step `outer` given the outer relative residual `err`
+// before it: the configured inner tolerance for the first step; later steps solve far
+// enough (by half a margin) that the step is expected to end the solve, since the
+// residual contracts by about the inner tolerance per step, but never below a tenth of
+// the configured value (the FP32 operator's own error sets the floor).
+double inner_tolerance(const eb_ctx* ctx, int outer, double err) {
+  const double t = ctx->opts.inner_tol;
+  if (outer <= 1 || !(err > 0.0)) return t;
+  return std::min(t, std::max(0.1 * t, 0.5 * ctx->opts.gmres_tol / err));
+}
+
 int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info* inf) {
   cudaStream_t s = ctx->stream;
   if (maxl > n) maxl = n;
@@ -754,8 +770,11 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->gZ.p, ctx->gR.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   inf->ierr = 1;
   double bnrm = 0.0;
+  double err_prev = 1.0;
   for (int outer = 1; outer <= ctx->opts.max_outer; ++outer) {
     inf->outer = outer;
+    const double itol = inner_tolerance(ctx, outer, err_prev);
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->gH.as<double>() + GM_TOL, &itol, sizeof(double), cudaMemcpyHostToDevice, s));
     EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, &head));
     if (head.status != EB_OK) {
       eb_set_last_error_msg("non-finite value in GMRES");
@@ -773,6 +792,7 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
       }
     }
     inf->err = std::sqrt(std::max(head.rnrm2, 0.0)) / bnrm;
+    err_prev = inf->err;
     if (!std::isfinite(inf->err)) {
       eb_set_last_error_msg("non-finite residual");
       return EB_ERR_NAN;
@@ -848,8 +868,8 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
       inf.outer = outer;
       int it = 0, ie = 0, nmv = 0;
       double e2 = 0;
-      st = gmres_cycle(g, op, EB_FP32, r, d, true, ctx->opts.inner_tol, maxl, &it, &e2, &ie, &nmv,
-                       rnrm);
+      st = gmres_cycle(g, op, EB_FP32, r, d, true, inner_tolerance(ctx, outer, inf.err), maxl, &it, &e2,
+                       &ie, &nmv, rnrm);
       inf.iters += it;
       inf.matvecs32 += nmv;
       if (st != EB_OK) break;

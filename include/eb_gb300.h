@@ -62,7 +62,9 @@ typedef struct eb_opts {
   double tol32;     /* M2L per-offset truncation tolerance, FP32 (0: 1e-7)     */
   int maxl;         /* GMRES Krylov dimension, MAXL (0: 100, electric.f:1011)  */
   double gmres_tol; /* GMRES relative residual tolerance (0: 1e-10)            */
-  double inner_tol; /* refined mode: inner FP32 GMRES relative tolerance (0: 1e-5) */
+  double inner_tol; /* refined mode: inner FP32 GMRES relative tolerance of the first
+                     * refinement step (0: 1e-5); later steps tighten it, to at most a
+                     * tenth, when that is expected to end the solve */
   int max_outer;    /* refined mode: maximum refinement steps (0: 8)           */
   int device;       /* CUDA device ordinal                                     */
   int graphs;       /* GMRES as CUDA graphs with a device-side Arnoldi loop:
