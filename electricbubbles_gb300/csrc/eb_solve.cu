@@ -47,14 +47,15 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 
 // Sums part[blk * ncol + j] over the blocks into out[j] (one warp per column, fixed
 // order); run by the last block of a kernel to finish, which also resets the ticket.
-__device__ void finish_columns(int nb, int ncol, const double* part, double* out,
+// Returns true in that block.
+__device__ bool finish_columns(int nb, int ncol, const double* part, double* out,
                                unsigned int* ticket) {
   __shared__ bool s_last;
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   __syncthreads();
-  if (!s_last) return;
+  if (!s_last) return false;
   __threadfence();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int j = w; j < ncol; j += nw) {
@@ -64,6 +65,7 @@ __device__ void finish_columns(int nb, int ncol, const double* part, double* out
     if (lane == 0) out[j] = s;
   }
   if (threadIdx.x == 0) *ticket = 0u;
+  return true;
 }
 
 // out[j] = V[:, j] . w for j < ncol. Each block takes a contiguous range of rows and
@@ -117,11 +119,12 @@ __global__ void k_update_vtw(int n, int ncol, const int* __restrict__ ncol_dev, 
   finish_columns(gridDim.x, ncol, part, out, ticket);
 }
 
-// w -= V[:, 0:ncol] h; if part != nullptr also ||w||^2 of the new w into *out.
-__global__ void k_gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
-                           size_t ldv, const double* __restrict__ h, double* __restrict__ w,
-                           double* __restrict__ part, double* __restrict__ out,
-                           unsigned int* __restrict__ ticket) {
+// w -= V[:, 0:ncol] h; if part != nullptr also ||w||^2 of the new w into *out (returns
+// true in the block that wrote it).
+__device__ bool gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                         size_t ldv, const double* __restrict__ h, double* __restrict__ w,
+                         double* __restrict__ part, double* __restrict__ out,
+                         unsigned int* __restrict__ ticket) {
   __shared__ double hs[128];
   if (ncol_dev) ncol = *ncol_dev;
   __shared__ double red[32];
@@ -135,11 +138,17 @@ __global__ void k_gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, co
     w[i] = v;
     sq = fma(v, v, sq);
   }
-  if (part) {
-    sq = block_sum(sq, red);
-    if (threadIdx.x == 0) part[blockIdx.x] = sq;
-    finish_columns(gridDim.x, 1, part, out, ticket);
-  }
+  if (!part) return false;
+  sq = block_sum(sq, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = sq;
+  return finish_columns(gridDim.x, 1, part, out, ticket);
+}
+
+__global__ void k_gemv_sub(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                           size_t ldv, const double* __restrict__ h, double* __restrict__ w,
+                           double* __restrict__ part, double* __restrict__ out,
+                           unsigned int* __restrict__ ticket) {
+  gemv_sub(n, ncol, ncol_dev, V, ldv, h, w, part, out, ticket);
 }
 
 // x += V[:, 0:ncol] y
@@ -439,7 +448,7 @@ __global__ void k_gm_store(int n, const GmCtl* __restrict__ c, const double* src
 
 // End of an Arnoldi step (DPIGMR, dpigmr.f:333-380): the Hessenberg column from the two
 // Gram-Schmidt passes, its Givens update (DHEQR), the residual estimate and the decision.
-__global__ void k_gm_arnoldi(GmCtl* c, const double* __restrict__ hdev, cudaGraphConditionalHandle h) {
+__device__ void gm_arnoldi_warp(GmCtl* c, const double* __restrict__ hdev, cudaGraphConditionalHandle h) {
   const int lane = threadIdx.x;
   const int ll = c->ll, ldh = c->maxl + 1;
   double* col = c->hes + (size_t)(ll - 1) * ldh;
@@ -474,6 +483,18 @@ __global__ void k_gm_arnoldi(GmCtl* c, const double* __restrict__ hdev, cudaGrap
   }
   c->cont = cont;
   cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+// The last Gram-Schmidt update (w -= V h with ||w||^2 into hdev[GM_NW]); the block that
+// finishes the norm then ends the Arnoldi step with its first warp.
+__global__ void k_gm_sub_arnoldi(int n, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                                 size_t ldv, const double* __restrict__ hcol, double* __restrict__ w,
+                                 double* __restrict__ part, double* hdev,
+                                 unsigned int* __restrict__ ticket, GmCtl* c,
+                                 cudaGraphConditionalHandle h) {
+  if (!gemv_sub(n, 0, ncol_dev, V, ldv, hcol, w, part, hdev + GM_NW, ticket)) return;
+  __syncthreads();
+  if (threadIdx.x < 32) gm_arnoldi_warp(c, hdev, h);
 }
 
 // DHELS (dhels.f:77-96) on the device: y = R^-1 Q^T (r0nrm e1), into ydev.
@@ -655,14 +676,13 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
     if (refine) {
       // one Gram-Schmidt pass for the inner FP32 cycle (the H2 slots stay zero)
-      k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_NW, ticket);
+      k_gm_sub_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev, ticket, ctl, h);
     } else {
       k_update_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_H2, ticket);
-      k_gemv_sub<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev + GM_NW, ticket);
+      k_gm_sub_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev, ticket, ctl, h);
     }
-    k_gm_arnoldi<<<1, 32, 0, s>>>(ctl, hdev, h);
     k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
-    ctx->launches += refine ? 4 : 5;
+    ctx->launches += refine ? 3 : 4;
     return eb_check_launch(ctx, "gmres graph (body)");
   });
   if (body_lost) lost = true;  // the body belongs to the graph; leave the whole graph alone
