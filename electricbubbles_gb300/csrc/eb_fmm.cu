@@ -428,6 +428,81 @@ __global__ void __launch_bounds__(128) k_m2l(int first, const int* __restrict__ 
   }
 }
 
+// The FP32 M2L for the default order P (20): lane m <= P owns output order m of both
+// expansions. Its binomial column C(m+k-1, m) stays in registers, the warp's entries are
+// accumulated in registers, the loops over k run to P with a_k = 0 beyond the entry's
+// truncation order pd, and outputs m > pd are skipped, so each entry gives exactly the
+// sums of k_m2l (same terms, same order).
+template <int E, int P>
+__global__ void __launch_bounds__(128) k_m2l_f32p(int first, const int* __restrict__ vlist,
+                                                  const unsigned char* __restrict__ vcode,
+                                                  const int* __restrict__ vcount,
+                                                  const float* __restrict__ binom, int ldb,
+                                                  const float2* __restrict__ dinv,
+                                                  const int* __restrict__ pdv,
+                                                  const float2* __restrict__ mpole,
+                                                  float2* __restrict__ local) {
+  constexpr int ldl = P + 1, ldd = P + 2;
+  __shared__ float2 sa[4][E][P];
+  __shared__ float2 sred[4][E][ldl];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = first + blockIdx.x;
+  const int nv = vcount[gid];
+  const int m = lane <= P ? lane : P;
+  float c2[P];
+#pragma unroll
+  for (int k = 1; k <= P; ++k) c2[k - 1] = binom[(size_t)(m + k - 1) * ldb + m];
+  float2 acc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) acc[e] = make_float2(0.f, 0.f);
+  for (int j = w; j < nv; j += 4) {
+    const int src = vlist[(size_t)gid * EB_VMAX + j];
+    const int code = vcode[(size_t)gid * EB_VMAX + j];
+    const int pd = pdv[code];
+    const float2* dv = dinv + (size_t)code * ldd;
+    const float2* ms = mpole + (size_t)src * E * P;
+    if (lane < P) {
+      const int kk = lane, k = kk + 1;
+      float2 v0 = make_float2(0.f, 0.f), v1 = v0;
+      if (kk < pd) {
+        const float2 sc = dv[k];
+        v0 = cmul<float>(ms[kk], sc);
+        if (E == 2) {
+          float2 mpsi = ms[P + kk];
+          const float dxr = (float)(code % 7 - 3), dyr = (float)(code / 7 - 3);
+          if (k >= 2) cfma<float>(mpsi, make_float2(-dxr * (float)(k - 1), dyr * (float)(k - 1)), ms[kk - 1]);
+          v1 = cmul<float>(mpsi, sc);
+        }
+      }
+      sa[w][0][kk] = v0;
+      if (E == 2) sa[w][1][kk] = v1;
+    }
+    __syncwarp();
+    if (lane <= pd) {
+      float2 post = dv[m];
+      if (m & 1) post = make_float2(-post.x, -post.y);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        float2 b = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < P; ++k) crfma<float>(b, c2[k], sa[w][e][k]);
+        cfma<float>(acc[e], post, b);
+      }
+    }
+    __syncwarp();
+  }
+  if (lane <= P) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) sred[w][e][lane] = acc[e];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < E * ldl; idx += blockDim.x) {
+    const int e = idx / ldl, mm = idx - e * ldl;
+    float2 v = cadd<float>(cadd<float>(sred[0][e][mm], sred[1][e][mm]), cadd<float>(sred[2][e][mm], sred[3][e][mm]));
+    local[(size_t)gid * E * ldl + idx] = v;
+  }
+}
+
 // ---------------------------------------------------------------------------------
 // The same M2L in double-float arithmetic (FP64-class accuracy on the FP32 pipes): the
 // multipoles, d^-j and binomial tables are double-float; each output's binomial sum is
@@ -1578,7 +1653,14 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     if (sm > 48 * 1024)
       EB_CUDA_TRY(cudaFuncSetAttribute(k_m2l<T, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     ProfScope ps(ctx, 1, st);
-    if (nt > 0) {
+    if (nt > 0 && sizeof(T) == 4 && p == 20) {
+      k_m2l_f32p<E, 20><<<nt, 128, 0, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
+                                            t.vcount.as<int>(), reinterpret_cast<const float*>(tb.binom.p), ldb,
+                                            reinterpret_cast<const float2*>(tb.dinv.p), tb.pd.as<int>(),
+                                            reinterpret_cast<const float2*>(w.mpole.p),
+                                            reinterpret_cast<float2*>(w.local.p));
+      eb_count_launch(ctx);
+    } else if (nt > 0) {
       k_m2l<T, E><<<nt, 128, sm, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                        t.vcount.as<int>(), p, tb.binom.as<T>(), ldb,
                                        tb.dinv.as<c_t<T>>(), tb.pd.as<int>(), w.mpole.as<c_t<T>>(),
