@@ -298,6 +298,7 @@ int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info) {
   info->levels = ctx->tree.L;
   info->nboxes = ctx->tree.nbox;
   info->nleaves = ctx->tree.nleaf;
+  EB_TRY(eb_tree_pairs(ctx, ctx->tree));
   info->v_pairs = ctx->tree.v_pairs;
   info->u_pairs = ctx->tree.u_pairs;
   info->p = ctx->last_p;

@@ -38,6 +38,17 @@ struct DevBuf {
   template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
 };
 
+// Page-locked host staging for the tree build's small device-to-host reads (so that one
+// stream synchronisation covers several of them).
+struct EbTreeHost {
+  double bbox[4];          // min x, max x, min y, max y
+  double sq[4];            // the bounding square: W, x0, y0, 2^20 / W
+  int bad;                 // a non-finite coordinate
+  int hist[EB_KEY_LEVELS + 1];
+  int last[6];             // counts and scans of the last leaf or box (groups, tiles, chunks)
+  unsigned long long pairs[2];  // near-field and V-list pair counts
+};
+
 // Sparse uniform-depth quadtree over a point set, built on the GPU.
 // Boxes of level l are stored in Morton order in the global box range
 // [lev_off[l], lev_off[l+1]); every box owns a contiguous range of the sorted points.
@@ -48,8 +59,11 @@ struct EbTree {
   int nleaf = 0;
   int lev_off[EB_KEY_LEVELS + 2] = {0};
   double x0 = 0, y0 = 0, W = 1;  // root square [x0, x0+W] x [y0, y0+W]
-  long long v_pairs = 0, u_pairs = 0;
+  long long v_pairs = 0, u_pairs = 0;  // read from host->pairs when first asked for
+  bool pairs_read = false;
   bool valid = false;
+  EbTreeHost* host = nullptr;  // page-locked (cudaMallocHost), freed with the tree
+  ~EbTree();
 
   DevBuf perm;     // int[n]: sorted index -> original index
   DevBuf zs;       // double2[n]: sorted positions
@@ -64,6 +78,7 @@ struct EbTree {
   DevBuf vlist;    // int[nbox*EB_VMAX]
   DevBuf vcode;    // unsigned char[nbox*EB_VMAX]
   DevBuf vcount;   // int[nbox]
+  DevBuf tcount, tstart;  // int[nleaf]: near-field tiles per leaf and their scan
   DevBuf ulist;    // int[nleaf*EB_UMAX] (global box ids)
   DevBuf ucount;   // int[nleaf]
   // near-field work items: groups of up to EB_GROUP targets of one leaf
@@ -75,7 +90,7 @@ struct EbTree {
   int ntile = 0;
   DevBuf tiles;    // int4[ntile]: (leaf, first, end, 0)
   DevBuf anc;      // int[nleaf*(L-1)]: each leaf's boxes at levels L, L-1, .., 2 (itself first)
-  DevBuf flags, scan, hist, bbox, partial, cubtmp;
+  DevBuf flags, scan, hist, bbox, partial, cubtmp, pairs;
   // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
   // EB_CHUNK points (coarser levels by M2M)
   int nchunk = 0;
@@ -190,6 +205,8 @@ struct eb_ctx {
 
 // tree.cu
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target);
+// The tree's pair counts (u_pairs, v_pairs), waiting for the build if it is in flight.
+int eb_tree_pairs(eb_ctx* ctx, EbTree& t);
 
 // fmm.cu
 struct EbPost;

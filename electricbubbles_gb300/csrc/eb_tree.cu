@@ -78,7 +78,10 @@ __global__ void k_bbox(const double2* __restrict__ z, int n, Box4* __restrict__ 
   if (threadIdx.x == 0) part[blockIdx.x] = mk_box4(s[0][0], s[1][0], s[2][0], s[3][0]);
 }
 
-__global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __restrict__ out) {
+// The bounding box and the root square sq = (W, x0, y0, 2^20 / W): the box's larger
+// side widened by 1e-9 relative, centred on the box (W = 1 for a single point).
+__global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __restrict__ out,
+                             double* __restrict__ sq) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   Box4 r = mk_box4(INFINITY, -INFINITY, INFINITY, -INFINITY);
   for (int i = 0; i < nb; ++i) {
@@ -86,13 +89,20 @@ __global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __rest
     r.x = fmin(r.x, p.x); r.y = fmax(r.y, p.y); r.z = fmin(r.z, p.z); r.w = fmax(r.w, p.w);
   }
   *out = r;
+  double w = fmax(__dadd_rn(r.y, -r.x), __dadd_rn(r.w, -r.z));
+  if (!(w > 0)) w = 1.0;
+  w = __dmul_rn(w, 1.0 + 1e-9);
+  sq[0] = w;
+  sq[1] = __dadd_rn(__dmul_rn(0.5, __dadd_rn(r.x, r.y)), -__dmul_rn(0.5, w));
+  sq[2] = __dadd_rn(__dmul_rn(0.5, __dadd_rn(r.z, r.w)), -__dmul_rn(0.5, w));
+  sq[3] = __ddiv_rn((double)(1u << EB_KEY_LEVELS), w);
 }
 
-__global__ void k_keys(const double2* __restrict__ z, int n, double x0, double y0,
-                       double inv_cell, unsigned long long* __restrict__ keys,
-                       int* __restrict__ idx) {
+__global__ void k_keys(const double2* __restrict__ z, int n, const double* __restrict__ sq,
+                       unsigned long long* __restrict__ keys, int* __restrict__ idx) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double x0 = sq[1], y0 = sq[2], inv_cell = sq[3];
   const double maxc = (double)((1u << EB_KEY_LEVELS) - 1);
   double fx = floor((z[i].x - x0) * inv_cell), fy = floor((z[i].y - y0) * inv_cell);
   fx = fmin(fmax(fx, 0.0), maxc);
@@ -438,39 +448,28 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   if (leaf_target < 1) leaf_target = 32;
   t.n = n;
   const int BS = 256;
-  // 1. bounding square
+  if (!t.host) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&t.host), sizeof(EbTreeHost)));
+  EbTreeHost* H = t.host;
+  t.pairs_read = false;
+  // 1. bounding square, on the device (read back with the level histogram below)
   int nbb = std::min(nblk(n, BS), 1024);
   EB_TRY(t.partial.ensure(sizeof(Box4) * (size_t)nbb));
-  EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(int) * 4));
-  int* bad = reinterpret_cast<int*>(t.bbox.as<char>() + sizeof(Box4));
+  EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(double) * 4 + sizeof(int) * 4));
+  double* sq = reinterpret_cast<double*>(t.bbox.as<char>() + sizeof(Box4));
+  int* bad = reinterpret_cast<int*>(sq + 4);
   EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
   k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
   eb_count_launch(ctx);
-  k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>());
+  k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
   eb_count_launch(ctx);
-  Box4 bb;
-  int hbad = 0;
-  EB_CUDA_TRY(cudaMemcpyAsync(&bb, t.bbox.p, sizeof(Box4), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaStreamSynchronize(st));
-  if (hbad) {
-    eb_set_last_error_msg("non-finite node coordinate");
-    return EB_ERR_NAN;
-  }
-  double w = std::max(bb.y - bb.x, bb.w - bb.z);
-  if (!(w > 0)) w = 1.0;
-  w *= 1.0 + 1e-9;
-  t.W = w;
-  t.x0 = 0.5 * (bb.x + bb.y) - 0.5 * w;
-  t.y0 = 0.5 * (bb.z + bb.w) - 0.5 * w;
-  // 2. keys and sort
+  EB_CUDA_TRY(cudaMemcpyAsync(H->sq, sq, sizeof(H->sq), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  // 2. keys and sort (a non-finite coordinate gives clamped keys; reported below)
   EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
   EB_TRY(t.keys_alt.ensure(sizeof(unsigned long long) * (size_t)n));
   EB_TRY(t.idx_alt.ensure(sizeof(int) * (size_t)n));
   EB_TRY(t.perm.ensure(sizeof(int) * (size_t)n));
-  double inv_cell = (double)(1u << EB_KEY_LEVELS) / w;
-  k_keys<<<nblk(n, BS), BS, 0, st>>>(z, n, t.x0, t.y0, inv_cell, t.keys_alt.as<unsigned long long>(),
-                                     t.idx_alt.as<int>());
+  k_keys<<<nblk(n, BS), BS, 0, st>>>(z, n, sq, t.keys_alt.as<unsigned long long>(), t.idx_alt.as<int>());
   eb_count_launch(ctx);
   size_t tmp_sort = 0, tmp_scan = 0;
   cub::DeviceRadixSort::SortPairs(nullptr, tmp_sort, t.keys_alt.as<unsigned long long>(),
@@ -495,9 +494,16 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   k_level_hist<<<std::min(nblk(n, BS), 1024), BS, 0, st>>>(t.keys.as<unsigned long long>(), n,
                                                           t.hist.as<int>());
   eb_count_launch(ctx);
-  int hist[EB_KEY_LEVELS + 1];
-  EB_CUDA_TRY(cudaMemcpyAsync(hist, t.hist.p, sizeof(hist), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(H->hist, t.hist.p, sizeof(H->hist), cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (H->bad) {
+    eb_set_last_error_msg("non-finite node coordinate");
+    return EB_ERR_NAN;
+  }
+  t.W = H->sq[0];
+  t.x0 = H->sq[1];
+  t.y0 = H->sq[2];
+  const int* hist = H->hist;
   int nb[EB_KEY_LEVELS + 1];
   nb[0] = 1;
   for (int l = 1; l <= EB_KEY_LEVELS; ++l) nb[l] = nb[l - 1] + hist[l];
@@ -567,64 +573,39 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   k_ulist<<<nblk(t.nleaf, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[L], t.nleaf, L,
                                              t.ulist.as<int>(), t.ucount.as<int>());
   eb_count_launch(ctx);
-  // 8. near-field work items: groups of EB_GROUP targets
-  {
-    int nl = t.nleaf;
-    k_group_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
-                                               t.flags.as<int>());
-    eb_count_launch(ctx);
-    tb = t.cubtmp.bytes;
-    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
-    eb_count_launch(ctx);
-    int last[2];
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaStreamSynchronize(st));
-    t.ngroup = last[0] + last[1];
-    EB_TRY(t.gleaf.ensure(sizeof(int) * (size_t)t.ngroup));
-    EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
-    k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
-                                              t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
-    eb_count_launch(ctx);
-  }
-  // 8a. shared-memory near-field tiles of at most EB_NTILE targets
-  {
-    int nl = t.nleaf;
-    k_tile_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
-                                              t.flags.as<int>());
-    eb_count_launch(ctx);
-    tb = t.cubtmp.bytes;
-    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
-    eb_count_launch(ctx);
-    int last[2];
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaStreamSynchronize(st));
-    t.ntile = last[0] + last[1];
-    EB_TRY(t.tiles.ensure(sizeof(int4) * (size_t)t.ntile));
-    k_tile_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
-                                             t.flags.as<int>(), t.scan.as<int>(), t.tiles.as<int4>());
-    eb_count_launch(ctx);
-  }
-  if (L >= 2) {
-    EB_TRY(t.anc.ensure(sizeof(int) * (size_t)t.nleaf * (L - 1)));
-    k_ancestors<<<nblk(t.nleaf, BS), BS, 0, st>>>(t.lev_off[L], t.nleaf, L - 1, t.parent.as<int>(),
-                                                  t.anc.as<int>());
-    eb_count_launch(ctx);
-  }
-  // 8b. chunks of at most EB_CHUNK points of every box of the EB_DIRECT_LEVELS finest
-  // levels (FP32 direct P2M)
+  // 8. work items, counted and scanned first so that one synchronisation sizes them all:
+  // near-field groups of EB_GROUP targets, shared-memory tiles of at most EB_NTILE
+  // targets, and FP32 direct-P2M chunks of at most EB_CHUNK points of every box of the
+  // chunked levels (every level up to 256K points, so that no dependent M2M launches
+  // remain on the critical path; above that the EB_DIRECT_LEVELS finest)
+  const int nl = t.nleaf;
+  EB_TRY(t.tcount.ensure(sizeof(int) * (size_t)nl));
+  EB_TRY(t.tstart.ensure(sizeof(int) * (size_t)nl));
+  k_group_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                             t.flags.as<int>());
+  eb_count_launch(ctx);
+  tb = t.cubtmp.bytes;
+  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
+  eb_count_launch(ctx);
+  k_tile_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                            t.tcount.as<int>());
+  eb_count_launch(ctx);
+  tb = t.cubtmp.bytes;
+  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.tcount.as<int>(), t.tstart.as<int>(), nl, st));
+  eb_count_launch(ctx);
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[2], t.tcount.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[3], t.tstart.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
   t.nchunk = 0;
-  // up to 256K points the multipoles of every level come directly from the points (no
-  // dependent M2M launches on the critical path); above, the EB_DIRECT_LEVELS finest
   t.chunk_lmin = n <= (1 << 18) ? 2 : std::max(2, L - EB_DIRECT_LEVELS + 1);
+  const int cfirst = t.lev_off[t.chunk_lmin], nb2 = t.nbox - cfirst;
   if (L >= 2) {
-    const int first = t.lev_off[t.chunk_lmin], nb2 = t.nbox - first;
     EB_TRY(t.ccount.ensure(sizeof(int) * (size_t)nb2));
     EB_TRY(t.cstart.ensure(sizeof(int) * (size_t)(nb2 + 1)));
     EB_TRY(t.cdone.ensure(sizeof(int) * (size_t)nb2));
     EB_CUDA_TRY(cudaMemsetAsync(t.cdone.p, 0, sizeof(int) * (size_t)nb2, st));
-    k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(first, nb2, t.pt0.as<int>(), t.pt1.as<int>(), t.ccount.as<int>());
+    k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(cfirst, nb2, t.pt0.as<int>(), t.pt1.as<int>(), t.ccount.as<int>());
     eb_count_launch(ctx);
     size_t need = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, need, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st);
@@ -632,14 +613,30 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     tb = t.cubtmp.bytes;
     EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st));
     eb_count_launch(ctx);
-    int last[2];
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[0], t.ccount.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaMemcpyAsync(&last[1], t.cstart.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaStreamSynchronize(st));
-    t.nchunk = last[0] + last[1];
+    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[4], t.ccount.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[5], t.cstart.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  }
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  t.ngroup = H->last[0] + H->last[1];
+  t.ntile = H->last[2] + H->last[3];
+  EB_TRY(t.gleaf.ensure(sizeof(int) * (size_t)t.ngroup));
+  EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
+  k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
+                                            t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
+  eb_count_launch(ctx);
+  EB_TRY(t.tiles.ensure(sizeof(int4) * (size_t)t.ntile));
+  k_tile_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+                                           t.tcount.as<int>(), t.tstart.as<int>(), t.tiles.as<int4>());
+  eb_count_launch(ctx);
+  if (L >= 2) {
+    EB_TRY(t.anc.ensure(sizeof(int) * (size_t)t.nleaf * (L - 1)));
+    k_ancestors<<<nblk(t.nleaf, BS), BS, 0, st>>>(t.lev_off[L], t.nleaf, L - 1, t.parent.as<int>(),
+                                                  t.anc.as<int>());
+    eb_count_launch(ctx);
+    t.nchunk = H->last[4] + H->last[5];
     EB_CUDA_TRY(cudaMemcpyAsync(t.cstart.as<int>() + nb2, &t.nchunk, sizeof(int), cudaMemcpyHostToDevice, st));
     EB_TRY(t.chunk_box.ensure(sizeof(int) * (size_t)t.nchunk));
-    k_chunk_fill<<<nblk(nb2, BS), BS, 0, st>>>(first, nb2, t.ccount.as<int>(), t.cstart.as<int>(),
+    k_chunk_fill<<<nblk(nb2, BS), BS, 0, st>>>(cfirst, nb2, t.ccount.as<int>(), t.cstart.as<int>(),
                                                t.chunk_box.as<int>());
     eb_count_launch(ctx);
   }
@@ -651,20 +648,32 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
                                         t.W / (double)(1u << L), t.wdf.as<float4>(),
                                         t.wdf_lo.as<float2>());
   eb_count_launch(ctx);
-  // 10. pair counts (the algorithmic work of the near field and M2L)
-  unsigned long long* cnt = reinterpret_cast<unsigned long long*>(t.partial.p);
+  // 10. pair counts (the algorithmic work of the near field and M2L), copied to the host
+  // without waiting; eb_tree_pairs reads them
+  EB_TRY(t.pairs.ensure(2 * sizeof(unsigned long long)));
+  unsigned long long* cnt = t.pairs.as<unsigned long long>();
   EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
   int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
   k_pair_counts<<<std::max(nblk(t.nleaf, BS), 1), BS, 0, st>>>(
       t.lev_off[L], t.nleaf, t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(),
       vfirst, vlast, t.vcount.as<int>(), cnt);
   eb_count_launch(ctx);
-  unsigned long long hc[2];
-  EB_CUDA_TRY(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  EB_CUDA_TRY(cudaMemcpyAsync(H->pairs, cnt, sizeof(H->pairs), cudaMemcpyDeviceToHost, st));
   EB_TRY(eb_check_launch(ctx, "tree build"));
-  t.u_pairs = (long long)hc[0];
-  t.v_pairs = (long long)hc[1];
   t.valid = true;
   return EB_OK;
+}
+
+int eb_tree_pairs(eb_ctx* ctx, EbTree& t) {
+  if (!t.pairs_read) {
+    EB_CUDA_TRY(cudaStreamSynchronize(eb_stream(ctx)));
+    t.u_pairs = (long long)t.host->pairs[0];
+    t.v_pairs = (long long)t.host->pairs[1];
+    t.pairs_read = true;
+  }
+  return EB_OK;
+}
+
+EbTree::~EbTree() {
+  if (host) cudaFreeHost(host);
 }
