@@ -141,58 +141,65 @@ __global__ void k_gather_points(const double2* __restrict__ z, const int* __rest
   zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
 }
 
-__global__ void k_heads(const unsigned long long* __restrict__ keys, int n, int shift,
-                        int* __restrict__ flags) {
+// Every level at once: flags[l*n + i] = 1 where sorted point i starts a box of level l
+// (l = 0..L). One exclusive scan over the concatenated rows then gives each head its
+// global box id (rows in level order: level l's ids start at lev_off[l]).
+__global__ void k_heads_all(const unsigned long long* __restrict__ keys, int n, int L,
+                            int* __restrict__ flags) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  flags[i] = (i == 0) || ((keys[i] >> shift) != (keys[i - 1] >> shift));
-}
-
-__global__ void k_leaf_fill(const unsigned long long* __restrict__ keys, int n, int shift,
-                            const int* __restrict__ flags, const int* __restrict__ scan,
-                            int off, unsigned long long* __restrict__ bkey,
-                            int* __restrict__ pt0, int* __restrict__ child0,
-                            int* __restrict__ nchild) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || !flags[i]) return;
-  int b = off + scan[i];
-  bkey[b] = keys[i] >> shift;
-  pt0[b] = i;
-  child0[b] = -1;
-  nchild[b] = 0;
-}
-
-__global__ void k_level_pt1(const int* __restrict__ pt0, int* __restrict__ pt1, int off,
-                            int nb, int n) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  pt1[off + b] = (b + 1 < nb) ? pt0[off + b + 1] : n;
-}
-
-__global__ void k_parent_fill(unsigned long long* __restrict__ bkey, int offc, int nbc,
-                              int offp, const int* __restrict__ flags,
-                              const int* __restrict__ scan, int* __restrict__ pt0,
-                              int* __restrict__ parent, int* __restrict__ child0) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbc) return;
-  // inclusive count of parent heads up to b, minus one: the parent's index
-  int P = offp + scan[b] + flags[b] - 1;
-  parent[offc + b] = P;
-  if (flags[b]) {
-    bkey[P] = bkey[offc + b] >> 2;
-    pt0[P] = pt0[offc + b];
-    child0[P] = offc + b;
+  const unsigned long long k = keys[i], kp = i > 0 ? keys[i - 1] : 0ull;
+  for (int l = 0; l <= L; ++l) {
+    const int sh = 2 * (EB_KEY_LEVELS - l);
+    flags[(size_t)l * n + i] = (i == 0) || ((k >> sh) != (kp >> sh));
   }
 }
 
-__global__ void k_parent_fin(int offp, int nbp, int offc, int nbc, int n,
-                             const int* __restrict__ child0, int* __restrict__ nchild,
-                             const int* __restrict__ pt0, int* __restrict__ pt1) {
-  int P = blockIdx.x * blockDim.x + threadIdx.x;
-  if (P >= nbp) return;
-  int next = (P + 1 < nbp) ? child0[offp + P + 1] : offc + nbc;
-  nchild[offp + P] = next - child0[offp + P];
-  pt1[offp + P] = (P + 1 < nbp) ? pt0[offp + P + 1] : n;
+// Box key, first point and parent of every box; a box whose head point also starts its
+// parent is the parent's first child.
+__global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, int L,
+                            const int* __restrict__ flags, const int* __restrict__ scan,
+                            unsigned long long* __restrict__ bkey, int* __restrict__ pt0,
+                            int* __restrict__ parent, int* __restrict__ child0) {
+  const long long tot = (long long)(L + 1) * n;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < tot;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (!flags[idx]) continue;
+    const int l = (int)(idx / n), i = (int)(idx - (long long)l * n);
+    const int b = scan[idx];
+    bkey[b] = keys[i] >> (2 * (EB_KEY_LEVELS - l));
+    pt0[b] = i;
+    if (l == 0) {
+      parent[b] = -1;
+    } else {
+      const size_t up = idx - n;
+      const int P = scan[up] + flags[up] - 1;
+      parent[b] = P;
+      if (flags[up]) child0[P] = b;
+    }
+  }
+}
+
+struct LevOffT {
+  int v[EB_KEY_LEVELS + 3];
+};
+
+// Point range end, children count (and no children at the leaf level) of every box.
+__global__ void k_boxes_fin(int nbox, LevOffT lo, int L, int n, int* __restrict__ child0,
+                            int* __restrict__ nchild, const int* __restrict__ pt0,
+                            int* __restrict__ pt1) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbox) return;
+  int l = 0;
+  while (b >= lo.v[l + 1]) ++l;
+  const bool last = b + 1 >= lo.v[l + 1];
+  pt1[b] = last ? n : pt0[b + 1];
+  if (l == L) {
+    child0[b] = -1;
+    nchild[b] = 0;
+  } else {
+    nchild[b] = (last ? lo.v[l + 2] : child0[b + 1]) - child0[b];
+  }
 }
 
 __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ bkey, int off,
@@ -522,41 +529,31 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   EB_TRY(t.parent.ensure(sizeof(int) * NB));
   EB_TRY(t.child0.ensure(sizeof(int) * NB));
   EB_TRY(t.nchild.ensure(sizeof(int) * NB));
-  EB_TRY(t.flags.ensure(sizeof(int) * (size_t)n));
-  EB_TRY(t.scan.ensure(sizeof(int) * (size_t)n));
-  // 5. leaf boxes
-  int shift = 2 * (EB_KEY_LEVELS - L);
-  k_heads<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, shift, t.flags.as<int>());
+  // 5. boxes of every level in three launches (heads, one scan, fill) and a finish
+  const size_t nflag = (size_t)(L + 1) * n;
+  EB_TRY(t.flags.ensure(sizeof(int) * nflag));
+  EB_TRY(t.scan.ensure(sizeof(int) * nflag));
+  k_heads_all<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, L, t.flags.as<int>());
   eb_count_launch(ctx);
+  {
+    size_t need = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, need, t.flags.as<int>(), t.scan.as<int>(), (int)nflag, st);
+    if (need > t.cubtmp.bytes) EB_TRY(t.cubtmp.ensure(need));
+  }
   tb = t.cubtmp.bytes;
-  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), n, st));
+  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), (int)nflag, st));
   eb_count_launch(ctx);
-  k_leaf_fill<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, shift, t.flags.as<int>(),
-                                          t.scan.as<int>(), t.lev_off[L],
-                                          t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
-                                          t.child0.as<int>(), t.nchild.as<int>());
+  k_boxes_all<<<std::min(nblk((long long)nflag, BS), 152 * 16), BS, 0, st>>>(
+      t.keys.as<unsigned long long>(), n, L, t.flags.as<int>(), t.scan.as<int>(),
+      t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.parent.as<int>(), t.child0.as<int>());
   eb_count_launch(ctx);
-  k_level_pt1<<<nblk(nb[L], BS), BS, 0, st>>>(t.pt0.as<int>(), t.pt1.as<int>(), t.lev_off[L], nb[L], n);
-  eb_count_launch(ctx);
-  // 6. coarser levels from the finer level's box keys
-  for (int l = L - 1; l >= 0; --l) {
-    int offc = t.lev_off[l + 1], nbc = nb[l + 1], offp = t.lev_off[l];
-    k_heads<<<nblk(nbc, BS), BS, 0, st>>>(t.bkey.as<unsigned long long>() + offc, nbc, 2,
-                                          t.flags.as<int>());
-    eb_count_launch(ctx);
-    tb = t.cubtmp.bytes;
-    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nbc, st));
-    eb_count_launch(ctx);
-    k_parent_fill<<<nblk(nbc, BS), BS, 0, st>>>(t.bkey.as<unsigned long long>(), offc, nbc, offp,
-                                                t.flags.as<int>(), t.scan.as<int>(), t.pt0.as<int>(),
-                                                t.parent.as<int>(), t.child0.as<int>());
-    eb_count_launch(ctx);
-    k_parent_fin<<<nblk(nb[l], BS), BS, 0, st>>>(offp, nb[l], offc, nbc, n, t.child0.as<int>(),
-                                                 t.nchild.as<int>(), t.pt0.as<int>(), t.pt1.as<int>());
+  {
+    LevOffT lo;
+    for (int l = 0; l < EB_KEY_LEVELS + 3; ++l) lo.v[l] = t.lev_off[std::min(l, L + 1)];
+    k_boxes_fin<<<nblk(t.nbox, BS), BS, 0, st>>>(t.nbox, lo, L, n, t.child0.as<int>(), t.nchild.as<int>(),
+                                                 t.pt0.as<int>(), t.pt1.as<int>());
     eb_count_launch(ctx);
   }
-  int minus1 = -1;
-  EB_CUDA_TRY(cudaMemcpyAsync(t.parent.as<int>(), &minus1, sizeof(int), cudaMemcpyHostToDevice, st));
   // 7. interaction lists
   EB_TRY(t.vlist.ensure(sizeof(int) * NB * EB_VMAX));
   EB_TRY(t.vcode.ensure(NB * EB_VMAX));
