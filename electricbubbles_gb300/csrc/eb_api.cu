@@ -69,17 +69,15 @@ __global__ void k_drop_reduce_stokes(const int* __restrict__ start, const double
   }
 }
 
-// Per-node weights of the singular-term sums, once per geometry.
-__global__ void k_pk_weights(int nbk, const int* __restrict__ drop_of, const double* __restrict__ hpt,
-                             const double2* __restrict__ z, const double2* __restrict__ dz,
-                             const double2* __restrict__ zk, double2* __restrict__ pkw) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nbk) return;
+// Per-node weight of the singular-term sums, once per geometry.
+__device__ __forceinline__ double2 pk_weight(int i, const int* __restrict__ drop_of,
+                                             const double* __restrict__ hpt, const double2* __restrict__ z,
+                                             const double2* __restrict__ dz, const double2* __restrict__ zk) {
   const double2 c = zk[drop_of[i]];
   const double2 d = make_double2(z[i].x - c.x, z[i].y - c.y);
   const double2 q = cdiv<double>(dz[i], cmul<double>(d, d));
   const double f = 2.0 * hpt[i] / EB_PI;
-  pkw[i] = make_double2(f * q.x, f * q.y);
+  return make_double2(f * q.x, f * q.y);
 }
 
 // Constraint sums the reference writes past YY(N) (laplace.f:252-259): h s' u per drop.
@@ -111,12 +109,17 @@ __global__ void k_fill_drop(int k, const int* __restrict__ start, int* __restric
   }
 }
 
+// Per-node coefficients of the post-processing and the singular-sum weights.
 __global__ void k_post_coefs(int nbk, const double2* __restrict__ dz, const double* __restrict__ dsda,
                              const double* __restrict__ kappa, const double* __restrict__ hpt,
                              double* __restrict__ c1, double2* __restrict__ c2, double* __restrict__ d,
-                             float* __restrict__ c1f, float2* __restrict__ c2f, float* __restrict__ df) {
+                             float* __restrict__ c1f, float2* __restrict__ c2f, float* __restrict__ df,
+                             const int* __restrict__ drop_of, const double2* __restrict__ z,
+                             const double2* __restrict__ zk, double2* __restrict__ pkw) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nbk) eb_post_coefs(t, dz, dsda, kappa, hpt, c1, c2, d, c1f, c2f, df);
+  if (t >= nbk) return;
+  eb_post_coefs(t, dz, dsda, kappa, hpt, c1, c2, d, c1f, c2f, df);
+  pkw[t] = pk_weight(t, drop_of, hpt, z, dz, zk);
 }
 
 int copy_in(eb_ctx* ctx, DevBuf& buf, const void* src, size_t bytes, int mem) {
@@ -349,15 +352,13 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   EB_TRY(ctx->pc2f.ensure(sizeof(float2) * nbk));
   EB_TRY(ctx->plapf.ensure(sizeof(float) * nbk));
   EB_TRY(ctx->pkw.ensure(sizeof(double2) * nbk));
-  k_pk_weights<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->drop_of.as<int>(), ctx->hpt.as<double>(),
-                                             ctx->z.as<double2>(), ctx->dz.as<double2>(),
-                                             ctx->zk.as<double2>(), ctx->pkw.as<double2>());
-  eb_count_launch(ctx);
   k_post_coefs<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->dz.as<double2>(), ctx->dsda.as<double>(),
                                              ctx->kappa.as<double>(), ctx->hpt.as<double>(),
                                              ctx->pc1.as<double>(), ctx->pc2.as<double2>(),
                                              ctx->plap.as<double>(), ctx->pc1f.as<float>(),
-                                             ctx->pc2f.as<float2>(), ctx->plapf.as<float>());
+                                             ctx->pc2f.as<float2>(), ctx->plapf.as<float>(),
+                                             ctx->drop_of.as<int>(), ctx->z.as<double2>(),
+                                             ctx->zk.as<double2>(), ctx->pkw.as<double2>());
   eb_count_launch(ctx);
   EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
   ctx->tree_pv.valid = false;

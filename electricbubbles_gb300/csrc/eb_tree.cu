@@ -215,12 +215,15 @@ __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ b
   return -1;
 }
 
-__global__ void k_vlist(const unsigned long long* __restrict__ bkey, int off, int nb, int lev,
+// V lists of every box of levels 2..L in one launch (the box's level from lev_off).
+__global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo, int first, int nbox,
                         int* __restrict__ vlist, unsigned char* __restrict__ vcode,
                         int* __restrict__ vcount) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  int gid = off + b;
+  const int gid = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nbox) return;
+  int lev = 0;
+  while (gid >= lo.v[lev + 1]) ++lev;
+  const int off = lo.v[lev], nb = lo.v[lev + 1] - off;
   unsigned long long key = bkey[gid];
   int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
   int px = ix >> 1, py = iy >> 1, half = 1 << (lev - 1), side = 1 << lev;
@@ -559,10 +562,13 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   EB_TRY(t.vcode.ensure(NB * EB_VMAX));
   EB_TRY(t.vcount.ensure(sizeof(int) * NB));
   EB_CUDA_TRY(cudaMemsetAsync(t.vcount.p, 0, sizeof(int) * NB, st));
-  for (int l = 2; l <= L; ++l) {
-    k_vlist<<<nblk(nb[l], 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[l], nb[l], l,
-                                              t.vlist.as<int>(), t.vcode.as<unsigned char>(),
-                                              t.vcount.as<int>());
+  if (L >= 2) {
+    LevOffT lo;
+    for (int l = 0; l < EB_KEY_LEVELS + 3; ++l) lo.v[l] = t.lev_off[std::min(l, L + 1)];
+    const int first = t.lev_off[2];
+    k_vlist<<<nblk(t.nbox - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox,
+                                                       t.vlist.as<int>(), t.vcode.as<unsigned char>(),
+                                                       t.vcount.as<int>());
     eb_count_launch(ctx);
   }
   EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)t.nleaf * EB_UMAX));
