@@ -641,16 +641,19 @@ __device__ __forceinline__ cdf cacc_value(const dfacc& rx, const dfacc& ry) {
 // P2M at the leaves from the leaf-relative offsets w (units of the leaf side) and the
 // charges qa/r, qb/r: M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 template <int E>
-__global__ void __launch_bounds__(128) k_p2m_df(int off, const int* __restrict__ pt0,
-                                               const int* __restrict__ pt1, const float4* __restrict__ wa,
-                                               const float4* __restrict__ q, int p,
-                                               float4* __restrict__ mpole) {
+__global__ void k_p2m_df(int off, const int* __restrict__ pt0, const int* __restrict__ pt1,
+                         const float4* __restrict__ wa, const float4* __restrict__ q, int p,
+                         float4* __restrict__ mpole) {
+  // thread (which, k) < NA p sums one of A_k, B_k, C_k over the leaf's points
+  constexpr int NA = E == 2 ? 3 : 1;
   extern __shared__ float4 sm4[];
   const int ps = p + 1;
   float4* pw = sm4;
   float4* sc = pw + 32 * ps;
   const int b = off + blockIdx.x, tid = threadIdx.x;
-  dfacc Ax{0.f, 0.f}, Ay{0.f, 0.f}, Bx{0.f, 0.f}, By{0.f, 0.f}, Cx{0.f, 0.f}, Cy{0.f, 0.f};
+  const int which = tid / p, kq = tid - which * p;
+  const bool acc_thread = which < NA;
+  dfacc Rx{0.f, 0.f}, Ry{0.f, 0.f};
   const int i0 = pt0[b], i1 = pt1[b];
   for (int base = i0; base < i1; base += 32) {
     const int cnt = min(32, i1 - base);
@@ -681,27 +684,22 @@ __global__ void __launch_bounds__(128) k_p2m_df(int off, const int* __restrict__
       }
       __syncthreads();
     }
-    if (tid < p) {
-      for (int s = 0; s < cnt; ++s) {
-        const cdf v = cdf_from_float4(pw[s * ps + tid]);
-        cacc_mul(Ax, Ay, cdf_from_float4(sc[s]), v);
-        if (E == 2) {
-          cacc_mul(Bx, By, cdf_from_float4(sc[32 + s]), v);
-          cacc_mul(Cx, Cy, cdf_from_float4(sc[64 + s]), v);
-        }
-      }
+    if (acc_thread) {
+      const float4* scw = sc + 32 * which;
+      for (int s2 = 0; s2 < cnt; ++s2) cacc_mul(Rx, Ry, cdf_from_float4(scw[s2]), cdf_from_float4(pw[s2 * ps + kq]));
     }
   }
   __syncthreads();
-  if (tid < p) pw[tid] = cdf_f4(cacc_value(Cx, Cy));
+  float4* red = pw;  // [NA][p]
+  if (acc_thread) red[which * p + kq] = cdf_f4(cacc_value(Rx, Ry));
   __syncthreads();
   if (tid < p) {
     float4* mp = mpole + (size_t)b * E * p;
-    const cdf A = cacc_value(Ax, Ay);
+    const cdf A = cdf_from_float4(red[tid]);
     mp[tid] = cdf_f4(cdf{dfl_neg(A.x), dfl_neg(A.y)});
     if (E == 2) {
-      cdf v = cacc_value(Bx, By);
-      if (tid >= 1) v = cdf_add(v, cdf_scale(cdf_from_float4(pw[tid - 1]), (float)tid));
+      cdf v = cdf_from_float4(red[p + tid]);
+      if (tid >= 1) v = cdf_add(v, cdf_scale(cdf_from_float4(red[2 * p + tid - 1]), (float)tid));
       mp[p + tid] = cdf_f4(cdf{dfl_neg(v.x), dfl_neg(v.y)});
     }
   }
@@ -1554,7 +1552,7 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   {
     size_t sm = sizeof(float4) * (32 * (size_t)(p + 1) + 96);
     if (sm > 48 * 1024) EB_CUDA_TRY(cudaFuncSetAttribute(k_p2m_df<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_p2m_df<E><<<t.nleaf, 128, sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
+    k_p2m_df<E><<<t.nleaf, std::max(128, round32((E == 2 ? 3 : 1) * p)), sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
                                           E == 2 ? w.qdf.as<float4>() : w.pqdf.as<float4>(), p, mp);
     eb_count_launch(ctx);
   }
