@@ -364,6 +364,20 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
   ctx->tree_pv.valid = false;
   ctx->geom_valid = true;
   ctx->geom_version++;
+  {
+    const EbTree& t = ctx->tree;
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the fields' bytes
+    auto mix = [&h](const void* p, size_t nb) {
+      const unsigned char* c = static_cast<const unsigned char*>(p);
+      for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    const int ints[] = {t.n, ctx->nbk, ctx->k, t.L, t.nbox, t.nleaf, t.ngroup, t.ntile, t.nchunk, t.chunk_lmin};
+    mix(ints, sizeof(ints));
+    mix(t.lev_off, sizeof(int) * (size_t)(t.L + 2));
+    const double dbl[] = {t.W, t.x0, t.y0};
+    mix(dbl, sizeof(dbl));
+    ctx->geom_shape = h;
+  }
   eb_devbuf_collect();
   return EB_OK;
 }

@@ -195,6 +195,10 @@ struct eb_ctx {
   DevBuf gCtl, gXin, gWbuf;        // graph mode: control block, operator input and output
   std::vector<double> hH;
   unsigned long long geom_version = 0;  // advanced by every geometry install
+  // hash of everything a captured solve graph takes from the geometry by value (counts,
+  // level offsets, work-item counts, the root square): graphs are reused across installs
+  // with the same hash (the device data they read is reloaded by every launch)
+  unsigned long long geom_shape = 0;
   cudaStream_t cap_stream = nullptr;    // private stream for graph capture
   cudaStream_t side_stream = nullptr;   // second stream for work that overlaps the FMM
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

@@ -724,7 +724,7 @@ int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
     key[1] = (unsigned long long)(uintptr_t)op;
     key[2] = (unsigned long long)n;
     key[3] = (unsigned long long)maxl;
-    key[4] = ctx->geom_version;
+    key[4] = ctx->geom_shape;
     key[5] = epoch;
     memcpy(&key[6], &t1, 8);
     memcpy(&key[7], &t2, 8);

@@ -85,3 +85,30 @@ def test_graph_zero_and_nonfinite_rhs(pair, mode):
     # the context stays usable
     x, info = g.solvei(np.ones(2 * cfg.nbk), mode)
     assert info["ierr"] == 0 and info["err"] <= 1e-10
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32_refined"])
+def test_graph_across_geometry_installs(mode):
+    """Captured graphs are reused only while everything they take by value from the
+    geometry is unchanged: re-installing the same geometry reproduces the first solve bit
+    for bit, and a different geometry of the same sizes solves as in a fresh context."""
+    a = configs.many_drops(8, 128, seed=21, box=5.0)
+    b = configs.many_drops(8, 128, seed=22, box=5.0)
+    g = Context(graphs=1)
+    f = Context(graphs=1)
+    try:
+        def solve(ctx, cfg):
+            ex = ctx.extractdat(cfg.nd, cfg.rku())
+            rhs = np.ascontiguousarray(-0.5 * ex["dz"] / ex["dsda"]).view(np.float64).copy()
+            return ctx.solvei(rhs, mode)
+        xa1, ia1 = solve(g, a)
+        xb, ib = solve(g, b)
+        xa2, ia2 = solve(g, a)
+        xf, jf = solve(f, b)
+        assert ia1["graph"] == ib["graph"] == ia2["graph"] == 1
+        assert np.array_equal(xa1, xa2) and ia1["iters"] == ia2["iters"]
+        assert ib["iters"] == jf["iters"]
+        assert np.array_equal(xb, xf)
+    finally:
+        g.close()
+        f.close()
