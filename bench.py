@@ -469,7 +469,11 @@ def run_gpu(args, rank, world, local):
                                "target-source pair; with k_m2l<float, 2> the largest kernel of the "
                                "refined solve)", "bound": "fp32",
                      "achieved": dom["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": dom["achieved_tflops"] / fp32_peak, "traffic": None,
+                     "frac": dom["achieved_tflops"] / fp32_peak,
+                     # DRAM bytes of one k_near32<2> launch of this workload (ncu
+                     # dram__bytes_read.sum + dram__bytes_write.sum: 1,407,232 + 0)
+                     "traffic": 1407232 if WORKLOAD == "many_drops_64x512" else None,
+                     "traffic_unit": "bytes per launch (ncu capture of this workload)",
                      "peak_source": "measured in-run FP32 FMA chain (MEASURED_PEAKS.json has no FP32 "
                                     "CUDA-core figure)",
                      "flops_per_launch": dom["flops_per_launch"], "avg_launch_ms": dom["avg_launch_ms"]},
