@@ -286,7 +286,7 @@ def run_gpu(args, rank, world, local):
             far_flops = 8.0 * p_ord * 2 * tree["npoints"] * min(levels_l2p, 6)
             kern["k_near32<2>"] = kentry(near_ms, nn, near_pair_flops)
             kern["k_far32<2>"] = kentry(leaf_ms, nl, far_flops)
-            kern["k_m2l<float, 2>"] = kentry(m2l_ms, nm, m2l_flops)
+            kern["k_m2l_f32p<2, 20>"] = kentry(m2l_ms, nm, m2l_flops)
         else:
             kern["k_leaf_df<2>"] = kentry(leaf_ms, nl, near_pair_flops + 8.0 * p_ord * 2 * tree["npoints"])
             kern["k_m2l_df<2>"] = kentry(m2l_ms, nm, m2l_flops)
@@ -466,8 +466,8 @@ def run_gpu(args, rank, world, local):
         "accuracy": {"refined_vs_fp64_rel_l2": rel_diff, "refined_true_residual": inf32[-1]["err"]},
         "tree": tree,
         "roofline": {"kernel": "k_near32<2> (FP32 near field P2P over the U lists, 40 flop per "
-                               "target-source pair; with k_m2l<float, 2> the largest kernel of the "
-                               "refined solve)", "bound": "fp32",
+                               "target-source pair; with k_m2l_f32p<2, 20> and k_p2m_chunks<2> the largest "
+                               "kernels of the refined solve)", "bound": "fp32",
                      "achieved": dom["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": dom["achieved_tflops"] / fp32_peak,
                      # DRAM bytes of one k_near32<2> launch of this workload (ncu
