@@ -35,7 +35,8 @@ class Opts(ctypes.Structure):
                 ("leaf32", ctypes.c_int), ("tol64", ctypes.c_double), ("tol32", ctypes.c_double),
                 ("maxl", ctypes.c_int), ("gmres_tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
-                ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int)]
+                ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int),
+                ("resid_df", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):

@@ -64,14 +64,16 @@ class Context:
     """One GPU context: geometry, trees, expansion work space and a CUDA stream."""
 
     def __init__(self, p64=0, p32=0, leaf64=0, leaf32=0, tol64=0.0, tol32=0.0, maxl=0,
-                 gmres_tol=0.0, inner_tol=0.0, max_outer=0, device=0, graphs=0, df64=0):
+                 gmres_tol=0.0, inner_tol=0.0, max_outer=0, device=0, graphs=0, df64=0,
+                 resid_df=0):
         self._lib = _lib.load()
         o = Opts()
         self._lib.eb_opts_default(ctypes.byref(o))
         for name, v in (("p64", p64), ("p32", p32), ("leaf64", leaf64), ("leaf32", leaf32),
                         ("tol64", tol64), ("tol32", tol32), ("maxl", maxl),
                         ("gmres_tol", gmres_tol), ("inner_tol", inner_tol),
-                        ("max_outer", max_outer), ("graphs", graphs), ("df64", df64)):
+                        ("max_outer", max_outer), ("graphs", graphs), ("df64", df64),
+                        ("resid_df", resid_df)):
             if v:
                 setattr(o, name, v)
         o.device = device

@@ -172,7 +172,8 @@ void eb_opts_default(eb_opts* o) {
   o->max_outer = 8;
   o->device = 0;
   o->graphs = 1;
-  o->df64 = 1;
+  o->df64 = -1;
+  o->resid_df = 1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -202,6 +203,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.max_outer <= 0) o.max_outer = d.max_outer;
     if (o.graphs == 0) o.graphs = d.graphs;
     if (o.df64 == 0) o.df64 = d.df64;
+    if (o.resid_df == 0) o.resid_df = d.resid_df;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {
@@ -211,6 +213,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
   }
   c->device = c->opts.device;
   e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   // The capture stream runs at the highest priority and the side stream (the near field,
   // concurrent with the latency-bound expansion chain) at the lowest, so that the

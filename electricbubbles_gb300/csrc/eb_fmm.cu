@@ -1688,7 +1688,7 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
 template <typename T, int E>
 int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2* dz,
             const double* hpt, const double2* q, double2* out, const EbPost* postp,
-            cudaEvent_t join) {
+            cudaEvent_t join, bool df_req) {
   EbPost post{};
   if (postp) post = *postp;
   cudaStream_t st = eb_stream(ctx);
@@ -1696,7 +1696,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   EbTables& tb = f64 ? ctx->tab64 : ctx->tab32;
   EbFmmWork& w = f64 ? ctx->work64 : ctx->work32;
   const int n = t.n;
-  const bool df = f64 && ctx->opts.df64 > 0;
+  const bool df = f64 && df_req;
   double rleaf = t.W / (double)(1 << t.L);
   if (df) {
     EB_TRY(w.pqdf.ensure(sizeof(float4) * 2 * (size_t)n));
@@ -1828,13 +1828,15 @@ int eb_fmm_apply(eb_ctx* ctx, EbTree& t, int kernel, int sign, int precision,
                  const EbPost* post, cudaEvent_t join) {
   if (!t.valid) return EB_ERR_NOGEOM;
   if (kernel != 0) return EB_ERR_ARG;
-  if (precision == EB_FP64) return fmm_run<double, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join);
-  return fmm_run<float, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join);
+  const bool df = precision == EB_PREC_DF || ctx->opts.df64 > 0;
+  if (precision != EB_FP32) return fmm_run<double, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join, df);
+  return fmm_run<float, 2>(ctx, t, sign, dens, dz, hpt, nullptr, out, post, join, false);
 }
 
 int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q, double2* out,
                         const EbPost* post) {
   if (!t.valid) return EB_ERR_NOGEOM;
-  if (precision == EB_FP64) return fmm_run<double, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr);
-  return fmm_run<float, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr);
+  const bool df = precision == EB_PREC_DF || ctx->opts.df64 > 0;
+  if (precision != EB_FP32) return fmm_run<double, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr, df);
+  return fmm_run<float, 1>(ctx, t, 0, nullptr, nullptr, nullptr, q, out, post, nullptr, false);
 }

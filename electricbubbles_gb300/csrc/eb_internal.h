@@ -17,6 +17,10 @@
 #define EB_NCODE 49
 #define EB_GROUP 8
 #define EB_NTILE 32
+// Internal precision value (beside EB_FP64 and EB_FP32): FP64-class arithmetic in
+// double-float on the FP32 pipes whatever eb_opts.df64 says. The refined solver's FP64
+// residuals use it when eb_opts.resid_df is on.
+#define EB_PREC_DF 2
 
 // ---------------------------------------------------------------------------------
 // Device buffer that grows on demand (never shrinks) and frees itself. Every
@@ -149,6 +153,7 @@ struct GmGraph {
 struct eb_ctx {
   eb_opts opts;
   int device = 0;
+  int nsm = 1;      // streaming multiprocessors of the device
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   long long launches = 0;
@@ -206,6 +211,10 @@ struct eb_ctx {
   GmGraph gcache[EB_GRAPH_CACHE];
   int gcache_next = 0;
 };
+
+// Precision of the refined solver's FP64 residual applies (and of the refined RK stage's
+// other FP64 sums): double-float when eb_opts.resid_df is on, else EB_FP64.
+inline int eb_resid_prec(const eb_ctx* ctx) { return ctx->opts.resid_df > 0 ? EB_PREC_DF : EB_FP64; }
 
 // tree.cu
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target);

@@ -88,15 +88,26 @@ __global__ void __launch_bounds__(kTile) k_noalloc_direct(int n, const double2* 
 }  // namespace
 
 // Set-up: the first call on each device (with that device current) looks up the device
-// address of g_noalloc_charges with cudaGetSymbolAddress and keeps it for later calls;
-// make that first call before capturing any stream into a graph. No call allocates:
-// there is no cudaMalloc, cudaFree or allocating library routine on this path.
+// address of g_noalloc_charges with cudaGetSymbolAddress and keeps it for later calls.
+// Under CUDA's default lazy module loading that lookup is also what loads this
+// library's device code onto the device, which reserves device memory for the code and
+// for the array: make the first call at start-up, outside allocator callbacks and before
+// capturing any stream into a graph. Later calls allocate nothing: there is no
+// cudaMalloc, cudaFree or allocating library routine on this path. The address belongs
+// to the device's primary context (the one the CUDA runtime uses); callers that run
+// their own driver-API contexts or reset the device must not use this entry point.
 // Calls that overlap on the GPU (concurrent streams, or several host threads on one
 // device) share g_noalloc_charges and race; order them on one stream.
 int eb_stokes_sum_noalloc(int n, const double* z, const double* dz, const double* h,
                           const double* dens, int sign, double* gradw, void* stream) {
   if (n <= 0 || !z || !dz || !h || !dens || !gradw || (sign != 1 && sign != -1)) {
     eb_set_last_error_msg("eb_stokes_sum_noalloc: invalid argument");
+    return EB_ERR_ARG;
+  }
+  // complex arrays are read and written as 16-byte double2 values, h as 8-byte doubles
+  if ((reinterpret_cast<uintptr_t>(z) | reinterpret_cast<uintptr_t>(dz) | reinterpret_cast<uintptr_t>(dens) |
+       reinterpret_cast<uintptr_t>(gradw)) & 15u || (reinterpret_cast<uintptr_t>(h) & 7u)) {
+    eb_set_last_error_msg("eb_stokes_sum_noalloc: z, dz, dens, gradw must be 16-byte aligned, h 8-byte aligned");
     return EB_ERR_ARG;
   }
   if (n > EB_NOALLOC_MAX_POINTS) {

@@ -29,7 +29,8 @@ namespace {
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 constexpr int RBS = 256;   // reduction block size
-constexpr int RMAXB = 304; // 2 blocks per SM on 152 SMs
+// Reduction grids: at most two blocks per SM of the context's GPU.
+inline int rmaxb(const eb_ctx* ctx) { return 2 * ctx->nsm; }
 
 __device__ __forceinline__ double block_sum(double v, double* red) {
   v = warp_sum<double>(v);
@@ -618,7 +619,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   EB_CUDA_TRY(cudaGraphCreate(&G.graph, 0));
   cudaGraphConditionalHandle h;
   EB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, G.graph, 0, cudaGraphCondAssignDefault));
-  const int nb = std::min(nblk(n, RBS), RMAXB);
+  const int nb = std::min(nblk(n, RBS), rmaxb(ctx));
   const size_t ldv = (size_t)n;
   double* V = ctx->gV.as<double>();
   double* part = ctx->gPart.as<double>();
@@ -697,7 +698,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
       double* x = ctx->gX.as<double>();
       k_gm_axpy<<<nb, RBS, 0, s>>>(n, ctl, xx, x);
       eb_count_launch(ctx);
-      EB_TRY(op(ctx, x, bb, EB_FP64));
+      EB_TRY(op(ctx, x, bb, eb_resid_prec(ctx)));
       k_resid<<<nb, RBS, 0, s>>>(n, ctx->gR.as<double>(), bb, bb, part, &ctl->rnrm2, ticket);
       eb_count_launch(ctx);
     }
@@ -734,13 +735,24 @@ int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
   if (!G) {
     G = &ctx->gcache[ctx->gcache_next];
     ctx->gcache_next = (ctx->gcache_next + 1) % EB_GRAPH_CACHE;
-    int st = build_graph(ctx, *G, kind, op, n, maxl);
+    // A buffer that grows during the capture moves: nodes captured before the growth
+    // hold its old address, which eb_devbuf_collect later frees. Such a graph is never
+    // kept; it is captured again once every buffer has its final size (a buffer's
+    // first allocation does not move it, so a second capture sees no growth).
+    int st = EB_OK;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+      const unsigned long long e0 = eb_devbuf_epoch();
+      st = build_graph(ctx, *G, kind, op, n, maxl);
+      if (st != EB_OK || eb_devbuf_epoch() == e0) break;
+      G->destroy();
+      st = GM_BUILD_FAILED;
+    }
     if (st != EB_OK) {
       G->destroy();
       cudaGetLastError();
       return GM_BUILD_FAILED;
     }
-    fill_key(eb_devbuf_epoch());  // buffers first allocated during capture stay in place
+    fill_key(eb_devbuf_epoch());
     memcpy(G->key, key, sizeof(key));
   }
   cudaStream_t s = ctx->stream;
@@ -828,13 +840,13 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
 int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mode,
           eb_solve_info* info, int mem) {
   cudaStream_t s = ctx->stream;
-  Gm g{ctx, n, std::min(nblk(n, RBS), RMAXB), s, nullptr};
+  Gm g{ctx, n, std::min(nblk(n, RBS), rmaxb(ctx)), s, nullptr};
   const int maxl = ctx->opts.maxl;
   if (maxl > 126) {
     eb_set_last_error_msg("maxl above 126 is not supported");
     return EB_ERR_WORKSPACE;
   }
-  EB_TRY(ctx->gPart.ensure(sizeof(double) * (size_t)RMAXB * (maxl + 2)));
+  EB_TRY(ctx->gPart.ensure(sizeof(double) * (size_t)rmaxb(ctx) * (maxl + 2)));
   EB_TRY(ctx->gH.ensure(sizeof(double) * std::max(3 * (maxl + 2), (int)GM_HSIZE)));
   EB_TRY(ctx->gTicket.ensure(sizeof(unsigned int)));
   EB_CUDA_TRY(cudaMemsetAsync(ctx->gTicket.p, 0, sizeof(unsigned int), s));
@@ -895,7 +907,7 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
       if (st != EB_OK) break;
       k_axpy<<<g.nb, RBS, 0, s>>>(n, 1.0, d, x);
       eb_count_launch(ctx);
-      EB_TRY(op(ctx, x, r, EB_FP64));
+      EB_TRY(op(ctx, x, r, eb_resid_prec(ctx)));
       inf.matvecs64++;
       double* part = ctx->gPart.as<double>();
       k_resid<<<g.nb, RBS, 0, s>>>(n, b, r, r, part, ctx->gH.as<double>(), g.ticket);

@@ -457,13 +457,9 @@ int eb_pvintev(eb_ctx* ctx, const double* uc, double* phi, int prec, int mem) {
   return EB_OK;
 }
 
-int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, double* dphi_dn,
-                      int prec, int mem) {
-  if (!ctx || !u || !dphi_dn) return EB_ERR_ARG;
-  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
-  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
-  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
-  cudaSetDevice(ctx->device);
+// DIRICH_NEU_MAP with any internal precision (EB_FP64, EB_FP32 or EB_PREC_DF)
+static int dirich_neu_map_impl(eb_ctx* ctx, const double* u, double* phi, double* psi, double* dphi_dn,
+                               int prec, int mem) {
   int nbk = ctx->nbk, nmax;
   EB_TRY(check_pow2(ctx, nmax));
   cudaStream_t s = ctx->stream;
@@ -499,17 +495,19 @@ int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, do
   return EB_OK;
 }
 
-int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
-                          double* flux, int prec, int mem) {
-  if (!ctx || !u || !zc || !un) return EB_ERR_ARG;
+int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, double* dphi_dn,
+                      int prec, int mem) {
+  if (!ctx || !u || !dphi_dn) return EB_ERR_ARG;
   if (!ctx->geom_valid) return EB_ERR_NOGEOM;
-  if (!ctx->ckern_valid) {
-    eb_set_last_error_msg("INTERFACENEW needs ckern: install the geometry with eb_extractdat");
-    return EB_ERR_NOGEOM;
-  }
   if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
   if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
   cudaSetDevice(ctx->device);
+  return dirich_neu_map_impl(ctx, u, phi, psi, dphi_dn, prec, mem);
+}
+
+// INTERFACENEW with any internal precision (EB_FP64, EB_FP32 or EB_PREC_DF)
+static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
+                                   double* flux, int prec, int mem) {
   int nbk = ctx->nbk, k = ctx->k;
   cudaStream_t s = ctx->stream;
   EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
@@ -549,6 +547,20 @@ int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   if (flux) *flux = fl;
   return EB_OK;
+}
+
+int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
+                          double* flux, int prec, int mem) {
+  if (!ctx || !u || !zc || !un) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (!ctx->ckern_valid) {
+    eb_set_last_error_msg("INTERFACENEW needs ckern: install the geometry with eb_extractdat");
+    return EB_ERR_NOGEOM;
+  }
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (prec != EB_FP64 && prec != EB_FP32) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  return interface_velocity_impl(ctx, u, zc, cap, un, flux, prec, mem);
 }
 
 // =================================================================================
@@ -739,15 +751,18 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   k_lap_bc<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->z.as<double2>(), rl);
   eb_count_launch(ctx);
   EB_TRY(eb_laplace_solve(ctx, nbk, rl, ul, m->mode, &li, EB_DEVICE));
-  EB_TRY(eb_dirich_neu_map(ctx, ul, phi, psi, dphi, EB_FP64, EB_DEVICE));
+  // the FP64 sums of the stage outside the solves: plain mode FP64 (native or
+  // double-float as df64 says), refined mode the arithmetic of its FP64 residuals
+  const int p64 = m->mode == EB_SOLVE_FP32_REFINED ? eb_resid_prec(ctx) : EB_FP64;
+  EB_TRY(dirich_neu_map_impl(ctx, ul, phi, psi, dphi, p64, EB_DEVICE));
   EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, ctx->st_rhs.as<double2>()));
   EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
                          EB_DEVICE));
   EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
   double* un = rl;  // the Laplace right-hand side is no longer needed
   double flux = 0.0;
-  EB_TRY(eb_interface_velocity(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, &flux,
-                               EB_FP64, EB_DEVICE));
+  EB_TRY(interface_velocity_impl(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, &flux,
+                                 p64, EB_DEVICE));
   size_t sm2 = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax / 2);
   EB_TRY(set_smem((const void*)k_equit_rkup, sm2));
   k_equit_rkup<<<k, SBS, sm2, s>>>(ctx->start.as<int>(), ctx->tha.as<double>(), un, ctx->dz.as<double2>(),

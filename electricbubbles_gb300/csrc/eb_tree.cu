@@ -374,6 +374,7 @@ void eb_devbuf_collect() {
     v.swap(g_deferred);
   }
   for (void* q : v) cudaFree(q);
+  if (!v.empty()) g_epoch++;  // no cached graph may keep an address freed here
 }
 
 int DevBuf::ensure(size_t nbytes) {
@@ -546,7 +547,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   tb = t.cubtmp.bytes;
   EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), (int)nflag, st));
   eb_count_launch(ctx);
-  k_boxes_all<<<std::min(nblk((long long)nflag, BS), 152 * 16), BS, 0, st>>>(
+  k_boxes_all<<<std::min(nblk((long long)nflag, BS), ctx->nsm * 16), BS, 0, st>>>(
       t.keys.as<unsigned long long>(), n, L, t.flags.as<int>(), t.scan.as<int>(),
       t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.parent.as<int>(), t.child0.as<int>());
   eb_count_launch(ctx);

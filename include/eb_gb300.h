@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define EB_GB300_VERSION 1
+#define EB_GB300_VERSION 2
 
 /* Status codes. The reference prints and STOPs on FMM/GMRES errors
  * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
@@ -69,8 +69,12 @@ typedef struct eb_opts {
   int device;       /* CUDA device ordinal                                     */
   int graphs;       /* GMRES as CUDA graphs with a device-side Arnoldi loop:
                        0 default (on), 1 on, -1 off (host-driven loop)          */
-  int df64;         /* FP64 near field (P2P + L2P) in double-float arithmetic on the
-                       FP32 pipes: 0 default (on), 1 on, -1 off (native FP64)   */
+  int df64;         /* plain FP64 operators in double-float arithmetic on the FP32
+                       pipes (FP64-class, <= 4e-13 from FP64 direct sums):
+                       0 default (off: native FP64 throughout), 1 on, -1 off    */
+  int resid_df;     /* refined mode: the FP64 residual of every refinement step (and
+                       the refined RK stage's PV and velocity sums) in double-float
+                       arithmetic: 0 default (on), 1 on, -1 off (native FP64)   */
 } eb_opts;
 
 typedef struct eb_solve_info {
@@ -182,11 +186,16 @@ int eb_stokes_sum(eb_ctx* ctx, int n, const double* dens, int sign, double* grad
  * no eb_ctx and allocates nothing: it evaluates the sum of eb_stokes_sum (CADAPDR for
  * sign = -1, CADAPMOD for sign = +1, self excluded) by direct FP64 summation for
  * n <= EB_NOALLOC_MAX_POINTS nodes, larger n returns EB_ERR_WORKSPACE. All arrays are
- * device pointers: z, dz, dens, gradw complex (n values), h real (the per-node weight
- * 2 pi / nd of the node's drop). Its scratch is a fixed 768 KiB array in the library's
- * device memory, held by every GPU that loads the library until exit and shared by all
- * calls: calls that overlap on the GPU race, so order them on one stream. The first call
- * on each device looks up that array's address; make it before any stream capture.
+ * device pointers: z, dz, dens, gradw complex (n values, 16-byte aligned), h real (the
+ * per-node weight 2 pi / nd of the node's drop, 8-byte aligned); misaligned pointers
+ * return EB_ERR_ARG. Its scratch is a fixed 768 KiB array in the library's device
+ * memory, held by every GPU that loads the library until exit and shared by all calls:
+ * calls that overlap on the GPU race, so order them on one stream. The first call on
+ * each device looks up that array's address, which under CUDA's lazy module loading
+ * also loads the library's device code (and so reserves device memory): make it at
+ * start-up, outside allocator callbacks and before any stream capture. The address
+ * belongs to the device's primary context, the one the CUDA runtime uses; callers with
+ * their own driver-API contexts, or that reset the device, cannot use this entry point.
  * The work is enqueued on `stream` (a cudaStream_t, NULL = default stream); the result
  * is ready when the stream reaches it. */
 #define EB_NOALLOC_MAX_POINTS 16384

@@ -1,8 +1,8 @@
-"""The FP64 near field in double-float arithmetic (df64, the default) against the native
-FP64 kernels (df64 = -1) and the oracle's FP64 direct sums. Both FMM paths share the
-FP64 far field; their near fields differ by the double-float rounding (about 2^-48 per
-operation against 2^-53), so the results agree within 5e-13 relative to the largest
-value, and both stay within 1e-12 of the direct sum."""
+"""The FP64-class operators in double-float arithmetic (df64 = 1, which the refined
+solver's residuals use) against the native FP64 kernels (df64 = -1, the default plain
+path) and the oracle's FP64 direct sums. The two differ by the double-float rounding
+(about 2^-48 per operation against 2^-53), so the results agree within 5e-13 relative to
+the largest value, and both stay within 1e-12 of the direct sum."""
 import numpy as np
 import pytest
 
