@@ -45,25 +45,31 @@ struct DevBuf {
 // Page-locked host staging for the tree build's small device-to-host reads (so that one
 // stream synchronisation covers several of them).
 struct EbTreeHost {
-  double bbox[4];          // min x, max x, min y, max y
   double sq[4];            // the bounding square: W, x0, y0, 2^20 / W
   int bad;                 // a non-finite coordinate
-  int hist[EB_KEY_LEVELS + 1];
-  int last[6];             // counts and scans of the last leaf or box (groups, tiles, chunks)
-  unsigned long long pairs[2];  // near-field and V-list pair counts
+  int lmax;                // deepest leaf level
+  int hist[EB_KEY_LEVELS + 1];  // boxes per level (heads of existing boxes)
+  int last[12];            // counts and scans of the last leaf or box (work items, lists)
+  unsigned long long pairs[3];  // near-field, V-list and W-list (M2P) pair counts
 };
 
-// Sparse uniform-depth quadtree over a point set, built on the GPU.
-// Boxes of level l are stored in Morton order in the global box range
-// [lev_off[l], lev_off[l+1]); every box owns a contiguous range of the sorted points.
+// Adaptive quadtree over a point set, built on the GPU. A box is split while it holds
+// more than `cap` points (DAASSI's rule, dapif1.f:1165-1255, with NAPB = cap); only
+// boxes whose parent is split exist, so leaves lie on any level up to L. Boxes of level
+// l are stored in Morton order in the global box range [lev_off[l], lev_off[l+1]);
+// every box owns a contiguous range of the sorted points, and the leaves, in point
+// order, partition them.
 struct EbTree {
   int n = 0;
-  int L = 0;                 // leaf level
+  int L = 0;                 // deepest leaf level
+  int cap = 32;              // points per leaf at most (unless at the deepest key level)
   int nbox = 0;
   int nleaf = 0;
+  int lend = 2;              // FP32 far field: levels <= lend hold L2L-accumulated locals
   int lev_off[EB_KEY_LEVELS + 2] = {0};
   double x0 = 0, y0 = 0, W = 1;  // root square [x0, x0+W] x [y0, y0+W]
-  long long v_pairs = 0, u_pairs = 0;  // read from host->pairs when first asked for
+  long long v_pairs = 0, u_pairs = 0, w_pairs = 0;  // read from host->pairs when first asked for
+  long long nu = 0, nw = 0;  // lengths of the U and W lists
   bool pairs_read = false;
   bool valid = false;
   EbTreeHost* host = nullptr;  // page-locked (cudaMallocHost), freed with the tree
@@ -72,29 +78,39 @@ struct EbTree {
   DevBuf perm;     // int[n]: sorted index -> original index
   DevBuf zs;       // double2[n]: sorted positions
   DevBuf zhl;      // float4[n]: sorted positions as float hi + lo, (hi.x, hi.y, lo.x, lo.y)
+  DevBuf plev;     // unsigned char[n]: level of the leaf holding each sorted point
   DevBuf wdf;      // float4[n]: offset from the leaf centre in leaf units, (x.hi, y.hi, x.mid, y.mid)
   DevBuf wdf_lo;   // float2[n]: (x.lo, y.lo) of the same offset
   DevBuf keys, keys_alt, idx_alt;  // sort buffers
+  DevBuf lcpw;     // unsigned char[n]: levels shared by the keys of points w and w + cap
   DevBuf bkey;     // unsigned long long[nbox]: Morton key of the box at its level
+  DevBuf blev;     // unsigned char[nbox]: level of the box
   DevBuf pt0, pt1; // int[nbox]: point range
   DevBuf parent;   // int[nbox]
-  DevBuf child0, nchild;  // int[nbox]
+  DevBuf child0, nchild;  // int[nbox] (nchild = 0: a leaf)
   DevBuf vlist;    // int[nbox*EB_VMAX]
   DevBuf vcode;    // unsigned char[nbox*EB_VMAX]
   DevBuf vcount;   // int[nbox]
+  DevBuf leaves;   // int[nleaf]: box of each leaf, in point order
+  DevBuf lflag, lscan;   // int[n]: leaf heads among the points and their scan
+  // U lists (leaves adjacent to the leaf, on any level: evaluated directly) and W lists
+  // (boxes below an adjacent box of the leaf's level that are not adjacent to the leaf
+  // but whose parent is: evaluated from their multipoles), CSR per leaf
+  DevBuf ucnt, ustart, ulist;
+  DevBuf wcnt, wstart, wlist;
   DevBuf tcount, tstart;  // int[nleaf]: near-field tiles per leaf and their scan
-  DevBuf ulist;    // int[nleaf*EB_UMAX] (global box ids)
-  DevBuf ucount;   // int[nleaf]
   // near-field work items: groups of up to EB_GROUP targets of one leaf
   int ngroup = 0;
-  DevBuf gleaf;    // int[ngroup]: leaf index (0-based within the leaf level)
+  DevBuf gleaf;    // int[ngroup]: leaf index
   DevBuf gfirst;   // int[ngroup]: first sorted target of the group
   // shared-memory near-field work items: tiles of up to EB_NTILE targets of one leaf,
   // a leaf's targets split evenly over its tiles
   int ntile = 0;
-  DevBuf tiles;    // int4[ntile]: (leaf, first, end, 0)
-  DevBuf anc;      // int[nleaf*(L-1)]: each leaf's boxes at levels L, L-1, .., 2 (itself first)
-  DevBuf flags, scan, hist, bbox, partial, cubtmp, pairs;
+  DevBuf tiles;    // int4[ntile]: (leaf index, first, end, 0)
+  // FP32 far field: per leaf its boxes at levels lev(leaf), .., max(2, min(lev(leaf), lend)),
+  // at most EB_FAR_LEVELS of them (the coarsest one holds the accumulated locals above)
+  DevBuf anc;      // int[nleaf*EB_FAR_LEVELS]
+  DevBuf flags, scan, hist, bbox, partial, cubtmp, pairs, ctr;
   // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
   // EB_CHUNK points (coarser levels by M2M)
   int nchunk = 0;
@@ -109,6 +125,7 @@ struct EbTree {
 #define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
 #define EB_FAR_LEVELS 6     // finest levels whose FP32 locals are evaluated at each target
                             // directly (coarser levels reach them by L2L)
+#define EB_LEAF_CAP 32      // default maximum points per leaf
 
 // Per-precision constant tables for the translation operators.
 struct EbTables {
@@ -217,7 +234,7 @@ struct eb_ctx {
 inline int eb_resid_prec(const eb_ctx* ctx) { return ctx->opts.resid_df > 0 ? EB_PREC_DF : EB_FP64; }
 
 // tree.cu
-int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target);
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_cap);
 // The tree's pair counts (u_pairs, v_pairs), waiting for the build if it is in flight.
 int eb_tree_pairs(eb_ctx* ctx, EbTree& t);
 
