@@ -51,7 +51,7 @@ class SolveInfo(ctypes.Structure):
 class TreeInfo(ctypes.Structure):
     _fields_ = [("npoints", ctypes.c_int), ("levels", ctypes.c_int), ("nboxes", ctypes.c_int),
                 ("nleaves", ctypes.c_int), ("v_pairs", ctypes.c_longlong),
-                ("u_pairs", ctypes.c_longlong), ("p", ctypes.c_int)]
+                ("u_pairs", ctypes.c_longlong), ("p", ctypes.c_int), ("w_pairs", ctypes.c_longlong)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

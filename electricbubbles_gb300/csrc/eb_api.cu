@@ -307,6 +307,7 @@ int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info) {
   EB_TRY(eb_tree_pairs(ctx, ctx->tree));
   info->v_pairs = ctx->tree.v_pairs;
   info->u_pairs = ctx->tree.u_pairs;
+  info->w_pairs = ctx->tree.w_pairs;
   info->p = ctx->last_p;
   return EB_OK;
 }
@@ -374,7 +375,8 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
       const unsigned char* c = static_cast<const unsigned char*>(p);
       for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
     };
-    const int ints[] = {t.n, ctx->nbk, ctx->k, t.L, t.nbox, t.nleaf, t.ngroup, t.ntile, t.nchunk, t.chunk_lmin};
+    const int ints[] = {t.n, ctx->nbk, ctx->k, t.L, t.nbox, t.nleaf, t.ngroup, t.ntile, t.nchunk, t.chunk_lmin,
+                        t.lend, t.cap, (int)t.nu, (int)t.nw};
     mix(ints, sizeof(ints));
     mix(t.lev_off, sizeof(int) * (size_t)(t.L + 2));
     const double dbl[] = {t.W, t.x0, t.y0};

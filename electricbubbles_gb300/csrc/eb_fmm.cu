@@ -86,15 +86,16 @@ __device__ __forceinline__ float4 df4(double2 v) {
   return make_float4(hx, __double2float_rn(v.x - (double)hx), hy, __double2float_rn(v.y - (double)hy));
 }
 
-// FP64 charges plus the double-float near-field data P, Q, A scaled by 1/r_leaf (the
-// near field works in leaf units).
+// FP64 charges plus the double-float near-field data P, Q, A scaled by 1/r_leaf, the
+// side of the point's own leaf (the near field works in leaf units): 2^lev / W.
 __global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const double2* __restrict__ dens,
                                     const double2* __restrict__ dz, const double* __restrict__ hpt,
-                                    double s, double rinv, float4* __restrict__ qdf,
-                                    float4* __restrict__ pq, float4* __restrict__ aa) {
+                                    double s, double winv, const unsigned char* __restrict__ plev,
+                                    float4* __restrict__ qdf, float4* __restrict__ pq, float4* __restrict__ aa) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int o = perm[i];
+  const double rinv = ldexp(winv, (int)plev[i]);
   double2 u = dens[o], d = dz[o];
   double h = hpt[o] * (1.0 / (2.0 * EB_PI));
   double2 w = cmul<double>(u, d);
@@ -119,10 +120,11 @@ __device__ __forceinline__ double2 cauchy_charge(int o, const double2* q, const 
 
 __global__ void k_charges_cauchy_df(int n, const int* __restrict__ perm, const double2* __restrict__ q,
                                     const double* __restrict__ lu, const double2* __restrict__ dz,
-                                    const double* __restrict__ hpt, double rinv,
-                                    float4* __restrict__ qdf) {
+                                    const double* __restrict__ hpt, double winv,
+                                    const unsigned char* __restrict__ plev, float4* __restrict__ qdf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double rinv = ldexp(winv, (int)plev[i]);
   double2 v = cauchy_charge(perm[i], q, lu, dz, hpt);
   qdf[i] = df4(make_double2(v.x * rinv, v.y * rinv));
 }
@@ -169,24 +171,27 @@ __device__ __forceinline__ c_t<T> cpow_int(c_t<T> u, int n) {
 
 // ---------------------------------------------------------------------------------
 // P2M at the leaves (SLMKXP, cadap2.f:412-468, with scaled coefficients and psi
-// relative to the box centre). One block per leaf: the leaf's points (32 at a time)
+// relative to the box centre). One block per leaf (of any level): the leaf's points (32 at a time)
 // write their powers w^j to shared memory, then thread j forms the power sums
 //   A_j = sum a w^j,  B_j = sum b w^j,  C_j = sum conj(w) a w^j   (a = qa/r, b = qb/r)
 // and M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 // ---------------------------------------------------------------------------------
 template <typename T, int E>
-__global__ void __launch_bounds__(64) k_p2m(int off, const unsigned long long* __restrict__ bkey,
+__global__ void __launch_bounds__(64) k_p2m(const int* __restrict__ leaves,
+                                            const unsigned long long* __restrict__ bkey,
+                                            const unsigned char* __restrict__ blev,
                                             const int* __restrict__ pt0, const int* __restrict__ pt1,
                                             const double2* __restrict__ zs,
                                             const c_t<T>* __restrict__ qa,
                                             const c_t<T>* __restrict__ qb, double x0, double y0,
-                                            double r, int p, c_t<T>* __restrict__ mpole) {
+                                            double W, int p, c_t<T>* __restrict__ mpole) {
   extern __shared__ unsigned char smem_raw[];
   const int ps = p + 1;  // odd row stride: conflict-free rows
   c_t<T>* pw = reinterpret_cast<c_t<T>*>(smem_raw);
   c_t<T>* sc = pw + 32 * ps;
-  int b = off + blockIdx.x;
+  const int b = leaves[blockIdx.x];
   int tid = threadIdx.x;
+  const double r = ldexp(W, -(int)blev[b]);
   double2 c = box_center(bkey[b], x0, y0, r);
   const T rinv = (T)(1.0 / r);
   c_t<T> A = cmk<T>(0, 0), B = cmk<T>(0, 0), C = cmk<T>(0, 0);
@@ -254,6 +259,7 @@ __global__ void k_m2m(int offp, const unsigned long long* __restrict__ bkey,
   const bool active = tid < nout;
   c_t<T> acc = cmk<T>(0, 0);
   int c0 = child0[P], nc = nchild[P];
+  if (nc == 0) return;  // a leaf: its multipole comes from its points
   for (int ci = 0; ci < nc; ++ci) {
     int c = c0 + ci;
     int q = quadrant(bkey[c]);
@@ -641,7 +647,7 @@ __device__ __forceinline__ cdf cacc_value(const dfacc& rx, const dfacc& ry) {
 // P2M at the leaves from the leaf-relative offsets w (units of the leaf side) and the
 // charges qa/r, qb/r: M_phi[k] = -A_{k-1}, M_psi[k] = -(B_{k-1} + (k-1) C_{k-2}).
 template <int E>
-__global__ void k_p2m_df(int off, const int* __restrict__ pt0, const int* __restrict__ pt1,
+__global__ void k_p2m_df(const int* __restrict__ leaves, const int* __restrict__ pt0, const int* __restrict__ pt1,
                          const float4* __restrict__ wa, const float4* __restrict__ q, int p,
                          float4* __restrict__ mpole) {
   // thread (which, k) < NA p sums one of A_k, B_k, C_k over the leaf's points
@@ -650,7 +656,7 @@ __global__ void k_p2m_df(int off, const int* __restrict__ pt0, const int* __rest
   const int ps = p + 1;
   float4* pw = sm4;
   float4* sc = pw + 32 * ps;
-  const int b = off + blockIdx.x, tid = threadIdx.x;
+  const int b = leaves[blockIdx.x], tid = threadIdx.x;
   const int which = tid / p, kq = tid - which * p;
   const bool acc_thread = which < NA;
   dfacc Rx{0.f, 0.f}, Ry{0.f, 0.f};
@@ -729,6 +735,7 @@ __global__ void k_m2m_df(int offp, const unsigned long long* __restrict__ bkey,
   float4* a = sm4;  // [child][E*p]
   const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
   const int c0 = child0[P], nc = nchild[P];
+  if (nc == 0) return;  // a leaf: its multipole comes from its points
   for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
     const int ci = idx / nout, o = idx - ci * nout;
     const int c = c0 + ci, q = quadrant(bkey[c]);
@@ -814,7 +821,8 @@ __global__ void k_l2l_df(int offc, const unsigned long long* __restrict__ bkey,
 // cadap2.f:412-468, scaled by the box side and relative to the box centre), and the
 // last chunk of a box to finish adds the chunks of the box in order. The offset of a point from an ancestor's centre in the
 // ancestor's units is u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2 from its leaf offset
-// u and leaf grid index i, exact apart from the rounding of u.
+// u and leaf grid index i (sh levels between the point's leaf and the box), exact apart
+// from the rounding of u.
 // ---------------------------------------------------------------------------------
 struct LevOff {
   int v[EB_KEY_LEVELS + 2];
@@ -822,7 +830,8 @@ struct LevOff {
 };
 
 template <int E>
-__global__ void __launch_bounds__(128) k_p2m_chunks(int L, int lmin, LevOff lo, int first2,
+__global__ void __launch_bounds__(128) k_p2m_chunks(LevOff lo, int first2, const unsigned char* __restrict__ blev,
+                                                    const unsigned char* __restrict__ plev,
                                                     const int* __restrict__ chunk_box,
                                                     const int* __restrict__ cstart,
                                                     const unsigned long long* __restrict__ keys,
@@ -842,21 +851,19 @@ __global__ void __launch_bounds__(128) k_p2m_chunks(int L, int lmin, LevOff lo, 
   __shared__ int s_last;
   const int c = blockIdx.x, tid = threadIdx.x;
   const int b = chunk_box[c];
-  int l = lmin;
-  while (l < L && b >= lo.v[l + 1]) ++l;
-  const int sh = L - l;
-  const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
+  const int l = blev[b];
   const float rinv = lo.rinv[l];
   const int bb = b - first2, c0 = cstart[bb], nc = cstart[bb + 1] - c0;
   const int i0 = pt0[b] + (c - c0) * EB_CHUNK;
   const int cnt = min(pt1[b], i0 + EB_CHUNK) - i0;
-  const int lshift = 2 * (EB_KEY_LEVELS - L);
   {
     // two threads per point: even and odd powers
     const int sp = tid >> 1, h = tid & 1;
     if (sp < cnt) {
       const int i = i0 + sp;
-      const unsigned long long kl = keys[i] >> lshift;
+      const int lam = plev[i], sh = lam - l;
+      const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
+      const unsigned long long kl = keys[i] >> (2 * (EB_KEY_LEVELS - lam));
       const unsigned int ix = compact2d(kl), iy = compact2d(kl >> 1);
       const float4 wv = wa[i];
       const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
@@ -930,6 +937,7 @@ __global__ void k_m2m_f32(int offp, const unsigned long long* __restrict__ bkey,
   float2* a = sm2;
   const int P = offp + blockIdx.x, tid = threadIdx.x, ld = p + 2, nout = E * p;
   const int c0 = child0[P], nc = nchild[P];
+  if (nc == 0) return;  // a leaf: its multipole comes from its points
   for (int idx = tid; idx < nc * nout; idx += blockDim.x) {
     const int ci = idx / nout, o = idx - ci * nout;
     const int c = c0 + ci, q = quadrant(bkey[c]);
@@ -1013,38 +1021,79 @@ __device__ __forceinline__ void l2p_part(const c_t<T>* lb, int p, int sl, c_t<T>
   l2p_range<T, E>(lb, p, m0, m1, u, s, gx, gy);
 }
 
+// M2P: the far field at u (the target's offset from the box centre in box units) of a
+// box's multipole expansions M (phi at M[0, p), psi relative to the centre at M[p, 2p),
+// coefficient k at index k - 1): phi = sum_k M_k u^-k, and GW += phi + s (u conj(phi_u) +
+// conj(psi)) for Stokes, F -= phi for Cauchy. The evaluation of SLMVALDR
+// (cadapdrop2.f:251-301) and DSLOR1 (dapif3.f:1724-1749), used for the W lists.
+template <typename T, int E>
+__device__ __forceinline__ void m2p_eval(const c_t<T>* M, int p, c_t<T> u, T s, T& gx, T& gy) {
+  const c_t<T> v = cinv<T>(u);
+  c_t<T> a = M[p - 1];
+  c_t<T> da = cscale<T>(M[p - 1], (T)p);
+  for (int k = p - 1; k >= 1; --k) {
+    a = cadd<T>(cmul<T>(a, v), M[k - 1]);
+    if (E == 2) da = cadd<T>(cmul<T>(da, v), cscale<T>(M[k - 1], (T)k));
+  }
+  const c_t<T> ph = cmul<T>(a, v);  // sum M_k v^k
+  if (E == 2) {
+    const c_t<T> dph = cmul<T>(da, cmul<T>(v, v));  // sum k M_k v^(k+1) = -phi_u
+    c_t<T> b = M[2 * p - 1];
+    for (int k = p - 1; k >= 1; --k) b = cadd<T>(cmul<T>(b, v), M[p + k - 1]);
+    const c_t<T> ps = cmul<T>(b, v);
+    const c_t<T> t = cmulc<T>(u, dph);  // -u conj(phi_u)
+    gx += ph.x + s * (ps.x - t.x);
+    gy += ph.y - s * (ps.y + t.y);
+  } else {
+    gx -= ph.x;
+    gy -= ph.y;
+  }
+}
+
 template <int E>
 __global__ void __launch_bounds__(128) k_leaf64(int ngroup, const int* __restrict__ gleaf,
-                                                const int* __restrict__ gfirst, int off, int has_far,
-                                                const unsigned long long* __restrict__ bkey,
+                                                const int* __restrict__ gfirst, const int* __restrict__ leaves,
+                                                int has_far, const unsigned long long* __restrict__ bkey,
+                                                const unsigned char* __restrict__ blev,
                                                 const int* __restrict__ pt0, const int* __restrict__ pt1,
-                                                const int* __restrict__ ulist,
-                                                const int* __restrict__ ucount,
+                                                const int* __restrict__ ustart, const int* __restrict__ ulist,
+                                                const int* __restrict__ wstart, const int* __restrict__ wlist,
                                                 const int* __restrict__ perm,
                                                 const double2* __restrict__ zs,
                                                 const double2* __restrict__ pq,
                                                 const double2* __restrict__ aa,
                                                 const double2* __restrict__ qa, double x0, double y0,
-                                                double r, int p, double s,
+                                                double W, int p, double s,
                                                 const double2* __restrict__ local,
+                                                const double2* __restrict__ mpole,
                                                 double2* __restrict__ out, EbPost post) {
   int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
-  const int leaf = gleaf[g], b = off + leaf;
+  const int leaf = gleaf[g], b = leaves[leaf];
   const int i = gfirst[g] + tg;
   const bool act = i < pt1[b];
   const int ii = act ? i : gfirst[g];
   const double2 zi = zs[ii];
   double gx = 0.0, gy = 0.0;
-  if (has_far) {
+  if (has_far && blev[b] >= 2) {
+    const double r = ldexp(W, -(int)blev[b]);
     double2 c = box_center(bkey[b], x0, y0, r);
     double2 u = make_double2((zi.x - c.x) / r, (zi.y - c.y) / r);
     l2p_part<double, E>(local + (size_t)b * E * (p + 1), p, sl, u, s, gx, gy);
   }
-  const int nu = ucount[leaf];
-  for (int jl = 0; jl < nu; ++jl) {
-    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
+  if (has_far) {
+    // W list: the lanes of a target take every 4th box
+    for (int jw = wstart[leaf] + sl; jw < wstart[leaf + 1]; jw += 4) {
+      const int w = wlist[jw];
+      const double rw = ldexp(W, -(int)blev[w]);
+      const double2 cw = box_center(bkey[w], x0, y0, rw);
+      m2p_eval<double, E>(mpole + (size_t)w * E * p, p, make_double2((zi.x - cw.x) / rw, (zi.y - cw.y) / rw),
+                          s, gx, gy);
+    }
+  }
+  for (int jl = ustart[leaf]; jl < ustart[leaf + 1]; ++jl) {
+    const int sb = ulist[jl];
     const int j1 = pt1[sb];
     for (int j = pt0[sb] + sl; j < j1; j += 4) {
       if (j == ii) continue;
@@ -1151,16 +1200,86 @@ __device__ __forceinline__ void l2p_part_df(const float4* L, int p, int sl, cdf 
   }
 }
 
+// Offset between the centres of a box of level lt (grid index it) and a box of level
+// ls = lt + ds (index is), in units of the second box's side: (c_t - c_s) / r_s =
+// ((2 it + 1) 2^ds - (2 is + 1)) / 2, formed in integers and exact in float for boxes
+// that touch or nearly touch.
+__device__ __forceinline__ float box_delta(int it, int is, int ds) {
+  long long num;
+  int e;
+  if (ds >= 0) {
+    num = ((2LL * it + 1) << ds) - (2LL * is + 1);
+    e = -1;
+  } else {
+    num = (2LL * it + 1) - ((2LL * is + 1) << (-ds));
+    e = ds - 1;
+  }
+  return ldexpf((float)num, e);
+}
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+
+// A target's position relative to the centre of a box ds levels below (ds < 0: above)
+// its leaf, in that box's units, as three floats: w 2^ds + (c_leaf - c_box) / r_box.
+__device__ __forceinline__ void frame_shift(float4 wa, float2 wb, int ds, int bx, int by, int sx, int sy,
+                                            float3& tx, float3& ty) {
+  const float f = pow2f(ds);
+  tx = tf_shift(wa.x * f, wa.z * f, wb.x * f, -box_delta(bx, sx, ds));
+  ty = tf_shift(wa.y * f, wa.w * f, wb.y * f, -box_delta(by, sy, ds));
+}
+
+__device__ __forceinline__ dfl tf_to_dfl(float3 t) {
+  return dfl_add(two_sum(t.x, t.y), dfl{t.z, 0.f});
+}
+
+// M2P in double-float (m2p_eval's sums): M the box's double-float multipoles, u the
+// target's offset in box units.
+template <int E>
+__device__ __forceinline__ void m2p_df(const float4* M, int p, cdf u, bool neg, dfacc& gx, dfacc& gy) {
+  const dfl rr = dfl_rcp(dfl_add(dfl_sqr(u.x), dfl_sqr(u.y)));
+  const cdf v = cdf{dfl_mul(u.x, rr), dfl_neg(dfl_mul(u.y, rr))};
+  cdf a = cdf_from_float4(M[p - 1]);
+  cdf da = cdf_scale(a, (float)p);
+  for (int k = p - 1; k >= 1; --k) {
+    const cdf mk = cdf_from_float4(M[k - 1]);
+    a = cdf_add(cdf_mul(a, v), mk);
+    if (E == 2) da = cdf_add(cdf_mul(da, v), cdf_scale(mk, (float)k));
+  }
+  const cdf ph = cdf_mul(a, v);
+  if (E == 2) {
+    const cdf dph = cdf_mul(da, cdf_mul(v, v));  // -phi_u
+    cdf b = cdf_from_float4(M[2 * p - 1]);
+    for (int k = p - 1; k >= 1; --k) b = cdf_add(cdf_mul(b, v), cdf_from_float4(M[p + k - 1]));
+    const cdf ps = cdf_mul(b, v);
+    const dfl tx = dfl_add(dfl_mul(u.x, dph.x), dfl_mul(u.y, dph.y));  // -u conj(phi_u)
+    const dfl ty = dfl_sub(dfl_mul(u.y, dph.x), dfl_mul(u.x, dph.y));
+    dfl sx = dfl_sub(ps.x, tx), sy = dfl_neg(dfl_add(ps.y, ty));
+    if (neg) {
+      sx = dfl_neg(sx);
+      sy = dfl_neg(sy);
+    }
+    acc_dfl(gx, ph.x);
+    acc_dfl(gx, sx);
+    acc_dfl(gy, ph.y);
+    acc_dfl(gy, sy);
+  } else {
+    acc_dfl(gx, dfl_neg(ph.x));
+    acc_dfl(gy, dfl_neg(ph.y));
+  }
+}
+
 // MODE 0: far and near field; 1: near field only, into nearbuf (sorted order);
 // 2: far field only, plus nearbuf, then the post-processing. Modes 1 and 2 let the near
 // field run concurrently with the expansion passes.
 template <int E, int MODE>
 __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restrict__ gleaf,
-                                                 const int* __restrict__ gfirst, int off, int has_far,
-                                                 const unsigned long long* __restrict__ bkey,
+                                                 const int* __restrict__ gfirst, const int* __restrict__ leaves,
+                                                 int has_far, const unsigned long long* __restrict__ bkey,
+                                                 const unsigned char* __restrict__ blev,
                                                  const int* __restrict__ pt0, const int* __restrict__ pt1,
-                                                 const int* __restrict__ ulist,
-                                                 const int* __restrict__ ucount,
+                                                 const int* __restrict__ ustart, const int* __restrict__ ulist,
+                                                 const int* __restrict__ wstart, const int* __restrict__ wlist,
+                                                 const float4* __restrict__ mpole,
                                                  const int* __restrict__ perm,
                                                  const float4* __restrict__ wa,
                                                  const float2* __restrict__ wb,
@@ -1172,7 +1291,7 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (g >= ngroup) return;
   const int lane = threadIdx.x & 31, tg = lane >> 2, sl = lane & 3;
-  const int leaf = gleaf[g], b = off + leaf;
+  const int leaf = gleaf[g], b = leaves[leaf];
   const int i = gfirst[g] + tg;
   const bool act = i < pt1[b];
   const int ii = act ? i : gfirst[g];
@@ -1180,17 +1299,29 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   const float2 wib = wb[ii];
   const cdf wi = cdf{{wia.x, wia.z}, {wia.y, wia.w}};
   const bool neg = s < 0.0;
+  const int lt = blev[b];
   dfacc gx{0.f, 0.f}, gy{0.f, 0.f};
-  if (MODE != 1 && has_far) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
+  if (MODE != 1 && has_far && lt >= 2) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
   const unsigned long long kb = bkey[b];
   const int bx = (int)compact2d(kb), by = (int)compact2d(kb >> 1);
-  const int nu = MODE == 2 ? 0 : ucount[leaf];
-  for (int jl = 0; jl < nu; ++jl) {
-    const int sb = ulist[(size_t)leaf * EB_UMAX + jl];
+  if (MODE != 1 && has_far) {
+    // W list: the lanes of a target take every 4th box
+    for (int jw = wstart[leaf] + sl; jw < wstart[leaf + 1]; jw += 4) {
+      const int w = wlist[jw];
+      const unsigned long long kw = bkey[w];
+      float3 tx, ty;
+      frame_shift(wia, wib, blev[w] - lt, bx, by, (int)compact2d(kw), (int)compact2d(kw >> 1), tx, ty);
+      m2p_df<E>(mpole + (size_t)w * E * p, p, cdf{tf_to_dfl(tx), tf_to_dfl(ty)}, neg, gx, gy);
+    }
+  }
+  const int u0 = ustart[leaf], u1 = MODE == 2 ? u0 : ustart[leaf + 1];
+  for (int jl = u0; jl < u1; ++jl) {
+    const int sb = ulist[jl];
     const unsigned long long ks = bkey[sb];
-    // the target relative to the source leaf's centre, in leaf units (three floats)
-    const float3 tx = tf_shift(wia.x, wia.z, wib.x, (float)((int)compact2d(ks) - bx));
-    const float3 ty = tf_shift(wia.y, wia.w, wib.y, (float)((int)compact2d(ks >> 1) - by));
+    // the target relative to the source leaf's centre, in that leaf's units (three
+    // floats); the source charges carry the factor 1 / r of their own leaf
+    float3 tx, ty;
+    frame_shift(wia, wib, blev[sb] - lt, bx, by, (int)compact2d(ks), (int)compact2d(ks >> 1), tx, ty);
     const int j1 = pt1[sb];
     for (int j = pt0[sb] + sl; j < j1; j += 4) {
       if (j == ii) continue;
@@ -1256,50 +1387,69 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 }
 
 // FP32 far field, one block per tile of the near field: the local expansions of the
-// leaf and of its nlev - 1 nearest ancestors are staged in shared memory, and each
-// expansion is evaluated directly about its own centre at every target (the sum equals
-// L2P of the L2L-accumulated leaf expansion; levels above these reach the coarsest of
-// them by L2L). Thread slice sl of 128 / EB_NTILE takes every slice-th level. Adds the
-// near-field sums of k_near32 and applies the post-processing.
+// leaf and of its nearest ancestors (at most EB_FAR_LEVELS boxes, the coarsest holding
+// the L2L-accumulated expansion of the levels above) are staged in shared memory, and
+// each expansion is evaluated directly about its own centre at every target (the sum
+// equals L2P of the L2L-accumulated leaf expansion). Thread slice sl of 128 / EB_NTILE
+// takes every slice-th level, and every slice-th box of the leaf's W list, whose
+// multipoles are evaluated at the targets (M2P). Adds the near-field sums of k_near32
+// and applies the post-processing.
 template <int E>
-__global__ void __launch_bounds__(128) k_far32(const int4* __restrict__ tiles, int off, int nlev, int nanc,
+__global__ void __launch_bounds__(128) k_far32(const int4* __restrict__ tiles, const int* __restrict__ leaves,
                                                const unsigned long long* __restrict__ bkey,
-                                               const int* __restrict__ anc,
+                                               const unsigned char* __restrict__ blev,
+                                               const int* __restrict__ anc, const int* __restrict__ wstart,
+                                               const int* __restrict__ wlist,
                                                const int* __restrict__ perm,
                                                const float4* __restrict__ wa, int p, float s,
                                                const float2* __restrict__ local,
+                                               const float2* __restrict__ mpole,
                                                double2* __restrict__ out, EbPost post,
                                                const double2* __restrict__ nearbuf) {
   constexpr int T = EB_NTILE, NS = 128 / T;
-  extern __shared__ float2 sloc[];  // [nlev][E][p + 1]
+  extern __shared__ float2 sloc[];  // [nf][E][p + 1]
   __shared__ float2 sred[NS][T];
   const int4 tl = tiles[blockIdx.x];
-  const int leaf = tl.x, b = off + leaf;
+  const int leaf = tl.x, b = leaves[leaf];
   const int tid = threadIdx.x, tt = tid % T, sl = tid / T;
   const int i = tl.y + tt;
   const bool act = i < tl.z;
   const int ii = act ? i : tl.y;
   const int ldl = p + 1, nco = E * ldl;
-  for (int idx = tid; idx < nlev * nco; idx += 128) {
+  const int* fb = anc + (size_t)leaf * EB_FAR_LEVELS;
+  int nf = 0;
+  while (nf < EB_FAR_LEVELS && fb[nf] >= 0) ++nf;
+  for (int idx = tid; idx < nf * nco; idx += 128) {
     const int q = idx / nco, o = idx - q * nco;
-    sloc[idx] = local[(size_t)anc[(size_t)leaf * nanc + q] * nco + o];
+    sloc[idx] = local[(size_t)fb[q] * nco + o];
   }
   __syncthreads();
   float fx = 0.f, fy = 0.f;
-  if (nlev > 0) {
-    // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
-    //   u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2   (i the leaf's grid index),
-    // whose constant part is exact in FP32 (i < 2^20).
-    const unsigned long long kb = bkey[b];
-    const unsigned int ix = compact2d(kb), iy = compact2d(kb >> 1);
-    const float4 wv = wa[ii];
-    for (int sh = sl; sh < nlev; sh += NS) {
-      const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
-      const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
-      const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
-      const float2 u = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
-      l2p_range<float, E>(sloc + sh * nco, p, 0, ldl, u, s, fx, fy);
-    }
+  const unsigned long long kb = bkey[b];
+  const unsigned int ix = compact2d(kb), iy = compact2d(kb >> 1);
+  const float4 wv = wa[ii];
+  // With u the leaf-scaled offset, the offset scaled to the ancestor sh levels up is
+  //   u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2   (i the leaf's grid index),
+  // whose constant part is exact in FP32 (i < 2^20).
+  for (int sh = sl; sh < nf; sh += NS) {
+    const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
+    const float gx = fmaf((float)ix + 0.5f, f, -((float)(ix >> sh) + 0.5f));
+    const float gy = fmaf((float)iy + 0.5f, f, -((float)(iy >> sh) + 0.5f));
+    const float2 u = make_float2(fmaf(wv.x, f, gx), fmaf(wv.y, f, gy));
+    l2p_range<float, E>(sloc + sh * nco, p, 0, ldl, u, s, fx, fy);
+  }
+  // W list (boxes below the leaf's level): the target's offset in the box's units is
+  // u 2^ds + (c_leaf - c_box) / r_box, the high part of u first, so that the cancelling
+  // terms meet exactly, then the middle part
+  const int lt = blev[b];
+  for (int jw = wstart[leaf] + sl; jw < wstart[leaf + 1]; jw += NS) {
+    const int w = wlist[jw];
+    const unsigned long long kw = bkey[w];
+    const int ds = blev[w] - lt;
+    const float f = pow2f(ds);
+    const float dx = box_delta((int)ix, (int)compact2d(kw), ds), dy = box_delta((int)iy, (int)compact2d(kw >> 1), ds);
+    const float2 u = make_float2(fmaf(wv.z, f, fmaf(wv.x, f, dx)), fmaf(wv.w, f, fmaf(wv.y, f, dy)));
+    m2p_eval<float, E>(mpole + (size_t)w * E * p, p, u, s, fx, fy);
   }
   sred[sl][tt] = make_float2(fx, fy);
   __syncthreads();
@@ -1316,16 +1466,17 @@ __global__ void __launch_bounds__(128) k_far32(const int4* __restrict__ tiles, i
 }
 
 // FP32 near field, one block per tile of up to EB_NTILE targets of one leaf: the sources
-// of the leaf's U list are staged through shared memory in slabs of NEAR_SLAB, and each
-// of the 128 / EB_NTILE warps sums one slice of every slab for all targets of the tile
-// (a shared-memory broadcast per source). Per-thread Kahan-compensated sums; the slices
-// are added in a fixed order. Writes the near-field sums in sorted order.
+// of the leaf's U list (32 boxes at a time) are staged through shared memory in slabs of
+// NEAR_SLAB, and each of the 128 / EB_NTILE warps sums one slice of every slab for all
+// targets of the tile (a shared-memory broadcast per source). Per-thread
+// Kahan-compensated sums; the slices are added in a fixed order. Writes the near-field
+// sums in sorted order. Positions are absolute (float hi + lo), so sources of any level
+// are alike.
 #define NEAR_SLAB 256
 template <int E>
-__global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tiles, int off,
+__global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tiles, const int* __restrict__ leaves,
                                                    const int* __restrict__ pt0, const int* __restrict__ pt1,
-                                                   const int* __restrict__ ulist,
-                                                   const int* __restrict__ ucount,
+                                                   const int* __restrict__ ustart, const int* __restrict__ ulist,
                                                    const float4* __restrict__ zhl,
                                                    const float2* __restrict__ pq,
                                                    const float2* __restrict__ aa,
@@ -1335,85 +1486,86 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
   __shared__ float4 sz[NEAR_SLAB];
   __shared__ float4 sp[E == 2 ? NEAR_SLAB : 1];
   __shared__ float2 sa[NEAR_SLAB];
-  __shared__ int spre[EB_UMAX + 1], sj0[EB_UMAX], sself;
+  __shared__ int spre[33], sj0[32], sself;
   __shared__ float2 sred[NS][T];
   const int4 tl = tiles[blockIdx.x];
-  const int leaf = tl.x, b = off + leaf;
+  const int leaf = tl.x, b = leaves[leaf];
   const int tid = threadIdx.x, tt = tid % T, sl = tid / T;
   const int i = tl.y + tt;
   const bool act = i < tl.z;
   const int ii = act ? i : tl.y;
-  if (tid < 32) {
-    const int nu = ucount[leaf];
-    int c = 0, j0 = 0, sb = -1;
-    if (tid < nu) {
-      sb = ulist[(size_t)leaf * EB_UMAX + tid];
-      j0 = pt0[sb];
-      c = pt1[sb] - j0;
-    }
-    int x = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (tid >= o) x += y;
-    }
-    if (tid < EB_UMAX) {
-      sj0[tid] = j0;
-      spre[tid + 1] = x;
-    }
-    if (tid == 0) spre[0] = 0;
-    const unsigned int m = __ballot_sync(0xffffffffu, sb == b);
-    if (tid == 0) sself = __ffs(m) - 1;
-  }
-  __syncthreads();
-  const int total = spre[EB_UMAX];
-  const int ks = sself;
-  // staged position of the target itself (its own leaf is in its U list)
-  const int selfpos = ks >= 0 ? spre[ks] + (ii - sj0[ks]) : -1;
   const float4 hl = zhl[ii];
   float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
-  for (int base = 0; base < total; base += NEAR_SLAB) {
-    const int ns = min(NEAR_SLAB, total - base);
-    if (base > 0) __syncthreads();
-    for (int s2 = tid; s2 < ns; s2 += 128) {
-      const int gs = base + s2;
-      int k = 0;
-#pragma unroll
-      for (int q = 1; q < EB_UMAX; ++q) k += gs >= spre[q];
-      const int j = sj0[k] + gs - spre[k];
-      sz[s2] = zhl[j];
-      if (E == 2) {
-        sp[s2] = reinterpret_cast<const float4*>(pq)[j];
-        sa[s2] = aa[j];
-      } else {
-        sa[s2] = qa[j];
+  const int ub = ustart[leaf], ue = ustart[leaf + 1];
+  for (int cb = ub; cb < ue; cb += 32) {
+    const int nc = min(32, ue - cb);
+    if (cb > ub) __syncthreads();  // the previous boxes' slabs are consumed
+    if (tid < 32) {
+      int c = 0, j0 = 0, sbx = -1;
+      if (tid < nc) {
+        sbx = ulist[cb + tid];
+        j0 = pt0[sbx];
+        c = pt1[sbx] - j0;
       }
+      int x = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (tid >= o) x += y;
+      }
+      sj0[tid] = j0;
+      spre[tid + 1] = x;
+      if (tid == 0) spre[0] = 0;
+      const unsigned int m = __ballot_sync(0xffffffffu, sbx == b);
+      if (tid == 0) sself = __ffs(m) - 1;
     }
     __syncthreads();
-    const int sp0 = selfpos - base;
-#pragma unroll 4
-    for (int jj = sl; jj < ns; jj += NS) {
-      const float4 hlj = sz[jj];
-      const float dx = (hlj.x - hl.x) + (hlj.z - hl.z);
-      const float dy = (hlj.y - hl.y) + (hlj.w - hl.w);
-      float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
-      rr = jj == sp0 ? 0.f : rr;  // the self pair (dx = dy = 0) contributes nothing
-      const float ix = dx * rr, iy = -dy * rr;
-      float tx_, ty_;
-      if (E == 2) {
-        const float4 PQ = sp[jj];
-        const float2 A = sa[jj];
-        const float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
-        const float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
-        tx_ = fmaf(PQ.x, ix, fmaf(-PQ.y, iy, fmaf(A.x, tx, -A.y * ty)));
-        ty_ = fmaf(PQ.z, iy, fmaf(PQ.w, ix, fmaf(A.x, ty, A.y * tx)));
-      } else {
-        const float2 q = sa[jj];
-        tx_ = fmaf(-q.x, ix, q.y * iy);
-        ty_ = fmaf(-q.x, iy, -q.y * ix);
+    const int total = spre[nc];
+    const int ks = sself;
+    // staged position of the target itself (its own leaf is in its U list)
+    const int selfpos = ks >= 0 ? spre[ks] + (ii - sj0[ks]) : -1;
+    for (int base = 0; base < total; base += NEAR_SLAB) {
+      const int ns = min(NEAR_SLAB, total - base);
+      if (base > 0) __syncthreads();
+      for (int s2 = tid; s2 < ns; s2 += 128) {
+        const int gs = base + s2;
+        int k = 0;
+        for (int q = 1; q < nc; ++q) k += gs >= spre[q];
+        const int j = sj0[k] + gs - spre[k];
+        sz[s2] = zhl[j];
+        if (E == 2) {
+          sp[s2] = reinterpret_cast<const float4*>(pq)[j];
+          sa[s2] = aa[j];
+        } else {
+          sa[s2] = qa[j];
+        }
       }
-      kahan_add(gx, cx, tx_);
-      kahan_add(gy, cy, ty_);
+      __syncthreads();
+      const int sp0 = selfpos - base;
+#pragma unroll 4
+      for (int jj = sl; jj < ns; jj += NS) {
+        const float4 hlj = sz[jj];
+        const float dx = (hlj.x - hl.x) + (hlj.z - hl.z);
+        const float dy = (hlj.y - hl.y) + (hlj.w - hl.w);
+        float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
+        rr = jj == sp0 ? 0.f : rr;  // the self pair (dx = dy = 0) contributes nothing
+        const float ix = dx * rr, iy = -dy * rr;
+        float tx_, ty_;
+        if (E == 2) {
+          const float4 PQ = sp[jj];
+          const float2 A = sa[jj];
+          const float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
+          const float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
+          tx_ = fmaf(PQ.x, ix, fmaf(-PQ.y, iy, fmaf(A.x, tx, -A.y * ty)));
+          ty_ = fmaf(PQ.z, iy, fmaf(PQ.w, ix, fmaf(A.x, ty, A.y * tx)));
+        } else {
+          const float2 q = sa[jj];
+          tx_ = fmaf(-q.x, ix, q.y * iy);
+          ty_ = fmaf(-q.x, iy, -q.y * ix);
+        }
+        kahan_add(gx, cx, tx_);
+        kahan_add(gy, cy, ty_);
+      }
     }
   }
   sred[sl][tt] = make_float2(gx - cx, gy - cy);
@@ -1552,7 +1704,7 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   {
     size_t sm = sizeof(float4) * (32 * (size_t)(p + 1) + 96);
     if (sm > 48 * 1024) EB_CUDA_TRY(cudaFuncSetAttribute(k_p2m_df<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_p2m_df<E><<<t.nleaf, std::max(128, round32((E == 2 ? 3 : 1) * p)), sm, st>>>(t.lev_off[L], t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
+    k_p2m_df<E><<<t.nleaf, std::max(128, round32((E == 2 ? 3 : 1) * p)), sm, st>>>(t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(), t.wdf.as<float4>(),
                                           E == 2 ? w.qdf.as<float4>() : w.pqdf.as<float4>(), p, mp);
     eb_count_launch(ctx);
   }
@@ -1596,14 +1748,12 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   const int ldb = 2 * p + 2;
   EB_TRY(w.mpole.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * p));
   EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)t.nbox * E * (p + 1)));
-  double rleaf = t.W / (double)(1 << L);
-  int offL = t.lev_off[L];
   // Upward pass. FP32: direct P2M (in chunks) for every box of the EB_DIRECT_LEVELS
   // finest levels in one launch, then M2M per coarser level. FP64: P2M and one M2M
   // launch per level.
   if (sizeof(T) == 4) {
     const int lmin = t.chunk_lmin;
-    const int first2 = t.lev_off[lmin], nout = E * p;
+    const int first2 = t.lev_off[2], nout = E * p;
     EB_TRY(w.mpart.ensure(sizeof(float2) * (size_t)t.nchunk * nout));
     LevOff lo;
     for (int l = 0; l < EB_KEY_LEVELS + 2; ++l) {
@@ -1611,7 +1761,8 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
       lo.rinv[l] = (float)((double)(1u << std::min(l, 30)) / t.W);
     }
     const size_t sm = sizeof(float2) * ((size_t)EB_CHUNK * (p + 1) + (E == 2 ? 3 : 1) * (EB_CHUNK + 2 * (size_t)p));
-    k_p2m_chunks<E><<<t.nchunk, 128, sm, st>>>(L, lmin, lo, first2, t.chunk_box.as<int>(), t.cstart.as<int>(),
+    k_p2m_chunks<E><<<t.nchunk, 128, sm, st>>>(lo, first2, t.blev.as<unsigned char>(), t.plev.as<unsigned char>(),
+                                              t.chunk_box.as<int>(), t.cstart.as<int>(),
                                               t.keys.as<unsigned long long>(), t.pt0.as<int>(), t.pt1.as<int>(),
                                               t.wdf.as<float4>(), reinterpret_cast<const float2*>(w.qa.p),
                                               reinterpret_cast<const float2*>(w.qb.p), t.W, p,
@@ -1629,9 +1780,10 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     }
   } else {
     size_t sm = sizeof(c_t<T>) * (32 * (size_t)(p + 1) + 96);
-    k_p2m<T, E><<<t.nleaf, 64, sm, st>>>(offL, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+    k_p2m<T, E><<<t.nleaf, 64, sm, st>>>(t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
+                                          t.blev.as<unsigned char>(), t.pt0.as<int>(),
                                           t.pt1.as<int>(), t.zs.as<double2>(), w.qa.as<c_t<T>>(),
-                                          w.qb.as<c_t<T>>(), t.x0, t.y0, rleaf, p,
+                                          w.qb.as<c_t<T>>(), t.x0, t.y0, t.W, p,
                                           w.mpole.as<c_t<T>>());
     eb_count_launch(ctx);
     for (int l = L - 1; l >= 2; --l) {
@@ -1667,11 +1819,12 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     }
     ps.done();
   }
-  // Downward pass. FP64: L2L level by level. FP32: L2L only into the coarsest of the
-  // EB_FAR_LEVELS finest levels; the far-field kernel evaluates the M2L expansions of
-  // those levels directly (cheap FP32 work instead of a dependent chain of shifts).
+  // Downward pass. FP64: L2L level by level. FP32: L2L only into the level lend, the
+  // coarsest of the EB_FAR_LEVELS finest levels; the far-field kernel evaluates the M2L
+  // expansions of the levels below it directly (cheap FP32 work instead of a dependent
+  // chain of shifts).
   {
-    const int lend = sizeof(T) == 8 ? L : L - std::min(L - 1, EB_FAR_LEVELS) + 1;
+    const int lend = sizeof(T) == 8 ? L : t.lend;
     for (int l = 3; l <= lend; ++l) {
       int nb = t.lev_off[l + 1] - t.lev_off[l];
       size_t sm = sizeof(c_t<T>) * E * (p + 1);
@@ -1697,7 +1850,6 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   EbFmmWork& w = f64 ? ctx->work64 : ctx->work32;
   const int n = t.n;
   const bool df = f64 && df_req;
-  double rleaf = t.W / (double)(1 << t.L);
   if (df) {
     EB_TRY(w.pqdf.ensure(sizeof(float4) * 2 * (size_t)n));
     EB_TRY(w.aadf.ensure(sizeof(float4) * (size_t)n));
@@ -1710,11 +1862,11 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   }
   if (df && E == 2) {
     k_charges_stokes_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
-                                                      1.0 / rleaf, w.qdf.as<float4>(), w.pqdf.as<float4>(),
-                                                      w.aadf.as<float4>());
+                                                      1.0 / t.W, t.plev.as<unsigned char>(), w.qdf.as<float4>(),
+                                                      w.pqdf.as<float4>(), w.aadf.as<float4>());
   } else if (df) {
     k_charges_cauchy_df<<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, post.u, post.dz, post.hpt,
-                                                      1.0 / rleaf, w.pqdf.as<float4>());
+                                                      1.0 / t.W, t.plev.as<unsigned char>(), w.pqdf.as<float4>());
   } else if (E == 2) {
     k_charges_stokes<T><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
                                                       w.qa.as<c_t<T>>(), w.qb.as<c_t<T>>(),
@@ -1725,7 +1877,6 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   }
   eb_count_launch(ctx);
   const int has_far = t.L >= 2;
-  int offL = t.lev_off[t.L];
   int blocks = nblk((long long)t.ngroup * 32, 128);
   // FP32 and double-float: the near field runs on the side stream while the expansion
   // passes run on the main stream, and the far-field kernel adds both. This pays while
@@ -1739,13 +1890,14 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     cudaStream_t ss = ctx->side_stream;
     if (df) {
       k_leaf_df<E, 1><<<blocks, 128, 0, ss>>>(
-          t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, 0, t.bkey.as<unsigned long long>(),
-          t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+          t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), t.leaves.as<int>(), 0, t.bkey.as<unsigned long long>(),
+          t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
+          t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
           t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
           (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
     } else {
-      k_near32<E><<<t.ntile, 128, 0, ss>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
-                                           t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
+      k_near32<E><<<t.ntile, 128, 0, ss>>>(t.tiles.as<int4>(), t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                           t.ustart.as<int>(), t.ulist.as<int>(), t.zhl.as<float4>(),
                                            w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
                                            w.nearbuf.as<double2>());
     }
@@ -1758,7 +1910,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     EB_TRY(w.local.ensure(sizeof(c_t<T>) * (size_t)(E * (tb.p + 1))));
     EB_TRY(w.local_df.ensure(sizeof(float4) * (size_t)(E * (tb.p + 1))));
   }
-  const int far_lev = has_far ? std::min(t.L - 1, EB_FAR_LEVELS) : 0;
+  const int far_lev = has_far ? std::min(t.L - 1, EB_FAR_LEVELS) : 0;  // far boxes per leaf, at most
   const size_t far_sm = sizeof(float2) * (size_t)far_lev * E * (tb.p + 1);
   if (split) EB_CUDA_TRY(cudaStreamWaitEvent(st, ctx->ev_p2p, 0));
   if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
@@ -1766,8 +1918,8 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
     // FP32 without the split: the near-field kernel, then the far field on the same stream
     EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
     ProfScope pn(ctx, 2, st);
-    k_near32<E><<<t.ntile, 128, 0, st>>>(t.tiles.as<int4>(), offL, t.pt0.as<int>(), t.pt1.as<int>(),
-                                         t.ulist.as<int>(), t.ucount.as<int>(), t.zhl.as<float4>(),
+    k_near32<E><<<t.ntile, 128, 0, st>>>(t.tiles.as<int4>(), t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                         t.ustart.as<int>(), t.ulist.as<int>(), t.zhl.as<float4>(),
                                          w.pq.as<float2>(), w.aa.as<float2>(), w.qa.as<float2>(),
                                          w.nearbuf.as<double2>());
     eb_count_launch(ctx);
@@ -1776,33 +1928,38 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   ProfScope ps(ctx, 0, st);
   if (df && split) {
     k_leaf_df<E, 2><<<blocks, 128, 0, st>>>(
-        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
-        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), t.leaves.as<int>(), has_far, t.bkey.as<unsigned long long>(),
+        t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
+        t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
   } else if (split) {
-    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), offL, far_lev, t.L - 1,
-                                             t.bkey.as<unsigned long long>(), t.anc.as<int>(), t.perm.as<int>(),
-                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(), out,
-                                             post, w.nearbuf.as<double2>());
+    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), t.leaves.as<int>(),
+                                             t.bkey.as<unsigned long long>(), t.blev.as<unsigned char>(),
+                                             t.anc.as<int>(), t.wstart.as<int>(), t.wlist.as<int>(), t.perm.as<int>(),
+                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(),
+                                             w.mpole.as<float2>(), out, post, w.nearbuf.as<double2>());
   } else if (df) {
     k_leaf_df<E, 0><<<blocks, 128, 0, st>>>(
-        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
-        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), t.leaves.as<int>(), has_far, t.bkey.as<unsigned long long>(),
+        t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
+        t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign,
         w.local_df.as<float4>(), out, post, nullptr);
   } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
-        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), offL, has_far, t.bkey.as<unsigned long long>(),
-        t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(), t.perm.as<int>(),
+        t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), t.leaves.as<int>(), has_far, t.bkey.as<unsigned long long>(),
+        t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
+        t.wstart.as<int>(), t.wlist.as<int>(), t.perm.as<int>(),
         t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(), w.qa.as<double2>(), t.x0, t.y0,
-        rleaf, tb.p, (double)sign, w.local.as<double2>(), out, post);
+        t.W, tb.p, (double)sign, w.local.as<double2>(), w.mpole.as<double2>(), out, post);
   } else {
-    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), offL, far_lev, t.L - 1,
-                                             t.bkey.as<unsigned long long>(), t.anc.as<int>(), t.perm.as<int>(),
-                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(), out,
-                                             post, w.nearbuf.as<double2>());
+    k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), t.leaves.as<int>(),
+                                             t.bkey.as<unsigned long long>(), t.blev.as<unsigned char>(),
+                                             t.anc.as<int>(), t.wstart.as<int>(), t.wlist.as<int>(), t.perm.as<int>(),
+                                             t.wdf.as<float4>(), tb.p, (float)sign, w.local.as<float2>(),
+                                             w.mpole.as<float2>(), out, post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
   ps.done();

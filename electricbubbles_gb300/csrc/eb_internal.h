@@ -110,15 +110,16 @@ struct EbTree {
   // FP32 far field: per leaf its boxes at levels lev(leaf), .., max(2, min(lev(leaf), lend)),
   // at most EB_FAR_LEVELS of them (the coarsest one holds the accumulated locals above)
   DevBuf anc;      // int[nleaf*EB_FAR_LEVELS]
-  DevBuf flags, scan, hist, bbox, partial, cubtmp, pairs, ctr;
-  // FP32 direct multipoles: the boxes of levels chunk_lmin..L split into chunks of
-  // EB_CHUNK points (coarser levels by M2M)
+  DevBuf gcount, gstart;  // groups per leaf and their scan
+  DevBuf flags, scan, hist, bbox, partial, cubtmp, pairs;
+  // FP32 direct multipoles: the boxes of levels chunk_lmin..L and the leaves above them,
+  // split into chunks of EB_CHUNK points (other boxes by M2M)
   int nchunk = 0;
   int chunk_lmin = 2;
-  DevBuf ccount;     // int[nbox - lev_off[chunk_lmin]]: chunks per box
-  DevBuf cstart;     // int[nbox - lev_off[chunk_lmin] + 1]: first chunk of each box
+  DevBuf ccount;     // int[nbox - lev_off[2]]: chunks per box of levels >= 2
+  DevBuf cstart;     // int[nbox - lev_off[2] + 1]: first chunk of each box
   DevBuf chunk_box;  // int[nchunk]: the box of each chunk
-  DevBuf cdone;      // int[nbox - lev_off[chunk_lmin]]: chunks of the box finished in the
+  DevBuf cdone;      // int[nbox - lev_off[2]]: chunks of the box finished in the
                      // current P2M (zero between launches: the box's last chunk resets it)
 };
 #define EB_CHUNK 64

@@ -5,10 +5,12 @@
 // not (DOINT0DR, cadapdrop2.f:84-197). Here the nodes are sorted once by a Morton key
 // at depth 20; the occupied boxes of every level are then the distinct key prefixes,
 // each owning a contiguous range of the sorted nodes. Only occupied boxes exist.
-// The leaf level is the shallowest one whose mean occupancy is at most `leaf_target`.
-// Interaction lists follow MKINTL (cadap2.f:780-828: children of the parent's
-// neighbours that are not adjacent, at most 27) and MKNBOR (cadap2.f:705-742: the
-// 3 x 3 neighbourhood at the leaf level).
+// The tree is adaptive: a box with more than `leaf_cap` points is split (DAASSI,
+// dapif1.f:1165-1255, with NAPB = leaf_cap), every point's leaf level following from
+// the number of points between it and the point leaf_cap places on. V lists follow MKINTL
+// (cadap2.f:780-828: children of the parent's neighbours that are not adjacent, at most
+// 27); the leaves' U and W lists follow DALI12/DALI34 (dapif2.f:3-356) for leaves of
+// different levels.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -111,25 +113,6 @@ __global__ void k_keys(const double2* __restrict__ z, int n, const double* __res
   idx[i] = i;
 }
 
-// Histogram of the first level at which consecutive sorted keys fall in different
-// boxes: occupied boxes at level l = 1 + sum_{l' <= l} hist[l'].
-__global__ void k_level_hist(const unsigned long long* __restrict__ keys, int n,
-                             int* __restrict__ hist) {
-  __shared__ int sh[EB_KEY_LEVELS + 1];
-  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x) sh[i] = 0;
-  __syncthreads();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += gridDim.x * blockDim.x) {
-    unsigned long long x = keys[i] ^ keys[i - 1];
-    if (x == 0) continue;
-    int hb = 63 - __clzll((long long)x);
-    int lfirst = EB_KEY_LEVELS - hb / 2;
-    atomicAdd(&sh[lfirst], 1);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x)
-    if (sh[i]) atomicAdd(&hist[i], sh[i]);
-}
-
 // sorted positions, also as float hi + lo pairs packed (hi.x, hi.y, lo.x, lo.y)
 __global__ void k_gather_points(const double2* __restrict__ z, const int* __restrict__ perm,
                                 int n, double2* __restrict__ zs, float4* __restrict__ zhl) {
@@ -141,26 +124,77 @@ __global__ void k_gather_points(const double2* __restrict__ z, const int* __rest
   zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
 }
 
-// Every level at once: flags[l*n + i] = 1 where sorted point i starts a box of level l
-// (l = 0..L). One exclusive scan over the concatenated rows then gives each head its
-// global box id (rows in level order: level l's ids start at lev_off[l]).
-__global__ void k_heads_all(const unsigned long long* __restrict__ keys, int n, int L,
-                            int* __restrict__ flags) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const unsigned long long k = keys[i], kp = i > 0 ? keys[i - 1] : 0ull;
-  for (int l = 0; l <= L; ++l) {
-    const int sh = 2 * (EB_KEY_LEVELS - l);
-    flags[(size_t)l * n + i] = (i == 0) || ((k >> sh) != (kp >> sh));
-  }
+// Levels shared by the keys a and b: the deepest level whose box holds both
+// (EB_KEY_LEVELS when the keys are equal, -1 never: the root holds every point).
+__device__ __forceinline__ int shared_levels(unsigned long long a, unsigned long long b) {
+  const unsigned long long x = a ^ b;
+  if (x == 0ull) return EB_KEY_LEVELS;
+  const int hb = 63 - __clzll((long long)x);
+  return EB_KEY_LEVELS - 1 - hb / 2;
 }
 
-// Box key, first point and parent of every box; a box whose head point also starts its
-// parent is the parent's first child.
+// lcpw[w] = levels shared by sorted points w and w + cap (w < n - cap). The box of level
+// l around a point holds more than cap points exactly when some window [w, w + cap]
+// containing the point has lcpw[w] >= l (a box is a contiguous range of sorted points).
+__global__ void k_lcp_window(const unsigned long long* __restrict__ keys, int n, int cap,
+                             unsigned char* __restrict__ lcpw) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n - cap) return;
+  lcpw[w] = (unsigned char)shared_levels(keys[w], keys[w + cap]);
+}
+
+// Leaf level of every sorted point: one more than the deepest level whose box around the
+// point holds more than cap points, at most EB_KEY_LEVELS (coincident points), 0 when
+// n <= cap. Also the deepest leaf level and the number of boxes of every level l >= 1:
+// a point starts a box of level l when l <= its leaf level and its key differs from the
+// previous point's at level l.
+__global__ void k_leaf_level(const unsigned long long* __restrict__ keys, int n, int cap,
+                             const unsigned char* __restrict__ lcpw, unsigned char* __restrict__ plev,
+                             int* __restrict__ lmax, int* __restrict__ hist) {
+  __shared__ int sh[EB_KEY_LEVELS + 1];
+  __shared__ int smax;
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x) sh[i] = 0;
+  if (threadIdx.x == 0) smax = 0;
+  __syncthreads();
+  int mymax = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int lam = 0;
+    if (n > cap) {
+      const int w0 = max(0, i - cap), w1 = min(i, n - 1 - cap);
+      int m = 0;
+      for (int w = w0; w <= w1; ++w) m = max(m, (int)lcpw[w]);
+      lam = min(EB_KEY_LEVELS, m + 1);
+    }
+    plev[i] = (unsigned char)lam;
+    mymax = max(mymax, lam);
+    const int sl = i > 0 ? shared_levels(keys[i - 1], keys[i]) : -1;
+    for (int l = max(1, sl + 1); l <= lam; ++l) atomicAdd(&sh[l], 1);
+  }
+  atomicMax(&smax, mymax);
+  __syncthreads();
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  if (threadIdx.x == 0) atomicMax(lmax, smax);
+}
+
+// Every level at once: flags[l*n + i] = 1 where sorted point i starts an existing box of
+// level l (l = 0..L). One exclusive scan over the concatenated rows then gives each head
+// its global box id (rows in level order: level l's ids start at lev_off[l]).
+__global__ void k_heads_all(const unsigned long long* __restrict__ keys, const unsigned char* __restrict__ plev,
+                            int n, int L, int* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int lam = plev[i];
+  const int sl = i > 0 ? shared_levels(keys[i - 1], keys[i]) : -1;
+  for (int l = 0; l <= L; ++l) flags[(size_t)l * n + i] = (l <= lam) && (l > sl);
+}
+
+// Box key, level, first point and parent of every box; a box whose head point also starts
+// its parent is the parent's first child (a split box's points all lie in its children).
 __global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, int L,
                             const int* __restrict__ flags, const int* __restrict__ scan,
-                            unsigned long long* __restrict__ bkey, int* __restrict__ pt0,
-                            int* __restrict__ parent, int* __restrict__ child0) {
+                            unsigned long long* __restrict__ bkey, unsigned char* __restrict__ blev,
+                            int* __restrict__ pt0, int* __restrict__ parent, int* __restrict__ child0) {
   const long long tot = (long long)(L + 1) * n;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < tot;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -168,6 +202,7 @@ __global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, 
     const int l = (int)(idx / n), i = (int)(idx - (long long)l * n);
     const int b = scan[idx];
     bkey[b] = keys[i] >> (2 * (EB_KEY_LEVELS - l));
+    blev[b] = (unsigned char)l;
     pt0[b] = i;
     if (l == 0) {
       parent[b] = -1;
@@ -184,22 +219,24 @@ struct LevOffT {
   int v[EB_KEY_LEVELS + 3];
 };
 
-// Point range end, children count (and no children at the leaf level) of every box.
-__global__ void k_boxes_fin(int nbox, LevOffT lo, int L, int n, int* __restrict__ child0,
-                            int* __restrict__ nchild, const int* __restrict__ pt0,
-                            int* __restrict__ pt1) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
+// Point range end of every box (binary search for the first key beyond the box's prefix)
+// and the children count of its parent.
+__global__ void k_boxes_fin(int nbox, const unsigned long long* __restrict__ keys, int n,
+                            const unsigned long long* __restrict__ bkey, const unsigned char* __restrict__ blev,
+                            const int* __restrict__ pt0, const int* __restrict__ parent,
+                            int* __restrict__ pt1, int* __restrict__ nchild) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbox) return;
-  int l = 0;
-  while (b >= lo.v[l + 1]) ++l;
-  const bool last = b + 1 >= lo.v[l + 1];
-  pt1[b] = last ? n : pt0[b + 1];
-  if (l == L) {
-    child0[b] = -1;
-    nchild[b] = 0;
-  } else {
-    nchild[b] = (last ? lo.v[l + 2] : child0[b + 1]) - child0[b];
+  const int l = blev[b], sh = 2 * (EB_KEY_LEVELS - l);
+  const unsigned long long k = bkey[b];
+  int lo = pt0[b] + 1, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if ((keys[mid] >> sh) > k) hi = mid;
+    else lo = mid + 1;
   }
+  pt1[b] = lo;
+  if (l > 0) atomicAdd(&nchild[parent[b]], 1);
 }
 
 __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ bkey, int off,
@@ -215,7 +252,10 @@ __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ b
   return -1;
 }
 
-// V lists of every box of levels 2..L in one launch (the box's level from lev_off).
+// V lists of every box of levels 2..L in one launch (MKINTL, cadap2.f:780-828: the
+// children of the parent's neighbours that are not adjacent to the box; DALI12's list 1,
+// dapif2.f:3-171). Only existing boxes are found, so the children of a neighbour that is
+// a leaf are absent: its points reach the box's leaves through their U lists.
 __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo, int first, int nbox,
                         int* __restrict__ vlist, unsigned char* __restrict__ vcode,
                         int* __restrict__ vcount) {
@@ -249,102 +289,208 @@ __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo,
   vcount[gid] = cnt;
 }
 
-__global__ void k_ulist(const unsigned long long* __restrict__ bkey, int off, int nb, int lev,
-                        int* __restrict__ ulist, int* __restrict__ ucount) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  unsigned long long key = bkey[off + b];
-  int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
-  int side = 1 << lev, cnt = 0;
-  for (int dy = -1; dy <= 1; ++dy)
-    for (int dx = -1; dx <= 1; ++dx) {
-      int sx = ix + dx, sy = iy + dy;
-      if (sx < 0 || sy < 0 || sx >= side || sy >= side) continue;
-      int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
-      if (s < 0) continue;
-      ulist[(size_t)b * EB_UMAX + cnt] = s;
-      ++cnt;
-    }
-  ucount[b] = cnt;
+// Leaves in point order: point i starts its leaf when it heads the box of its leaf level.
+__global__ void k_leaf_heads(int n, const unsigned char* __restrict__ plev, const int* __restrict__ flags,
+                             int* __restrict__ lflag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  lflag[i] = flags[(size_t)plev[i] * n + i];
 }
 
-__global__ void k_pair_counts(int off, int nleaf, const int* __restrict__ pt0,
-                              const int* __restrict__ pt1, const int* __restrict__ ulist,
-                              const int* __restrict__ ucount, int vfirst, int vlast,
-                              const int* __restrict__ vcount,
+__global__ void k_leaf_fill(int n, const unsigned char* __restrict__ plev, const int* __restrict__ lflag,
+                            const int* __restrict__ lscan, const int* __restrict__ scan,
+                            int* __restrict__ leaves) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !lflag[i]) return;
+  leaves[lscan[i]] = scan[(size_t)plev[i] * n + i];
+}
+
+// The leaf count, from the exclusive scan of the leaf heads.
+__global__ void k_leaf_count(int n, const int* __restrict__ lflag, const int* __restrict__ lscan,
+                             int* __restrict__ nleaf) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *nleaf = lscan[n - 1] + lflag[n - 1];
+}
+
+#define EB_LIST_STACK 72
+
+// U and W lists of every leaf (DALI12 / DALI34, dapif2.f:3-356, for an adaptive tree
+// without level restriction). For leaf b of level l:
+//  * every existing box C of level l adjacent to b (b itself included): a leaf C goes to
+//    U; below a split C, the boxes adjacent to b are followed down to leaves (U), and a
+//    box that is not adjacent to b while its parent is goes to W (its multipole is
+//    evaluated at b's points: M2P, DABARR's list-3 evaluation);
+//  * every leaf of a coarser level m adjacent to b's ancestor of level m goes to U (the
+//    dual list 4, evaluated directly: such a leaf holds at most cap points).
+// Every pair of points is then covered exactly once by U, W or a V list of a common
+// level. FILL = false counts, FILL = true writes at ustart / wstart.
+template <bool FILL>
+__global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves, const unsigned long long* __restrict__ bkey,
+                             const unsigned char* __restrict__ blev, LevOffT lo,
+                             const int* __restrict__ child0, const int* __restrict__ nchild,
+                             int* __restrict__ ucnt, int* __restrict__ wcnt,
+                             const int* __restrict__ ustart, const int* __restrict__ wstart,
+                             int* __restrict__ ulist, int* __restrict__ wlist, int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nleaf_d) nleaf = *nleaf_d;  // counting pass: launched for an upper bound
+  if (t >= nleaf) return;
+  const int b = leaves[t], l = blev[b];
+  const unsigned long long kb = bkey[b];
+  const int ix = (int)compact2(kb), iy = (int)compact2(kb >> 1);
+  int nu = 0, nw = 0;
+  int* uo = FILL ? ulist + ustart[t] : nullptr;
+  int* wo = FILL ? wlist + wstart[t] : nullptr;
+  int stack[EB_LIST_STACK];
+  const int side = 1 << l;
+  for (int dy = -1; dy <= 1; ++dy) {
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int sx = ix + dx, sy = iy + dy;
+      if (sx < 0 || sy < 0 || sx >= side || sy >= side) continue;
+      const int C = find_box(bkey, lo.v[l], lo.v[l + 1] - lo.v[l], morton((unsigned)sx, (unsigned)sy));
+      if (C < 0) continue;
+      if (nchild[C] == 0) {
+        if (FILL) uo[nu] = C;
+        ++nu;
+        continue;
+      }
+      int sp = 0;
+      for (int c = 0; c < nchild[C]; ++c) stack[sp++] = child0[C] + c;
+      while (sp > 0) {
+        const int D = stack[--sp];
+        const int f = blev[D] - l;
+        const unsigned long long kd = bkey[D];
+        const int jx = (int)compact2(kd), jy = (int)compact2(kd >> 1);
+        const int x0 = ix << f, x1 = ((ix + 1) << f) - 1, y0 = iy << f, y1 = ((iy + 1) << f) - 1;
+        const bool adj = jx >= x0 - 1 && jx <= x1 + 1 && jy >= y0 - 1 && jy <= y1 + 1;
+        if (!adj) {
+          if (FILL) wo[nw] = D;
+          ++nw;
+        } else if (nchild[D] == 0) {
+          if (FILL) uo[nu] = D;
+          ++nu;
+        } else if (sp + nchild[D] <= EB_LIST_STACK) {
+          for (int c = 0; c < nchild[D]; ++c) stack[sp++] = child0[D] + c;
+        } else {
+          atomicOr(err, 1);
+        }
+      }
+    }
+  }
+  for (int m = l - 1; m >= 0; --m) {
+    const int ax = ix >> (l - m), ay = iy >> (l - m), sm = 1 << m;
+    for (int dy = -1; dy <= 1; ++dy) {
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (dx == 0 && dy == 0) continue;
+        const int sx = ax + dx, sy = ay + dy;
+        if (sx < 0 || sy < 0 || sx >= sm || sy >= sm) continue;
+        const int N = find_box(bkey, lo.v[m], lo.v[m + 1] - lo.v[m], morton((unsigned)sx, (unsigned)sy));
+        if (N < 0 || nchild[N] != 0) continue;
+        if (FILL) uo[nu] = N;
+        ++nu;
+      }
+    }
+  }
+  if (!FILL) {
+    ucnt[t] = nu;
+    wcnt[t] = nw;
+  }
+}
+
+// Algorithmic work of the built tree: near-field pairs (self excluded), M2P evaluations
+// (W-list box, target point) and M2L pairs.
+__global__ void k_pair_counts(int nleaf, const int* __restrict__ leaves, const int* __restrict__ pt0,
+                              const int* __restrict__ pt1, const int* __restrict__ ustart,
+                              const int* __restrict__ ulist, const int* __restrict__ wstart,
+                              int vfirst, int vlast, const int* __restrict__ vcount,
                               unsigned long long* __restrict__ out) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long up = 0, vp = 0;
-  if (b < nleaf) {
-    int nt = pt1[off + b] - pt0[off + b];
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long up = 0, vp = 0, wp = 0;
+  if (t < nleaf) {
+    const int b = leaves[t];
+    const long long nt = pt1[b] - pt0[b];
     long long ns = 0;
-    for (int j = 0; j < ucount[b]; ++j) {
-      int s = ulist[(size_t)b * EB_UMAX + j];
+    for (int j = ustart[t]; j < ustart[t + 1]; ++j) {
+      const int s = ulist[j];
       ns += pt1[s] - pt0[s];
     }
     up = (unsigned long long)(nt * ns - nt);
+    wp = (unsigned long long)(nt * (wstart[t + 1] - wstart[t]));
   }
   for (int g = vfirst + blockIdx.x * blockDim.x + threadIdx.x; g < vlast; g += gridDim.x * blockDim.x)
     vp += (unsigned long long)vcount[g];
   up = warp_sum<unsigned long long>(up);
   vp = warp_sum<unsigned long long>(vp);
+  wp = warp_sum<unsigned long long>(wp);
   if ((threadIdx.x & 31) == 0) {
     atomicAdd(&out[0], up);
     atomicAdd(&out[1], vp);
+    atomicAdd(&out[2], wp);
   }
 }
 
-__global__ void k_group_count(int off, int nleaf, const int* __restrict__ pt0,
-                              const int* __restrict__ pt1, int* __restrict__ cnt) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nleaf) return;
-  cnt[b] = (pt1[off + b] - pt0[off + b] + EB_GROUP - 1) / EB_GROUP;
+__global__ void k_group_count(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves,
+                              const int* __restrict__ pt0, const int* __restrict__ pt1, int* __restrict__ cnt) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= *nleaf_d) return;
+  const int b = leaves[t];
+  cnt[t] = (pt1[b] - pt0[b] + EB_GROUP - 1) / EB_GROUP;
 }
 
-__global__ void k_group_fill(int off, int nleaf, const int* __restrict__ pt0,
+__global__ void k_group_fill(int nleaf, const int* __restrict__ leaves, const int* __restrict__ pt0,
                              const int* __restrict__ cnt, const int* __restrict__ start,
                              int* __restrict__ gleaf, int* __restrict__ gfirst) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nleaf) return;
-  int g0 = start[b];
-  for (int g = 0; g < cnt[b]; ++g) {
-    gleaf[g0 + g] = b;
-    gfirst[g0 + g] = pt0[off + b] + g * EB_GROUP;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nleaf) return;
+  const int b = leaves[t], g0 = start[t];
+  for (int g = 0; g < cnt[t]; ++g) {
+    gleaf[g0 + g] = t;
+    gfirst[g0 + g] = pt0[b] + g * EB_GROUP;
   }
 }
 
-__global__ void k_tile_count(int off, int nleaf, const int* __restrict__ pt0,
-                             const int* __restrict__ pt1, int* __restrict__ cnt) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nleaf) return;
-  cnt[b] = (pt1[off + b] - pt0[off + b] + EB_NTILE - 1) / EB_NTILE;
+__global__ void k_tile_count(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves,
+                             const int* __restrict__ pt0, const int* __restrict__ pt1, int* __restrict__ cnt) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= *nleaf_d) return;
+  const int b = leaves[t];
+  cnt[t] = (pt1[b] - pt0[b] + EB_NTILE - 1) / EB_NTILE;
 }
 
-__global__ void k_tile_fill(int off, int nleaf, const int* __restrict__ pt0, const int* __restrict__ pt1,
-                            const int* __restrict__ cnt, const int* __restrict__ start,
-                            int4* __restrict__ tiles) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nleaf) return;
-  const int g0 = start[b], c = cnt[b], a = pt0[off + b], nt = pt1[off + b] - a;
+__global__ void k_tile_fill(int nleaf, const int* __restrict__ leaves, const int* __restrict__ pt0,
+                            const int* __restrict__ pt1, const int* __restrict__ cnt,
+                            const int* __restrict__ start, int4* __restrict__ tiles) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nleaf) return;
+  const int b = leaves[t];
+  const int g0 = start[t], c = cnt[t], a = pt0[b], nt = pt1[b] - a;
   for (int g = 0; g < c; ++g)
-    tiles[g0 + g] = make_int4(b, a + (int)((long long)g * nt / c), a + (int)((long long)(g + 1) * nt / c), 0);
+    tiles[g0 + g] = make_int4(t, a + (int)((long long)g * nt / c), a + (int)((long long)(g + 1) * nt / c), 0);
 }
 
-__global__ void k_ancestors(int off, int nleaf, int na, const int* __restrict__ parent, int* __restrict__ anc) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nleaf) return;
-  int a = off + b;
-  for (int q = 0; q < na; ++q) {
-    anc[(size_t)b * na + q] = a;
-    if (q + 1 < na) a = parent[a];
+// The FP32 far field's boxes of each leaf: the leaf and its ancestors down to level
+// max(2, min(lev, lend)), -1 beyond (levels <= lend hold the L2L-accumulated locals).
+__global__ void k_far_boxes(int nleaf, const int* __restrict__ leaves, const unsigned char* __restrict__ blev,
+                            const int* __restrict__ parent, int lend, int* __restrict__ anc) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nleaf) return;
+  int a = leaves[t];
+  const int l = blev[a], lmin = max(2, min(l, lend));
+  for (int q = 0; q < EB_FAR_LEVELS; ++q) {
+    const int lev = l - q;
+    anc[(size_t)t * EB_FAR_LEVELS + q] = lev >= lmin ? a : -1;
+    if (lev > lmin) a = parent[a];
   }
 }
 
-__global__ void k_chunk_count(int first, int nb, const int* __restrict__ pt0, const int* __restrict__ pt1,
-                              int* __restrict__ cnt) {
+// Chunks of the boxes whose FP32 multipoles come directly from their points: every box
+// of the levels >= lmin and every leaf above them (coarser levels get theirs by M2M).
+__global__ void k_chunk_count(int first, int nb, int lmin, const unsigned char* __restrict__ blev,
+                              const int* __restrict__ nchild, const int* __restrict__ pt0,
+                              const int* __restrict__ pt1, int* __restrict__ cnt) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb) return;
-  cnt[b] = (pt1[first + b] - pt0[first + b] + EB_CHUNK - 1) / EB_CHUNK;
+  const int g = first + b;
+  const bool direct = blev[g] >= lmin || nchild[g] == 0;
+  cnt[b] = direct ? (pt1[g] - pt0[g] + EB_CHUNK - 1) / EB_CHUNK : 0;
 }
 
 __global__ void k_chunk_fill(int first, int nb, const int* __restrict__ cnt, const int* __restrict__ start,
@@ -435,13 +581,14 @@ __device__ __forceinline__ void split3(double w, float& hi, float& mid, float& l
   lo = __double2float_rn(r1 - (double)mid);
 }
 
-__global__ void k_leaf_coords(int offL, const unsigned long long* __restrict__ bkey,
-                              const int* __restrict__ pt0, const int* __restrict__ pt1,
-                              const double2* __restrict__ zs, double x0, double y0, double r,
-                              float4* __restrict__ wa, float2* __restrict__ wb) {
-  const int b = offL + blockIdx.x;
+__global__ void k_leaf_coords(const int* __restrict__ leaves, const unsigned long long* __restrict__ bkey,
+                              const unsigned char* __restrict__ blev, const int* __restrict__ pt0,
+                              const int* __restrict__ pt1, const double2* __restrict__ zs, double x0, double y0,
+                              double W, float4* __restrict__ wa, float2* __restrict__ wb) {
+  const int b = leaves[blockIdx.x];
   const unsigned long long k = bkey[b];
   const unsigned int ix = compact2(k), iy = compact2(k >> 1);
+  const double r = ldexp(W, -(int)blev[b]);  // W / 2^level, exact
   for (int i = pt0[b] + threadIdx.x; i < pt1[b]; i += blockDim.x) {
     double2 z = zs[i];
     float xh, xm, xl, yh, ym, yl;
@@ -452,29 +599,31 @@ __global__ void k_leaf_coords(int offL, const unsigned long long* __restrict__ b
   }
 }
 
-int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target) {
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap) {
   cudaStream_t st = eb_stream(ctx);
   t.valid = false;
   if (n <= 0) return EB_ERR_ARG;
-  if (leaf_target < 1) leaf_target = 32;
+  if (leaf_cap < 1) leaf_cap = EB_LEAF_CAP;
   t.n = n;
+  t.cap = leaf_cap;
   const int BS = 256;
   if (!t.host) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&t.host), sizeof(EbTreeHost)));
   EbTreeHost* H = t.host;
   t.pairs_read = false;
-  // 1. bounding square, on the device (read back with the level histogram below)
+  // 1. bounding square, on the device
   int nbb = std::min(nblk(n, BS), 1024);
   EB_TRY(t.partial.ensure(sizeof(Box4) * (size_t)nbb));
   EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(double) * 4 + sizeof(int) * 4));
   double* sq = reinterpret_cast<double*>(t.bbox.as<char>() + sizeof(Box4));
   int* bad = reinterpret_cast<int*>(sq + 4);
-  EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  int* lmax_d = bad + 1;
+  int* lerr_d = bad + 2;
+  int* nleaf_d = bad + 3;
+  EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int) * 3, st));
   k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
   eb_count_launch(ctx);
   k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
   eb_count_launch(ctx);
-  EB_CUDA_TRY(cudaMemcpyAsync(H->sq, sq, sizeof(H->sq), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaMemcpyAsync(&H->bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
   // 2. keys and sort (a non-finite coordinate gives clamped keys; reported below)
   EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
   EB_TRY(t.keys_alt.ensure(sizeof(unsigned long long) * (size_t)n));
@@ -493,18 +642,27 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
                                               t.keys.as<unsigned long long>(), t.idx_alt.as<int>(),
                                               t.perm.as<int>(), n, 0, 2 * EB_KEY_LEVELS, st));
   eb_count_launch(ctx);
+  const unsigned long long* keys = t.keys.as<unsigned long long>();
   // 3. sorted positions
   EB_TRY(t.zs.ensure(sizeof(double2) * (size_t)n));
   EB_TRY(t.zhl.ensure(sizeof(float4) * (size_t)n));
-  k_gather_points<<<nblk(n, BS), BS, 0, st>>>(z, t.perm.as<int>(), n, t.zs.as<double2>(),
-                                              t.zhl.as<float4>());
+  k_gather_points<<<nblk(n, BS), BS, 0, st>>>(z, t.perm.as<int>(), n, t.zs.as<double2>(), t.zhl.as<float4>());
   eb_count_launch(ctx);
-  // 4. occupied boxes per level, leaf level
+  // 4. leaf level of every point, deepest level, boxes per level
+  EB_TRY(t.lcpw.ensure((size_t)n));
+  EB_TRY(t.plev.ensure((size_t)n));
   EB_TRY(t.hist.ensure(sizeof(int) * (EB_KEY_LEVELS + 1)));
   EB_CUDA_TRY(cudaMemsetAsync(t.hist.p, 0, sizeof(int) * (EB_KEY_LEVELS + 1), st));
-  k_level_hist<<<std::min(nblk(n, BS), 1024), BS, 0, st>>>(t.keys.as<unsigned long long>(), n,
-                                                          t.hist.as<int>());
+  if (n > leaf_cap) {
+    k_lcp_window<<<nblk(n - leaf_cap, BS), BS, 0, st>>>(keys, n, leaf_cap, t.lcpw.as<unsigned char>());
+    eb_count_launch(ctx);
+  }
+  k_leaf_level<<<std::min(nblk(n, BS), ctx->nsm * 8), BS, 0, st>>>(keys, n, leaf_cap, t.lcpw.as<unsigned char>(),
+                                                                  t.plev.as<unsigned char>(), lmax_d,
+                                                                  t.hist.as<int>());
   eb_count_launch(ctx);
+  EB_CUDA_TRY(cudaMemcpyAsync(H->sq, sq, sizeof(H->sq), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->bad, bad, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaMemcpyAsync(H->hist, t.hist.p, sizeof(H->hist), cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaStreamSynchronize(st));
   if (H->bad) {
@@ -514,30 +672,26 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   t.W = H->sq[0];
   t.x0 = H->sq[1];
   t.y0 = H->sq[2];
-  const int* hist = H->hist;
-  int nb[EB_KEY_LEVELS + 1];
-  nb[0] = 1;
-  for (int l = 1; l <= EB_KEY_LEVELS; ++l) nb[l] = nb[l - 1] + hist[l];
-  int L = EB_KEY_LEVELS;
-  for (int l = 0; l <= EB_KEY_LEVELS; ++l)
-    if ((double)n / nb[l] <= (double)leaf_target) { L = l; break; }
+  const int L = H->lmax;
   t.L = L;
   t.lev_off[0] = 0;
-  for (int l = 0; l <= L; ++l) t.lev_off[l + 1] = t.lev_off[l] + nb[l];
+  for (int l = 0; l <= L; ++l) t.lev_off[l + 1] = t.lev_off[l] + (l == 0 ? 1 : H->hist[l]);
+  for (int l = L + 1; l <= EB_KEY_LEVELS; ++l) t.lev_off[l + 1] = t.lev_off[L + 1];
   t.nbox = t.lev_off[L + 1];
-  t.nleaf = nb[L];
-  size_t NB = (size_t)t.nbox;
+  t.lend = std::max(2, L - EB_FAR_LEVELS + 1);
+  const size_t NB = (size_t)t.nbox;
   EB_TRY(t.bkey.ensure(sizeof(unsigned long long) * NB));
+  EB_TRY(t.blev.ensure(NB));
   EB_TRY(t.pt0.ensure(sizeof(int) * NB));
   EB_TRY(t.pt1.ensure(sizeof(int) * NB));
   EB_TRY(t.parent.ensure(sizeof(int) * NB));
   EB_TRY(t.child0.ensure(sizeof(int) * NB));
   EB_TRY(t.nchild.ensure(sizeof(int) * NB));
-  // 5. boxes of every level in three launches (heads, one scan, fill) and a finish
+  // 5. boxes of every level: heads, one scan, fill, finish
   const size_t nflag = (size_t)(L + 1) * n;
   EB_TRY(t.flags.ensure(sizeof(int) * nflag));
   EB_TRY(t.scan.ensure(sizeof(int) * nflag));
-  k_heads_all<<<nblk(n, BS), BS, 0, st>>>(t.keys.as<unsigned long long>(), n, L, t.flags.as<int>());
+  k_heads_all<<<nblk(n, BS), BS, 0, st>>>(keys, t.plev.as<unsigned char>(), n, L, t.flags.as<int>());
   eb_count_launch(ctx);
   {
     size_t need = 0;
@@ -547,69 +701,100 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   tb = t.cubtmp.bytes;
   EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), (int)nflag, st));
   eb_count_launch(ctx);
+  EB_CUDA_TRY(cudaMemsetAsync(t.child0.p, 0xff, sizeof(int) * NB, st));  // -1: no children
+  EB_CUDA_TRY(cudaMemsetAsync(t.nchild.p, 0, sizeof(int) * NB, st));
   k_boxes_all<<<std::min(nblk((long long)nflag, BS), ctx->nsm * 16), BS, 0, st>>>(
-      t.keys.as<unsigned long long>(), n, L, t.flags.as<int>(), t.scan.as<int>(),
-      t.bkey.as<unsigned long long>(), t.pt0.as<int>(), t.parent.as<int>(), t.child0.as<int>());
+      keys, n, L, t.flags.as<int>(), t.scan.as<int>(), t.bkey.as<unsigned long long>(),
+      t.blev.as<unsigned char>(), t.pt0.as<int>(), t.parent.as<int>(), t.child0.as<int>());
   eb_count_launch(ctx);
-  {
-    LevOffT lo;
-    for (int l = 0; l < EB_KEY_LEVELS + 3; ++l) lo.v[l] = t.lev_off[std::min(l, L + 1)];
-    k_boxes_fin<<<nblk(t.nbox, BS), BS, 0, st>>>(t.nbox, lo, L, n, t.child0.as<int>(), t.nchild.as<int>(),
-                                                 t.pt0.as<int>(), t.pt1.as<int>());
-    eb_count_launch(ctx);
-  }
-  // 7. interaction lists
+  k_boxes_fin<<<nblk(t.nbox, BS), BS, 0, st>>>(t.nbox, keys, n, t.bkey.as<unsigned long long>(),
+                                              t.blev.as<unsigned char>(), t.pt0.as<int>(), t.parent.as<int>(),
+                                              t.pt1.as<int>(), t.nchild.as<int>());
+  eb_count_launch(ctx);
+  LevOffT lo;
+  for (int l = 0; l < EB_KEY_LEVELS + 3; ++l) lo.v[l] = t.lev_off[std::min(l, L + 1)];
+  // 6. leaves in point order
+  EB_TRY(t.lflag.ensure(sizeof(int) * (size_t)n));
+  EB_TRY(t.lscan.ensure(sizeof(int) * (size_t)n));
+  EB_TRY(t.leaves.ensure(sizeof(int) * NB));
+  k_leaf_heads<<<nblk(n, BS), BS, 0, st>>>(n, t.plev.as<unsigned char>(), t.flags.as<int>(), t.lflag.as<int>());
+  eb_count_launch(ctx);
+  tb = t.cubtmp.bytes;
+  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.lflag.as<int>(), t.lscan.as<int>(), n, st));
+  eb_count_launch(ctx);
+  k_leaf_fill<<<nblk(n, BS), BS, 0, st>>>(n, t.plev.as<unsigned char>(), t.lflag.as<int>(), t.lscan.as<int>(),
+                                          t.scan.as<int>(), t.leaves.as<int>());
+  eb_count_launch(ctx);
+  // 7. V lists of every box of levels >= 2
   EB_TRY(t.vlist.ensure(sizeof(int) * NB * EB_VMAX));
   EB_TRY(t.vcode.ensure(NB * EB_VMAX));
   EB_TRY(t.vcount.ensure(sizeof(int) * NB));
   EB_CUDA_TRY(cudaMemsetAsync(t.vcount.p, 0, sizeof(int) * NB, st));
   if (L >= 2) {
-    LevOffT lo;
-    for (int l = 0; l < EB_KEY_LEVELS + 3; ++l) lo.v[l] = t.lev_off[std::min(l, L + 1)];
     const int first = t.lev_off[2];
     k_vlist<<<nblk(t.nbox - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox,
                                                        t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                                        t.vcount.as<int>());
     eb_count_launch(ctx);
   }
-  EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)t.nleaf * EB_UMAX));
-  EB_TRY(t.ucount.ensure(sizeof(int) * (size_t)t.nleaf));
-  k_ulist<<<nblk(t.nleaf, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.lev_off[L], t.nleaf, L,
-                                             t.ulist.as<int>(), t.ucount.as<int>());
+  // 8. per-leaf counts, scanned so that one synchronisation sizes them all: U and W list
+  // lengths, near-field groups of EB_GROUP targets, shared-memory tiles of at most
+  // EB_NTILE targets, and FP32 direct-P2M chunks of at most EB_CHUNK points of every box
+  // of the chunked levels (every level up to 256K points, so that no dependent M2M
+  // launches remain on the critical path; above that the EB_DIRECT_LEVELS finest).
+  // The leaf count is known on the device only: the counting kernels run over nbox
+  // threads, stop at that count and leave zeros beyond it, and the scans span nbox + 1
+  // entries, so that their last entries are the totals.
+  const int NBi = t.nbox;
+  EB_TRY(t.ucnt.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.wcnt.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.ustart.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.wstart.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.tcount.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.tstart.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.gcount.ensure(sizeof(int) * (NB + 1)));
+  EB_TRY(t.gstart.ensure(sizeof(int) * (NB + 1)));
+  k_leaf_count<<<1, 32, 0, st>>>(n, t.lflag.as<int>(), t.lscan.as<int>(), nleaf_d);
   eb_count_launch(ctx);
-  // 8. work items, counted and scanned first so that one synchronisation sizes them all:
-  // near-field groups of EB_GROUP targets, shared-memory tiles of at most EB_NTILE
-  // targets, and FP32 direct-P2M chunks of at most EB_CHUNK points of every box of the
-  // chunked levels (every level up to 256K points, so that no dependent M2M launches
-  // remain on the critical path; above that the EB_DIRECT_LEVELS finest)
-  const int nl = t.nleaf;
-  EB_TRY(t.tcount.ensure(sizeof(int) * (size_t)nl));
-  EB_TRY(t.tstart.ensure(sizeof(int) * (size_t)nl));
-  k_group_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
-                                             t.flags.as<int>());
-  eb_count_launch(ctx);
-  tb = t.cubtmp.bytes;
-  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.flags.as<int>(), t.scan.as<int>(), nl, st));
-  eb_count_launch(ctx);
-  k_tile_count<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
-                                            t.tcount.as<int>());
-  eb_count_launch(ctx);
-  tb = t.cubtmp.bytes;
-  EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.tcount.as<int>(), t.tstart.as<int>(), nl, st));
-  eb_count_launch(ctx);
-  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[0], t.flags.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[1], t.scan.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[2], t.tcount.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[3], t.tstart.as<int>() + nl - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+  for (DevBuf* d : {&t.ucnt, &t.wcnt, &t.tcount, &t.gcount})
+    EB_CUDA_TRY(cudaMemsetAsync(d->p, 0, sizeof(int) * (NB + 1), st));
+  k_leaf_lists<false><<<nblk(NBi, 128), 128, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
+                                                       t.blev.as<unsigned char>(), lo, t.child0.as<int>(),
+                                                       t.nchild.as<int>(), t.ucnt.as<int>(), t.wcnt.as<int>(),
+                                                       nullptr, nullptr, nullptr, nullptr, lerr_d);
+  k_group_count<<<nblk(NBi, BS), BS, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                              t.gcount.as<int>());
+  k_tile_count<<<nblk(NBi, BS), BS, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                             t.tcount.as<int>());
+  ctx->launches += 3;
+  {
+    size_t need = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, need, t.ucnt.as<int>(), t.ustart.as<int>(), NBi + 1, st);
+    if (need > t.cubtmp.bytes) EB_TRY(t.cubtmp.ensure(need));
+  }
+  for (auto pr : {std::make_pair(&t.ucnt, &t.ustart), std::make_pair(&t.wcnt, &t.wstart),
+                  std::make_pair(&t.gcount, &t.gstart), std::make_pair(&t.tcount, &t.tstart)}) {
+    tb = t.cubtmp.bytes;
+    EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, pr.first->as<int>(), pr.second->as<int>(), NBi + 1, st));
+    eb_count_launch(ctx);
+  }
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[0], nleaf_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[1], t.gstart.as<int>() + NBi, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[2], t.tstart.as<int>() + NBi, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[3], t.ustart.as<int>() + NBi, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[4], t.wstart.as<int>() + NBi, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->last[5], lerr_d, sizeof(int), cudaMemcpyDeviceToHost, st));
   t.nchunk = 0;
   t.chunk_lmin = n <= (1 << 18) ? 2 : std::max(2, L - EB_DIRECT_LEVELS + 1);
-  const int cfirst = t.lev_off[t.chunk_lmin], nb2 = t.nbox - cfirst;
-  if (L >= 2) {
+  const int cfirst = t.lev_off[std::min(2, L + 1)], nb2 = t.nbox - cfirst;
+  if (L >= 2 && nb2 > 0) {
     EB_TRY(t.ccount.ensure(sizeof(int) * (size_t)nb2));
     EB_TRY(t.cstart.ensure(sizeof(int) * (size_t)(nb2 + 1)));
     EB_TRY(t.cdone.ensure(sizeof(int) * (size_t)nb2));
     EB_CUDA_TRY(cudaMemsetAsync(t.cdone.p, 0, sizeof(int) * (size_t)nb2, st));
-    k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(cfirst, nb2, t.pt0.as<int>(), t.pt1.as<int>(), t.ccount.as<int>());
+    k_chunk_count<<<nblk(nb2, BS), BS, 0, st>>>(cfirst, nb2, t.chunk_lmin, t.blev.as<unsigned char>(),
+                                                t.nchild.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                                t.ccount.as<int>());
     eb_count_launch(ctx);
     size_t need = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, need, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st);
@@ -617,50 +802,66 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     tb = t.cubtmp.bytes;
     EB_CUDA_TRY(cub::DeviceScan::ExclusiveSum(t.cubtmp.p, tb, t.ccount.as<int>(), t.cstart.as<int>(), nb2, st));
     eb_count_launch(ctx);
-    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[4], t.ccount.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[5], t.cstart.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[6], t.ccount.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(&H->last[7], t.cstart.as<int>() + nb2 - 1, sizeof(int), cudaMemcpyDeviceToHost, st));
   }
   EB_CUDA_TRY(cudaStreamSynchronize(st));
-  t.ngroup = H->last[0] + H->last[1];
-  t.ntile = H->last[2] + H->last[3];
+  if (H->last[5]) {
+    eb_set_last_error_msg("tree build: interaction-list traversal deeper than its stack");
+    return EB_ERR_WORKSPACE;
+  }
+  const int nl = H->last[0];
+  t.nleaf = nl;
+  t.ngroup = H->last[1];
+  t.ntile = H->last[2];
+  t.nu = H->last[3];
+  t.nw = H->last[4];
+  // 9. fill the lists and work items
+  EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nu, 1)));
+  EB_TRY(t.wlist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nw, 1)));
+  k_leaf_lists<true><<<nblk(nl, 128), 128, 0, st>>>(nl, nullptr, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
+                                                     t.blev.as<unsigned char>(), lo, t.child0.as<int>(),
+                                                     t.nchild.as<int>(), nullptr, nullptr, t.ustart.as<int>(),
+                                                     t.wstart.as<int>(), t.ulist.as<int>(), t.wlist.as<int>(),
+                                                     lerr_d);
+  eb_count_launch(ctx);
   EB_TRY(t.gleaf.ensure(sizeof(int) * (size_t)t.ngroup));
   EB_TRY(t.gfirst.ensure(sizeof(int) * (size_t)t.ngroup));
-  k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.flags.as<int>(),
-                                            t.scan.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
+  k_group_fill<<<nblk(nl, BS), BS, 0, st>>>(nl, t.leaves.as<int>(), t.pt0.as<int>(), t.gcount.as<int>(),
+                                            t.gstart.as<int>(), t.gleaf.as<int>(), t.gfirst.as<int>());
   eb_count_launch(ctx);
   EB_TRY(t.tiles.ensure(sizeof(int4) * (size_t)t.ntile));
-  k_tile_fill<<<nblk(nl, BS), BS, 0, st>>>(t.lev_off[L], nl, t.pt0.as<int>(), t.pt1.as<int>(),
+  k_tile_fill<<<nblk(nl, BS), BS, 0, st>>>(nl, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
                                            t.tcount.as<int>(), t.tstart.as<int>(), t.tiles.as<int4>());
   eb_count_launch(ctx);
-  if (L >= 2) {
-    EB_TRY(t.anc.ensure(sizeof(int) * (size_t)t.nleaf * (L - 1)));
-    k_ancestors<<<nblk(t.nleaf, BS), BS, 0, st>>>(t.lev_off[L], t.nleaf, L - 1, t.parent.as<int>(),
-                                                  t.anc.as<int>());
-    eb_count_launch(ctx);
-    t.nchunk = H->last[4] + H->last[5];
+  EB_TRY(t.anc.ensure(sizeof(int) * (size_t)nl * EB_FAR_LEVELS));
+  k_far_boxes<<<nblk(nl, BS), BS, 0, st>>>(nl, t.leaves.as<int>(), t.blev.as<unsigned char>(), t.parent.as<int>(),
+                                           t.lend, t.anc.as<int>());
+  eb_count_launch(ctx);
+  if (L >= 2 && nb2 > 0) {
+    t.nchunk = H->last[6] + H->last[7];
     EB_CUDA_TRY(cudaMemcpyAsync(t.cstart.as<int>() + nb2, &t.nchunk, sizeof(int), cudaMemcpyHostToDevice, st));
-    EB_TRY(t.chunk_box.ensure(sizeof(int) * (size_t)t.nchunk));
+    EB_TRY(t.chunk_box.ensure(sizeof(int) * (size_t)std::max(t.nchunk, 1)));
     k_chunk_fill<<<nblk(nb2, BS), BS, 0, st>>>(cfirst, nb2, t.ccount.as<int>(), t.cstart.as<int>(),
                                                t.chunk_box.as<int>());
     eb_count_launch(ctx);
   }
-  // 9. leaf-relative coordinates for the double-float near field
+  // 10. leaf-relative coordinates for the double-float kernels and the FP32 P2M / far field
   EB_TRY(t.wdf.ensure(sizeof(float4) * (size_t)n));
   EB_TRY(t.wdf_lo.ensure(sizeof(float2) * (size_t)n));
-  k_leaf_coords<<<t.nleaf, 64, 0, st>>>(t.lev_off[L], t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
-                                        t.pt1.as<int>(), t.zs.as<double2>(), t.x0, t.y0,
-                                        t.W / (double)(1u << L), t.wdf.as<float4>(),
-                                        t.wdf_lo.as<float2>());
+  k_leaf_coords<<<nl, 64, 0, st>>>(t.leaves.as<int>(), t.bkey.as<unsigned long long>(), t.blev.as<unsigned char>(),
+                                   t.pt0.as<int>(), t.pt1.as<int>(), t.zs.as<double2>(), t.x0, t.y0, t.W,
+                                   t.wdf.as<float4>(), t.wdf_lo.as<float2>());
   eb_count_launch(ctx);
-  // 10. pair counts (the algorithmic work of the near field and M2L), copied to the host
-  // without waiting; eb_tree_pairs reads them
-  EB_TRY(t.pairs.ensure(2 * sizeof(unsigned long long)));
+  // 11. pair counts (the algorithmic work of the near field, M2P and M2L), copied to the
+  // host without waiting; eb_tree_pairs reads them
+  EB_TRY(t.pairs.ensure(3 * sizeof(unsigned long long)));
   unsigned long long* cnt = t.pairs.as<unsigned long long>();
-  EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), st));
+  EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
   int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
-  k_pair_counts<<<std::max(nblk(t.nleaf, BS), 1), BS, 0, st>>>(
-      t.lev_off[L], t.nleaf, t.pt0.as<int>(), t.pt1.as<int>(), t.ulist.as<int>(), t.ucount.as<int>(),
-      vfirst, vlast, t.vcount.as<int>(), cnt);
+  k_pair_counts<<<std::max(nblk(nl, BS), 1), BS, 0, st>>>(nl, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
+                                                         t.ustart.as<int>(), t.ulist.as<int>(), t.wstart.as<int>(),
+                                                         vfirst, vlast, t.vcount.as<int>(), cnt);
   eb_count_launch(ctx);
   EB_CUDA_TRY(cudaMemcpyAsync(H->pairs, cnt, sizeof(H->pairs), cudaMemcpyDeviceToHost, st));
   EB_TRY(eb_check_launch(ctx, "tree build"));
@@ -673,6 +874,7 @@ int eb_tree_pairs(eb_ctx* ctx, EbTree& t) {
     EB_CUDA_TRY(cudaStreamSynchronize(eb_stream(ctx)));
     t.u_pairs = (long long)t.host->pairs[0];
     t.v_pairs = (long long)t.host->pairs[1];
+    t.w_pairs = (long long)t.host->pairs[2];
     t.pairs_read = true;
   }
   return EB_OK;

@@ -56,8 +56,8 @@ enum eb_solve_mode { EB_SOLVE_FP64 = 0, EB_SOLVE_FP32_REFINED = 1 };
 typedef struct eb_opts {
   int p64;          /* FP64 expansion order (0: default 44)                    */
   int p32;          /* FP32 expansion order (0: default 20)                    */
-  int leaf64;       /* target mean points per occupied leaf, FP64 (0: 32)      */
-  int leaf32;       /* target mean points per occupied leaf, FP32 (0: 32)      */
+  int leaf64;       /* maximum points per leaf of the adaptive tree (0: 32)    */
+  int leaf32;       /* reserved (0)                                            */
   double tol64;     /* M2L per-offset truncation tolerance, FP64 (0: 1e-15)    */
   double tol32;     /* M2L per-offset truncation tolerance, FP32 (0: 1e-7)     */
   int maxl;         /* GMRES Krylov dimension, MAXL (0: 100, electric.f:1011)  */
@@ -89,12 +89,13 @@ typedef struct eb_solve_info {
 
 typedef struct eb_tree_info {
   int npoints;      /* points in the tree                                     */
-  int levels;       /* leaf level L (root is level 0)                         */
-  int nboxes;       /* occupied boxes over all levels                         */
-  int nleaves;      /* occupied leaves                                        */
+  int levels;       /* deepest leaf level (root is level 0)                   */
+  int nboxes;       /* boxes over all levels                                  */
+  int nleaves;      /* leaves (on any level)                                  */
   long long v_pairs;/* M2L (source box, target box) pairs                     */
   long long u_pairs;/* near-field (target point, source point) pairs          */
   int p;            /* expansion order of the last apply                      */
+  long long w_pairs;/* M2P (W-list box, target point) evaluations             */
 } eb_tree_info;
 
 /* Physical parameters of the RK right-hand side F (electric.f:968-1109), the values the
