@@ -32,7 +32,7 @@ class EbError(RuntimeError):
 
 class Opts(ctypes.Structure):
     _fields_ = [("p64", ctypes.c_int), ("p32", ctypes.c_int), ("leaf64", ctypes.c_int),
-                ("leaf32", ctypes.c_int), ("tol64", ctypes.c_double), ("tol32", ctypes.c_double),
+                ("leaf_cap", ctypes.c_int), ("tol64", ctypes.c_double), ("tol32", ctypes.c_double),
                 ("maxl", ctypes.c_int), ("gmres_tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
                 ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int),
@@ -110,6 +110,7 @@ SIGNATURES = {
     "eb_rk_f": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo), _I]),
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
                          _I]),
+    "eb_batch_define": (_I, [_P, _I, _P, _P]),
     "eb_bubbin_read": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _P]),
     "eb_geoinit": (_I, [_I, _P, _P, _P, _P, _P, _P]),
     "eb_dumpdata": (_I, [ctypes.c_char_p, _I, _P, _D, _D, _P, _P, _P]),

@@ -63,13 +63,13 @@ def _host(a, dtype):
 class Context:
     """One GPU context: geometry, trees, expansion work space and a CUDA stream."""
 
-    def __init__(self, p64=0, p32=0, leaf64=0, leaf32=0, tol64=0.0, tol32=0.0, maxl=0,
+    def __init__(self, p64=0, p32=0, leaf64=0, leaf_cap=0, tol64=0.0, tol32=0.0, maxl=0,
                  gmres_tol=0.0, inner_tol=0.0, max_outer=0, device=0, graphs=0, df64=0,
                  resid_df=0):
         self._lib = _lib.load()
         o = Opts()
         self._lib.eb_opts_default(ctypes.byref(o))
-        for name, v in (("p64", p64), ("p32", p32), ("leaf64", leaf64), ("leaf32", leaf32),
+        for name, v in (("p64", p64), ("p32", p32), ("leaf64", leaf64), ("leaf_cap", leaf_cap),
                         ("tol64", tol64), ("tol32", tol32), ("maxl", maxl),
                         ("gmres_tol", gmres_tol), ("inner_tol", inner_tol),
                         ("max_outer", max_outer), ("graphs", graphs), ("df64", df64),
@@ -137,6 +137,17 @@ class Context:
         t = TreeInfo()
         check("eb_ctx_tree_info", self._lib.eb_ctx_tree_info(self._h, ctypes.byref(t)))
         return t.as_dict()
+
+    def batch_define(self, sim_k, e0=None):
+        """Make the context hold independent simulations: simulation s is the next
+        sim_k[s] drops of every geometry installed from now on, with its own E0 (e0[s]).
+        An empty sim_k returns to one simulation."""
+        sim_k = _host(sim_k, np.int32)
+        e = None if e0 is None else _host(e0, np.float64)
+        check("eb_batch_define", self._lib.eb_batch_define(
+            self._h, int(sim_k.shape[0]), _ptr(sim_k) if sim_k.shape[0] else None,
+            _ptr(e) if e is not None else None))
+        self._batch_keep = (sim_k, e)
 
     # ---- geometry ------------------------------------------------------------
     def set_geometry(self, nd, z, dz, dsda, kappa, zk):

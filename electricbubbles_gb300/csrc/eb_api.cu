@@ -163,7 +163,7 @@ void eb_opts_default(eb_opts* o) {
   o->p64 = 44;
   o->p32 = 20;
   o->leaf64 = 32;
-  o->leaf32 = 32;
+  o->leaf_cap = EB_LEAF_CAP;
   o->tol64 = 1e-15;
   o->tol32 = 1e-7;
   o->maxl = 100;
@@ -194,7 +194,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.p64 <= 0) o.p64 = d.p64;
     if (o.p32 <= 0) o.p32 = d.p32;
     if (o.leaf64 <= 0) o.leaf64 = d.leaf64;
-    if (o.leaf32 <= 0) o.leaf32 = d.leaf32;
+    if (o.leaf_cap <= 0) o.leaf_cap = d.leaf_cap;
     if (o.tol64 <= 0) o.tol64 = d.tol64;
     if (o.tol32 <= 0) o.tol32 = d.tol32;
     if (o.maxl <= 0) o.maxl = d.maxl;
@@ -254,6 +254,7 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->ev_near0) cudaEventDestroy(ctx->ev_near0);
   if (ctx->ev_near1) cudaEventDestroy(ctx->ev_near1);
   for (GmGraph& g : ctx->gcache) g.destroy();
+  if (ctx->b_host_act) cudaFreeHost(ctx->b_host_act);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
@@ -364,7 +365,13 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
                                              ctx->drop_of.as<int>(), ctx->z.as<double2>(),
                                              ctx->zk.as<double2>(), ctx->pkw.as<double2>());
   eb_count_launch(ctx);
-  EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64));
+  if (ctx->nsim > 0) {
+    // a batch: the tree is a forest of the simulations moved into their own cells
+    EB_TRY(eb_batch_install(ctx));
+    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->zt.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap, ctx->b_sq, ctx->b_R));
+  } else {
+    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap));
+  }
   ctx->tree_pv.valid = false;
   ctx->geom_valid = true;
   ctx->geom_version++;
@@ -414,7 +421,7 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   EbPost post{1, dens, nullptr, ctx->z.as<double2>(), ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                ctx->pc1.as<double>(), ctx->pc2.as<double2>(), ctx->drop_of.as<int>(),
                ctx->za.as<double2>(), ctx->pk.as<double>(), y, ctx->pc1f.as<float>(),
-               ctx->pc2f.as<float2>()};
+               ctx->pc2f.as<float2>(), ctx->nsim > 0 ? ctx->b_pinf.as<int>() : nullptr};
   EB_TRY(eb_fmm_apply(ctx, ctx->tree, 0, -1, prec, dens, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                       nullptr, &post, ctx->ev_join));
   return eb_check_launch(ctx, "stokes matvec");
@@ -427,7 +434,7 @@ int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   // FMM's charge kernel from u (EbPost::u)
   EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->hpt.as<double>(),
                ctx->plap.as<double>(), nullptr, nullptr, nullptr, nullptr, y, ctx->plapf.as<float>(),
-               nullptr};
+               nullptr, nullptr};
   EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree, prec, nullptr, nullptr, &post));
   return eb_check_launch(ctx, "laplace matvec");
 }
@@ -509,7 +516,7 @@ int eb_cauchy_sum(eb_ctx* ctx, int n, const double* z, const double* q, double* 
     qd = ctx->pvq.as<double2>();
     fd = ctx->pvout.as<double2>();
   }
-  EB_TRY(eb_tree_build(ctx, ctx->tree_tmp, zd, n, ctx->opts.leaf64));
+  EB_TRY(eb_tree_build(ctx, ctx->tree_tmp, zd, n, ctx->opts.leaf64, ctx->opts.leaf_cap));
   EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree_tmp, prec, qd, fd));
   if (mem == EB_HOST) {
     EB_CUDA_TRY(cudaMemcpyAsync(field, fd, sizeof(double2) * n, cudaMemcpyDeviceToHost, s));

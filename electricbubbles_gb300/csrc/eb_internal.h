@@ -53,9 +53,11 @@ struct EbTreeHost {
   unsigned long long pairs[3];  // near-field, V-list and W-list (M2P) pair counts
 };
 
-// Adaptive quadtree over a point set, built on the GPU. A box is split while it holds
-// more than `cap` points (DAASSI's rule, dapif1.f:1165-1255, with NAPB = cap); only
-// boxes whose parent is split exist, so leaves lie on any level up to L. Boxes of level
+// Adaptive quadtree over a point set, built on the GPU. Every box above a minimum level
+// is split (for one problem the shallowest level of mean occupancy at most the leaf
+// target; for a forest the level of its cells), and below it a box is split while it
+// holds more than `cap` points (DAASSI's rule, dapif1.f:1165-1255, with NAPB = cap);
+// only boxes whose parent is split exist, so leaves lie on any level up to L. Boxes of level
 // l are stored in Morton order in the global box range [lev_off[l], lev_off[l+1]);
 // every box owns a contiguous range of the sorted points, and the leaves, in point
 // order, partition them.
@@ -63,6 +65,8 @@ struct EbTree {
   int n = 0;
   int L = 0;                 // deepest leaf level
   int cap = 32;              // points per leaf at most (unless at the deepest key level)
+  int R = 0;                 // a forest of independent problems: the boxes of level R hold
+                             // one problem each and no interaction list crosses them
   int nbox = 0;
   int nleaf = 0;
   int lend = 2;              // FP32 far field: levels <= lend hold L2L-accumulated locals
@@ -126,7 +130,7 @@ struct EbTree {
 #define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
 #define EB_FAR_LEVELS 6     // finest levels whose FP32 locals are evaluated at each target
                             // directly (coarser levels reach them by L2L)
-#define EB_LEAF_CAP 32      // default maximum points per leaf
+#define EB_LEAF_CAP 64      // default maximum points per leaf
 
 // Per-precision constant tables for the translation operators.
 struct EbTables {
@@ -167,6 +171,7 @@ struct GmGraph {
   void destroy();
 };
 #define EB_GRAPH_CACHE 4
+#define EB_GM_MAXL 126
 
 struct eb_ctx {
   eb_opts opts;
@@ -228,14 +233,38 @@ struct eb_ctx {
   cudaEvent_t ev_c = nullptr, ev_p2p = nullptr;  // FMM: near field forked after the charges
   GmGraph gcache[EB_GRAPH_CACHE];
   int gcache_next = 0;
+
+  // a batch of independent simulations (eb_batch_define; nsim = 0: one problem)
+  int nsim = 0;
+  std::vector<int> sim_k;          // drops per simulation
+  std::vector<double> sim_e0;      // E0 per simulation
+  bool sim_has_e0 = false;
+  std::vector<int> sim_node0;      // first node of each simulation (nsim + 1)
+  DevBuf b_sim_of_drop, b_pinf, b_e0, b_alpha, b_seg1, b_seg2, b_sim_of_node, b_box, b_shift;
+  DevBuf zt;                       // nodes moved into their simulation's cell of the forest
+  int b_R = 0;                     // the forest's cells are the boxes of level b_R
+  double b_sq[3] = {1, 0, 0};      // the forest's root square (W, x0, y0)
+  DevBuf b_G, b_CS, b_ctl, b_misc; // batched GMRES state
+  int* b_host_act = nullptr;       // page-locked counters read back per Arnoldi step
 };
+
+typedef int (*eb_op_fn)(eb_ctx*, const double*, double*, int);
+
+// batch.cu
+int eb_batch_install(eb_ctx* ctx);
+int eb_batch_translate_fine(eb_ctx* ctx, double2* zf);
+int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* rhs, double* soln, int mode,
+                   eb_solve_info* info, int mem);
 
 // Precision of the refined solver's FP64 residual applies (and of the refined RK stage's
 // other FP64 sums): double-float when eb_opts.resid_df is on, else EB_FP64.
 inline int eb_resid_prec(const eb_ctx* ctx) { return ctx->opts.resid_df > 0 ? EB_PREC_DF : EB_FP64; }
 
 // tree.cu
-int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_cap);
+// root_sq (W, x0, y0) and root_level: an explicit root square whose boxes of level
+// root_level each hold one independent problem (null: the bounding square, one problem)
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target, int leaf_cap,
+                  const double* root_sq = nullptr, int root_level = 0);
 // The tree's pair counts (u_pairs, v_pairs), waiting for the build if it is in flight.
 int eb_tree_pairs(eb_ctx* ctx, EbTree& t);
 

@@ -19,6 +19,8 @@ struct EbPost {
   double* y;              // kind 1: complex w (interleaved); kind 2: real w
   const float* c1f;       // float copies of c1 and c2 for the FP32 operator
   const float2* c2f;
+  const int* pinf_drop;   // kind 1: per drop, the drop whose pressure is pinf (the first
+                          // drop of its simulation); null: drop 0
 };
 
 // Per-node coefficients of the post-processing, formed once per geometry (they hold the
@@ -53,7 +55,7 @@ __device__ __forceinline__ void eb_post_store_f32(const EbPost& P, int t, float2
     const float c1 = P.c1f[t];
     const float2 c2 = P.c2f[t];
     const float2 zself = make_float2(c1 * u.x - (u.x * c2.x + u.y * c2.y), c1 * u.y - (u.x * c2.y - u.y * c2.x));
-    const float pinf = -(float)P.pk[0];
+    const float pinf = -(float)P.pk[P.pinf_drop ? P.pinf_drop[b] : 0];
     const float pkb = (float)P.pk[b] + pinf;
     const float f = -0.5f * (pinf - pkb);
     const double2 zz = P.z[t];
@@ -80,7 +82,7 @@ __device__ __forceinline__ void eb_post_store(const EbPost& P, int t, double2 g,
     const double c1 = P.c1[t];
     // zself = c1 u - c1 conj(u) n^2
     const double2 zself = csub<double>(cscale<double>(u, c1), cmul<double>(cconj<double>(u), P.c2[t]));
-    const double pinf = -P.pk[0];
+    const double pinf = -P.pk[P.pinf_drop ? P.pinf_drop[b] : 0];
     const double pkb = P.pk[b] + pinf;
     const double f = -0.5 * (pinf - pkb);  // times i z
     const double2 zz = P.z[t];

@@ -369,7 +369,6 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
 // of once per Krylov step. Operator launches depend only on the installed geometry,
 // so a captured graph is reused until the geometry or a work buffer changes.
 // =================================================================================
-#define EB_GM_MAXL 126
 
 struct GmCtl {
   int ll;         // Krylov column the next Arnoldi step produces (DPIGMR's LL)
@@ -839,6 +838,8 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
 
 int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mode,
           eb_solve_info* info, int mem) {
+  if (ctx->nsim > 0)  // a batch of simulations: GMRES per simulation, in lockstep
+    return eb_batch_solve(ctx, n, op, op == eb_stokes_matvec_dev, rhs, soln, mode, info, mem);
   cudaStream_t s = ctx->stream;
   Gm g{ctx, n, std::min(nblk(n, RBS), rmaxb(ctx)), s, nullptr};
   const int maxl = ctx->opts.maxl;

@@ -353,7 +353,13 @@ int pvintev_dev(eb_ctx* ctx, const double2* uc, double2* phi, int prec) {
                                       ctx->pvz.as<double2>(), ctx->pvq.as<double2>(), nmax,
                                       need_tree ? 1 : 0);
   eb_count_launch(ctx);
-  if (need_tree) EB_TRY(eb_tree_build(ctx, ctx->tree_pv, ctx->pvz.as<double2>(), 2 * nbk, ctx->opts.leaf64));
+  if (need_tree && ctx->nsim > 0) {
+    EB_TRY(eb_batch_translate_fine(ctx, ctx->pvz.as<double2>()));
+    EB_TRY(eb_tree_build(ctx, ctx->tree_pv, ctx->pvz.as<double2>(), 2 * nbk, ctx->opts.leaf64, ctx->opts.leaf_cap, ctx->b_sq,
+                         ctx->b_R));
+  } else if (need_tree) {
+    EB_TRY(eb_tree_build(ctx, ctx->tree_pv, ctx->pvz.as<double2>(), 2 * nbk, ctx->opts.leaf64, ctx->opts.leaf_cap));
+  }
   EB_TRY(eb_fmm_apply_cauchy(ctx, ctx->tree_pv, prec, ctx->pvq.as<double2>(), ctx->pvout.as<double2>()));
   k_pv_extract<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->pvout.as<double2>(), phi);
   eb_count_launch(ctx);
@@ -591,11 +597,14 @@ __device__ void spectral_int(double2* a, int n) {
 __global__ void k_setvelf(const int* __restrict__ start, const double2* __restrict__ z,
                           const double2* __restrict__ dz, const double* __restrict__ dsda,
                           const double* __restrict__ dphi, double cap, double e0,
-                          double alpha_stale, double2* __restrict__ rhs, int nmax) {
+                          double alpha_stale, const double* __restrict__ e0_drop,
+                          const double* __restrict__ alpha_drop, double2* __restrict__ rhs, int nmax) {
   extern __shared__ double2 sm[];
   __shared__ double2 s_c0, s_f0;
   int b = blockIdx.x;
   int i0 = start[b], n = start[b + 1] - i0;
+  if (e0_drop) e0 = e0_drop[b];  // a batch: the drop's simulation's E0 and last-drop alpha
+  if (alpha_drop) alpha_stale = alpha_drop[b];
   double2* a = sm;
   double2* tw = sm + nmax;
   make_twiddles(tw, n);
@@ -637,7 +646,9 @@ int setvelf_dev(eb_ctx* ctx, const double* dphi, double cap, double e0, double2*
   EB_TRY(set_smem((const void*)k_setvelf, sm));
   k_setvelf<<<ctx->k, SBS, sm, ctx->stream>>>(ctx->start.as<int>(), ctx->z.as<double2>(),
                                               ctx->dz.as<double2>(), ctx->dsda.as<double>(), dphi,
-                                              cap, e0, alpha_stale, rhs, nmax);
+                                              cap, e0, alpha_stale,
+                                              ctx->nsim > 0 && ctx->sim_has_e0 ? ctx->b_e0.as<double>() : nullptr,
+                                              ctx->nsim > 0 ? ctx->b_alpha.as<double>() : nullptr, rhs, nmax);
   eb_count_launch(ctx);
   return eb_check_launch(ctx, "setvelf");
 }

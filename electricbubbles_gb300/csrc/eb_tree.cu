@@ -5,9 +5,10 @@
 // not (DOINT0DR, cadapdrop2.f:84-197). Here the nodes are sorted once by a Morton key
 // at depth 20; the occupied boxes of every level are then the distinct key prefixes,
 // each owning a contiguous range of the sorted nodes. Only occupied boxes exist.
-// The tree is adaptive: a box with more than `leaf_cap` points is split (DAASSI,
-// dapif1.f:1165-1255, with NAPB = leaf_cap), every point's leaf level following from
-// the number of points between it and the point leaf_cap places on. V lists follow MKINTL
+// The tree is adaptive: below a uniform floor (the shallowest level of mean occupancy at
+// most `leaf_target`), a box with more than `leaf_cap` points is split (DAASSI,
+// dapif1.f:1165-1255, with NAPB = leaf_cap); every point's leaf level follows from the
+// keys of the points leaf_cap places before and after it in sorted order. V lists follow MKINTL
 // (cadap2.f:780-828: children of the parent's neighbours that are not adjacent, at most
 // 27); the leaves' U and W lists follow DALI12/DALI34 (dapif2.f:3-356) for leaves of
 // different levels.
@@ -100,6 +101,15 @@ __global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __rest
   sq[3] = __ddiv_rn((double)(1u << EB_KEY_LEVELS), w);
 }
 
+// An explicit root square (a forest of independent problems in a grid of cells).
+__global__ void k_set_square(double W, double x0, double y0, double* __restrict__ sq) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  sq[0] = W;
+  sq[1] = x0;
+  sq[2] = y0;
+  sq[3] = __ddiv_rn((double)(1u << EB_KEY_LEVELS), W);
+}
+
 __global__ void k_keys(const double2* __restrict__ z, int n, const double* __restrict__ sq,
                        unsigned long long* __restrict__ keys, int* __restrict__ idx) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -124,6 +134,40 @@ __global__ void k_gather_points(const double2* __restrict__ z, const int* __rest
   zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
 }
 
+// Histogram of the first level at which consecutive sorted keys fall in different boxes:
+// the occupied boxes of level l in a uniform tree number 1 + sum_{l' <= l} hist[l'].
+__global__ void k_level_hist(const unsigned long long* __restrict__ keys, int n, int* __restrict__ hist) {
+  __shared__ int sh[EB_KEY_LEVELS + 1];
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long x = keys[i] ^ keys[i - 1];
+    if (x == 0) continue;
+    const int hb = 63 - __clzll((long long)x);
+    atomicAdd(&sh[EB_KEY_LEVELS - hb / 2], 1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// The minimum leaf level: for one problem the shallowest level whose occupied boxes
+// hold at most `target` points on average (a uniform floor, which keeps leaves of one
+// level, and so no W lists, wherever the points are evenly spread), for a forest the
+// level of its cells.
+__global__ void k_pick_level(int n, int target, int R, const int* __restrict__ hist, int* __restrict__ lmin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int L0 = EB_KEY_LEVELS, nb = 1;
+  for (int l = 0; l <= EB_KEY_LEVELS; ++l) {
+    if (l > 0) nb += hist[l];
+    if ((double)n / nb <= (double)target) {
+      L0 = l;
+      break;
+    }
+  }
+  *lmin = R > 0 ? R : L0;
+}
+
 // Levels shared by the keys a and b: the deepest level whose box holds both
 // (EB_KEY_LEVELS when the keys are equal, -1 never: the root holds every point).
 __device__ __forceinline__ int shared_levels(unsigned long long a, unsigned long long b) {
@@ -145,12 +189,13 @@ __global__ void k_lcp_window(const unsigned long long* __restrict__ keys, int n,
 
 // Leaf level of every sorted point: one more than the deepest level whose box around the
 // point holds more than cap points, at most EB_KEY_LEVELS (coincident points), 0 when
-// n <= cap. Also the deepest leaf level and the number of boxes of every level l >= 1:
+// n <= cap, and at least lmin (k_pick_level). Also the deepest leaf level and the number of boxes of every level l >= 1:
 // a point starts a box of level l when l <= its leaf level and its key differs from the
 // previous point's at level l.
 __global__ void k_leaf_level(const unsigned long long* __restrict__ keys, int n, int cap,
-                             const unsigned char* __restrict__ lcpw, unsigned char* __restrict__ plev,
-                             int* __restrict__ lmax, int* __restrict__ hist) {
+                             const int* __restrict__ lmin_d, const unsigned char* __restrict__ lcpw,
+                             unsigned char* __restrict__ plev, int* __restrict__ lmax, int* __restrict__ hist) {
+  const int lmin = *lmin_d;
   __shared__ int sh[EB_KEY_LEVELS + 1];
   __shared__ int smax;
   for (int i = threadIdx.x; i <= EB_KEY_LEVELS; i += blockDim.x) sh[i] = 0;
@@ -165,6 +210,7 @@ __global__ void k_leaf_level(const unsigned long long* __restrict__ keys, int n,
       for (int w = w0; w <= w1; ++w) m = max(m, (int)lcpw[w]);
       lam = min(EB_KEY_LEVELS, m + 1);
     }
+    lam = max(lam, lmin);
     plev[i] = (unsigned char)lam;
     mymax = max(mymax, lam);
     const int sl = i > 0 ? shared_levels(keys[i - 1], keys[i]) : -1;
@@ -191,7 +237,7 @@ __global__ void k_heads_all(const unsigned long long* __restrict__ keys, const u
 
 // Box key, level, first point and parent of every box; a box whose head point also starts
 // its parent is the parent's first child (a split box's points all lie in its children).
-__global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, int L,
+__global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, int L, int nbox,
                             const int* __restrict__ flags, const int* __restrict__ scan,
                             unsigned long long* __restrict__ bkey, unsigned char* __restrict__ blev,
                             int* __restrict__ pt0, int* __restrict__ parent, int* __restrict__ child0) {
@@ -201,6 +247,7 @@ __global__ void k_boxes_all(const unsigned long long* __restrict__ keys, int n, 
     if (!flags[idx]) continue;
     const int l = (int)(idx / n), i = (int)(idx - (long long)l * n);
     const int b = scan[idx];
+    if (b >= nbox) continue;  // cannot happen: the flags and the level counts agree
     bkey[b] = keys[i] >> (2 * (EB_KEY_LEVELS - l));
     blev[b] = (unsigned char)l;
     pt0[b] = i;
@@ -256,7 +303,7 @@ __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ b
 // children of the parent's neighbours that are not adjacent to the box; DALI12's list 1,
 // dapif2.f:3-171). Only existing boxes are found, so the children of a neighbour that is
 // a leaf are absent: its points reach the box's leaves through their U lists.
-__global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo, int first, int nbox,
+__global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo, int first, int nbox, int R,
                         int* __restrict__ vlist, unsigned char* __restrict__ vcode,
                         int* __restrict__ vcount) {
   const int gid = first + blockIdx.x * blockDim.x + threadIdx.x;
@@ -265,6 +312,11 @@ __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo,
   while (gid >= lo.v[lev + 1]) ++lev;
   const int off = lo.v[lev], nb = lo.v[lev + 1] - off;
   unsigned long long key = bkey[gid];
+  if (lev <= R) {  // a forest's boxes of level <= R hold different problems
+    vcount[gid] = 0;
+    return;
+  }
+  const unsigned long long root = key >> (2 * (lev - R));
   int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
   int px = ix >> 1, py = iy >> 1, half = 1 << (lev - 1), side = 1 << lev;
   int cnt = 0;
@@ -279,7 +331,7 @@ __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo,
           if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) continue;
           if (sx >= side || sy >= side) continue;
           int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
-          if (s < 0) continue;
+          if (s < 0 || (bkey[s] >> (2 * (lev - R))) != root) continue;
           vlist[(size_t)gid * EB_VMAX + cnt] = s;
           vcode[(size_t)gid * EB_VMAX + cnt] = (unsigned char)((dy + 3) * 7 + (dx + 3));
           ++cnt;
@@ -324,8 +376,9 @@ __global__ void k_leaf_count(int n, const int* __restrict__ lflag, const int* __
 // Every pair of points is then covered exactly once by U, W or a V list of a common
 // level. FILL = false counts, FILL = true writes at ustart / wstart.
 template <bool FILL>
-__global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves, const unsigned long long* __restrict__ bkey,
-                             const unsigned char* __restrict__ blev, LevOffT lo,
+__global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves,
+                             const unsigned long long* __restrict__ bkey,
+                             const unsigned char* __restrict__ blev, LevOffT lo, int R,
                              const int* __restrict__ child0, const int* __restrict__ nchild,
                              int* __restrict__ ucnt, int* __restrict__ wcnt,
                              const int* __restrict__ ustart, const int* __restrict__ wstart,
@@ -336,6 +389,7 @@ __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const i
   const int b = leaves[t], l = blev[b];
   const unsigned long long kb = bkey[b];
   const int ix = (int)compact2(kb), iy = (int)compact2(kb >> 1);
+  const unsigned long long root = kb >> (2 * (l - R));  // the leaf's problem (R <= l)
   int nu = 0, nw = 0;
   int* uo = FILL ? ulist + ustart[t] : nullptr;
   int* wo = FILL ? wlist + wstart[t] : nullptr;
@@ -346,7 +400,7 @@ __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const i
       const int sx = ix + dx, sy = iy + dy;
       if (sx < 0 || sy < 0 || sx >= side || sy >= side) continue;
       const int C = find_box(bkey, lo.v[l], lo.v[l + 1] - lo.v[l], morton((unsigned)sx, (unsigned)sy));
-      if (C < 0) continue;
+      if (C < 0 || (bkey[C] >> (2 * (l - R))) != root) continue;
       if (nchild[C] == 0) {
         if (FILL) uo[nu] = C;
         ++nu;
@@ -375,7 +429,7 @@ __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const i
       }
     }
   }
-  for (int m = l - 1; m >= 0; --m) {
+  for (int m = l - 1; m >= R; --m) {
     const int ax = ix >> (l - m), ay = iy >> (l - m), sm = 1 << m;
     for (int dy = -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
@@ -383,7 +437,7 @@ __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const i
         const int sx = ax + dx, sy = ay + dy;
         if (sx < 0 || sy < 0 || sx >= sm || sy >= sm) continue;
         const int N = find_box(bkey, lo.v[m], lo.v[m + 1] - lo.v[m], morton((unsigned)sx, (unsigned)sy));
-        if (N < 0 || nchild[N] != 0) continue;
+        if (N < 0 || nchild[N] != 0 || (bkey[N] >> (2 * (m - R))) != root) continue;
         if (FILL) uo[nu] = N;
         ++nu;
       }
@@ -599,13 +653,16 @@ __global__ void k_leaf_coords(const int* __restrict__ leaves, const unsigned lon
   }
 }
 
-int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap) {
+int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target, int leaf_cap,
+                  const double* root_sq, int root_level) {
   cudaStream_t st = eb_stream(ctx);
   t.valid = false;
   if (n <= 0) return EB_ERR_ARG;
+  if (leaf_target < 1) leaf_target = 32;
   if (leaf_cap < 1) leaf_cap = EB_LEAF_CAP;
   t.n = n;
   t.cap = leaf_cap;
+  t.R = root_sq ? root_level : 0;
   const int BS = 256;
   if (!t.host) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&t.host), sizeof(EbTreeHost)));
   EbTreeHost* H = t.host;
@@ -613,16 +670,18 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   // 1. bounding square, on the device
   int nbb = std::min(nblk(n, BS), 1024);
   EB_TRY(t.partial.ensure(sizeof(Box4) * (size_t)nbb));
-  EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(double) * 4 + sizeof(int) * 4));
+  EB_TRY(t.bbox.ensure(sizeof(Box4) + sizeof(double) * 4 + sizeof(int) * 8));
   double* sq = reinterpret_cast<double*>(t.bbox.as<char>() + sizeof(Box4));
   int* bad = reinterpret_cast<int*>(sq + 4);
   int* lmax_d = bad + 1;
   int* lerr_d = bad + 2;
   int* nleaf_d = bad + 3;
+  int* lmin_d = bad + 4;
   EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int) * 3, st));
   k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
   eb_count_launch(ctx);
-  k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
+  if (root_sq) k_set_square<<<1, 32, 0, st>>>(root_sq[0], root_sq[1], root_sq[2], sq);
+  else k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
   eb_count_launch(ctx);
   // 2. keys and sort (a non-finite coordinate gives clamped keys; reported below)
   EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
@@ -653,11 +712,15 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   EB_TRY(t.plev.ensure((size_t)n));
   EB_TRY(t.hist.ensure(sizeof(int) * (EB_KEY_LEVELS + 1)));
   EB_CUDA_TRY(cudaMemsetAsync(t.hist.p, 0, sizeof(int) * (EB_KEY_LEVELS + 1), st));
+  k_level_hist<<<std::min(nblk(n, BS), ctx->nsm * 4), BS, 0, st>>>(keys, n, t.hist.as<int>());
+  k_pick_level<<<1, 32, 0, st>>>(n, leaf_target, t.R, t.hist.as<int>(), lmin_d);
+  EB_CUDA_TRY(cudaMemsetAsync(t.hist.p, 0, sizeof(int) * (EB_KEY_LEVELS + 1), st));
+  ctx->launches += 2;
   if (n > leaf_cap) {
     k_lcp_window<<<nblk(n - leaf_cap, BS), BS, 0, st>>>(keys, n, leaf_cap, t.lcpw.as<unsigned char>());
     eb_count_launch(ctx);
   }
-  k_leaf_level<<<std::min(nblk(n, BS), ctx->nsm * 8), BS, 0, st>>>(keys, n, leaf_cap, t.lcpw.as<unsigned char>(),
+  k_leaf_level<<<std::min(nblk(n, BS), ctx->nsm * 8), BS, 0, st>>>(keys, n, leaf_cap, lmin_d, t.lcpw.as<unsigned char>(),
                                                                   t.plev.as<unsigned char>(), lmax_d,
                                                                   t.hist.as<int>());
   eb_count_launch(ctx);
@@ -704,7 +767,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   EB_CUDA_TRY(cudaMemsetAsync(t.child0.p, 0xff, sizeof(int) * NB, st));  // -1: no children
   EB_CUDA_TRY(cudaMemsetAsync(t.nchild.p, 0, sizeof(int) * NB, st));
   k_boxes_all<<<std::min(nblk((long long)nflag, BS), ctx->nsm * 16), BS, 0, st>>>(
-      keys, n, L, t.flags.as<int>(), t.scan.as<int>(), t.bkey.as<unsigned long long>(),
+      keys, n, L, t.nbox, t.flags.as<int>(), t.scan.as<int>(), t.bkey.as<unsigned long long>(),
       t.blev.as<unsigned char>(), t.pt0.as<int>(), t.parent.as<int>(), t.child0.as<int>());
   eb_count_launch(ctx);
   k_boxes_fin<<<nblk(t.nbox, BS), BS, 0, st>>>(t.nbox, keys, n, t.bkey.as<unsigned long long>(),
@@ -732,7 +795,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   EB_CUDA_TRY(cudaMemsetAsync(t.vcount.p, 0, sizeof(int) * NB, st));
   if (L >= 2) {
     const int first = t.lev_off[2];
-    k_vlist<<<nblk(t.nbox - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox,
+    k_vlist<<<nblk(t.nbox - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox, t.R,
                                                        t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                                        t.vcount.as<int>());
     eb_count_launch(ctx);
@@ -759,7 +822,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   for (DevBuf* d : {&t.ucnt, &t.wcnt, &t.tcount, &t.gcount})
     EB_CUDA_TRY(cudaMemsetAsync(d->p, 0, sizeof(int) * (NB + 1), st));
   k_leaf_lists<false><<<nblk(NBi, 128), 128, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
-                                                       t.blev.as<unsigned char>(), lo, t.child0.as<int>(),
+                                                       t.blev.as<unsigned char>(), lo, t.R, t.child0.as<int>(),
                                                        t.nchild.as<int>(), t.ucnt.as<int>(), t.wcnt.as<int>(),
                                                        nullptr, nullptr, nullptr, nullptr, lerr_d);
   k_group_count<<<nblk(NBi, BS), BS, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
@@ -820,7 +883,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap)
   EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nu, 1)));
   EB_TRY(t.wlist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nw, 1)));
   k_leaf_lists<true><<<nblk(nl, 128), 128, 0, st>>>(nl, nullptr, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
-                                                     t.blev.as<unsigned char>(), lo, t.child0.as<int>(),
+                                                     t.blev.as<unsigned char>(), lo, t.R, t.child0.as<int>(),
                                                      t.nchild.as<int>(), nullptr, nullptr, t.ustart.as<int>(),
                                                      t.wstart.as<int>(), t.ulist.as<int>(), t.wlist.as<int>(),
                                                      lerr_d);

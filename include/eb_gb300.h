@@ -56,8 +56,8 @@ enum eb_solve_mode { EB_SOLVE_FP64 = 0, EB_SOLVE_FP32_REFINED = 1 };
 typedef struct eb_opts {
   int p64;          /* FP64 expansion order (0: default 44)                    */
   int p32;          /* FP32 expansion order (0: default 20)                    */
-  int leaf64;       /* maximum points per leaf of the adaptive tree (0: 32)    */
-  int leaf32;       /* reserved (0)                                            */
+  int leaf64;       /* tree: mean points per leaf of its uniform floor (0: 32)  */
+  int leaf_cap;     /* tree: maximum points per leaf below the floor (0: 64)   */
   double tol64;     /* M2L per-offset truncation tolerance, FP64 (0: 1e-15)    */
   double tol32;     /* M2L per-offset truncation tolerance, FP32 (0: 1e-7)     */
   int maxl;         /* GMRES Krylov dimension, MAXL (0: 100, electric.f:1011)  */
@@ -252,6 +252,21 @@ int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup,
  * state never leaves device memory. */
 int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar,
                 const eb_model* model, eb_stage_info* info, int mem);
+
+/* Many independent simulations in one context; no counterpart in the reference, which
+ * advances one simulation per process (electric.f:134-251). After eb_batch_define, the
+ * drops of every geometry the context installs (eb_set_geometry, eb_extractdat, eb_rk_f,
+ * eb_rk2_step) form nsim simulations, simulation s holding the next sim_k[s] drops, and
+ *  - no layer sum mixes simulations (the FMM tree is a forest with one cell per
+ *    simulation);
+ *  - eb_stokes_solve and eb_laplace_solve run GMRES per simulation (its own Krylov space
+ *    and stopping test; the simulations iterate in lockstep in the same launches); the
+ *    info holds the largest iteration count, residual and IERR over the simulations;
+ *  - FASMVP's far-field pressure is that of each simulation's first drop, and SETVELF
+ *    takes E0 per simulation (e0[s]; NULL: the eb_model's e0 for all) and the alpha of
+ *    each simulation's last drop (stokesbubb.f:125).
+ * nsim = 0 returns the context to one simulation. */
+int eb_batch_define(eb_ctx* ctx, int nsim, const int* sim_k, const double* e0);
 
 /* Input deck and checkpoint files of the reference (host only, no context).
  * eb_bubbin_read: the first deck of a `bubbin` file as READINI reads it
