@@ -463,9 +463,7 @@ int bg_cycle(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bo
   int* hact = ctx->b_host_act;
   int j = 0;
   for (; j < B.maxl; ++j) {
-    // the operator reads its input in one contiguous buffer
-    EB_CUDA_TRY(cudaMemcpyAsync(B.xin, B.V + (size_t)j * ldv, sizeof(double) * B.n, cudaMemcpyDeviceToDevice, st));
-    EB_TRY(op(ctx, B.xin, B.w, prec));
+    EB_TRY(op(ctx, B.V + (size_t)j * ldv, B.w, prec));
     EB_CUDA_TRY(cudaMemsetAsync(B.nact, 0, sizeof(int), st));
     k_bg_arnoldi<<<B.S, BBS, 0, st>>>(j, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact);
     eb_count_launch(ctx);
@@ -500,7 +498,7 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
   EB_TRY(ctx->b_G.ensure(sizeof(double) * (size_t)S * (maxl + 1)));
   EB_TRY(ctx->b_CS.ensure(sizeof(double) * (size_t)S * 2 * maxl));
   EB_TRY(ctx->b_ctl.ensure(sizeof(BCtl) * (size_t)S));
-  EB_TRY(ctx->b_misc.ensure(sizeof(int) * 4 + sizeof(int) * (size_t)S + sizeof(double) * 5 * (size_t)S));
+  EB_TRY(ctx->b_misc.ensure(sizeof(int) * (6 + (size_t)S) + sizeof(double) * 5 * (size_t)S));
   EB_TRY(ctx->gWbuf.ensure(sizeof(double) * n));
   EB_TRY(ctx->gXin.ensure(sizeof(double) * n));
   EB_TRY(ctx->gR.ensure(sizeof(double) * n));
