@@ -369,51 +369,36 @@ def run_gpu(args, rank, world, local):
     r, info = rk_rate(single, "fp64", 20)
     rk["single_drop_n256/fp64"] = {"steps_per_s": r, "last_step": info}
 
-    # independent single-drop simulations of uneven sizes (N in [128, 4096], E0 U[0.1, 1]),
-    # FP32-refined RK2 steps: a bounded sample (the first 32 of the 256 seeded
-    # simulations, 4 steps each), on one context, then on 8 contexts with their own
-    # streams driven by host threads
-    import threading
-    sims = configs.uneven_simulations()[:32]
-    steps_per_sim = 4
-
-    def run_sims(nctx):
-        ctxs = [Context(device=local, graphs=graphs) for _ in range(nctx)]
-        strs = [torch.cuda.Stream(device=dev) for _ in range(nctx)]
-        for c, s_ in zip(ctxs, strs):
-            c.set_stream(s_.cuda_stream)
-        states = [torch.from_numpy(sm.rku()).to(dev) for sm in sims]
-        torch.cuda.synchronize()
-        err = []
-
-        def worker(w):
-            try:
-                for j in range(w, len(sims), nctx):
-                    for _ in range(steps_per_sim):
-                        ctxs[w].rk2(sims[j].nd, 1e-3, states[j], e0=sims[j].params["E0"],
-                                    mode="fp32_refined")
-            except Exception as exc:  # reported in the JSON line
-                err.append(repr(exc))
-
-        t0 = time.perf_counter()
-        th = [threading.Thread(target=worker, args=(w,)) for w in range(nctx)]
-        for x_ in th:
-            x_.start()
-        for x_ in th:
-            x_.join()
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        for c in ctxs:
-            c.close()
-        return len(sims) * steps_per_sim / wall, err
-
-    run_sims(8)  # warm-up: graph capture and buffers
-    sim_rate1, e1 = run_sims(1)
-    sim_rate8, e8 = run_sims(8)
-    uneven = {"workload": "uneven_simulations (first 32 of 256, seed 4)", "steps_per_sim": steps_per_sim,
-              "nodes": [int(sm.nbk) for sm in sims], "mode": "fp32_refined",
-              "sim_steps_per_s_1ctx": sim_rate1, "sim_steps_per_s_8ctx": sim_rate8,
-              "errors": e1 + e8}
+    # the 256 independent single-drop simulations of uneven sizes (N log-uniform in
+    # [128, 4096], E0 U[0.1, 1], seed 4) as one batch in one context: every kernel
+    # launch covers all simulations, GMRES per simulation; 50 FP32-refined RK2 steps
+    # (dt = 1e-3), timed on the device after one untimed step
+    sims = configs.uneven_simulations()
+    bnd = np.concatenate([sm.nd for sm in sims])
+    be0 = np.array([sm.params["E0"] for sm in sims])
+    by = torch.from_numpy(np.concatenate([sm.rku() for sm in sims])).to(dev)
+    bctx = Context(device=local, graphs=graphs)
+    bctx.set_stream(stream.cuda_stream)
+    bctx.batch_define([sm.k for sm in sims], be0)
+    uneven_steps = 50
+    binfo = bctx.rk2(bnd, 1e-3, by, mode="fp32_refined")
+    torch.cuda.synchronize()
+    ea_, eb2_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ea_.record(stream)
+    l0 = bctx.launch_count()
+    for _ in range(uneven_steps):
+        binfo = bctx.rk2(bnd, 1e-3, by, mode="fp32_refined")
+    eb2_.record(stream)
+    torch.cuda.synchronize()
+    bms = ea_.elapsed_time(eb2_)
+    uneven = {"workload": "uneven_simulations_256 (N log-uniform in [128, 4096], seed 4)",
+              "simulations": len(sims), "nodes": int(bnd.sum()), "steps": uneven_steps, "mode": "fp32_refined",
+              "batched": "one context, one launch per kernel for all simulations, GMRES per simulation",
+              "ms_per_step": bms / uneven_steps,
+              "sim_steps_per_s": len(sims) * uneven_steps / (bms * 1e-3),
+              "launches_per_step": (bctx.launch_count() - l0) / uneven_steps,
+              "last_step": binfo, "tree": bctx.tree_info()}
+    bctx.close()
 
     # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
     big = configs.large_drops()
@@ -449,9 +434,12 @@ def run_gpu(args, rank, world, local):
             import oracle as O
             ncores = O.max_threads()
             times, _, xr = cpu_reference_solves(cfg, 2, ncores)
+            # the reference is serial: one solve on one thread as well
+            times1, _, _ = cpu_reference_solves(cfg, 1, 1)
             cpu = {"value": 2 / sum(times), "unit": "solves/s", "cores": ncores, "kind": "port",
                    "sample": "2 full Stokes solves of the 64x512 workload with the restated "
                              "CADAPDR FMM + SLATEC GMRES",
+                   "value_1thread": 1 / sum(times1),
                    "gpu_vs_cpu_solution_rel": float(np.linalg.norm(x.cpu().numpy() - xr) / np.linalg.norm(xr))}
         except Exception as exc:  # the baseline must not hide the GPU result
             cpu = {"value": None, "unit": "solves/s", "cores": ncores, "kind": "port",

@@ -36,7 +36,19 @@ class Opts(ctypes.Structure):
                 ("maxl", ctypes.c_int), ("gmres_tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
                 ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int),
-                ("resid_df", ctypes.c_int)]
+                ("resid_df", ctypes.c_int), ("m2l_tc", ctypes.c_int)]
+
+
+class TuneInfo(ctypes.Structure):
+    _fields_ = [("leaf64", ctypes.c_int), ("leaf_cap", ctypes.c_int), ("ncand", ctypes.c_int),
+                ("leaf_target", ctypes.c_int * 8), ("leaf_cap_cand", ctypes.c_int * 8),
+                ("apply_us", ctypes.c_double * 8)]
+
+    def as_dict(self):
+        k = self.ncand
+        return {"leaf64": self.leaf64, "leaf_cap": self.leaf_cap,
+                "candidates": [{"leaf64": self.leaf_target[i], "leaf_cap": self.leaf_cap_cand[i],
+                                "apply_us": self.apply_us[i]} for i in range(k)]}
 
 
 class SolveInfo(ctypes.Structure):
@@ -111,6 +123,7 @@ SIGNATURES = {
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
                          _I]),
     "eb_batch_define": (_I, [_P, _I, _P, _P]),
+    "eb_autotune": (_I, [_P, ctypes.POINTER(TuneInfo)]),
     "eb_bubbin_read": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _P]),
     "eb_geoinit": (_I, [_I, _P, _P, _P, _P, _P, _P]),
     "eb_dumpdata": (_I, [ctypes.c_char_p, _I, _P, _D, _D, _P, _P, _P]),

@@ -174,6 +174,7 @@ void eb_opts_default(eb_opts* o) {
   o->graphs = 1;
   o->df64 = -1;
   o->resid_df = 1;
+  o->m2l_tc = -1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -204,6 +205,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.graphs == 0) o.graphs = d.graphs;
     if (o.df64 == 0) o.df64 = d.df64;
     if (o.resid_df == 0) o.resid_df = d.resid_df;
+    if (o.m2l_tc == 0) o.m2l_tc = d.m2l_tc;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {
@@ -365,16 +367,24 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
                                              ctx->drop_of.as<int>(), ctx->z.as<double2>(),
                                              ctx->zk.as<double2>(), ctx->pkw.as<double2>());
   eb_count_launch(ctx);
-  if (ctx->nsim > 0) {
-    // a batch: the tree is a forest of the simulations moved into their own cells
-    EB_TRY(eb_batch_install(ctx));
-    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->zt.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap, ctx->b_sq, ctx->b_R));
-  } else {
-    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap));
-  }
-  ctx->tree_pv.valid = false;
+  if (ctx->nsim > 0) EB_TRY(eb_batch_install(ctx));  // a batch: nodes moved into their cells
+  EB_TRY(eb_geom_tree(ctx));
   ctx->geom_valid = true;
   ctx->geom_version++;
+  eb_devbuf_collect();
+  return EB_OK;
+}
+
+// The node tree of the installed geometry (a forest for a batch of simulations), and
+// the hash of everything a captured solve graph takes from it by value.
+int eb_geom_tree(eb_ctx* ctx) {
+  const int nbk = ctx->nbk;
+  if (ctx->nsim > 0)
+    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->zt.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap,
+                         ctx->b_sq, ctx->b_R));
+  else
+    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap));
+  ctx->tree_pv.valid = false;
   {
     const EbTree& t = ctx->tree;
     unsigned long long h = 1469598103934665603ull;  // FNV-1a over the fields' bytes
@@ -390,7 +400,6 @@ int eb_set_geometry(eb_ctx* ctx, int k, const int* nd, const double* z, const do
     mix(dbl, sizeof(dbl));
     ctx->geom_shape = h;
   }
-  eb_devbuf_collect();
   return EB_OK;
 }
 

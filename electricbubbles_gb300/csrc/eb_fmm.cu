@@ -1803,7 +1803,12 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     if (sm > 48 * 1024)
       EB_CUDA_TRY(cudaFuncSetAttribute(k_m2l<T, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     ProfScope ps(ctx, 1, st);
-    if (nt > 0 && sizeof(T) == 4 && p == 20) {
+    if (nt > 0 && sizeof(T) == 4 && p == 20 && ctx->opts.m2l_tc > 0) {
+      EB_TRY(eb_m2l_tc(ctx, E, first, nt, t.vlist.as<int>(), t.vcode.as<unsigned char>(), t.vcount.as<int>(),
+                       reinterpret_cast<const float*>(tb.binom.p), ldb, reinterpret_cast<const float2*>(tb.dinv.p),
+                       tb.pd.as<int>(), reinterpret_cast<const float2*>(w.mpole.p),
+                       reinterpret_cast<float2*>(w.local.p), st));
+    } else if (nt > 0 && sizeof(T) == 4 && p == 20) {
       k_m2l_f32p<E, 20><<<nt, 128, 0, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                             t.vcount.as<int>(), reinterpret_cast<const float*>(tb.binom.p), ldb,
                                             reinterpret_cast<const float2*>(tb.dinv.p), tb.pd.as<int>(),

@@ -130,7 +130,7 @@ struct EbTree {
 #define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
 #define EB_FAR_LEVELS 6     // finest levels whose FP32 locals are evaluated at each target
                             // directly (coarser levels reach them by L2L)
-#define EB_LEAF_CAP 64      // default maximum points per leaf
+#define EB_LEAF_CAP 96      // default maximum points per leaf
 
 // Per-precision constant tables for the translation operators.
 struct EbTables {
@@ -285,6 +285,14 @@ int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q,
 int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw, int prec);
 int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
 int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
+
+// m2l_tc.cu: the FP32 M2L of order 20 on the tensor cores
+int eb_m2l_tc(eb_ctx* ctx, int E, int first, int ntarget, const int* vlist, const unsigned char* vcode,
+              const int* vcount, const float* binom, int ldb, const float2* dinv, const int* pd,
+              const float2* mpole, float2* local, cudaStream_t st);
+
+// api.cu: (re)build the installed geometry's tree with the current eb_opts
+int eb_geom_tree(eb_ctx* ctx);
 
 // api.cu helpers
 cudaStream_t eb_stream(eb_ctx* ctx);

@@ -57,7 +57,7 @@ typedef struct eb_opts {
   int p64;          /* FP64 expansion order (0: default 44)                    */
   int p32;          /* FP32 expansion order (0: default 20)                    */
   int leaf64;       /* tree: mean points per leaf of its uniform floor (0: 32)  */
-  int leaf_cap;     /* tree: maximum points per leaf below the floor (0: 64)   */
+  int leaf_cap;     /* tree: maximum points per leaf below the floor (0: 96)   */
   double tol64;     /* M2L per-offset truncation tolerance, FP64 (0: 1e-15)    */
   double tol32;     /* M2L per-offset truncation tolerance, FP32 (0: 1e-7)     */
   int maxl;         /* GMRES Krylov dimension, MAXL (0: 100, electric.f:1011)  */
@@ -75,6 +75,8 @@ typedef struct eb_opts {
   int resid_df;     /* refined mode: the FP64 residual of every refinement step (and
                        the refined RK stage's PV and velocity sums) in double-float
                        arithmetic: 0 default (on), 1 on, -1 off (native FP64)   */
+  int m2l_tc;       /* FP32 M2L (order 20) as a 3xTF32 contraction on the tensor
+                       cores (tcgen05): 0 default (off), 1 on, -1 off          */
 } eb_opts;
 
 typedef struct eb_solve_info {
@@ -144,6 +146,21 @@ long long eb_ctx_launch_count(eb_ctx* ctx);
 int eb_ctx_set_profiling(eb_ctx* ctx, int enable);
 int eb_ctx_kernel_time(eb_ctx* ctx, int kernel_class, long long* launches, double* total_ms);
 int eb_ctx_tree_info(eb_ctx* ctx, eb_tree_info* info);
+/* Autotuner of the tree's leaf sizes for the installed geometry; no counterpart in the
+ * reference (its leaf rule is fixed: LEVMAX = 7 in CADAPDR, NAPB = 30 in DAPIF2). Each
+ * candidate (eb_opts.leaf64, eb_opts.leaf_cap) is installed and the FP32 Stokes operator,
+ * the refined solver's inner operator, is timed on the GPU; the fastest is kept in the
+ * context's options (and used by later installs) and reported in info. */
+#define EB_TUNE_MAX 8
+typedef struct eb_tune_info {
+  int leaf64, leaf_cap;           /* the chosen leaf sizes                         */
+  int ncand;                      /* candidates timed                              */
+  int leaf_target[EB_TUNE_MAX];   /* candidate i: eb_opts.leaf64                   */
+  int leaf_cap_cand[EB_TUNE_MAX]; /* candidate i: eb_opts.leaf_cap                 */
+  double apply_us[EB_TUNE_MAX];   /* candidate i: microseconds per FP32 apply      */
+} eb_tune_info;
+int eb_autotune(eb_ctx* ctx, eb_tune_info* info);
+
 /* FP64 FMA throughput of the context's GPU in TFLOP/s (a short calibration kernel):
  * the roofline denominator of the FP64 FMM kernels. No counterpart in the reference. */
 int eb_measure_fp64_peak(eb_ctx* ctx, double* tflops);

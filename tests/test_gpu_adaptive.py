@@ -2,8 +2,8 @@
 
 A small dense drop (4,096 nodes on a circle of radius 0.1) sits among unit drops of 128
 nodes: a uniform-depth tree would give it leaves of hundreds of points (quadratic near
-field), while the adaptive tree (boxes split while they hold more than the leaf cap,
-DAASSI, dapif1.f:1165-1255) refines only there. Leaves of different levels then meet,
+field), while the adaptive tree (below its uniform floor, boxes split while they hold
+more than the leaf cap, DAASSI, dapif1.f:1165-1255) refines only there. Leaves of different levels then meet,
 so the U lists hold leaves of other levels (evaluated directly) and the W lists boxes
 below the leaf's level (evaluated from their multipoles, M2P), which every sum here
 exercises. Tolerances as in the other parity tests: FP64 1e-12, FP32 1e-5 relative to
@@ -56,9 +56,8 @@ def test_stokes_sum_multiscale(ctxs, oracle, case, sign):
     assert relmax(ctxs["native"].stokes_sum(dens, sign, "fp32"), ref) < 1e-5
     t = ctxs["native"].tree_info()
     assert t["w_pairs"] > 0  # the W lists are exercised
-    # the dense drop's leaves lie deeper than the unit drops' ones: leaves hold at most
-    # the cap (32) points, so the tree's deepest level exceeds what a uniform tree of
-    # mean occupancy 32 would use
+    # the dense drop's leaves lie deeper than the unit drops' ones and hold at most the
+    # leaf cap (96) points, so its near field is far below the all-pairs count
     assert t["u_pairs"] < 0.25 * cfg.nbk * cfg.nd[0]
 
 
@@ -95,3 +94,23 @@ def test_solve_multiscale(ctxs, oracle):
         got, info = ctx.solvei(rhs, mode)
         assert info["ierr"] == 0 and info["err"] <= 1e-10, mode
         assert relmax(got, ref) < 1e-9, mode
+
+
+def test_autotune_picks_a_candidate_and_keeps_parity(gpu_ctx_factory, oracle):
+    """eb_autotune times the FP32 operator for every leaf-size candidate on the installed
+    geometry and keeps the fastest; the operators are as accurate afterwards."""
+    cfg = configs.many_drops(16, 256, seed=11, box=8.0)
+    ctx = gpu_ctx_factory()
+    ctx.extractdat(cfg.nd, cfg.rku())
+    t = ctx.autotune()
+    cands = t["candidates"]
+    assert len(cands) >= 4 and all(c["apply_us"] > 0 for c in cands)
+    best = min(cands, key=lambda c: c["apply_us"])
+    assert (t["leaf64"], t["leaf_cap"]) == (best["leaf64"], best["leaf_cap"])
+    g = oracle.Geometry.from_extract(cfg.nd, oracle.extractdat(cfg.nd, cfg.rku()))
+    u = np.random.default_rng(53).standard_normal(2 * cfg.nbk)
+    ref = oracle.fasmvp(g, u, 0)
+    assert relmax(ctx.fasmvp(u, "fp64"), ref) < 1e-12
+    assert relmax(ctx.fasmvp(u, "fp32"), ref) < 1e-5
+    got, info = ctx.solvei(u, "fp32_refined")
+    assert info["ierr"] == 0 and info["err"] <= 1e-10
