@@ -123,6 +123,8 @@ SIGNATURES = {
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
                          _I]),
     "eb_batch_define": (_I, [_P, _I, _P, _P]),
+    "eb_getfourier": (_I, [_P, _I, _P, _P, _P, _P, _I]),
+    "eb_double": (_I, [_P, _I, _P, _P, _P, _P, _I]),
     "eb_autotune": (_I, [_P, ctypes.POINTER(TuneInfo)]),
     "eb_bubbin_read": (_I, [ctypes.c_char_p, _I, _P, _P, _P, _P]),
     "eb_geoinit": (_I, [_I, _P, _P, _P, _P, _P, _P]),

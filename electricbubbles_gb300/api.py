@@ -138,6 +138,29 @@ class Context:
         check("eb_ctx_tree_info", self._lib.eb_ctx_tree_info(self._h, ctypes.byref(t)))
         return t.as_dict()
 
+    def getfourier(self, nd, rku):
+        """GETFOURIER per drop: (idoub flags, fmode per drop)."""
+        nd = _host(nd, np.int32)
+        rku = _host(rku, np.float64)
+        k = int(nd.shape[0])
+        idoub = np.zeros(k, np.int32)
+        fmode = np.zeros(int(nd.sum()))
+        check("eb_getfourier", self._lib.eb_getfourier(self._h, k, _ptr(nd), _ptr(rku), _ptr(idoub),
+                                                      _ptr(fmode), EB_HOST))
+        starts = np.r_[0, np.cumsum(nd)]
+        return idoub, [fmode[a:a + n // 2] for a, n in zip(starts[:-1], nd)]
+
+    def double(self, nd, rku, idoub):
+        """DOUBLE: (new nd, new RK state) with the flagged drops resampled to 2 nd."""
+        nd = _host(nd, np.int32)
+        rku = _host(rku, np.float64)
+        idoub = _host(idoub, np.int32)
+        nd2 = np.where(idoub != 0, 2 * nd, nd).astype(np.int32)
+        out = np.zeros(2 * int(nd2.sum()))
+        check("eb_double", self._lib.eb_double(self._h, int(nd.shape[0]), _ptr(nd), _ptr(rku), _ptr(idoub),
+                                              _ptr(out), EB_HOST))
+        return nd2, out
+
     def autotune(self):
         """Pick the tree's leaf sizes for the installed geometry by timing the FP32
         operator; returns the chosen sizes and every candidate's time."""

@@ -245,6 +245,7 @@ struct eb_ctx {
   int b_R = 0;                     // the forest's cells are the boxes of level b_R
   double b_sq[3] = {1, 0, 0};      // the forest's root square (W, x0, y0)
   DevBuf b_G, b_CS, b_ctl, b_misc; // batched GMRES state
+  DevBuf b_st1, b_st2, b_flag;     // GETFOURIER / DOUBLE: drop starts and flags
   int* b_host_act = nullptr;       // page-locked counters read back per Arnoldi step
 };
 

@@ -221,6 +221,62 @@ __global__ void k_pv_interp(const int* __restrict__ start, const double2* __rest
   }
 }
 
+// GETFOURIER (electric.f:531-570) per drop: c = DCFFTF(z)/nd, fmode_0 = |c_0|,
+// fmode_i = |c_i| + |c_{nd-i}| (i < nd/2), and the doubling test: a mode among the ten
+// below the Nyquist mode (i = nd/2-10 .. nd/2-1) above 1e-11.
+__global__ void k_getfourier(const int* __restrict__ start, const double2* __restrict__ z,
+                             double* __restrict__ fmode, int* __restrict__ idoub, int nmax) {
+  extern __shared__ double2 sm[];
+  __shared__ int s_flag;
+  const int b = blockIdx.x, i0 = start[b], n = start[b + 1] - i0, h = n / 2;
+  double2* a = sm;
+  double2* tw = sm + nmax;
+  make_twiddles(tw, n);
+  if (threadIdx.x == 0) s_flag = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = z[i0 + i];
+  smem_fft(a, n, tw, n, -1);
+  const double inv = 1.0 / (double)n;
+  for (int i = threadIdx.x; i < h; i += blockDim.x) {
+    const double2 c = a[i];
+    double f = hypot(c.x, c.y) * inv;
+    if (i > 0) f += hypot(a[n - i].x, a[n - i].y) * inv;
+    if (fmode) fmode[i0 + i] = f;
+    if (i >= h - 10 && i >= 1 && f > 1e-11) s_flag = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) idoub[b] = s_flag;
+}
+
+// DOUBLE (electric.f:721-757): a flagged drop's nodes resampled to 2 nd points by
+// FINTERC's spectral interpolation (pv_integral.f:276-328: Nyquist mode dropped, the
+// spectrum zero-padded); other drops copied.
+__global__ void k_double(const int* __restrict__ start, const int* __restrict__ start2,
+                         const int* __restrict__ flag, const double2* __restrict__ z,
+                         double2* __restrict__ z2, int nmax) {
+  extern __shared__ double2 sm[];
+  const int b = blockIdx.x, i0 = start[b], n = start[b + 1] - i0, o0 = start2[b];
+  if (!flag[b]) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) z2[o0 + i] = z[i0 + i];
+    return;
+  }
+  const int nf = 2 * n, ny = n / 2;
+  double2* w = sm;              // 2 n
+  double2* tw = sm + 2 * nmax;  // twiddles of the size-2n transform
+  make_twiddles(tw, nf);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = z[i0 + i];
+  smem_fft(w, n, tw, nf, -1);
+  if (threadIdx.x == 0) w[ny] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int m = ny + 1 + threadIdx.x; m < n; m += blockDim.x) w[m + n] = w[m];
+  __syncthreads();
+  for (int m = ny + threadIdx.x; m <= n + ny; m += blockDim.x) w[m] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const double inv = 1.0 / (double)n;
+  for (int m = threadIdx.x; m < nf; m += blockDim.x) w[m] = make_double2(w[m].x * inv, w[m].y * inv);
+  smem_fft(w, nf, tw, nf, +1);
+  for (int m = threadIdx.x; m < nf; m += blockDim.x) z2[o0 + m] = w[m];
+}
+
 // PHICMPLX = -FIELD/(2 pi i) at the even fine nodes (pv_integral.f:194-201).
 __global__ void k_pv_extract(int nbk, const double2* __restrict__ cf, double2* __restrict__ phi) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,6 +479,87 @@ int eb_extractdat(eb_ctx* ctx, int k, const int* nd, const double* rku, double* 
   if (area) EB_CUDA_TRY(cudaMemcpyAsync(area, area_d.p, sizeof(double) * k, ko, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   ctx->ckern_valid = true;
+  return EB_OK;
+}
+
+// Per-drop starts of nd (host) on the device (in `buf`), checking the drop sizes.
+static int drop_starts(eb_ctx* ctx, int k, const int* nd, DevBuf& buf, std::vector<int>& st, int& nmax,
+                       int scale_flags, const int* flags) {
+  st.assign(k + 1, 0);
+  nmax = 0;
+  for (int b = 0; b < k; ++b) {
+    if (nd[b] < 4 || (nd[b] & (nd[b] - 1)) != 0) {
+      eb_set_last_error_msg("spectral routines need power-of-two drop sizes >= 4");
+      return EB_ERR_ARG;
+    }
+    st[b + 1] = st[b] + (scale_flags && flags[b] ? 2 * nd[b] : nd[b]);
+    nmax = std::max(nmax, nd[b]);
+  }
+  EB_TRY(buf.ensure(sizeof(int) * (k + 1)));
+  EB_CUDA_TRY(cudaMemcpyAsync(buf.p, st.data(), sizeof(int) * (k + 1), cudaMemcpyHostToDevice, ctx->stream));
+  return EB_OK;
+}
+
+int eb_getfourier(eb_ctx* ctx, int k, const int* nd, const double* rku, int* idoub, double* fmode, int mem) {
+  if (!ctx || k <= 0 || !nd || !rku || !idoub) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  std::vector<int> st;
+  int nmax = 0;
+  EB_TRY(drop_starts(ctx, k, nd, ctx->b_st1, st, nmax, 0, nullptr));
+  const int nbk = st[k];
+  const double2* zd = reinterpret_cast<const double2*>(rku);
+  if (mem == EB_HOST) {
+    EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, rku, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
+    zd = ctx->vin.as<double2>();
+  }
+  EB_TRY(ctx->vout.ensure(sizeof(double) * nbk + sizeof(int) * (k + 1)));
+  double* fm = ctx->vout.as<double>();
+  int* fl = reinterpret_cast<int*>(fm + nbk);
+  size_t sm = sizeof(double2) * ((size_t)nmax + (size_t)nmax / 2);
+  EB_TRY(set_smem((const void*)k_getfourier, sm));
+  k_getfourier<<<k, SBS, sm, s>>>(ctx->b_st1.as<int>(), zd, fm, fl, nmax);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "getfourier"));
+  if (fmode)
+    EB_CUDA_TRY(cudaMemcpyAsync(fmode, fm, sizeof(double) * nbk,
+                                mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(idoub, fl, sizeof(int) * k, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}
+
+int eb_double(eb_ctx* ctx, int k, const int* nd, const double* rku, const int* idoub, double* rku2, int mem) {
+  if (!ctx || k <= 0 || !nd || !rku || !idoub || !rku2) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  std::vector<int> st, st2;
+  int nmax = 0;
+  EB_TRY(drop_starts(ctx, k, nd, ctx->b_st1, st, nmax, 0, nullptr));
+  EB_TRY(drop_starts(ctx, k, nd, ctx->b_st2, st2, nmax, 1, idoub));
+  const int nbk = st[k], nbk2 = st2[k];
+  EB_TRY(ctx->b_flag.ensure(sizeof(int) * k));
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_flag.p, idoub, sizeof(int) * k, cudaMemcpyHostToDevice, s));
+  const double2* zd = reinterpret_cast<const double2*>(rku);
+  double2* z2 = reinterpret_cast<double2*>(rku2);
+  if (mem == EB_HOST) {
+    EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
+    EB_TRY(ctx->vout.ensure(sizeof(double2) * nbk2));
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, rku, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
+    zd = ctx->vin.as<double2>();
+    z2 = ctx->vout.as<double2>();
+  }
+  size_t sm = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax);
+  EB_TRY(set_smem((const void*)k_double, sm));
+  k_double<<<k, SBS, sm, s>>>(ctx->b_st1.as<int>(), ctx->b_st2.as<int>(), ctx->b_flag.as<int>(), zd, z2, nmax);
+  eb_count_launch(ctx);
+  EB_TRY(eb_check_launch(ctx, "double"));
+  if (mem == EB_HOST)
+    EB_CUDA_TRY(cudaMemcpyAsync(rku2, z2, sizeof(double2) * nbk2, cudaMemcpyDeviceToHost, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
   return EB_OK;
 }
 

@@ -270,6 +270,20 @@ int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup,
 int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar,
                 const eb_model* model, eb_stage_info* info, int mem);
 
+/* The point-doubling policy of the time loop (electric.f:181-219) on the GPU.
+ * eb_getfourier is GETFOURIER (electric.f:531-570) for every drop of the RK state rku
+ * (interleaved x, y; drop sizes nd, powers of two): the Fourier coefficients c of z/nd, and
+ * idoub[b] = 1 (host array of k) when one of the ten modes below drop b's Nyquist mode
+ * has |c_i| + |c_{nd-i}| > 1e-11. fmode (optional, nbk doubles in rku's memory) receives
+ * per drop at its node offset |c_0| and |c_i| + |c_{nd-i}|, i < nd/2.
+ * eb_double is DOUBLE (electric.f:721-757): the drops with idoub[b] = 1 resampled to
+ * 2 nd[b] nodes by FINTERC's spectral interpolation (pv_integral.f:276-328), the others
+ * copied, into rku2 laid out with the new sizes. */
+int eb_getfourier(eb_ctx* ctx, int k, const int* nd, const double* rku, int* idoub, double* fmode,
+                  int mem);
+int eb_double(eb_ctx* ctx, int k, const int* nd, const double* rku, const int* idoub, double* rku2,
+              int mem);
+
 /* Many independent simulations in one context; no counterpart in the reference, which
  * advances one simulation per process (electric.f:134-251). After eb_batch_define, the
  * drops of every geometry the context installs (eb_set_geometry, eb_extractdat, eb_rk_f,
