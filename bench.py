@@ -296,6 +296,22 @@ def run_gpu(args, rank, world, local):
             kern["k_leaf64<2>"] = kentry(leaf_ms, nl, near_pair_flops + 8.0 * p_ord * 2 * tree["npoints"])
             kern["k_m2l<double, 2>"] = kentry(m2l_ms, nm, m2l_flops)
     ctx_df.close()
+    # the FP32 M2L on the tensor cores (tcgen05, 3xTF32) against the CUDA-core M2L
+    ctx_tc = Context(device=local, graphs=graphs, m2l_tc=1)
+    ctx_tc.set_stream(stream.cuda_stream)
+    ctx_tc.extractdat(cfg.nd, cfg.rku())
+    ctx_tc.set_profiling(True)
+    for _ in range(10):
+        ctx_tc.fasmvp(u, "fp32", out=y)
+    ntc, tc_ms = ctx_tc.kernel_time(1)
+    ctx_tc.set_profiling(False)
+    kern["k_m2l_tc<2> (tcgen05)"] = kentry(tc_ms, ntc, 2 * 8.0 * 20 * 20 * tree["v_pairs"])
+    ms_tc, _, _ = timed("fp32_refined", args.steps, args.warmup, ctx_tc)
+    m2l_ab = {"k_m2l_f32p_us": 1e3 * kern["k_m2l_f32p<2, 20>"]["avg_launch_ms"],
+              "k_m2l_tc_us": 1e3 * tc_ms / max(ntc, 1),
+              "refined_solves_per_s_tc": world * args.steps / (ms_tc * 1e-3),
+              "kept": "CUDA-core k_m2l_f32p (eb_opts.m2l_tc off by default)"}
+    ctx_tc.close()
     for name, k in kern.items():
         if name in ("k_leaf64<2>", "k_m2l<double, 2>"):
             k["peak_tflops"] = fp64_peak
@@ -478,6 +494,7 @@ def run_gpu(args, rank, world, local):
                                     "CUDA-core figure)",
                      "flops_per_launch": dom["flops_per_launch"], "avg_launch_ms": dom["avg_launch_ms"]},
         "kernels": kern,
+        "m2l_tensor_ab": m2l_ab,
         "peaks_measured_in_run": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
         "cpu_baseline": cpu,
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "solves/s",

@@ -39,6 +39,7 @@ constexpr int TC_A_BYTES = TC_ROWS * TC_K * 4;  // 12 KiB
 constexpr int TC_B_BYTES = TC_N * TC_K * 4;     // 3 KiB
 constexpr int TC_LD = 33;                        // epilogue staging row stride (floats)
 constexpr long long TC_WAIT_LIMIT = 1ll << 22;
+constexpr int TC_PARTS = 3;                      // epilogue threads per output (3 x 42 <= 128)
 
 // byte offset of element (row, k) in the blocked K-major layout
 __device__ __forceinline__ int tc_off(int row, int k) {
@@ -130,26 +131,35 @@ __global__ void __launch_bounds__(128) k_m2l_tc(int first, int ntarget, const in
       s_pd[tid] = pdv[code];
     }
     __syncthreads();
-    // A: row 4j + q, q = Re / Im of a_phi, Re / Im of a_psi of entry j; k-1 in columns
-    for (int idx = tid; idx < TC_ROWS * TC_K; idx += 128) {
-      const int row = idx / TC_K, kk = idx - row * TC_K;
-      const int j = row >> 2, q = row & 3;
-      float v = 0.f;
-      if (j < nv && q < 2 * E && kk < s_pd[j]) {
+    // A: row 4j + q, q = Re / Im of a_phi, Re / Im of a_psi of entry j; k-1 in columns.
+    // One thread per (entry, k) forms both expansions' a_k and writes its four rows.
+    for (int idx = tid; idx < (TC_ROWS / 4) * TC_K; idx += 128) {
+      const int j = idx / TC_K, kk = idx - j * TC_K;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (j < nv && kk < s_pd[j]) {
         const int code = s_code[j], k = kk + 1;
         const float2* ms = mpole + (size_t)s_src[j] * E * TC_P;
         const float2 sc = dinv[(size_t)code * ldd + k];
-        float2 mv = ms[(q >> 1) * TC_P + kk];
-        if (q >= 2 && k >= 2) {
-          const float dxr = (float)(code % 7 - 3), dyr = (float)(code / 7 - 3);
-          cfma<float>(mv, make_float2(-dxr * (float)(k - 1), dyr * (float)(k - 1)), ms[kk - 1]);
+        const float2 a = cmul<float>(ms[kk], sc);
+        v[0] = a.x;
+        v[1] = a.y;
+        if (E == 2) {
+          float2 mv = ms[TC_P + kk];
+          if (k >= 2) {
+            const float dxr = (float)(code % 7 - 3), dyr = (float)(code / 7 - 3);
+            cfma<float>(mv, make_float2(-dxr * (float)(k - 1), dyr * (float)(k - 1)), ms[kk - 1]);
+          }
+          const float2 b = cmul<float>(mv, sc);
+          v[2] = b.x;
+          v[3] = b.y;
         }
-        const float2 a = cmul<float>(mv, sc);
-        v = (q & 1) ? a.y : a.x;
       }
-      const float h = tf32_round(v);
-      *reinterpret_cast<float*>(sAh + tc_off(row, kk)) = h;
-      *reinterpret_cast<float*>(sAl + tc_off(row, kk)) = tf32_round(v - h);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float h = tf32_round(v[q]);
+        *reinterpret_cast<float*>(sAh + tc_off(4 * j + q, kk)) = h;
+        *reinterpret_cast<float*>(sAl + tc_off(4 * j + q, kk)) = tf32_round(v[q] - h);
+      }
     }
     // make the generic-proxy stores visible to the tensor cores' (async) proxy
     asm volatile("fence.proxy.async.shared::cta;");
@@ -205,17 +215,26 @@ __global__ void __launch_bounds__(128) k_m2l_tc(int first, int ntarget, const in
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    // L_m = sum_j (-1)^m d_j^-m (b_re + i b_im), m <= pd_j, entries in order
-    if (tid < E * ldl) {
-      const int e = tid / ldl, m = tid - e * ldl;
+    // L_m = sum_j (-1)^m d_j^-m (b_re + i b_im), m <= pd_j: each output's entries are
+    // split over TC_PARTS threads (every TC_PARTS-th entry), their sums added in order
+    float2* spart = reinterpret_cast<float2*>(sAh);  // A is consumed: reuse it
+    if (tid < TC_PARTS * E * ldl) {
+      const int part = tid / (E * ldl), o = tid - part * (E * ldl);
+      const int e = o / ldl, m = o - e * ldl;
       float2 acc = make_float2(0.f, 0.f);
-      for (int j = 0; j < nv; ++j) {
+      for (int j = part; j < nv; j += TC_PARTS) {
         if (m > s_pd[j]) continue;
         float2 post = dinv[(size_t)s_code[j] * ldd + m];
         if (m & 1) post = make_float2(-post.x, -post.y);
         const float2 b = make_float2(sD[(4 * j + 2 * e) * TC_LD + m], sD[(4 * j + 2 * e + 1) * TC_LD + m]);
         cfma<float>(acc, post, b);
       }
+      spart[tid] = acc;
+    }
+    __syncthreads();
+    if (tid < E * ldl) {
+      float2 acc = spart[tid];
+      for (int part = 1; part < TC_PARTS; ++part) acc = cadd<float>(acc, spart[part * E * ldl + tid]);
       local[(size_t)gid * E * ldl + tid] = acc;
     }
     __syncthreads();
