@@ -240,6 +240,23 @@ def run_gpu(args, rank, world, local):
     launches = timed.launches
     rel_diff = float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
 
+    # Laplace solves (SOLVE_LAPL, laplace.f:335-425) on the same geometry, GETBCs' -2 Re z
+    rl = torch.from_numpy(np.ascontiguousarray(-2.0 * np.ascontiguousarray(geo["z"]).real)).to(dev)
+    xl = torch.empty_like(rl)
+    lap = {}
+    for mode in ("fp64", "fp32_refined"):
+        for _ in range(args.warmup):
+            ctx.solve_lapl(rl, mode, out=xl)
+        torch.cuda.synchronize()
+        ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea0.record(stream)
+        for _ in range(args.steps):
+            _, linfo = ctx.solve_lapl(rl, mode, out=xl)
+        ea1.record(stream)
+        torch.cuda.synchronize()
+        lap[mode + "_solves_per_s"] = world * args.steps / (ea0.elapsed_time(ea1) * 1e-3)
+        lap[mode + "_info"] = linfo
+
     # FMM Mpts/s: single Stokes operator applies, FP64 and FP32
     u = torch.randn(n, dtype=torch.float64, device=dev)
     y = torch.empty_like(u)
@@ -452,10 +469,18 @@ def run_gpu(args, rank, world, local):
             times, _, xr = cpu_reference_solves(cfg, 2, ncores)
             # the reference is serial: one solve on one thread as well
             times1, _, _ = cpu_reference_solves(cfg, 1, 1)
+            # Laplace: SOLVE_LAPL with the restated DAPIF2 FMM (NAPB 30, TOL 1e-11)
+            exo = O.extractdat(cfg.nd, cfg.rku())
+            go = O.Geometry.from_extract(cfg.nd, exo)
+            t0l = time.perf_counter()
+            O.solve_lapl(go, -2.0 * exo["z"].real, nthreads=ncores, mode=1)
+            lap_cpu = 1.0 / (time.perf_counter() - t0l)
             cpu = {"value": 2 / sum(times), "unit": "solves/s", "cores": ncores, "kind": "port",
                    "sample": "2 full Stokes solves of the 64x512 workload with the restated "
                              "CADAPDR FMM + SLATEC GMRES",
                    "value_1thread": 1 / sum(times1),
+                   "laplace_solves_per_s": lap_cpu,
+                   "laplace_solver": "SOLVE_LAPL with the restated DAPIF2 FMM (NAPB 30, TOL 1e-11)",
                    "gpu_vs_cpu_solution_rel": float(np.linalg.norm(x.cpu().numpy() - xr) / np.linalg.norm(xr))}
         except Exception as exc:  # the baseline must not hide the GPU result
             cpu = {"value": None, "unit": "solves/s", "cores": ncores, "kind": "port",
@@ -495,6 +520,7 @@ def run_gpu(args, rank, world, local):
                      "flops_per_launch": dom["flops_per_launch"], "avg_launch_ms": dom["avg_launch_ms"]},
         "kernels": kern,
         "m2l_tensor_ab": m2l_ab,
+        "laplace": lap,
         "peaks_measured_in_run": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
         "cpu_baseline": cpu,
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "solves/s",

@@ -659,10 +659,287 @@ void eb_or_fasmvp(const eb_or_geom* g, const double* u, double* w, int mode,
   free(dens); free(stress); free(za); free(pk); free(h);
 }
 
+/* ======================================================================
+ * DAPIF2 with IFLAG7 = 3 (dapif1.f:458-1077): the Cauchy sum
+ *   field_i = sum_{j != i} q_j / (z_i - z_j)
+ * by the Carrier-Greengard-Rokhlin adaptive FMM the reference cites (dapif1.f:468-471).
+ * Restated: the points scaled into the root square with factor 0.99 (dapif1.f:743-767);
+ * a box with more than napb points split into four (DAASSI, dapif1.f:1165-1255);
+ * NTERMS = -nint(log2 tol) + 3 expansion terms (dapif1.f:688); the lists of DALI12 /
+ * DALI34 (dapif2.f:3-356): list 1 the adjacent leaves (direct sum, DABARR's pair loop,
+ * dapif3.f:460-545), list 2 the children of the parent's colleagues that are not
+ * adjacent (M2L, DAFLEX), list 3 the descendants of the colleagues that are not adjacent
+ * while their parents are (M2P, DSLOR1, dapif3.f:1724-1749) and its dual list 4 (P2L,
+ * DSLOT3, dapif3.f:1387-1410); upward pass P2M + M2M (DAUPWD, dapif2.f:478-595),
+ * downward pass L2L + L2P (DADNWD, dapif3.f:553-680). Expansions are scaled by the box
+ * side r: field = (1/r) sum_k a_k / u^(k+1) (multipole), (1/r) sum_m L_m v^m (local),
+ * u, v the offsets from the centre in units of r. The reference's 90-degree symmetry
+ * shortcut of M2L (DAINSY/DASYME) and its per-distance reduced orders are not restated:
+ * they change the cost, not the sums.
+ * ====================================================================== */
+typedef struct {
+  cplx c;           /* centre */
+  double r;         /* side */
+  int level, parent, child[4], nchild, start, count, ix, iy;
+  int *ul, nu, *vl, nv, *wl, nw, *xl, nx; /* lists 1-4 */
+  int cu, cv, cw, cx;                     /* capacities */
+} dbox;
+
+static void dl_push(int** a, int* n, int* cap, int v) {
+  if (*n == *cap) {
+    *cap = *cap ? 2 * *cap : 8;
+    *a = (int*)realloc(*a, sizeof(int) * (size_t)*cap);
+  }
+  (*a)[(*n)++] = v;
+}
+
+static int dbox_adjacent(const dbox* a, const dbox* b) {
+  /* boxes of levels la <= lb touch (or coincide) iff b's grid cell, seen at a's level
+   * with one cell of margin, overlaps a */
+  const dbox* s = a->level <= b->level ? a : b;
+  const dbox* t = a->level <= b->level ? b : a;
+  int f = t->level - s->level;
+  long x0 = (long)s->ix << f, x1 = ((long)(s->ix + 1) << f) - 1;
+  long y0 = (long)s->iy << f, y1 = ((long)(s->iy + 1) << f) - 1;
+  return t->ix >= x0 - 1 && t->ix <= x1 + 1 && t->iy >= y0 - 1 && t->iy <= y1 + 1;
+}
+
+void eb_or_dapif2(int n, const cplx* z, const cplx* q, double tol, int napb, cplx* field,
+                  int nthreads) {
+  nthreads = clamp_threads(nthreads);
+  int p = -(int)lround(log(tol) / log(2.0)) + 3;
+  if (p < 4) p = 4;
+  if (p > 60) p = 60;
+  double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+  for (int i = 0; i < n; ++i) {
+    xmin = fmin(xmin, creal(z[i])); xmax = fmax(xmax, creal(z[i]));
+    ymin = fmin(ymin, cimag(z[i])); ymax = fmax(ymax, cimag(z[i]));
+  }
+  double side = fmax(xmax - xmin, ymax - ymin) / 0.99;
+  if (!(side > 0)) side = 1.0;
+  int* perm = (int*)malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  int nb = 1, capb = 1024;
+  dbox* B = (dbox*)calloc((size_t)capb, sizeof(dbox));
+  B[0].c = 0.5 * (xmin + xmax) + 0.5 * (ymin + ymax) * I;
+  B[0].r = side;
+  B[0].parent = -1;
+  B[0].count = n;
+  /* DAASSI: split boxes with more than napb points, level by level */
+  int* tmp = (int*)malloc(sizeof(int) * (size_t)n);
+  for (int b = 0; b < nb; ++b) {
+    if (B[b].count <= napb || B[b].level >= 40) continue;
+    int cnt[4] = {0, 0, 0, 0};
+    const int s0 = B[b].start, m = B[b].count;
+    for (int t = 0; t < m; ++t) {
+      cplx w = z[perm[s0 + t]] - B[b].c;
+      int qd = (creal(w) >= 0 ? 1 : 0) + (cimag(w) >= 0 ? 2 : 0);
+      cnt[qd]++;
+    }
+    int off[4] = {0, cnt[0], cnt[0] + cnt[1], cnt[0] + cnt[1] + cnt[2]};
+    int pos[4] = {off[0], off[1], off[2], off[3]};
+    for (int t = 0; t < m; ++t) {
+      cplx w = z[perm[s0 + t]] - B[b].c;
+      int qd = (creal(w) >= 0 ? 1 : 0) + (cimag(w) >= 0 ? 2 : 0);
+      tmp[pos[qd]++] = perm[s0 + t];
+    }
+    memcpy(perm + s0, tmp, sizeof(int) * (size_t)m);
+    for (int qd = 0; qd < 4; ++qd) {
+      if (!cnt[qd]) continue;
+      if (nb == capb) {
+        capb *= 2;
+        B = (dbox*)realloc(B, sizeof(dbox) * (size_t)capb);
+      }
+      dbox* c = &B[nb];
+      memset(c, 0, sizeof(dbox));
+      double h = 0.25 * B[b].r;
+      c->c = B[b].c + ((qd & 1) ? h : -h) + ((qd & 2) ? h : -h) * I;
+      c->r = 0.5 * B[b].r;
+      c->level = B[b].level + 1;
+      c->parent = b;
+      c->start = s0 + off[qd];
+      c->count = cnt[qd];
+      c->ix = 2 * B[b].ix + (qd & 1);
+      c->iy = 2 * B[b].iy + ((qd >> 1) & 1);
+      B[b].child[B[b].nchild++] = nb;
+      nb++;
+    }
+  }
+  free(tmp);
+  int L = 0;
+  for (int b = 0; b < nb; ++b) L = B[b].level > L ? B[b].level : L;
+  /* colleagues (same level, adjacent, self included), then the lists */
+  int** col = (int**)calloc((size_t)nb, sizeof(int*));
+  int* ncol = (int*)calloc((size_t)nb, sizeof(int));
+  for (int b = 0; b < nb; ++b) {
+    col[b] = (int*)malloc(sizeof(int) * 9);
+    if (B[b].parent < 0) {
+      col[b][ncol[b]++] = b;
+      continue;
+    }
+    int P = B[b].parent;
+    for (int a = 0; a < ncol[P]; ++a) {
+      int Q = col[P][a];
+      for (int cc = 0; cc < B[Q].nchild; ++cc) {
+        int C = B[Q].child[cc];
+        if (abs(B[C].ix - B[b].ix) <= 1 && abs(B[C].iy - B[b].iy) <= 1 && ncol[b] < 9) col[b][ncol[b]++] = C;
+      }
+    }
+  }
+  for (int b = 0; b < nb; ++b) {
+    dbox* X = &B[b];
+    int P = X->parent;
+    if (P >= 0) /* list 2 */
+      for (int a = 0; a < ncol[P]; ++a) {
+        int Q = col[P][a];
+        for (int cc = 0; cc < B[Q].nchild; ++cc) {
+          int C = B[Q].child[cc];
+          if (!(abs(B[C].ix - X->ix) <= 1 && abs(B[C].iy - X->iy) <= 1)) dl_push(&X->vl, &X->nv, &X->cv, C);
+        }
+      }
+    if (X->nchild) continue;
+    /* lists 1 and 3 of a leaf: colleagues, and below the split ones */
+    int stack[256], sp = 0;
+    for (int a = 0; a < ncol[b]; ++a) {
+      int C = col[b][a];
+      if (!B[C].nchild) {
+        dl_push(&X->ul, &X->nu, &X->cu, C);
+        continue;
+      }
+      for (int cc = 0; cc < B[C].nchild; ++cc) stack[sp++] = B[C].child[cc];
+      while (sp > 0) {
+        int D = stack[--sp];
+        if (!dbox_adjacent(X, &B[D])) {
+          dl_push(&X->wl, &X->nw, &X->cw, D);                 /* list 3 */
+          dl_push(&B[D].xl, &B[D].nx, &B[D].cx, b);           /* its dual, list 4 */
+        } else if (!B[D].nchild) {
+          dl_push(&X->ul, &X->nu, &X->cu, D);                 /* finer adjacent leaf */
+          dl_push(&B[D].ul, &B[D].nu, &B[D].cu, b);           /* and the converse */
+        } else {
+          for (int cc = 0; cc < B[D].nchild && sp < 250; ++cc) stack[sp++] = B[D].child[cc];
+        }
+      }
+    }
+  }
+  /* binomials C(i, j), i, j < 2p + 2 */
+  const int lb = 2 * p + 2;
+  double* bin = (double*)calloc((size_t)lb * lb, sizeof(double));
+  for (int i = 0; i < lb; ++i) {
+    bin[i * lb] = 1.0;
+    for (int j = 1; j <= i; ++j) bin[i * lb + j] = bin[(i - 1) * lb + j - 1] + bin[(i - 1) * lb + j];
+  }
+  cplx* M = (cplx*)calloc((size_t)nb * p, sizeof(cplx));
+  cplx* Lc = (cplx*)calloc((size_t)nb * p, sizeof(cplx));
+  /* upward pass: P2M at leaves, M2M level by level */
+  for (int l = L; l >= 0; --l) {
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+    for (int b = 0; b < nb; ++b) {
+      if (B[b].level != l) continue;
+      cplx* mb = M + (size_t)b * p;
+      if (!B[b].nchild) {
+        for (int t = 0; t < B[b].count; ++t) {
+          int j = perm[B[b].start + t];
+          cplx w = (z[j] - B[b].c) / B[b].r, pw = 1.0;
+          for (int k = 0; k < p; ++k) { mb[k] += q[j] * pw; pw *= w; }
+        }
+      } else {
+        for (int cc = 0; cc < B[b].nchild; ++cc) {
+          int C = B[b].child[cc];
+          cplx e = (B[C].c - B[b].c) / B[b].r, ep[64], hp = 1.0;
+          ep[0] = 1.0;
+          for (int k = 1; k < p; ++k) ep[k] = ep[k - 1] * e;
+          cplx a[64];
+          for (int k = 0; k < p; ++k) { a[k] = M[(size_t)C * p + k] * hp; hp *= 0.5; }
+          for (int k = 0; k < p; ++k) {
+            cplx s = 0;
+            for (int l2 = 0; l2 <= k; ++l2) s += bin[k * lb + l2] * ep[k - l2] * a[l2];
+            mb[k] += s;
+          }
+        }
+      }
+    }
+  }
+  /* list 2 (M2L) and list 4 (P2L) into every box's local expansion */
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+  for (int b = 0; b < nb; ++b) {
+    cplx* lbx = Lc + (size_t)b * p;
+    for (int a = 0; a < B[b].nv; ++a) {
+      int S = B[b].vl[a];
+      cplx d = (B[b].c - B[S].c) / B[b].r, dinv = 1.0 / d, dp[130];
+      dp[0] = dinv;
+      for (int k = 1; k < 2 * p + 1; ++k) dp[k] = dp[k - 1] * dinv;
+      const cplx* ms = M + (size_t)S * p;
+      for (int m = 0; m < p; ++m) {
+        cplx s = 0;
+        for (int k = 0; k < p; ++k) s += ms[k] * bin[(m + k) * lb + k] * dp[m + k];
+        lbx[m] += (m & 1) ? -s : s;
+      }
+    }
+    for (int a = 0; a < B[b].nx; ++a) {
+      int S = B[b].xl[a];
+      for (int t = 0; t < B[S].count; ++t) {
+        int j = perm[B[S].start + t];
+        cplx ws = (z[j] - B[b].c) / B[b].r, wi = 1.0 / ws, pw = wi;
+        for (int m = 0; m < p; ++m) { lbx[m] -= q[j] * pw; pw *= wi; }
+      }
+    }
+  }
+  /* L2L level by level */
+  for (int l = 1; l <= L; ++l) {
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+    for (int b = 0; b < nb; ++b) {
+      if (B[b].level != l) continue;
+      int P = B[b].parent;
+      cplx e = (B[b].c - B[P].c) / B[P].r, ep[64];
+      ep[0] = 1.0;
+      for (int k = 1; k < p; ++k) ep[k] = ep[k - 1] * e;
+      const cplx* lp = Lc + (size_t)P * p;
+      cplx* lc = Lc + (size_t)b * p;
+      double hj = 0.5;  /* (r_c / r_p) 2^-j */
+      for (int j = 0; j < p; ++j) {
+        cplx s = 0;
+        for (int m = j; m < p; ++m) s += lp[m] * bin[m * lb + j] * ep[m - j];
+        lc[j] += hj * s;
+        hj *= 0.5;
+      }
+    }
+  }
+  /* leaves: L2P, list 3 (M2P) and list 1 (direct) */
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
+  for (int b = 0; b < nb; ++b) {
+    if (B[b].nchild) continue;
+    const dbox* X = &B[b];
+    for (int t = 0; t < X->count; ++t) {
+      int i = perm[X->start + t];
+      cplx v = (z[i] - X->c) / X->r, s = 0, pw = 1.0;
+      const cplx* lbx = Lc + (size_t)b * p;
+      for (int m = 0; m < p; ++m) { s += lbx[m] * pw; pw *= v; }
+      cplx f = s / X->r;
+      for (int a = 0; a < X->nw; ++a) {
+        int W = X->wl[a];
+        cplx u = (z[i] - B[W].c) / B[W].r, ui = 1.0 / u, pu = ui, sm = 0;
+        const cplx* mw = M + (size_t)W * p;
+        for (int k = 0; k < p; ++k) { sm += mw[k] * pu; pu *= ui; }
+        f += sm / B[W].r;
+      }
+      for (int a = 0; a < X->nu; ++a) {
+        int S = X->ul[a];
+        for (int tt = 0; tt < B[S].count; ++tt) {
+          int j = perm[B[S].start + tt];
+          if (j != i) f += q[j] / (z[i] - z[j]);
+        }
+      }
+      field[i] = f;
+    }
+  }
+  for (int b = 0; b < nb; ++b) { free(B[b].ul); free(B[b].vl); free(B[b].wl); free(B[b].xl); free(col[b]); }
+  free(col); free(ncol); free(B); free(perm); free(bin); free(M); free(Lc);
+}
+
 /* FASMVP_LAP, laplace.f:159-262 (the Laplace matvec behind MATVEC_LAPL,
  * laplace.f:429-465). Only the first nbk entries of w are written; the reference
  * also accumulates k constraint sums past the end (:252-259). */
-void eb_or_fasmvp_lap(const eb_or_geom* g, const double* u, double* w, int nthreads) {
+void eb_or_fasmvp_lap2(const eb_or_geom* g, const double* u, double* w, int mode, int nthreads) {
   int nbk = g->nbk;
   cplx* q = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
   cplx* cf = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
@@ -673,7 +950,10 @@ void eb_or_fasmvp_lap(const eb_or_geom* g, const double* u, double* w, int nthre
     for (int i = 0; i < g->nd[b]; ++i) q[ist + i] = u[ist + i] * g->dz[ist + i] * hb;
     ist += g->nd[b];
   }
-  eb_or_cauchy_direct(nbk, g->z, nbk, g->z, q, 1, cf, nthreads);
+  if (mode == EB_OR_CADAP)
+    eb_or_dapif2(nbk, g->z, q, 1e-11, 30, cf, nthreads);  /* laplace.f:211: TOL 1e-11, NAPB 30 */
+  else
+    eb_or_cauchy_direct(nbk, g->z, nbk, g->z, q, 1, cf, nthreads);
   ist = 0;
   for (int b = 0; b < g->k; ++b) {
     double hs = 2.0 * EB_PI / g->nd[b];
@@ -691,11 +971,15 @@ void eb_or_fasmvp_lap(const eb_or_geom* g, const double* u, double* w, int nthre
   free(cf);
 }
 
+void eb_or_fasmvp_lap(const eb_or_geom* g, const double* u, double* w, int nthreads) {
+  eb_or_fasmvp_lap2(g, u, w, EB_OR_DIRECT, nthreads);
+}
+
 /* PVINTEV, pv_integral.f:53-204: principal-value Cauchy integral by the alternating
  * point rule on the 2x Fourier-interpolated curve (charges on the odd fine nodes,
  * evaluation at the even fine nodes, which are the original nodes). */
-void eb_or_pvintev(int k, const int* nd, const cplx* z, const cplx* ucmplx,
-                   cplx* phicmplx, int nthreads) {
+static void pvintev_impl(int k, const int* nd, const cplx* z, const cplx* ucmplx,
+                         cplx* phicmplx, int mode, int nthreads) {
   int nbk = 0, ndmax = 0;
   for (int b = 0; b < k; ++b) { nbk += nd[b]; ndmax = nd[b] > ndmax ? nd[b] : ndmax; }
   cplx* zsrc = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
@@ -724,20 +1008,41 @@ void eb_or_pvintev(int k, const int* nd, const cplx* z, const cplx* ucmplx,
    * ones are never targets, so only odd-source -> original-node pairs contribute.
    * The evaluation points are FINTER's even fine nodes, equal to z up to roundoff;
    * the original nodes are used. */
-  eb_or_cauchy_direct(nbk, z, nbk, zsrc, qs, 0, cf, nthreads);
+  if (mode == EB_OR_CADAP) {
+    /* DAPIF2 on all 2N fine points, TOL 1e-10 (pv_integral.f:176): charges on the odd
+     * fine nodes, the field read at the even ones (the original nodes) */
+    cplx* zall = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)nbk);
+    cplx* qall = (cplx*)calloc(2 * (size_t)nbk, sizeof(cplx));
+    cplx* fall = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)nbk);
+    for (int i = 0; i < nbk; ++i) {
+      zall[2 * i] = z[i];
+      zall[2 * i + 1] = zsrc[i];
+      qall[2 * i + 1] = qs[i];
+    }
+    eb_or_dapif2(2 * nbk, zall, qall, 1e-10, 30, fall, nthreads);
+    for (int i = 0; i < nbk; ++i) cf[i] = fall[2 * i];
+    free(zall); free(qall); free(fall);
+  } else {
+    eb_or_cauchy_direct(nbk, z, nbk, zsrc, qs, 0, cf, nthreads);
+  }
   const cplx z2pii = 1.0 / (2.0 * EB_PI * I);
   for (int i = 0; i < nbk; ++i) phicmplx[i] = -z2pii * cf[i];
   free(zsrc); free(qs); free(u2); free(xc); free(yc); free(x2); free(y2); free(cf);
 }
 
+void eb_or_pvintev(int k, const int* nd, const cplx* z, const cplx* ucmplx, cplx* phicmplx,
+                   int nthreads) {
+  pvintev_impl(k, nd, z, ucmplx, phicmplx, EB_OR_DIRECT, nthreads);
+}
+
 /* DIRICH_NEU_MAP, laplace.f:266-331. */
-void eb_or_dirich_neu_map(const eb_or_geom* g, const double* u, double* phi,
-                          double* psi, double* dphi_dn, int nthreads) {
+static void dirich_neu_map_impl(const eb_or_geom* g, const double* u, double* phi,
+                                double* psi, double* dphi_dn, int mode, int nthreads) {
   int nbk = g->nbk;
   cplx* uc = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
   cplx* ph = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
   for (int i = 0; i < nbk; ++i) uc[i] = u[i] * g->dz[i];
-  eb_or_pvintev(g->k, g->nd, g->z, uc, ph, nthreads);
+  pvintev_impl(g->k, g->nd, g->z, uc, ph, mode, nthreads);
   int ndmax = 0;
   for (int b = 0; b < g->k; ++b) ndmax = g->nd[b] > ndmax ? g->nd[b] : ndmax;
   cplx* zf = (cplx*)malloc(sizeof(cplx) * (size_t)ndmax);
@@ -756,6 +1061,11 @@ void eb_or_dirich_neu_map(const eb_or_geom* g, const double* u, double* phi,
     ist += n;
   }
   free(uc); free(ph); free(zf); free(zfi);
+}
+
+void eb_or_dirich_neu_map(const eb_or_geom* g, const double* u, double* phi, double* psi,
+                          double* dphi_dn, int nthreads) {
+  dirich_neu_map_impl(g, u, phi, psi, dphi_dn, EB_OR_DIRECT, nthreads);
 }
 
 /* INTERFACENEW, electric.f:791-912 (free space, iwall = 0): interface normal
@@ -1053,7 +1363,7 @@ static void mv_stokes(int n, const double* x, double* y, void* ud) {
 static void mv_lapl(int n, const double* x, double* y, void* ud) {
   (void)n;
   mv_ud* m = (mv_ud*)ud;
-  eb_or_fasmvp_lap(m->g, x, y, m->nthreads);
+  eb_or_fasmvp_lap2(m->g, x, y, m->mode, m->nthreads);
 }
 
 /* F, electric.f:968-1109, free space (zbond = 0 keeps iwall = 0). */
@@ -1088,7 +1398,7 @@ void eb_or_f(eb_or_model* m, int k, const int* nd, const double* rku, double* rk
   for (int i = 0; i < nbk; ++i) rhs[i] = -2.0 * creal(z[i]);
   for (int i = 0; i < nbk; ++i) ulap[i] = rhs[i];
   eb_or_gmres(nbk, rhs, ulap, mv_lapl, &ud, m->maxl, m->gmres_tol, &m->lap_iter, &m->lap_err);
-  eb_or_dirich_neu_map(&g, ulap, phi, psi, dphi, m->nthreads);
+  dirich_neu_map_impl(&g, ulap, phi, psi, dphi, m->mode, m->nthreads);
   /* Stokes solve: SETVELF then SOLVEI (x0 = rhs). */
   eb_or_setvelf(&g, zc, m->zbond, m->cap, m->e0, dphi, rhs);
   for (int i = 0; i < 2 * nbk; ++i) soln[i] = rhs[i];

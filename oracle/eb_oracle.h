@@ -71,6 +71,11 @@ enum { EB_OR_DIRECT = 0, EB_OR_CADAP = 1 };
 void eb_or_fasmvp(const eb_or_geom* g, const double* u, double* w, int mode,
                   int nthreads);
 void eb_or_fasmvp_lap(const eb_or_geom* g, const double* u, double* w, int nthreads);
+/* mode EB_OR_CADAP: the Cauchy sum by the restated DAPIF2 (TOL 1e-11, NAPB 30) */
+void eb_or_fasmvp_lap2(const eb_or_geom* g, const double* u, double* w, int mode, int nthreads);
+/* DAPIF2 (IFLAG7 = 3): field_i = sum_{j != i} q_j / (z_i - z_j), adaptive FMM */
+void eb_or_dapif2(int n, const eb_or_cplx* z, const eb_or_cplx* q, double tol, int napb,
+                  eb_or_cplx* field, int nthreads);
 void eb_or_pvintev(int k, const int* nd, const eb_or_cplx* z, const eb_or_cplx* ucmplx,
                    eb_or_cplx* phicmplx, int nthreads);
 void eb_or_dirich_neu_map(const eb_or_geom* g, const double* u, double* phi,
@@ -91,7 +96,9 @@ int eb_or_gmres(int n, const double* b, double* x, eb_or_matvec_fn mv, void* ud,
 typedef struct {
   double cap, e0;
   eb_or_cplx zbond;
-  int mode;       /* EB_OR_DIRECT or EB_OR_CADAP for the Stokes sums */
+  int mode;       /* EB_OR_DIRECT: direct sums; EB_OR_CADAP: the reference's FMMs
+                     (restated CADAPDR for the Stokes sums, DAPIF2 for the Laplace
+                     and PV sums) */
   int nthreads;
   int maxl;
   double gmres_tol;

@@ -58,6 +58,8 @@ def lib():
             "eb_or_cauchy_direct": (None, [_I, _P, _I, _P, _P, _I, _P, _I]),
             "eb_or_fasmvp": (None, [ctypes.POINTER(Geom), _P, _P, _I, _I]),
             "eb_or_fasmvp_lap": (None, [ctypes.POINTER(Geom), _P, _P, _I]),
+            "eb_or_fasmvp_lap2": (None, [ctypes.POINTER(Geom), _P, _P, _I, _I]),
+            "eb_or_dapif2": (None, [_I, _P, _P, _D, _I, _P, _I]),
             "eb_or_pvintev": (None, [_I, _P, _P, _P, _P, _I]),
             "eb_or_dirich_neu_map": (None, [ctypes.POINTER(Geom), _P, _P, _P, _P, _I]),
             "eb_or_interfacenew": (None, [ctypes.POINTER(Geom), _P, _P, _D, _P, _P, _P, _I, _I]),
@@ -221,11 +223,20 @@ def fasmvp(g, u, mode=0, nthreads=0):
     return w
 
 
-def fasmvp_lap(g, u, nthreads=0):
+def fasmvp_lap(g, u, nthreads=0, mode=0):
+    """FASMVP_LAP; mode 1: the Cauchy sum by the restated DAPIF2 FMM (TOL 1e-11)."""
     u = _r(u)
     w = np.empty(g.nbk)
-    lib().eb_or_fasmvp_lap(ctypes.byref(g.s), _p(u), _p(w), int(nthreads))
+    lib().eb_or_fasmvp_lap2(ctypes.byref(g.s), _p(u), _p(w), int(mode), int(nthreads))
     return w
+
+
+def dapif2(z, q, tol=1e-11, napb=30, nthreads=0):
+    """DAPIF2 with IFLAG7 = 3: sum_{j != i} q_j / (z_i - z_j) by the adaptive FMM."""
+    z, q = _c(z), _c(q)
+    f = np.empty_like(z)
+    lib().eb_or_dapif2(z.shape[0], _p(z), _p(q), float(tol), int(napb), _p(f), int(nthreads))
+    return f
 
 
 def pvintev(nd, z, ucmplx, nthreads=0):
@@ -290,8 +301,8 @@ def solvei(g, rhs, mode=0, nthreads=0, maxl=100, tol=1e-10):
     return gmres(lambda x: fasmvp(g, x, mode, nthreads), rhs, rhs, maxl, tol)
 
 
-def solve_lapl(g, rhs, nthreads=0, maxl=100, tol=1e-10):
-    return gmres(lambda x: fasmvp_lap(g, x, nthreads), rhs, rhs, maxl, tol)
+def solve_lapl(g, rhs, nthreads=0, maxl=100, tol=1e-10, mode=0):
+    return gmres(lambda x: fasmvp_lap(g, x, nthreads, mode), rhs, rhs, maxl, tol)
 
 
 def make_model(cap=0.0, e0=0.5, zbond=0j, mode=0, nthreads=0, maxl=100, gmres_tol=1e-10):

@@ -147,3 +147,21 @@ def test_rk2_conserves_area(oracle):
     a1 = oracle.extractdat(cfg.nd, y)["area"].sum()
     assert abs(a1 - a0) / a0 < 1e-8
     assert abs(m.flux) < 1e-8
+
+
+@pytest.mark.parametrize("n", [40, 3000])
+def test_dapif2_restatement_matches_direct_sum(oracle, n):
+    """The restated DAPIF2 FMM (IFLAG7 = 3, dapif1.f:458-1077; NAPB 30, TOL 1e-11) against
+    the exact Cauchy sum, on random points and on drop curves."""
+    rng = np.random.default_rng(n)
+    z = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    q = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = oracle.cauchy_direct(z, z, q, True)
+    got = oracle.dapif2(z, q)
+    assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-11
+    from electricbubbles_gb300 import configs
+    cfg = configs.small_drops(3, 256)
+    g = oracle.Geometry.from_extract(cfg.nd, oracle.extractdat(cfg.nd, cfg.rku()))
+    u = rng.standard_normal(cfg.nbk)
+    a, b = oracle.fasmvp_lap(g, u), oracle.fasmvp_lap(g, u, mode=1)
+    assert np.abs(a - b).max() / np.abs(a).max() < 1e-11
