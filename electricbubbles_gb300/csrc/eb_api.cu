@@ -257,6 +257,7 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->ev_near1) cudaEventDestroy(ctx->ev_near1);
   for (GmGraph& g : ctx->gcache) g.destroy();
   if (ctx->b_host_act) cudaFreeHost(ctx->b_host_act);
+  for (GmGraph& g : ctx->bgraph) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);

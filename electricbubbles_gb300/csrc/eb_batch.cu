@@ -150,10 +150,12 @@ __global__ void k_bg_init(const int* __restrict__ seg, const double* __restrict_
 // of the Hessenberg matrix, DHEQR's Givens update (dheqr.f:82-176) and the stopping
 // test on |g_(j+1)| (DPIGMR's RHO, dpigmr.f:340-355). nact counts the simulations still
 // active after the step.
-__global__ void __launch_bounds__(BBS) k_bg_arnoldi(int j, const int* __restrict__ seg, double* __restrict__ V,
-                                                    size_t ldv, double* __restrict__ w, BCtl* __restrict__ ctl,
-                                                    double* __restrict__ Hh, double* __restrict__ G,
-                                                    double* __restrict__ CS, int maxl, int* __restrict__ nact) {
+__global__ void __launch_bounds__(BBS) k_bg_arnoldi(const int* __restrict__ jdev, const int* __restrict__ seg,
+                                                    double* __restrict__ V, size_t ldv, double* __restrict__ w,
+                                                    BCtl* __restrict__ ctl, double* __restrict__ Hh,
+                                                    double* __restrict__ G, double* __restrict__ CS, int maxl,
+                                                    int* __restrict__ nact) {
+  const int j = *jdev;
   __shared__ double red[33];
   __shared__ double h1[EB_GM_MAXL + 2];
   __shared__ double h2[EB_GM_MAXL + 2];
@@ -279,6 +281,40 @@ __global__ void k_br_update(const int* __restrict__ seg, const double* __restric
       itol[s] = fmin(itol0, fmax(0.1 * itol0, 0.5 * tol / e));
     }
   }
+}
+
+// Loop control of a cycle, in jdev = {j, continue}: j = 0 and continue = (a simulation is
+// active) at the start; after each step j += 1 and continue = (still active, j < maxl),
+// resetting the step's counter of active simulations. With use_h the WHILE node's
+// condition is set to `continue` as well (the host-driven loop reads jdev[1]).
+__global__ void k_bg_start(int nsim, const BCtl* __restrict__ ctl, int* __restrict__ jdev, int* __restrict__ nact,
+                           cudaGraphConditionalHandle h, int use_h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int any = 0;
+  for (int s = 0; s < nsim; ++s) any |= ctl[s].active;
+  jdev[0] = 0;
+  jdev[1] = any;
+  *nact = 0;
+  if (use_h) cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
+__global__ void k_bg_next(int maxl, int* __restrict__ jdev, int* __restrict__ nact, cudaGraphConditionalHandle h,
+                          int use_h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int a = *nact;
+  *nact = 0;
+  const int j = jdev[0] + 1;
+  const int cont = (a > 0 && j < maxl) ? 1 : 0;
+  jdev[0] = j;
+  jdev[1] = cont;
+  if (use_h) cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+// the operator's input: Krylov column j
+__global__ void k_bg_col(int n, const int* __restrict__ jdev, const double* __restrict__ V, size_t ldv,
+                         double* __restrict__ xin) {
+  const double* v = V + (size_t)(*jdev) * ldv;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) xin[i] = v[i];
 }
 
 __global__ void k_bg_axpy(const int* __restrict__ seg, const int* __restrict__ skip, const double* __restrict__ d,
@@ -444,40 +480,125 @@ struct BatchWork {
   double *V, *H, *G, *CS, *w, *xin;
   BCtl* ctl;
   int* nact;
+  int* jdev;  // {step j, continue}
 };
 
 // One GMRES cycle on every simulation not marked in skip: solves A x = b per segment to
-// the per-simulation relative tolerance in ctl (x0 = x when have_x0, else 0).
-int bg_cycle(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bool have_x0,
-             const int* skip, int* total_iters) {
+// the per-simulation relative tolerance in ctl (x0 = x when have_x0, else 0). The Arnoldi
+// steps run until no simulation is active or MAXL is reached, each step one operator
+// apply and one k_bg_arnoldi over all simulations.
+int bg_enqueue_pre(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bool have_x0,
+                   const int* skip, cudaGraphConditionalHandle h, int use_h) {
+  eb_ctx* ctx = B.ctx;
+  cudaStream_t st = ctx->stream;
+  if (have_x0) EB_TRY(op(ctx, x, B.w, prec));
+  k_bg_init<<<B.S, BBS, 0, st>>>(B.seg, b, have_x0 ? B.w : nullptr, nullptr, B.V, B.ctl, B.G, skip, B.maxl);
+  k_bg_start<<<1, 32, 0, st>>>(B.S, B.ctl, B.jdev, B.nact, h, use_h);
+  ctx->launches += 2;
+  return eb_check_launch(ctx, "batched gmres (start)");
+}
+
+int bg_enqueue_step(BatchWork& B, eb_op_fn op, int prec, cudaGraphConditionalHandle h, int use_h) {
   eb_ctx* ctx = B.ctx;
   cudaStream_t st = ctx->stream;
   const size_t ldv = (size_t)B.n;
-  if (have_x0) {
-    EB_TRY(op(ctx, x, B.w, prec));
-    k_bg_init<<<B.S, BBS, 0, st>>>(B.seg, b, B.w, nullptr, B.V, B.ctl, B.G, skip, B.maxl);
-  } else {
-    k_bg_init<<<B.S, BBS, 0, st>>>(B.seg, b, nullptr, nullptr, B.V, B.ctl, B.G, skip, B.maxl);
-  }
+  k_bg_col<<<std::min(nblk(B.n, 256), 2 * ctx->nsm), 256, 0, st>>>(B.n, B.jdev, B.V, ldv, B.xin);
   eb_count_launch(ctx);
-  int* hact = ctx->b_host_act;
-  int j = 0;
-  for (; j < B.maxl; ++j) {
-    EB_TRY(op(ctx, B.V + (size_t)j * ldv, B.w, prec));
-    EB_CUDA_TRY(cudaMemsetAsync(B.nact, 0, sizeof(int), st));
-    k_bg_arnoldi<<<B.S, BBS, 0, st>>>(j, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact);
-    eb_count_launch(ctx);
-    EB_CUDA_TRY(cudaMemcpyAsync(hact, B.nact, sizeof(int), cudaMemcpyDeviceToHost, st));
-    EB_CUDA_TRY(cudaStreamSynchronize(st));
-    if (*hact == 0) {
-      ++j;
-      break;
+  EB_TRY(op(ctx, B.xin, B.w, prec));
+  k_bg_arnoldi<<<B.S, BBS, 0, st>>>(B.jdev, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact);
+  k_bg_next<<<1, 32, 0, st>>>(B.maxl, B.jdev, B.nact, h, use_h);
+  ctx->launches += 2;
+  return eb_check_launch(ctx, "batched gmres (step)");
+}
+
+int bg_enqueue_post(BatchWork& B, bool have_x0, const int* skip, double* x) {
+  eb_ctx* ctx = B.ctx;
+  k_bg_finish<<<B.S, BBS, 0, ctx->stream>>>(B.seg, B.V, (size_t)B.n, B.ctl, B.H, B.G, B.maxl, have_x0 ? 0 : 1,
+                                            skip, x);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "batched gmres (finish)");
+}
+
+// The cycle as one CUDA graph (pre, a conditional WHILE node over the steps, post),
+// cached under the geometry's shape and the buffer epoch like the single solves' graphs.
+int bg_cycle_graph(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bool have_x0,
+                   const int* skip, int slot) {
+  eb_ctx* ctx = B.ctx;
+  unsigned long long key[8] = {(unsigned long long)slot, (unsigned long long)(uintptr_t)op,
+                               (unsigned long long)B.n, (unsigned long long)B.maxl, ctx->geom_shape,
+                               eb_devbuf_epoch(), (unsigned long long)B.S, (unsigned long long)prec};
+  GmGraph& G = ctx->bgraph[slot];
+  if (!G.valid || !std::equal(key, key + 8, G.key)) {
+    G.destroy();
+    const unsigned long long e0 = eb_devbuf_epoch();
+    EB_CUDA_TRY(cudaGraphCreate(&G.graph, 0));
+    cudaGraphConditionalHandle h;
+    EB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, G.graph, 0, cudaGraphCondAssignDefault));
+    std::vector<cudaGraphNode_t> sinks;
+    bool lost = false;
+    int st = eb_capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, &lost,
+                             [&]() { return bg_enqueue_pre(B, op, prec, b, x, have_x0, skip, h, 1); });
+    if (st != EB_OK) {
+      if (lost) G.graph = nullptr;
+      G.destroy();
+      return st;
     }
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t ncond;
+    EB_CUDA_TRY(cudaGraphAddNode(&ncond, G.graph, sinks.data(), nullptr, sinks.size(), &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    bool body_lost = false;
+    st = eb_capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, &body_lost,
+                         [&]() { return bg_enqueue_step(B, op, prec, h, 1); });
+    if (st == EB_OK)
+      st = eb_capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, &lost,
+                           [&]() { return bg_enqueue_post(B, have_x0, skip, x); });
+    if (st == EB_OK && eb_devbuf_epoch() != e0) st = EB_ERR_CUDA;  // a buffer moved: retry later
+    if (st != EB_OK) {
+      if (lost || body_lost) G.graph = nullptr;
+      G.destroy();
+      cudaGetLastError();
+      return st;
+    }
+    EB_CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, cudaGraphInstantiateFlagUseNodePriority));
+    memcpy(G.key, key, sizeof(key));
+    G.valid = true;
   }
-  *total_iters += j;
-  k_bg_finish<<<B.S, BBS, 0, st>>>(B.seg, B.V, ldv, B.ctl, B.H, B.G, B.maxl, have_x0 ? 0 : 1, skip, x);
-  eb_count_launch(ctx);
-  return eb_check_launch(ctx, "batched gmres");
+  EB_CUDA_TRY(cudaGraphLaunch(G.exec, ctx->stream));
+  return EB_OK;
+}
+
+int bg_cycle(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bool have_x0,
+             const int* skip, int* total_iters, int slot) {
+  eb_ctx* ctx = B.ctx;
+  cudaStream_t st = ctx->stream;
+  const long long l0 = ctx->launches;
+  bool done = false;
+  if (ctx->opts.graphs > 0 && !ctx->profiling) {
+    // a failed capture (a buffer grew while capturing) falls back to the host loop once
+    done = bg_cycle_graph(B, op, prec, b, x, have_x0, skip, slot) == EB_OK;
+  }
+  if (!done) {
+    ctx->launches = l0;
+    cudaGraphConditionalHandle h0 = 0;
+    EB_TRY(bg_enqueue_pre(B, op, prec, b, x, have_x0, skip, h0, 0));
+    int* hact = ctx->b_host_act;
+    for (int j = 0; j < B.maxl; ++j) {
+      EB_CUDA_TRY(cudaMemcpyAsync(hact, B.jdev + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+      EB_CUDA_TRY(cudaStreamSynchronize(st));
+      if (*hact == 0) break;
+      EB_TRY(bg_enqueue_step(B, op, prec, h0, 0));
+    }
+    EB_TRY(bg_enqueue_post(B, have_x0, skip, x));
+  }
+  EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_host_act + 2, B.jdev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  *total_iters += ctx->b_host_act[2];
+  return EB_OK;
 }
 
 }  // namespace
@@ -516,6 +637,7 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
   int* misc = ctx->b_misc.as<int>();
   B.nact = misc;
   int* nleft = misc + 1;
+  B.jdev = misc + 2;
   int* skip = misc + 4;
   double* err = reinterpret_cast<double*>(skip + S + (S & 1));  // 8-byte aligned
   double* itol = err + S;
@@ -532,7 +654,7 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
     k_bg_set_tol<<<nblk(S, 128), 128, 0, st>>>(S, B.ctl, ctx->opts.gmres_tol, nullptr);
     eb_count_launch(ctx);
     int its = 0;
-    EB_TRY(bg_cycle(B, op, EB_FP64, b, x, true, nullptr, &its));
+    EB_TRY(bg_cycle(B, op, EB_FP64, b, x, true, nullptr, &its, 0));
     k_bg_gather<<<nblk(S, 128), 128, 0, st>>>(S, B.ctl, gat);
     EB_CUDA_TRY(cudaMemcpyAsync(hg.data(), gat, sizeof(double) * 3 * S, cudaMemcpyDeviceToHost, st));
     EB_CUDA_TRY(cudaStreamSynchronize(st));
@@ -556,7 +678,7 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
       k_bg_set_tol<<<nblk(S, 128), 128, 0, st>>>(S, B.ctl, ctx->opts.inner_tol, outer > 1 ? itol : nullptr);
       eb_count_launch(ctx);
       int its = 0;
-      EB_TRY(bg_cycle(B, op, EB_FP32, r, dd, false, skip, &its));
+      EB_TRY(bg_cycle(B, op, EB_FP32, r, dd, false, skip, &its, 1));
       inf.iters += its;
       inf.matvecs32 += its;
       // x += d on the simulations that took part

@@ -246,10 +246,58 @@ struct eb_ctx {
   double b_sq[3] = {1, 0, 0};      // the forest's root square (W, x0, y0)
   DevBuf b_G, b_CS, b_ctl, b_misc; // batched GMRES state
   DevBuf b_st1, b_st2, b_flag;     // GETFOURIER / DOUBLE: drop starts and flags
-  int* b_host_act = nullptr;       // page-locked counters read back per Arnoldi step
+  int* b_host_act = nullptr;       // page-locked counters read back per cycle
+  GmGraph bgraph[2];               // batched GMRES cycles as graphs (plain, refinement inner)
 };
 
 typedef int (*eb_op_fn)(eb_ctx*, const double*, double*, int);
+
+// Enqueues `f` on the capture stream into graph `gr` after `deps`; records the sink
+// nodes of the capture and the kernel launches it issued.
+template <typename F>
+inline int eb_capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* deps, size_t ndeps,
+                 std::vector<cudaGraphNode_t>* sinks, long long* nlaunch, bool* graph_lost, F f) {
+  cudaStream_t saved = ctx->stream;
+  const long long l0 = ctx->launches;
+  ctx->stream = ctx->cap_stream;
+  eb_devbuf_set_capturing(true);
+  int st = EB_OK;
+  cudaError_t e = cudaStreamBeginCaptureToGraph(ctx->cap_stream, gr, deps, nullptr, ndeps,
+                                                cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) {
+    eb_set_last_cuda_error(e, "cudaStreamBeginCaptureToGraph", __FILE__, __LINE__);
+    st = EB_ERR_CUDA;
+  } else {
+    st = f();
+    if (sinks) {
+      cudaStreamCaptureStatus cs;
+      const cudaGraphNode_t* d = nullptr;
+      size_t nd = 0;
+      e = cudaStreamGetCaptureInfo(ctx->cap_stream, &cs, nullptr, nullptr, &d, nullptr, &nd);
+      if (e == cudaSuccess && d) sinks->assign(d, d + nd);
+      else if (st == EB_OK) {
+        eb_set_last_cuda_error(e, "cudaStreamGetCaptureInfo", __FILE__, __LINE__);
+        st = EB_ERR_CUDA;
+      }
+    }
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(ctx->cap_stream, &out);
+    if (e != cudaSuccess || out == nullptr) {
+      // an invalidated capture: the graph is not ours to destroy any more
+      if (graph_lost) *graph_lost = true;
+      if (st == EB_OK) {
+        eb_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        st = EB_ERR_CUDA;
+      }
+    }
+  }
+  eb_devbuf_set_capturing(false);
+  ctx->stream = saved;
+  *nlaunch = ctx->launches - l0;
+  ctx->launches = l0;
+  return st;
+}
+
 
 // batch.cu
 int eb_batch_install(eb_ctx* ctx);

@@ -565,52 +565,6 @@ __global__ void k_gm_axpy(int n, const GmCtl* __restrict__ c, const double* __re
 enum { GM_PLAIN = 0, GM_REFINE = 1 };
 constexpr int GM_BUILD_FAILED = -100;  // internal: fall back to the host-driven loop
 
-// Enqueues `f` on the capture stream into graph `gr` after `deps`; records the sink
-// nodes of the capture and the kernel launches it issued.
-template <typename F>
-int capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* deps, size_t ndeps,
-                 std::vector<cudaGraphNode_t>* sinks, long long* nlaunch, bool* graph_lost, F f) {
-  cudaStream_t saved = ctx->stream;
-  const long long l0 = ctx->launches;
-  ctx->stream = ctx->cap_stream;
-  eb_devbuf_set_capturing(true);
-  int st = EB_OK;
-  cudaError_t e = cudaStreamBeginCaptureToGraph(ctx->cap_stream, gr, deps, nullptr, ndeps,
-                                                cudaStreamCaptureModeRelaxed);
-  if (e != cudaSuccess) {
-    eb_set_last_cuda_error(e, "cudaStreamBeginCaptureToGraph", __FILE__, __LINE__);
-    st = EB_ERR_CUDA;
-  } else {
-    st = f();
-    if (sinks) {
-      cudaStreamCaptureStatus cs;
-      const cudaGraphNode_t* d = nullptr;
-      size_t nd = 0;
-      e = cudaStreamGetCaptureInfo(ctx->cap_stream, &cs, nullptr, nullptr, &d, nullptr, &nd);
-      if (e == cudaSuccess && d) sinks->assign(d, d + nd);
-      else if (st == EB_OK) {
-        eb_set_last_cuda_error(e, "cudaStreamGetCaptureInfo", __FILE__, __LINE__);
-        st = EB_ERR_CUDA;
-      }
-    }
-    cudaGraph_t out = nullptr;
-    e = cudaStreamEndCapture(ctx->cap_stream, &out);
-    if (e != cudaSuccess || out == nullptr) {
-      // an invalidated capture: the graph is not ours to destroy any more
-      if (graph_lost) *graph_lost = true;
-      if (st == EB_OK) {
-        eb_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
-        st = EB_ERR_CUDA;
-      }
-    }
-  }
-  eb_devbuf_set_capturing(false);
-  ctx->stream = saved;
-  *nlaunch = ctx->launches - l0;
-  ctx->launches = l0;
-  return st;
-}
-
 // Builds the graph of one plain GMRES cycle (x0 = x, tolerance gmres_tol) or of one
 // refinement step (inner FP32 cycle on r from x0 = 0 to inner_tol, x += d, r = b - A x).
 int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
@@ -639,7 +593,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     if (lost) G.graph = nullptr;  // not destroyed by G.destroy()
     return st;
   };
-  int cst = capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, &lost, [&]() -> int {
+  int cst = eb_capture_into(ctx, G.graph, nullptr, 0, &sinks, &G.n_pre, &lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     k_vtw<<<nb, RBS, 0, s>>>(n, 1, nullptr, bb, ldv, bb, part, hdev + GM_BN, ticket);
     eb_count_launch(ctx);
@@ -670,7 +624,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   // body: one Arnoldi step
   const int* lld = &ctl->ll;
   bool body_lost = false;
-  cst = capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, &body_lost, [&]() -> int {
+  cst = eb_capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, &body_lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
@@ -688,7 +642,7 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   if (body_lost) lost = true;  // the body belongs to the graph; leave the whole graph alone
   if (cst != EB_OK) return fail(cst);
   // post: DHELS, x update; refined: x += d, r = b - A64 x with ||r||^2
-  cst = capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, &lost, [&]() -> int {
+  cst = eb_capture_into(ctx, G.graph, &ncond, 1, nullptr, &G.n_post, &lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     k_gm_finish<<<1, 128, 0, s>>>(ctl, hdev + GM_Y);
     k_gm_add<<<nb, RBS, 0, s>>>(n, ctl, V, ldv, hdev + GM_Y, xx);
