@@ -85,12 +85,24 @@ __global__ void k_bbox(const double2* __restrict__ z, int n, Box4* __restrict__ 
 // side widened by 1e-9 relative, centred on the box (W = 1 for a single point).
 __global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __restrict__ out,
                              double* __restrict__ sq) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ Box4 sb[256];
   Box4 r = mk_box4(INFINITY, -INFINITY, INFINITY, -INFINITY);
-  for (int i = 0; i < nb; ++i) {
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
     Box4 p = part[i];
     r.x = fmin(r.x, p.x); r.y = fmax(r.y, p.y); r.z = fmin(r.z, p.z); r.w = fmax(r.w, p.w);
   }
+  sb[threadIdx.x] = r;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const Box4 q = sb[threadIdx.x + o];
+      Box4& a = sb[threadIdx.x];
+      a.x = fmin(a.x, q.x); a.y = fmax(a.y, q.y); a.z = fmin(a.z, q.z); a.w = fmax(a.w, q.w);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  r = sb[0];
   *out = r;
   double w = fmax(__dadd_rn(r.y, -r.x), __dadd_rn(r.w, -r.z));
   if (!(w > 0)) w = 1.0;
@@ -303,42 +315,50 @@ __device__ __forceinline__ int find_box(const unsigned long long* __restrict__ b
 // children of the parent's neighbours that are not adjacent to the box; DALI12's list 1,
 // dapif2.f:3-171). Only existing boxes are found, so the children of a neighbour that is
 // a leaf are absent: its points reach the box's leaves through their U lists.
+// One warp per box: the 36 candidates (the children of the 3 x 3 parents around the
+// box's parent, in the fixed order qy, qx, cy, cx) are looked up by the lanes, two each,
+// and the hits written in candidate order.
 __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo, int first, int nbox, int R,
                         int* __restrict__ vlist, unsigned char* __restrict__ vcode,
                         int* __restrict__ vcount) {
-  const int gid = first + blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= nbox) return;
+  const int gid = first + (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (gid >= nbox) return;  // whole warps leave together
   int lev = 0;
   while (gid >= lo.v[lev + 1]) ++lev;
   const int off = lo.v[lev], nb = lo.v[lev + 1] - off;
-  unsigned long long key = bkey[gid];
+  const unsigned long long key = bkey[gid];
   if (lev <= R) {  // a forest's boxes of level <= R hold different problems
-    vcount[gid] = 0;
+    if (lane == 0) vcount[gid] = 0;
     return;
   }
   const unsigned long long root = key >> (2 * (lev - R));
-  int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
-  int px = ix >> 1, py = iy >> 1, half = 1 << (lev - 1), side = 1 << lev;
+  const int ix = (int)compact2(key), iy = (int)compact2(key >> 1);
+  const int px = ix >> 1, py = iy >> 1, half = 1 << (lev - 1), side = 1 << lev;
   int cnt = 0;
-  for (int qy = py - 1; qy <= py + 1; ++qy) {
-    if (qy < 0 || qy >= half) continue;
-    for (int qx = px - 1; qx <= px + 1; ++qx) {
-      if (qx < 0 || qx >= half) continue;
-      for (int cy = 0; cy < 2; ++cy)
-        for (int cx = 0; cx < 2; ++cx) {
-          int sx = 2 * qx + cx, sy = 2 * qy + cy;
-          int dx = ix - sx, dy = iy - sy;
-          if (dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1) continue;
-          if (sx >= side || sy >= side) continue;
-          int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
-          if (s < 0 || (bkey[s] >> (2 * (lev - R))) != root) continue;
-          vlist[(size_t)gid * EB_VMAX + cnt] = s;
-          vcode[(size_t)gid * EB_VMAX + cnt] = (unsigned char)((dy + 3) * 7 + (dx + 3));
-          ++cnt;
-        }
+  for (int base = 0; base < 36; base += 32) {
+    const int c = base + lane;
+    int s = -1, code = 0;
+    if (c < 36) {
+      const int qy = py - 1 + c / 12, qx = px - 1 + (c / 4) % 3, cy = (c >> 1) & 1, cx = c & 1;
+      const int sx = 2 * qx + cx, sy = 2 * qy + cy, dx = ix - sx, dy = iy - sy;
+      const bool inside = qy >= 0 && qy < half && qx >= 0 && qx < half && sx < side && sy < side;
+      const bool adjacent = dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1;
+      if (inside && !adjacent) {
+        s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
+        if (s >= 0 && (bkey[s] >> (2 * (lev - R))) != root) s = -1;
+        code = (dy + 3) * 7 + (dx + 3);
+      }
     }
+    const unsigned int m = __ballot_sync(0xffffffffu, s >= 0);
+    if (s >= 0) {
+      const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+      vlist[(size_t)gid * EB_VMAX + pos] = s;
+      vcode[(size_t)gid * EB_VMAX + pos] = (unsigned char)code;
+    }
+    cnt += __popc(m);
   }
-  vcount[gid] = cnt;
+  if (lane == 0) vcount[gid] = cnt;
 }
 
 // Leaves in point order: point i starts its leaf when it heads the box of its leaf level.
@@ -379,6 +399,7 @@ template <bool FILL>
 __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const int* __restrict__ leaves,
                              const unsigned long long* __restrict__ bkey,
                              const unsigned char* __restrict__ blev, LevOffT lo, int R,
+                             const int* __restrict__ floor_d,
                              const int* __restrict__ child0, const int* __restrict__ nchild,
                              int* __restrict__ ucnt, int* __restrict__ wcnt,
                              const int* __restrict__ ustart, const int* __restrict__ wstart,
@@ -429,7 +450,9 @@ __global__ void k_leaf_lists(int nleaf, const int* __restrict__ nleaf_d, const i
       }
     }
   }
-  for (int m = l - 1; m >= R; --m) {
+  // no leaf lies above the tree's floor (every box there is split)
+  const int mstop = max(R, *floor_d);
+  for (int m = l - 1; m >= mstop; --m) {
     const int ax = ix >> (l - m), ay = iy >> (l - m), sm = 1 << m;
     for (int dy = -1; dy <= 1; ++dy) {
       for (int dx = -1; dx <= 1; ++dx) {
@@ -681,7 +704,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
   eb_count_launch(ctx);
   if (root_sq) k_set_square<<<1, 32, 0, st>>>(root_sq[0], root_sq[1], root_sq[2], sq);
-  else k_bbox_final<<<1, 32, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
+  else k_bbox_final<<<1, 256, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
   eb_count_launch(ctx);
   // 2. keys and sort (a non-finite coordinate gives clamped keys; reported below)
   EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
@@ -795,7 +818,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   EB_CUDA_TRY(cudaMemsetAsync(t.vcount.p, 0, sizeof(int) * NB, st));
   if (L >= 2) {
     const int first = t.lev_off[2];
-    k_vlist<<<nblk(t.nbox - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox, t.R,
+    k_vlist<<<nblk(32LL * (t.nbox - first), 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox, t.R,
                                                        t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                                        t.vcount.as<int>());
     eb_count_launch(ctx);
@@ -822,7 +845,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   for (DevBuf* d : {&t.ucnt, &t.wcnt, &t.tcount, &t.gcount})
     EB_CUDA_TRY(cudaMemsetAsync(d->p, 0, sizeof(int) * (NB + 1), st));
   k_leaf_lists<false><<<nblk(NBi, 128), 128, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
-                                                       t.blev.as<unsigned char>(), lo, t.R, t.child0.as<int>(),
+                                                       t.blev.as<unsigned char>(), lo, t.R, lmin_d, t.child0.as<int>(),
                                                        t.nchild.as<int>(), t.ucnt.as<int>(), t.wcnt.as<int>(),
                                                        nullptr, nullptr, nullptr, nullptr, lerr_d);
   k_group_count<<<nblk(NBi, BS), BS, 0, st>>>(NBi, nleaf_d, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
@@ -883,7 +906,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   EB_TRY(t.ulist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nu, 1)));
   EB_TRY(t.wlist.ensure(sizeof(int) * (size_t)std::max<long long>(t.nw, 1)));
   k_leaf_lists<true><<<nblk(nl, 128), 128, 0, st>>>(nl, nullptr, t.leaves.as<int>(), t.bkey.as<unsigned long long>(),
-                                                     t.blev.as<unsigned char>(), lo, t.R, t.child0.as<int>(),
+                                                     t.blev.as<unsigned char>(), lo, t.R, lmin_d, t.child0.as<int>(),
                                                      t.nchild.as<int>(), nullptr, nullptr, t.ustart.as<int>(),
                                                      t.wstart.as<int>(), t.ulist.as<int>(), t.wlist.as<int>(),
                                                      lerr_d);
