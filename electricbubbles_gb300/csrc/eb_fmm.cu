@@ -1378,14 +1378,6 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   }
 }
 
-// Kahan-compensated FP32 sum.
-__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
-  float y = v - c;
-  float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
 // FP32 far field, one block per tile of the near field: the local expansions of the
 // leaf and of its nearest ancestors (at most EB_FAR_LEVELS boxes, the coarsest holding
 // the L2L-accumulated expansion of the levels above) are staged in shared memory, and
@@ -1465,14 +1457,35 @@ __global__ void __launch_bounds__(128) k_far32(const int4* __restrict__ tiles, c
   }
 }
 
-// FP32 near field, one block per tile of up to EB_NTILE targets of one leaf: the sources
-// of the leaf's U list (32 boxes at a time) are staged through shared memory in slabs of
-// NEAR_SLAB, and each of the 128 / EB_NTILE warps sums one slice of every slab for all
-// targets of the tile (a shared-memory broadcast per source). Per-thread
-// Kahan-compensated sums; the slices are added in a fixed order. Writes the near-field
-// sums in sorted order. Positions are absolute (float hi + lo), so sources of any level
-// are alike.
+// FP32 near field, one block per tile of up to EB_NTILE (32) targets of one leaf: the
+// sources of the leaf's U list (32 boxes at a time) are staged through shared memory in
+// slabs of NEAR_SLAB. Each thread holds two targets of the tile (lanes l and l + 16 of
+// the tile) and each half-warp takes one of 8 source slices, so every staged source is
+// read once per two targets (a broadcast within the half-warp). The slices are added in
+// a fixed order. The self pair needs no test: its offset is exactly zero, and with the
+// squared distance offset by 1e-36 its terms are exact zeros. Plain FP32 sums: the error
+// of the FP32 terms themselves (~1e-6 of the largest) dominates the summation error, so
+// compensated sums buy nothing. Writes the near-field sums in sorted order. Positions are
+// absolute (float hi + lo), so sources of any level are alike.
 #define NEAR_SLAB 256
+template <int E>
+__device__ __forceinline__ void near_pair(const float4 hlj, const float4 PQ, const float2 A, const float4 hl,
+                                          float& gx, float& gy) {
+  const float dx = (hlj.x - hl.x) + (hlj.z - hl.z);
+  const float dy = (hlj.y - hl.y) + (hlj.w - hl.w);
+  const float rr = __fdividef(1.0f, fmaf(dx, dx, fmaf(dy, dy, 1e-36f)));
+  const float ix = dx * rr, iy = -dy * rr;  // 1 / (z_s - z_t)
+  if (E == 2) {
+    const float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
+    const float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
+    gx = fmaf(PQ.x, ix, fmaf(-PQ.y, iy, fmaf(A.x, tx, fmaf(-A.y, ty, gx))));
+    gy = fmaf(PQ.z, iy, fmaf(PQ.w, ix, fmaf(A.x, ty, fmaf(A.y, tx, gy))));
+  } else {
+    gx = fmaf(-A.x, ix, fmaf(A.y, iy, gx));
+    gy = fmaf(-A.x, iy, fmaf(-A.y, ix, gy));
+  }
+}
+
 template <int E>
 __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tiles, const int* __restrict__ leaves,
                                                    const int* __restrict__ pt0, const int* __restrict__ pt1,
@@ -1482,28 +1495,29 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
                                                    const float2* __restrict__ aa,
                                                    const float2* __restrict__ qa,
                                                    double2* __restrict__ nearbuf) {
-  constexpr int T = EB_NTILE, NS = 128 / T;
+  static_assert(EB_NTILE == 32, "two targets per thread over 16 lanes");
+  constexpr int NS = 8;
   __shared__ float4 sz[NEAR_SLAB];
   __shared__ float4 sp[E == 2 ? NEAR_SLAB : 1];
   __shared__ float2 sa[NEAR_SLAB];
-  __shared__ int spre[33], sj0[32], sself;
-  __shared__ float2 sred[NS][T];
+  __shared__ int spre[33], sj0[32];
+  __shared__ float2 sred[NS][EB_NTILE];
   const int4 tl = tiles[blockIdx.x];
-  const int leaf = tl.x, b = leaves[leaf];
-  const int tid = threadIdx.x, tt = tid % T, sl = tid / T;
-  const int i = tl.y + tt;
-  const bool act = i < tl.z;
-  const int ii = act ? i : tl.y;
-  const float4 hl = zhl[ii];
-  float gx = 0.f, gy = 0.f, cx = 0.f, cy = 0.f;
+  const int leaf = tl.x;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int sl = 2 * (tid >> 5) + (lane >> 4);  // source slice 0..7
+  const int t0 = lane & 15;                       // targets t0 and t0 + 16 of the tile
+  const int i0 = tl.y + t0, i1 = i0 + 16;
+  const float4 h0 = zhl[i0 < tl.z ? i0 : tl.y], h1 = zhl[i1 < tl.z ? i1 : tl.y];
+  float gx0 = 0.f, gy0 = 0.f, gx1 = 0.f, gy1 = 0.f;
   const int ub = ustart[leaf], ue = ustart[leaf + 1];
   for (int cb = ub; cb < ue; cb += 32) {
     const int nc = min(32, ue - cb);
     if (cb > ub) __syncthreads();  // the previous boxes' slabs are consumed
     if (tid < 32) {
-      int c = 0, j0 = 0, sbx = -1;
+      int c = 0, j0 = 0;
       if (tid < nc) {
-        sbx = ulist[cb + tid];
+        const int sbx = ulist[cb + tid];
         j0 = pt0[sbx];
         c = pt1[sbx] - j0;
       }
@@ -1516,22 +1530,21 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
       sj0[tid] = j0;
       spre[tid + 1] = x;
       if (tid == 0) spre[0] = 0;
-      const unsigned int m = __ballot_sync(0xffffffffu, sbx == b);
-      if (tid == 0) sself = __ffs(m) - 1;
     }
     __syncthreads();
     const int total = spre[nc];
-    const int ks = sself;
-    // staged position of the target itself (its own leaf is in its U list)
-    const int selfpos = ks >= 0 ? spre[ks] + (ii - sj0[ks]) : -1;
     for (int base = 0; base < total; base += NEAR_SLAB) {
       const int ns = min(NEAR_SLAB, total - base);
       if (base > 0) __syncthreads();
       for (int s2 = tid; s2 < ns; s2 += 128) {
         const int gs = base + s2;
-        int k = 0;
-        for (int q = 1; q < nc; ++q) k += gs >= spre[q];
-        const int j = sj0[k] + gs - spre[k];
+        int lo = 0, hi = nc;  // the box k with spre[k] <= gs < spre[k + 1]
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (spre[mid] <= gs) lo = mid;
+          else hi = mid;
+        }
+        const int j = sj0[lo] + gs - spre[lo];
         sz[s2] = zhl[j];
         if (E == 2) {
           sp[s2] = reinterpret_cast<const float4*>(pq)[j];
@@ -1541,43 +1554,27 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
         }
       }
       __syncthreads();
-      const int sp0 = selfpos - base;
-#pragma unroll 4
+#pragma unroll 2
       for (int jj = sl; jj < ns; jj += NS) {
         const float4 hlj = sz[jj];
-        const float dx = (hlj.x - hl.x) + (hlj.z - hl.z);
-        const float dy = (hlj.y - hl.y) + (hlj.w - hl.w);
-        float rr = __fdividef(1.0f, fmaf(dx, dx, dy * dy));
-        rr = jj == sp0 ? 0.f : rr;  // the self pair (dx = dy = 0) contributes nothing
-        const float ix = dx * rr, iy = -dy * rr;
-        float tx_, ty_;
-        if (E == 2) {
-          const float4 PQ = sp[jj];
-          const float2 A = sa[jj];
-          const float w2x = fmaf(ix, ix, -iy * iy), w2y = -2.0f * ix * iy;
-          const float tx = fmaf(dx, w2x, -dy * w2y), ty = fmaf(dx, w2y, dy * w2x);
-          tx_ = fmaf(PQ.x, ix, fmaf(-PQ.y, iy, fmaf(A.x, tx, -A.y * ty)));
-          ty_ = fmaf(PQ.z, iy, fmaf(PQ.w, ix, fmaf(A.x, ty, A.y * tx)));
-        } else {
-          const float2 q = sa[jj];
-          tx_ = fmaf(-q.x, ix, q.y * iy);
-          ty_ = fmaf(-q.x, iy, -q.y * ix);
-        }
-        kahan_add(gx, cx, tx_);
-        kahan_add(gy, cy, ty_);
+        const float4 PQ = E == 2 ? sp[jj] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 A = sa[jj];
+        near_pair<E>(hlj, PQ, A, h0, gx0, gy0);
+        near_pair<E>(hlj, PQ, A, h1, gx1, gy1);
       }
     }
   }
-  sred[sl][tt] = make_float2(gx - cx, gy - cy);
+  sred[sl][t0] = make_float2(gx0, gy0);
+  sred[sl][t0 + 16] = make_float2(gx1, gy1);
   __syncthreads();
-  if (sl == 0 && act) {
-    float2 v = sred[0][tt];
+  if (tid < EB_NTILE && tl.y + tid < tl.z) {
+    float2 v = sred[0][tid];
 #pragma unroll
     for (int q = 1; q < NS; ++q) {
-      v.x += sred[q][tt].x;
-      v.y += sred[q][tt].y;
+      v.x += sred[q][tid].x;
+      v.y += sred[q][tid].y;
     }
-    nearbuf[i] = make_double2((double)v.x, (double)v.y);
+    nearbuf[tl.y + tid] = make_double2((double)v.x, (double)v.y);
   }
 }
 

@@ -1,0 +1,79 @@
+"""A short run of every stage of the hot path, for kernel profilers.
+
+    python -m electricbubbles_gb300.profcase [stage ...]
+
+Stages (all by default), on the 64-drop x 512-node workload unless named otherwise:
+  tree     geometry install: EXTRACTDAT and the adaptive tree build
+  solve    one FP32-refined Stokes solve with the GMRES loop driven from the host, so
+           that every kernel is its own launch (the Arnoldi, FP32 and double-float
+           operator kernels)
+  apply    ten FP32 Stokes operator applies, then ten double-float ones
+  rk2      one FP32-refined RK2 step (the spectral kernels, SETVELF, EQUIT, both solves)
+  batch    one FP32-refined RK2 step of 64 of the uneven simulations as one batch
+
+Each stage runs once; the device holds well under 1 GB. Prints "ok" at the end.
+"""
+import sys
+
+import numpy as np
+
+from . import configs
+from .api import Context
+
+
+def _tree(ctx, cfg):
+    return ctx.extractdat(cfg.nd, cfg.rku())
+
+
+def stage_tree():
+    ctx = Context(graphs=-1)
+    _tree(ctx, configs.many_drops())
+
+
+def stage_solve():
+    cfg = configs.many_drops()
+    ctx = Context(graphs=-1)
+    g = _tree(ctx, cfg)
+    rhs = np.ascontiguousarray(-0.5 * g["dz"] / g["dsda"]).view(np.float64).copy()
+    ctx.solvei(rhs, "fp32_refined")
+
+
+def stage_apply():
+    cfg = configs.many_drops()
+    rng = np.random.default_rng(5)
+    dens = rng.standard_normal(cfg.nbk) + 1j * rng.standard_normal(cfg.nbk)
+    for prec, df64 in (("fp32", 0), ("fp64", 1)):
+        ctx = Context(graphs=-1, df64=df64)
+        _tree(ctx, cfg)
+        for _ in range(10):
+            ctx.stokes_sum(dens, -1, prec)
+        ctx.close()
+
+
+def stage_rk2():
+    cfg = configs.many_drops()
+    ctx = Context(graphs=-1)
+    ctx.rk2(cfg.nd, 1e-3, cfg.rku(), e0=0.5, mode="fp32_refined")
+
+
+def stage_batch():
+    sims = configs.uneven_simulations()[:64]
+    ctx = Context()
+    ctx.batch_define([s.k for s in sims], np.array([s.params["E0"] for s in sims]))
+    nd = np.concatenate([s.nd for s in sims])
+    y = np.concatenate([s.rku() for s in sims])
+    ctx.rk2(nd, 1e-3, y, mode="fp32_refined")
+
+
+STAGES = {"tree": stage_tree, "solve": stage_solve, "apply": stage_apply, "rk2": stage_rk2,
+          "batch": stage_batch}
+
+
+def main(argv):
+    for name in argv or list(STAGES):
+        STAGES[name]()
+    print("ok")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
