@@ -177,3 +177,23 @@ def small_drops(k=3, n=64, seed=7, box=3.0, gap=0.3):
     rng = np.random.default_rng(seed)
     c, r = _place(rng, k, lambda g, m: g.uniform(0.5, 1.0, m), box, gap, 1.05)
     return _build("small_%dx%d" % (k, n), np.full(k, n), c, r, np.full(k, 0.05), {"seed": seed})
+
+
+def wall_drops(k=16, n=256, seed=8, box=8.0, gap=0.3, zbond=-0.2 + 0j):
+    """16 drops of 256 nodes above the wall y = 0 (wall-bounded flow, zbond != 0): radii
+    U[0.5, 1.0], centres x in [-8, 8], y in [gap + r, gap + r + box/2], at least `gap`
+    from the wall and from each other."""
+    rng = np.random.default_rng(seed)
+    radii = rng.uniform(0.5, 1.0, k)
+    centres, rr = [], []
+    for r in radii:
+        for _ in range(1_000_000):
+            c = rng.uniform(-box, box) + 1j * (1.06 * r + gap + rng.uniform(0.0, 0.5 * box))
+            if all(abs(c - c2) > 1.05 * (r + r2) + gap for c2, r2 in zip(centres, rr)):
+                centres.append(c)
+                rr.append(r)
+                break
+        else:
+            raise RuntimeError("could not place drops without overlap")
+    return _build("wall_%dx%d" % (k, n), np.full(k, n), np.array(centres), np.array(rr), np.full(k, 0.05),
+                  {"seed": seed, "E0": 0.5, "cap": 0.0, "zbond": zbond, "dt": 1e-3})

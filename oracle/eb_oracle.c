@@ -409,23 +409,105 @@ static int mkintl(int nside, int ix, int iy, int* out) {
 int eb_or_cadap_fmm(int n, const cplx* zin, const cplx* dzin, const double* hpt,
                     const cplx* dens, int sign, int levmax, double tol, cplx* gradw,
                     int nthreads) {
+  return eb_or_cadap_fmm_w(n, zin, dzin, hpt, dens, sign, levmax, tol, 0, 0.0, 0.0, gradw, nthreads);
+}
+
+/* MPREFLECT, cadap2.f:1468-1507: the expansions of PHI and PSI (1-based m1, m2 about
+ * zc, absolute PSI) reflected across the wall y = 0, about conj(zc). */
+static void mpreflect(cplx zc, const cplx* m1, const cplx* m2, int p, cplx* r1, cplx* r2) {
+  r1[1] = conj(m1[1] - m2[1]);
+  r2[1] = r1[1] - conj(m1[1]);
+  for (int k = 2; k <= p; ++k) {
+    r1[k] = conj(-m2[k] + (double)k * m1[k] + (double)(k - 1) * m1[k - 1] * zc);
+    r2[k] = -conj(m1[k]) + (double)k * r1[k] + (double)(k - 1) * r1[k - 1] * conj(zc);
+  }
+}
+
+/* The column range of MKINTL / MKINTR (cadap2.f:780-877), 0-based: the children of the
+ * parent columns next to the parent of column c. */
+static void mk_colrange(int nside, int c, int* lo, int* hi) {
+  int col = c + 1;
+  if (col % 2 == 0) { *lo = col - 3 > 1 ? col - 3 : 1; *hi = col + 2 < nside ? col + 2 : nside; }
+  else { *lo = col - 2 > 1 ? col - 2 : 1; *hi = col + 3 < nside ? col + 3 : nside; }
+  *lo -= 1;
+  *hi -= 1;
+}
+
+/* The image sources of target box (tx, ty): the source boxes of the first two rows whose
+ * MKINTR list (cadap2.f:830-877) holds the target, in increasing box order. MKINTR of a
+ * source in row IROWB takes the columns of its parent's neighbours in rows 1 and 2, and
+ * row 1 only when IROWB = 2 or the columns differ by more than one; the relation is
+ * symmetric in the two boxes' columns. */
+static int mkintr_sources(int nside, int tx, int ty, int* out) {
+  int n = 0, lo, hi;
+  if (ty > 1) return 0;
+  mk_colrange(nside, tx, &lo, &hi);
+  for (int sy = 0; sy <= 1 && sy < nside; ++sy)
+    for (int sx = lo; sx <= hi; ++sx) {
+      if (ty == 0 && sy == 0 && abs(sx - tx) <= 1) continue;
+      out[n++] = sy * nside + sx;
+    }
+  return n;
+}
+
+/* SLDREFDR (cadapdrop2.f:857-934, sign -1) / SLDREF (cadap2.f:1509-1586, sign +1) with
+ * I1 = 0: the reflected sources of one box at one target. */
+static cplx sldref(cplx zt, int nin, const int* idx, const cplx* zs, const cplx* qa,
+                   const cplx* qb, const cplx* qc, double s) {
+  cplx phil = 0, phipl = 0, psil = 0;
+  for (int jj = 0; jj < nin; ++jj) {
+    int j = idx[jj];
+    cplx zd = conj(zs[j]) - zt, zd2 = zd * zd, zd3 = zd2 * zd;
+    cplx g1 = -conj(qb[j]) + conj(qa[j]);
+    cplx d1 = -conj(qb[j]);
+    cplx g2 = -conj(qc[j]) - conj(qa[j] * zs[j]);
+    cplx d2 = 2.0 * g2 - conj(zs[j]) * g1;
+    cplx d3 = -2.0 * conj(zs[j]) * g2;
+    phil += g1 / zd;
+    phil += g2 / zd2;
+    phipl += g1 / zd2;
+    phipl += 2.0 * g2 / zd3;
+    psil += d1 / zd;
+    psil += d2 / zd2;
+    psil += d3 / zd3;
+  }
+  return phil + s * (zt * conj(phipl) + conj(psil));
+}
+
+/* CADAPDR / CADAPMOD with IFLAG2 = 1 (wall-bounded, iwall != 0): the sources are scaled
+ * into the square [xleft, xleft + slength] x [0, slength] (cadapdrop.f:142-145), whose
+ * bottom edge is the wall; every level adds the reflected multipoles of the first two
+ * rows (MPREFLECT + MKINTR, cadapdrop2.f:159-197), and the finest level the reflected
+ * near field of the first row (MKNBRRFL + SLDREFDR, cadapdrop2.f:690-721). */
+int eb_or_cadap_fmm_w(int n, const cplx* zin, const cplx* dzin, const double* hpt,
+                      const cplx* dens, int sign, int levmax, double tol, int iwall,
+                      double xleft, double slength, cplx* gradw, int nthreads) {
   int nterms = -(int)lround(log(tol) / log(2.0));
   if (nterms > 60) return 4;
   const int p = nterms, nlmax = nterms / 2;
   const double s = (double)sign;
   int nt = clamp_threads(nthreads);
   (void)nt;
-  double rminx = creal(zin[0]), rmaxx = creal(zin[0]);
-  double rminy = cimag(zin[0]), rmaxy = cimag(zin[n > 1 ? 1 : 0]);
-  for (int i = 0; i < n; ++i) {
-    double x = creal(zin[i]), y = cimag(zin[i]);
-    if (x > rmaxx) rmaxx = x;
-    if (y > rmaxy) rmaxy = y;
-    if (x < rminx) rminx = x;
-    if (y < rminy) rminy = y;
+  double rminx, rminy, rscal;
+  if (iwall) {
+    rscal = 64.0 / slength;
+    rminx = xleft;
+    rminy = 0.0;
+  } else {
+    rminx = creal(zin[0]);
+    double rmaxx = creal(zin[0]);
+    rminy = cimag(zin[0]);
+    double rmaxy = cimag(zin[n > 1 ? 1 : 0]);
+    for (int i = 0; i < n; ++i) {
+      double x = creal(zin[i]), y = cimag(zin[i]);
+      if (x > rmaxx) rmaxx = x;
+      if (y > rmaxy) rmaxy = y;
+      if (x < rminx) rminx = x;
+      if (y < rminy) rminy = y;
+    }
+    double rsx = rmaxx - rminx, rsy = rmaxy - rminy;
+    rscal = 64.0 / (rsx > rsy ? rsx : rsy);
   }
-  double rsx = rmaxx - rminx, rsy = rmaxy - rminy;
-  double rscal = 64.0 / (rsx > rsy ? rsx : rsy);
   const cplx z2pi = 1.0 / (2.0 * 4.0 * atan(1.0) * I);
   cplx* zs = (cplx*)malloc(sizeof(cplx) * (size_t)n);
   cplx* qa = (cplx*)malloc(sizeof(cplx) * (size_t)n);
@@ -455,6 +537,9 @@ int eb_or_cadap_fmm(int n, const cplx* zin, const cplx* dzin, const double* hpt,
   int* icnt = (int*)malloc(sizeof(int) * nbmax);
   cplx* mp1 = (cplx*)malloc(sizeof(cplx) * nbmax * (size_t)(p + 1));
   cplx* mp2 = (cplx*)malloc(sizeof(cplx) * nbmax * (size_t)(p + 1));
+  /* reflected multipoles of the first two rows (wall) */
+  cplx* mr1 = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)nsidemax * (size_t)(p + 1));
+  cplx* mr2 = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)nsidemax * (size_t)(p + 1));
 
   for (int ilev = 1; ilev <= levmax; ++ilev) {
     int nside = 1 << ilev;
@@ -486,6 +571,9 @@ int eb_or_cadap_fmm(int n, const cplx* zin, const cplx* dzin, const double* hpt,
       cplx zc = ((b % nside) + 0.5) * hbox + ((b / nside) + 0.5) * hbox * I;
       slmkxp(zc, nin, iatadr + ioffst[b], zs, qa, qb, qc, mp1 + (size_t)b * (p + 1),
              mp2 + (size_t)b * (p + 1), p);
+      if (iwall && b < 2 * nside)
+        mpreflect(zc, mp1 + (size_t)b * (p + 1), mp2 + (size_t)b * (p + 1), p,
+                  mr1 + (size_t)b * (p + 1), mr2 + (size_t)b * (p + 1));
     }
     /* Interaction lists, per target box (DOINT0DR, cadapdrop2.f:84-197) and the
      * local-expansion evaluation (:200-234). */
@@ -494,18 +582,27 @@ int eb_or_cadap_fmm(int n, const cplx* zin, const cplx* dzin, const double* hpt,
       int ntin = ioffst[t + 1] - ioffst[t];
       if (ntin <= 0) continue;
       int tx = t % nside, ty = t / nside;
-      int list[40];
+      int list[40], rlist[16];
       int nl = mkintl(nside, tx, ty, list);
+      int nr = iwall ? mkintr_sources(nside, tx, ty, rlist) : 0;
       cplx zct = (tx + 0.5) * hbox + (ty + 0.5) * hbox * I;
       cplx l1[64], l2[64];
       for (int j = 0; j <= p; ++j) { l1[j] = 0; l2[j] = 0; }
-      for (int q = 0; q < nl; ++q) {
-        int sb = list[q];
+      /* source boxes in increasing order, each with its direct then its reflected part
+       * (the order of DOINT0DR's source loop, cadapdrop2.f:84-197) */
+      for (int q = 0, qr = 0; q < nl || qr < nr;) {
+        int refl = q >= nl || (qr < nr && rlist[qr] < list[q]);
+        int sb = refl ? rlist[qr++] : list[q++];
         int nsin = ioffst[sb + 1] - ioffst[sb];
         if (nsin <= 0) continue;
         cplx zcs = ((sb % nside) + 0.5) * hbox + ((sb / nside) + 0.5) * hbox * I;
         const cplx* m1 = mp1 + (size_t)sb * (p + 1);
         const cplx* m2 = mp2 + (size_t)sb * (p + 1);
+        if (refl) {
+          zcs = conj(zcs);
+          m1 = mr1 + (size_t)sb * (p + 1);
+          m2 = mr2 + (size_t)sb * (p + 1);
+        }
         if (ntin <= nlmax) {
           for (int kk = 0; kk < ntin; ++kk) {
             int jt = iatadr[ioffst[t] + kk];
@@ -566,12 +663,93 @@ int eb_or_cadap_fmm(int n, const cplx* zin, const cplx* dzin, const double* hpt,
           }
         }
       }
+      /* reflected near field of the first row (DONN0DR's IFLAG2 loop, after the direct
+       * near field of every box): the first-row source boxes next to the target box */
+      if (iwall && ty == 0) {
+        for (int sx = tx - 1; sx <= tx + 1; ++sx) {
+          if (sx < 0 || sx >= nside) continue;
+          int s0 = ioffst[sx], nsin = ioffst[sx + 1] - s0;
+          if (nsin <= 0) continue;
+          for (int kk = 0; kk < ntin; ++kk) {
+            int it = iatadr[ioffst[t] + kk];
+            gradw[it] += sldref(zs[it], nsin, iatadr + s0, zs, qa, qb, qc, s);
+          }
+        }
+      }
     }
   }
   for (int j = 0; j < n; ++j) gradw[j] *= rscal;
   free(zs); free(qa); free(qb); free(qc); free(binom); free(ibox); free(iatadr);
-  free(ioffst); free(icnt); free(mp1); free(mp2);
+  free(ioffst); free(icnt); free(mp1); free(mp2); free(mr1); free(mr2);
   return 0;
+}
+
+/* Exact value of the reflected part of the wall-bounded sum (IFLAG2 = 1): the images of
+ * all sources across y = 0, the target's own image included, with the pair terms of
+ * SLDREFDR (sign -1) / SLDREF (sign +1) in physical coordinates. With qc = -conj(z) qa,
+ *   gamma1 = conj(qa) - conj(qb), gamma2 = 2 i y_j conj(qa), delta1 = -conj(qb),
+ *   Phi = gamma1/zeta + gamma2/zeta^2,  zeta = conj(z_j) - z_t,
+ * and z_t conj(Phi') + conj(Psi) = (z_t - z_j) conj(gamma1/zeta^2 + 2 gamma2/zeta^3)
+ * + 2 conj(gamma2/zeta^2) + conj(delta1/zeta) (no terms of size |z|). */
+void eb_or_stokes_image_direct(int n, const cplx* z, const cplx* dz, const double* hpt,
+                               const cplx* dens, int sign, cplx* gimg, int nthreads) {
+  cplx* qa = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+  cplx* qb = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+  stokes_charges(n, dz, hpt, dens, qa, qb);
+  const double s = (double)sign;
+  int nt = clamp_threads(nthreads);
+  (void)nt;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 16)
+  for (int t = 0; t < n; ++t) {
+    cplx acc = 0, zt = z[t];
+    for (int j = 0; j < n; ++j) {
+      cplx g1 = conj(qa[j]) - conj(qb[j]), d1 = -conj(qb[j]);
+      cplx g2 = 2.0 * I * cimag(z[j]) * conj(qa[j]);
+      cplx tz = 1.0 / (conj(z[j]) - zt), t2 = tz * tz, dd = zt - z[j];
+      acc += g1 * tz + g2 * t2 +
+             s * (dd * conj(g1 * t2 + 2.0 * g2 * t2 * tz) + 2.0 * conj(g2 * t2) + conj(d1 * tz));
+    }
+    gimg[t] = acc;
+  }
+  free(qa);
+  free(qb);
+}
+
+/* REFSING, reflect.f:28-86: the images across y = 0 of the log sources zc at the drop
+ * centres zk and of the poles zb, added to phi, phi' and psi at ztarg. */
+void eb_or_refsing(cplx zt, int k, const cplx* zk, const cplx* zc, const cplx* zb, cplx* phi,
+                   cplx* phip, cplx* psi) {
+  for (int j = 0; j < k; ++j) {
+    cplx zdis = zt - conj(zk[j]), zdis2 = zdis * zdis;
+    cplx gamma1 = -conj(zb[j]), delta1 = gamma1, delta2 = conj(zk[j]) * gamma1;
+    *phi += gamma1 / zdis;
+    *phip -= gamma1 / zdis2;
+    *psi += delta1 / zdis;
+    *psi += delta2 / zdis2;
+    *phi -= zc[j] * clog(zdis);
+    *phip -= zc[j] / zdis;
+    *psi -= conj(zc[j]) * clog(zdis);
+    cplx alpha1 = conj(zc[j]) * (zk[j] - conj(zk[j]));
+    cplx beta1 = zc[j] * conj(zk[j]) + alpha1, beta2 = alpha1 * conj(zk[j]);
+    *phi += alpha1 / zdis;
+    *phip -= alpha1 / zdis2;
+    *psi += beta1 / zdis;
+    *psi += beta2 / zdis2;
+  }
+}
+
+/* The wall data of EXTRACTDAT (electric.f:657-711): xleft = min x, slength =
+ * max(max x - min x, max y) over all nodes. */
+void eb_or_wallinfo(int nbk, const cplx* z, double* xleft, double* slength) {
+  double xmin = 1e10, xmax = -1e10, ymax = -1e10;
+  for (int i = 0; i < nbk; ++i) {
+    double x = creal(z[i]), y = cimag(z[i]);
+    xmin = x < xmin ? x : xmin;
+    xmax = x > xmax ? x : xmax;
+    ymax = y > ymax ? y : ymax;
+  }
+  *xleft = xmin;
+  *slength = xmax - xmin > ymax ? xmax - xmin : ymax;
 }
 
 /* ======================================================================
@@ -610,6 +788,15 @@ static double* per_point_h(const eb_or_geom* g) {
   return h;
 }
 
+/* gw += the exact reflected part of the wall-bounded sum */
+static void add_images(const eb_or_geom* g, const double* h, const cplx* dens, int sign, cplx* gw,
+                       int nthreads) {
+  cplx* gi = (cplx*)malloc(sizeof(cplx) * (size_t)g->nbk);
+  eb_or_stokes_image_direct(g->nbk, g->z, g->dz, h, dens, sign, gi, nthreads);
+  for (int i = 0; i < g->nbk; ++i) gw[i] += gi[i];
+  free(gi);
+}
+
 /* FASMVP, stokesbubb.f:496-614 (the Stokes matvec behind MATVEC,
  * stokesbubb.f:419-465): u is the interleaved real vector of length 2 nbk. */
 void eb_or_fasmvp(const eb_or_geom* g, const double* u, double* w, int mode,
@@ -636,10 +823,14 @@ void eb_or_fasmvp(const eb_or_geom* g, const double* u, double* w, int mode,
   }
   double pinf = -pk[0];
   for (int b = 0; b < k; ++b) pk[b] += pinf;
-  if (mode == EB_OR_CADAP)
-    eb_or_cadap_fmm(nbk, g->z, g->dz, h, dens, -1, 7, 1e-13, stress, nthreads);
-  else
+  /* CADAPDR with IFLAG2 = iwall (stokesbubb.f:553-563) */
+  if (mode == EB_OR_CADAP) {
+    eb_or_cadap_fmm_w(nbk, g->z, g->dz, h, dens, -1, 7, 1e-13, g->iwall, g->xleft, g->slength, stress,
+                      nthreads);
+  } else {
     eb_or_stokes_direct(nbk, g->z, g->dz, h, dens, -1, stress, nthreads);
+    if (g->iwall) add_images(g, h, dens, -1, stress, nthreads);
+  }
   ist = 0;
   for (int b = 0; b < k; ++b) {
     double qwi = 2.0 * EB_PI / g->nd[b];
@@ -1082,10 +1273,14 @@ void eb_or_interfacenew(const eb_or_geom* g, const cplx* ckern, const cplx* zc,
     eb_or_fdifff(g->nd[b], u + ist, udot + ist);
     ist += g->nd[b];
   }
-  if (mode == EB_OR_CADAP)
-    eb_or_cadap_fmm(nbk, g->z, g->dz, h, u, +1, 7, 1e-13, gw, nthreads);
-  else
+  /* CADAPMOD with IFLAG2 = iwall (electric.f:828-837) */
+  if (mode == EB_OR_CADAP) {
+    eb_or_cadap_fmm_w(nbk, g->z, g->dz, h, u, +1, 7, 1e-13, g->iwall, g->xleft, g->slength, gw, nthreads);
+  } else {
     eb_or_stokes_direct(nbk, g->z, g->dz, h, u, +1, gw, nthreads);
+    if (g->iwall) add_images(g, h, u, +1, gw, nthreads);
+  }
+  cplx* zb = (cplx*)calloc((size_t)(k > 0 ? k : 1), sizeof(cplx)); /* zb = 0 (electric.f:823) */
   const cplx z2pii = 1.0 / (2.0 * EB_PI * I);
   double fl = 0.0;
   ist = 0;
@@ -1104,8 +1299,9 @@ void eb_or_interfacenew(const eb_or_geom* g, const cplx* ckern, const cplx* zc,
         cplx zdis = z - g->zk[nb];
         zck = zck + 2.0 * zc[nb] * log(cabs(zdis)) + conj(zc[nb]) * zdis / conj(zdis);
       }
-      cplx zpsi = -I * 0.5 * cap * z;
-      cplx gwr = conj(zpsi);
+      cplx zphi = 0, zphip = 0, zpsi = -I * 0.5 * cap * z;
+      if (g->iwall) eb_or_refsing(z, k, g->zk, zc, zb, &zphi, &zphip, &zpsi);
+      cplx gwr = zphi + z * conj(zphip) + conj(zpsi);
       gw[t] = gw[t] + gwr + zck;
       cplx zvel = -I * gw[t];
       un[t] = creal(zvel * conj(zn));
@@ -1114,14 +1310,18 @@ void eb_or_interfacenew(const eb_or_geom* g, const cplx* ckern, const cplx* zc,
     ist += g->nd[b];
   }
   if (flux) *flux = fl;
-  free(udot); free(gw); free(h);
+  free(udot); free(gw); free(h); free(zb);
 }
 
-/* SETVELF, stokesbubb.f:4-135 (free space, iwall = 0): right-hand side of the
- * Stokes equation. Restated as written, including the electric-stress loop's use
- * of `alpha` left over from the previous loops (:125; its last value is
- * 2 pi (nd_k - 1)/nd_k of the last drop). The C_k loop (:73-102) contributes
- * exactly zero when every zc is zero, and is skipped then. */
+/* SETVELF, stokesbubb.f:4-135: right-hand side of the Stokes equation, with iwall = 1
+ * when zbond != 0 (READINI, electric.f:321-326). Restated as written, including the
+ * electric-stress loop's use of `alpha` left over from the previous loops (:125; its
+ * last value is 2 pi (nd_k - 1)/nd_k of the last drop). The C_k loop (:73-102)
+ * contributes exactly zero when every zc is zero, and is skipped then. The wall branch
+ * (:53-60) subtracts the reflected log sources (REFSING with zb = 0) and then `zstr`,
+ * which that branch never assigns (:67): it is taken here as the capillary term of the
+ * free-space branch, -conj(-i cap z / 2), the term INTERFACENEW keeps in both cases
+ * (electric.f:868-871); the two readings agree when cap = 0. */
 void eb_or_setvelf(const eb_or_geom* g, const cplx* zc, cplx zbond, double cap,
                    double e0, const double* dphi_dn, double* rhs) {
   int k = g->k, ndmax = 0;
@@ -1130,6 +1330,7 @@ void eb_or_setvelf(const eb_or_geom* g, const cplx* zc, cplx zbond, double cap,
   cplx* zfi = (cplx*)malloc(sizeof(cplx) * (size_t)ndmax);
   int anyzc = 0;
   for (int b = 0; b < k; ++b) if (zc[b] != 0) anyzc = 1;
+  cplx* zb0 = (cplx*)calloc((size_t)(k > 0 ? k : 1), sizeof(cplx)); /* zb = 0 (stokesbubb.f:26-28) */
   double alpha = 0.0;
   int ist = 0;
   for (int b = 0; b < k; ++b) {
@@ -1145,6 +1346,11 @@ void eb_or_setvelf(const eb_or_geom* g, const cplx* zc, cplx zbond, double cap,
       cplx zn = -0.5 * g->dz[ist + i] / g->dsda[ist + i];
       cplx zgrav = -I * 0.25 * (alpha * zfi[0] + zf[i]);
       cplx r = zn + zgrav;
+      if (zbond != 0) {
+        cplx zphi = 0, zphip = 0, zpsi0 = 0, zz = g->z[ist + i];
+        eb_or_refsing(zz, k, g->zk, zc, zb0, &zphi, &zphip, &zpsi0);
+        r -= zphi - zz * conj(zphip) - conj(zpsi0);
+      }
       cplx zpsi = -I * 0.5 * cap * g->z[ist + i];
       cplx zstr = -conj(zpsi);
       r -= zstr;
@@ -1195,6 +1401,7 @@ void eb_or_setvelf(const eb_or_geom* g, const cplx* zc, cplx zbond, double cap,
   }
   free(zf);
   free(zfi);
+  free(zb0);
 }
 
 /* EQUIT, electric.f:1270-1302: tangential velocity keeping nodes equi-arclength. */
@@ -1392,7 +1599,11 @@ void eb_or_f(eb_or_model* m, int k, const int* nd, const double* rku, double* rk
   cplx* zf = (cplx*)malloc(sizeof(cplx) * (size_t)ndmax);
   eb_or_extractdat(k, nd, rku, z, zk, dz, tha, dsda, kappa, ckern, area);
   for (int b = 0; b < k; ++b) zc[b] = I * m->zbond * area[b] / (8.0 * EB_PI);
-  eb_or_geom g = {k, nd, nbk, z, dz, dsda, kappa, zk};
+  eb_or_geom g = {k, nd, nbk, z, dz, dsda, kappa, zk, 0, 0.0, 0.0};
+  if (m->zbond != 0) { /* wall-bounded (READINI, electric.f:321-326) */
+    g.iwall = 1;
+    eb_or_wallinfo(nbk, z, &g.xleft, &g.slength);
+  }
   mv_ud ud = {&g, m->mode, m->nthreads};
   /* Laplace solve: GETBCs (laplace.f:5-25) then SOLVE_LAPL (x0 = rhs). */
   for (int i = 0; i < nbk; ++i) rhs[i] = -2.0 * creal(z[i]);

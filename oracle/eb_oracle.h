@@ -38,6 +38,8 @@ typedef struct {
   const double* dsda;      /* |dz| */
   const double* kappa;     /* curvature */
   const eb_or_cplx* zk;    /* drop centroids */
+  int iwall;               /* 1: wall-bounded (the wall is y = 0) */
+  double xleft, slength;   /* wall data of EXTRACTDAT (electric.f:710-711) */
 } eb_or_geom;
 
 /* ---- spectral (dcfft.f, electric.f, pv_integral.f) ---- */
@@ -63,6 +65,18 @@ void eb_or_stokes_direct_at(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
 int eb_or_cadap_fmm(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
                     const double* hpt, const eb_or_cplx* dens, int sign, int levmax,
                     double tol, eb_or_cplx* gradw, int nthreads);
+/* CADAPDR / CADAPMOD with IFLAG2 = iwall (images across the wall y = 0) */
+int eb_or_cadap_fmm_w(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
+                      const double* hpt, const eb_or_cplx* dens, int sign, int levmax,
+                      double tol, int iwall, double xleft, double slength,
+                      eb_or_cplx* gradw, int nthreads);
+/* the exact reflected part of the wall-bounded sum (all images, own image included) */
+void eb_or_stokes_image_direct(int n, const eb_or_cplx* z, const eb_or_cplx* dz,
+                               const double* hpt, const eb_or_cplx* dens, int sign,
+                               eb_or_cplx* gimg, int nthreads);
+void eb_or_refsing(eb_or_cplx zt, int k, const eb_or_cplx* zk, const eb_or_cplx* zc,
+                   const eb_or_cplx* zb, eb_or_cplx* phi, eb_or_cplx* phip, eb_or_cplx* psi);
+void eb_or_wallinfo(int nbk, const eb_or_cplx* z, double* xleft, double* slength);
 void eb_or_cauchy_direct(int nt, const eb_or_cplx* zt, int ns, const eb_or_cplx* zsrc,
                          const eb_or_cplx* q, int self, eb_or_cplx* field, int nthreads);
 

@@ -25,7 +25,7 @@ class C2(ctypes.Structure):
 
 class Geom(ctypes.Structure):
     _fields_ = [("k", _I), ("nd", _P), ("nbk", _I), ("z", _P), ("dz", _P), ("dsda", _P),
-                ("kappa", _P), ("zk", _P)]
+                ("kappa", _P), ("zk", _P), ("iwall", _I), ("xleft", _D), ("slength", _D)]
 
 
 class Model(ctypes.Structure):
@@ -55,6 +55,10 @@ def lib():
             "eb_or_stokes_direct": (None, [_I, _P, _P, _P, _P, _I, _P, _I]),
             "eb_or_stokes_direct_at": (None, [_I, _P, _P, _P, _P, _I, _I, _P, _P, _I]),
             "eb_or_cadap_fmm": (_I, [_I, _P, _P, _P, _P, _I, _I, _D, _P, _I]),
+            "eb_or_cadap_fmm_w": (_I, [_I, _P, _P, _P, _P, _I, _I, _D, _I, _D, _D, _P, _I]),
+            "eb_or_stokes_image_direct": (None, [_I, _P, _P, _P, _P, _I, _P, _I]),
+            "eb_or_refsing": (None, [C2, _I, _P, _P, _P, _P, _P, _P]),
+            "eb_or_wallinfo": (None, [_I, _P, _P, _P]),
             "eb_or_cauchy_direct": (None, [_I, _P, _I, _P, _P, _I, _P, _I]),
             "eb_or_fasmvp": (None, [ctypes.POINTER(Geom), _P, _P, _I, _I]),
             "eb_or_fasmvp_lap": (None, [ctypes.POINTER(Geom), _P, _P, _I]),
@@ -190,6 +194,48 @@ def cadap_fmm(z, dz, hpt, dens, sign, levmax=7, tol=1e-13, nthreads=0):
     return g
 
 
+def cadap_fmm_wall(z, dz, hpt, dens, sign, xleft, slength, levmax=7, tol=1e-13, nthreads=0):
+    """CADAPDR (sign -1) / CADAPMOD (sign +1) with IFLAG2 = 1: the wall y = 0."""
+    z, dz, dens = _c(z), _c(dz), _c(dens)
+    hpt = _r(hpt)
+    g = np.empty_like(z)
+    st = lib().eb_or_cadap_fmm_w(z.shape[0], _p(z), _p(dz), _p(hpt), _p(dens), int(sign),
+                                 int(levmax), float(tol), 1, float(xleft), float(slength), _p(g),
+                                 int(nthreads))
+    if st != 0:
+        raise RuntimeError("cadap_fmm IER=%d" % st)
+    return g
+
+
+def stokes_image_direct(z, dz, hpt, dens, sign, nthreads=0):
+    """The exact reflected part of the wall-bounded Stokes sum (images across y = 0)."""
+    z, dz, dens = _c(z), _c(dz), _c(dens)
+    hpt = _r(hpt)
+    g = np.empty_like(z)
+    lib().eb_or_stokes_image_direct(z.shape[0], _p(z), _p(dz), _p(hpt), _p(dens), int(sign), _p(g),
+                                    int(nthreads))
+    return g
+
+
+def refsing(zt, zk, zc, zb=None):
+    """REFSING (reflect.f:28-86) from zero: (phi, phi', psi) of the reflected singularities."""
+    zk, zc = _c(zk), _c(zc)
+    zb = np.zeros_like(zk) if zb is None else _c(zb)
+    out = np.zeros(3, np.complex128)
+    zt = complex(zt)
+    lib().eb_or_refsing(C2(zt.real, zt.imag), zk.shape[0], _p(zk), _p(zc), _p(zb),
+                        _p(out[0:1]), _p(out[1:2]), _p(out[2:3]))
+    return out[0], out[1], out[2]
+
+
+def wallinfo(z):
+    """EXTRACTDAT's xleft, slength (electric.f:657-711)."""
+    z = _c(z)
+    xl, sl = _D(), _D()
+    lib().eb_or_wallinfo(z.shape[0], _p(z), ctypes.byref(xl), ctypes.byref(sl))
+    return xl.value, sl.value
+
+
 def cauchy_direct(zt, zs, q, self_exclude, nthreads=0):
     zt, zs, q = _c(zt), _c(zs), _c(q)
     f = np.empty_like(zt)
@@ -202,18 +248,20 @@ def cauchy_direct(zt, zs, q, self_exclude, nthreads=0):
 class Geometry:
     """Geometry arrays kept alive together with the C struct that points at them."""
 
-    def __init__(self, nd, z, dz, dsda, kappa, zk):
+    def __init__(self, nd, z, dz, dsda, kappa, zk, wall=False):
         self.nd = _i(nd)
         self.z, self.dz, self.zk = _c(z), _c(dz), _c(zk)
         self.dsda, self.kappa = _r(dsda), _r(kappa)
         self.nbk = int(self.nd.sum())
         self.k = int(self.nd.shape[0])
+        xl, sl = wallinfo(self.z) if wall else (0.0, 0.0)
+        self.xleft, self.slength = xl, sl
         self.s = Geom(self.k, _p(self.nd), self.nbk, _p(self.z), _p(self.dz), _p(self.dsda),
-                      _p(self.kappa), _p(self.zk))
+                      _p(self.kappa), _p(self.zk), 1 if wall else 0, xl, sl)
 
     @classmethod
-    def from_extract(cls, nd, ex):
-        return cls(nd, ex["z"], ex["dz"], ex["dsda"], ex["kappa"], ex["zk"])
+    def from_extract(cls, nd, ex, wall=False):
+        return cls(nd, ex["z"], ex["dz"], ex["dsda"], ex["kappa"], ex["zk"], wall)
 
 
 def fasmvp(g, u, mode=0, nthreads=0):

@@ -165,3 +165,58 @@ def test_dapif2_restatement_matches_direct_sum(oracle, n):
     u = rng.standard_normal(cfg.nbk)
     a, b = oracle.fasmvp_lap(g, u), oracle.fasmvp_lap(g, u, mode=1)
     assert np.abs(a - b).max() / np.abs(a).max() < 1e-11
+
+
+# ---- wall-bounded flow (IFLAG2 = 1) ------------------------------------------------
+def _wall_case(oracle, k=6, n=128):
+    from electricbubbles_gb300 import configs
+    cfg = configs.wall_drops(k=k, n=n)
+    ex = oracle.extractdat(cfg.nd, cfg.rku())
+    rng = np.random.default_rng(2)
+    dens = rng.standard_normal(cfg.nbk) + 1j * rng.standard_normal(cfg.nbk)
+    return cfg, ex, oracle.point_h(cfg.nd), dens
+
+
+def test_refsing_images_cancel_log_sources_on_the_wall(oracle):
+    """REFSING's reflected system cancels the free field of the log sources
+    (INTERFACENEW's zck, electric.f:861-866) on y = 0: the no-slip wall."""
+    zk = np.array([0.3 + 1.2j, -1 + 0.7j, 2.0 + 0.4j])
+    zc = np.array([0.2 - 0.5j, -0.1 + 0.3j, 0.05 + 0.02j])
+    for x in (-2.0, 0.1, 1.5, 4.0):
+        z = complex(x, 0.0)
+        zck = sum(2 * c * np.log(abs(z - k)) + np.conj(c) * (z - k) / np.conj(z - k) for c, k in zip(zc, zk))
+        phi, phip, psi = oracle.refsing(z, zk, zc)
+        assert abs(zck + phi + z * np.conj(phip) + np.conj(psi)) < 1e-14
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_wall_images_on_the_wall(oracle, sign):
+    """The image sum of SLDREF / SLDREFDR on the wall itself: with the sign of CADAPMOD
+    (the velocity of INTERFACENEW) the images cancel the direct sum (no slip); with the
+    sign of CADAPDR they equal it. Probes at y = 1e-12 carry no density."""
+    cfg, ex, h, dens = _wall_case(oracle)
+    xp = np.linspace(-9.0, 9.0, 7) + 1e-12j
+    z = np.concatenate([ex["z"], xp])
+    dz = np.concatenate([ex["dz"], np.ones(xp.shape[0])])
+    hh = np.concatenate([h, np.ones(xp.shape[0])])
+    d = np.concatenate([dens, np.zeros(xp.shape[0])])
+    free = oracle.stokes_direct(z, dz, hh, d, sign)[cfg.nbk:]
+    img = oracle.stokes_image_direct(z, dz, hh, d, sign)[cfg.nbk:]
+    scale = np.abs(free).max()
+    if sign == 1:
+        assert np.abs(free + img).max() < 1e-10 * scale
+    else:
+        assert np.abs(free - img).max() < 1e-10 * scale
+
+
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_cadap_wall_restatement_matches_exact_images(oracle, sign):
+    """The restated wall-bounded CADAPDR / CADAPMOD (MPREFLECT, MKINTR, MKNBRRFL and
+    SLDREFDR / SLDREF) reproduces the exact direct plus image sum."""
+    cfg, ex, h, dens = _wall_case(oracle)
+    xl, sl = oracle.wallinfo(ex["z"])
+    got = oracle.cadap_fmm_wall(ex["z"], ex["dz"], h, dens, sign, xl, sl)
+    ref = oracle.stokes_direct(ex["z"], ex["dz"], h, dens, sign) + \
+        oracle.stokes_image_direct(ex["z"], ex["dz"], h, dens, sign)
+    assert np.abs(got - ref).max() < 1e-11 * np.abs(ref).max()
+    assert np.abs(oracle.stokes_image_direct(ex["z"], ex["dz"], h, dens, sign)).max() > 1e-2 * np.abs(ref).max()
