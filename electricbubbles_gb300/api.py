@@ -341,13 +341,30 @@ class Context:
             PRECISION[precision], EB_HOST))
         return un, flux.value
 
-    def setvelf(self, dphi_dn, cap=0.0, e0=0.0):
-        """SETVELF (free space): the Stokes right-hand side, 2 nbk reals."""
+    def setvelf(self, dphi_dn, cap=0.0, e0=0.0, zbond=0.0, zc=None):
+        """SETVELF: the Stokes right-hand side, 2 nbk reals. zbond != 0 needs the
+        per-drop C_k zc; in wall mode (set_wall) the reflected log sources join in."""
         d = _host(dphi_dn, np.float64)
         rhs = np.empty(2 * self.nbk)
-        check("eb_setvelf", self._lib.eb_setvelf(self._h, _ptr(d), float(cap), float(e0),
-                                                 _ptr(rhs), EB_HOST))
+        if zbond == 0:
+            check("eb_setvelf", self._lib.eb_setvelf(self._h, _ptr(d), float(cap), float(e0),
+                                                     _ptr(rhs), EB_HOST))
+            return rhs
+        zb = np.array([np.real(zbond), np.imag(zbond)], np.float64)
+        zc = _host(zc, np.complex128)
+        check("eb_setvelf_bond", self._lib.eb_setvelf_bond(self._h, _ptr(d), float(cap), float(e0), _ptr(zb),
+                                                           _ptr(zc), _ptr(rhs), EB_HOST))
         return rhs
+
+    def set_wall(self, iwall=1):
+        """Wall-bounded flow (the wall is y = 0): every Stokes sum adds the images."""
+        check("eb_set_wall", self._lib.eb_set_wall(self._h, int(iwall)))
+
+    def get_wall(self):
+        """(iwall, xleft, slength) of the installed geometry."""
+        w, xl, sl = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        check("eb_get_wall", self._lib.eb_get_wall(self._h, ctypes.byref(w), ctypes.byref(xl), ctypes.byref(sl)))
+        return w.value, xl.value, sl.value
 
     # ---- RK stage ------------------------------------------------------------
     @staticmethod

@@ -384,8 +384,13 @@ int eb_geom_tree(eb_ctx* ctx) {
     EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->zt.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap,
                          ctx->b_sq, ctx->b_R));
   else
-    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap));
+    EB_TRY(eb_tree_build(ctx, ctx->tree, ctx->z.as<double2>(), nbk, ctx->opts.leaf64, ctx->opts.leaf_cap,
+                         nullptr, 0, ctx->iwall));
   ctx->tree_pv.valid = false;
+  if (ctx->iwall) {  // EXTRACTDAT's xleft and slength (the root square without its 1e-9 margin)
+    ctx->xleft = ctx->tree.x0;
+    ctx->slength = ctx->tree.W / (1.0 + 1e-9);
+  }
   {
     const EbTree& t = ctx->tree;
     unsigned long long h = 1469598103934665603ull;  // FNV-1a over the fields' bytes
@@ -394,13 +399,43 @@ int eb_geom_tree(eb_ctx* ctx) {
       for (size_t i = 0; i < nb; ++i) h = (h ^ c[i]) * 1099511628211ull;
     };
     const int ints[] = {t.n, ctx->nbk, ctx->k, t.L, t.nbox, t.nleaf, t.ngroup, t.ntile, t.nchunk, t.chunk_lmin,
-                        t.lend, t.cap, (int)t.nu, (int)t.nw};
+                        t.lend, t.cap, (int)t.nu, (int)t.nw, t.wall, t.ld};
     mix(ints, sizeof(ints));
     mix(t.lev_off, sizeof(int) * (size_t)(t.L + 2));
     const double dbl[] = {t.W, t.x0, t.y0};
     mix(dbl, sizeof(dbl));
     ctx->geom_shape = h;
   }
+  return EB_OK;
+}
+
+int eb_set_wall(eb_ctx* ctx, int iwall) {
+  if (!ctx) return EB_ERR_ARG;
+  iwall = iwall ? 1 : 0;
+  if (iwall && ctx->nsim > 0) {
+    eb_set_last_error_msg("wall-bounded flow is not available for a batch of simulations");
+    return EB_ERR_ARG;
+  }
+  if (iwall == ctx->iwall) return EB_OK;
+  cudaSetDevice(ctx->device);
+  ctx->iwall = iwall;
+  if (ctx->geom_valid) {
+    const int st = eb_geom_tree(ctx);
+    if (st != EB_OK) {
+      ctx->geom_valid = false;
+      return st;
+    }
+    ctx->geom_version++;
+    eb_devbuf_collect();
+  }
+  return EB_OK;
+}
+
+int eb_get_wall(eb_ctx* ctx, int* iwall, double* xleft, double* slength) {
+  if (!ctx) return EB_ERR_ARG;
+  if (iwall) *iwall = ctx->iwall;
+  if (xleft) *xleft = ctx->xleft;
+  if (slength) *slength = ctx->slength;
   return EB_OK;
 }
 

@@ -345,6 +345,10 @@ __global__ void k_bg_gather(int nsim, const BCtl* __restrict__ ctl, double* __re
 // ---------------------------------------------------------------------------------
 int eb_batch_define(eb_ctx* ctx, int nsim, const int* sim_k, const double* e0) {
   if (!ctx || nsim < 0 || (nsim > 0 && !sim_k)) return EB_ERR_ARG;
+  if (nsim > 0 && ctx->iwall) {
+    eb_set_last_error_msg("a batch of simulations is not available in wall mode");
+    return EB_ERR_ARG;
+  }
   cudaSetDevice(ctx->device);
   ctx->geom_valid = false;
   ctx->tree.valid = false;

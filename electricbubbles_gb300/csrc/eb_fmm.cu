@@ -40,6 +40,14 @@ __device__ __forceinline__ unsigned int compact2d(unsigned long long x) {
   return (unsigned int)x;
 }
 
+// Morton key of the box (x, y) of a level (the even bits hold x)
+__device__ __forceinline__ unsigned long long morton_key(unsigned int x, unsigned int y) {
+  unsigned long long r = 0;
+  for (int b = 0; b < 32; ++b)
+    r |= ((unsigned long long)((x >> b) & 1u) << (2 * b)) | ((unsigned long long)((y >> b) & 1u) << (2 * b + 1));
+  return r;
+}
+
 __device__ __forceinline__ double2 box_center(unsigned long long key, double x0, double y0,
                                               double r) {
   unsigned int ix = compact2d(key), iy = compact2d(key >> 1);
@@ -381,7 +389,7 @@ __global__ void __launch_bounds__(128) k_m2l(int first, const int* __restrict__ 
                                              const c_t<T>* __restrict__ dinv,
                                              const int* __restrict__ pdv,
                                              const c_t<T>* __restrict__ mpole,
-                                             c_t<T>* __restrict__ local) {
+                                             c_t<T>* __restrict__ local, int accumulate) {
   extern __shared__ unsigned char smem_raw[];
   const int ldc = p + 1, ldl = p + 1, ldd = p + 2;
   // C2[(k-1)*(p+1) + m] = C(m+k-1, m), k = 1..p, m = 0..p
@@ -430,6 +438,7 @@ __global__ void __launch_bounds__(128) k_m2l(int first, const int* __restrict__ 
   const int tot = E * ldl;
   for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
     c_t<T> v = cadd<T>(cadd<T>(sacc[idx], sacc[tot + idx]), cadd<T>(sacc[2 * tot + idx], sacc[3 * tot + idx]));
+    if (accumulate) v = cadd<T>(local[(size_t)gid * tot + idx], v);
     local[(size_t)gid * tot + idx] = v;
   }
 }
@@ -447,7 +456,7 @@ __global__ void __launch_bounds__(128) k_m2l_f32p(int first, const int* __restri
                                                   const float2* __restrict__ dinv,
                                                   const int* __restrict__ pdv,
                                                   const float2* __restrict__ mpole,
-                                                  float2* __restrict__ local) {
+                                                  float2* __restrict__ local, int accumulate) {
   constexpr int ldl = P + 1, ldd = P + 2;
   __shared__ float2 sa[4][E][P];
   __shared__ float2 sred[4][E][ldl];
@@ -505,6 +514,7 @@ __global__ void __launch_bounds__(128) k_m2l_f32p(int first, const int* __restri
   for (int idx = threadIdx.x; idx < E * ldl; idx += blockDim.x) {
     const int e = idx / ldl, mm = idx - e * ldl;
     float2 v = cadd<float>(cadd<float>(sred[0][e][mm], sred[1][e][mm]), cadd<float>(sred[2][e][mm], sred[3][e][mm]));
+    if (accumulate) v = cadd<float>(local[(size_t)gid * E * ldl + idx], v);
     local[(size_t)gid * E * ldl + idx] = v;
   }
 }
@@ -562,7 +572,7 @@ __global__ void __launch_bounds__(128) k_m2l_df(int first, const int* __restrict
                                                 const float4* __restrict__ dinv,
                                                 const int* __restrict__ pdv,
                                                 const float4* __restrict__ mpole,
-                                                float4* __restrict__ local) {
+                                                float4* __restrict__ local, int accumulate) {
   extern __shared__ float4 smem_f4[];
   const int ldc = p + 1, ldl = p + 1, ldd = p + 2;
   float2* C2 = reinterpret_cast<float2*>(smem_f4);
@@ -614,7 +624,9 @@ __global__ void __launch_bounds__(128) k_m2l_df(int first, const int* __restrict
   for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
     cdf v01 = cdf_add(cdf_from_float4(sacc[idx]), cdf_from_float4(sacc[tot + idx]));
     cdf v23 = cdf_add(cdf_from_float4(sacc[2 * tot + idx]), cdf_from_float4(sacc[3 * tot + idx]));
-    local[(size_t)gid * tot + idx] = cdf_f4(cdf_add(v01, v23));
+    cdf v = cdf_add(v01, v23);
+    if (accumulate) v = cdf_add(cdf_from_float4(local[(size_t)gid * tot + idx]), v);
+    local[(size_t)gid * tot + idx] = cdf_f4(v);
   }
 }
 
@@ -622,7 +634,6 @@ __global__ void __launch_bounds__(128) k_m2l_df(int first, const int* __restrict
 // Upward and downward passes of the double-float pipeline: the P2M, M2M and L2L of the
 // FP64 kernels above with double-float operands and compensated sums.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ cdf cdf_zero() { return cdf{{0.f, 0.f}, {0.f, 0.f}}; }
 __device__ __forceinline__ cdf cdf_conj(cdf a) { return cdf{a.x, dfl_neg(a.y)}; }
 __device__ __forceinline__ cdf cdf_scale(cdf a, float f) { return cdf{dfl_mul_f(a.x, f), dfl_mul_f(a.y, f)}; }
 
@@ -1578,6 +1589,171 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Wall-bounded flow (IFLAG2 = 1 of CADAPDR / CADAPMOD): the images of the sources across
+// the wall y = 0, the bottom edge of the root square.
+// ---------------------------------------------------------------------------------
+// MPREFLECT (cadap2.f:1468-1507) for scaled coefficients with psi relative to the
+// centre: a box of centre c, side r and height yh = Im(c) / r = iy + 1/2 has the
+// mirrored expansions about conj(c)
+//   Mphi'[k] = conj(-Mpsi[k] + (k+1) Mphi[k] + 2 i yh k Mphi[k-1]),
+//   Mpsi'[k] = -conj(Mphi[k]) + (k+1) Mphi'[k] - 2 i yh k Mphi'[k-1]
+// (the reference's formulas with its absolute psi, psi = psi_c - conj(c) phi', and the
+// factor r^(k+1) of each coefficient taken out). One thread per (box, k).
+// Mphi'[k] from Mphi[k], Mpsi[k] and Mphi[k-1]:
+template <typename T>
+__device__ __forceinline__ c_t<T> reflect_phi(c_t<T> phk, c_t<T> psk, c_t<T> phk1, int k, T yh) {
+  c_t<T> v = csub<T>(cscale<T>(phk, (T)(k + 1)), psk);
+  const T f = (T)2 * yh * (T)k;  // + 2 i yh k Mphi[k-1]
+  v.x -= f * phk1.y;
+  v.y += f * phk1.x;
+  return cconj<T>(v);
+}
+
+// Mphi'[k] and Mpsi'[k] from the orders k, k-1 and k-2 (zeros below order 0)
+template <typename T>
+__device__ __forceinline__ void reflect_pair(c_t<T> phk, c_t<T> psk, c_t<T> phk1, c_t<T> psk1, c_t<T> phk2,
+                                             int k, T yh, c_t<T>& a, c_t<T>& b) {
+  a = reflect_phi<T>(phk, psk, phk1, k, yh);
+  b = csub<T>(cscale<T>(a, (T)(k + 1)), cconj<T>(phk));
+  if (k >= 1) {
+    const c_t<T> a1 = reflect_phi<T>(phk1, psk1, phk2, k - 1, yh);
+    const T f = (T)2 * yh * (T)k;  // - 2 i yh k Mphi'[k-1]
+    b.x += f * a1.y;
+    b.y -= f * a1.x;
+  }
+}
+
+template <typename T>
+__global__ void k_reflect(int first, int nb, const unsigned long long* __restrict__ bkey, int p,
+                          const c_t<T>* __restrict__ mpole, c_t<T>* __restrict__ mimg) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)nb * p) return;
+  const int b = first + (int)(idx / p), k = (int)(idx % p);
+  const T yh = (T)compact2d(bkey[b] >> 1) + (T)0.5;
+  const c_t<T>* m = mpole + (size_t)b * 2 * p;
+  const c_t<T> z = cmk<T>(0, 0);
+  c_t<T> a, c;
+  reflect_pair<T>(m[k], m[p + k], k >= 1 ? m[k - 1] : z, k >= 1 ? m[p + k - 1] : z, k >= 2 ? m[k - 2] : z, k, yh,
+                  a, c);
+  mimg[(size_t)b * 2 * p + k] = a;
+  mimg[(size_t)b * 2 * p + p + k] = c;
+}
+
+// The same for double-float multipoles, the mirror formed in FP64
+__global__ void k_reflect_df(int first, int nb, const unsigned long long* __restrict__ bkey, int p,
+                             const float4* __restrict__ mpole, float4* __restrict__ mimg) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)nb * p) return;
+  const int b = first + (int)(idx / p), k = (int)(idx % p);
+  const double yh = (double)compact2d(bkey[b] >> 1) + 0.5;
+  const float4* m = mpole + (size_t)b * 2 * p;
+  auto ld = [&](int i, int lo) {
+    if (i < lo) return make_double2(0.0, 0.0);
+    const float4 v = m[i];
+    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+  };
+  double2 a, c;
+  reflect_pair<double>(ld(k, 0), ld(p + k, 0), ld(k - 1, 0), ld(p + k - 1, p), ld(k - 2, 0), k, yh, a, c);
+  mimg[(size_t)b * 2 * p + k] = df4(a);
+  mimg[(size_t)b * 2 * p + p + k] = df4(c);
+}
+
+// The reflected near field: for every box T of level ld in the first row (on the wall),
+// the images of the points of the first-row boxes next to T and of T's own at T's points
+// (DONN0DR's IFLAG2 loop with MKNBRRFL, cadapdrop2.f:690-721, and the pair terms of
+// SLDREFDR / SLDREF, cadapdrop2.f:857-934 and cadap2.f:1509-1586), in FP64 whatever the
+// operator's arithmetic, added to the operator's output. With qc = -conj(z) qa,
+//   gamma1 = conj(qa) - conj(qb), gamma2 = 2 i y_j conj(qa), delta1 = -conj(qb),
+//   t = 1 / (conj(z_j) - z):  Phi = gamma1 t + gamma2 t^2, and
+//   z conj(Phi') + conj(Psi) = (z - z_j) conj(gamma1 t^2 + 2 gamma2 t^3)
+//                              + 2 conj(gamma2 t^2) + conj(delta1 t),
+// which has no terms of size |z|. One block per box of level ld (blocks off the wall
+// return at once); sources staged through shared memory.
+#define IMG_TILE 128
+__global__ void __launch_bounds__(IMG_TILE) k_img_near(int off, int nb, int lev,
+                                                       const unsigned long long* __restrict__ bkey,
+                                                       const int* __restrict__ pt0, const int* __restrict__ pt1,
+                                                       const double2* __restrict__ zs, const int* __restrict__ perm,
+                                                       const double2* __restrict__ dens,
+                                                       const double2* __restrict__ dz,
+                                                       const double* __restrict__ hpt, double s,
+                                                       double2* __restrict__ dst) {
+  __shared__ double2 sz[IMG_TILE], sg1[IMG_TILE], sg2[IMG_TILE], sd1[IMG_TILE];
+  const int b = off + blockIdx.x;
+  const unsigned long long key = bkey[b];
+  if (compact2d(key >> 1) != 0) return;
+  const int ix = (int)compact2d(key), side = 1 << lev;
+  int src[3], nsrc = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int sx = ix + dx;
+    if (sx < 0 || sx >= side) continue;
+    const unsigned long long kk = morton_key((unsigned)sx, 0u);
+    int lo = 0, hi = nb - 1, f = -1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      const unsigned long long v = bkey[off + mid];
+      if (v == kk) {
+        f = off + mid;
+        break;
+      }
+      if (v < kk) lo = mid + 1;
+      else hi = mid - 1;
+    }
+    if (f >= 0) src[nsrc++] = f;
+  }
+  const double c2pi = 1.0 / (2.0 * EB_PI);
+  for (int tb = pt0[b]; tb < pt1[b]; tb += IMG_TILE) {
+    const int i = tb + threadIdx.x;
+    const bool act = i < pt1[b];
+    const double2 zt = zs[act ? i : pt0[b]];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int q = 0; q < nsrc; ++q) {
+      for (int jb = pt0[src[q]]; jb < pt1[src[q]]; jb += IMG_TILE) {
+        const int cnt = min(IMG_TILE, pt1[src[q]] - jb);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+          const int j = jb + threadIdx.x, o = perm[j];
+          const double2 u = dens[o], d = dz[o];
+          const double h = hpt[o] * c2pi;
+          const double2 w = cmul<double>(u, d);
+          const double2 qa = make_double2(w.y * h, -w.x * h);  // u dz h / (2 pi i)
+          const double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
+          const double2 qb = make_double2(v.y * h, -v.x * h);
+          const double2 zj = zs[j];
+          sz[threadIdx.x] = zj;
+          sg1[threadIdx.x] = make_double2(qa.x - qb.x, qb.y - qa.y);            // conj(qa) - conj(qb)
+          sg2[threadIdx.x] = make_double2(2.0 * zj.y * qa.y, 2.0 * zj.y * qa.x);  // 2 i y conj(qa)
+          sd1[threadIdx.x] = make_double2(-qb.x, qb.y);                         // -conj(qb)
+        }
+        __syncthreads();
+        if (act) {
+          for (int jj = 0; jj < cnt; ++jj) {
+            const double2 zj = sz[jj], g1 = sg1[jj], g2 = sg2[jj], d1 = sd1[jj];
+            const double2 ze = make_double2(zj.x - zt.x, -zj.y - zt.y);  // conj(z_j) - z
+            const double rd = 1.0 / (ze.x * ze.x + ze.y * ze.y);
+            const double2 t1 = make_double2(ze.x * rd, -ze.y * rd);
+            const double2 t2 = cmul<double>(t1, t1);
+            const double2 dd = make_double2(zt.x - zj.x, zt.y - zj.y);
+            const double2 g2t2 = cmul<double>(g2, t2);
+            const double2 phi = cadd<double>(cmul<double>(g1, t1), g2t2);
+            const double2 dphi = cadd<double>(cmul<double>(g1, t2), cscale<double>(cmul<double>(g2t2, t1), 2.0));
+            const double2 r = cadd<double>(cmul<double>(dd, cconj<double>(dphi)),
+                                           cadd<double>(cscale<double>(cconj<double>(g2t2), 2.0),
+                                                        cconj<double>(cmul<double>(d1, t1))));
+            acc.x += phi.x + s * r.x;
+            acc.y += phi.y + s * r.y;
+          }
+        }
+      }
+    }
+    if (act) {
+      const int o = perm[i];
+      dst[o] = make_double2(dst[o].x + acc.x, dst[o].y + acc.y);
+    }
+  }
+}
+
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 inline int round32(int n) { return (n + 31) & ~31; }
 template <typename T>
@@ -1722,8 +1898,18 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     if (nt > 0) {
       k_m2l_df<E><<<nt, 128, sm, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(), t.vcount.as<int>(),
                                        p, tb.binom_df.as<float2>(), ldb, tb.dinv_df.as<float4>(), tb.pd.as<int>(),
-                                       mp, lo);
+                                       mp, lo, 0);
       eb_count_launch(ctx);
+    }
+    if (E == 2 && t.wall && t.ld >= 2) {  // the wall's reflected boxes
+      const int nimg = t.lev_off[t.ld + 1], nbi = nimg - first;
+      EB_TRY(w.mimg.ensure(sizeof(float4) * (size_t)nimg * E * p));
+      k_reflect_df<<<nblk((long long)nbi * p, 128), 128, 0, st>>>(first, nbi, t.bkey.as<unsigned long long>(), p,
+                                                                 mp, w.mimg.as<float4>());
+      k_m2l_df<E><<<nbi, 128, sm, st>>>(first, t.ilist.as<int>(), t.icode.as<unsigned char>(), t.icount.as<int>(),
+                                        p, tb.binom_df.as<float2>(), ldb, tb.dinv_df.as<float4>(), tb.pd.as<int>(),
+                                        w.mimg.as<float4>(), lo, 1);
+      ctx->launches += 2;
     }
     ps.done();
   }
@@ -1810,14 +1996,31 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
                                             t.vcount.as<int>(), reinterpret_cast<const float*>(tb.binom.p), ldb,
                                             reinterpret_cast<const float2*>(tb.dinv.p), tb.pd.as<int>(),
                                             reinterpret_cast<const float2*>(w.mpole.p),
-                                            reinterpret_cast<float2*>(w.local.p));
+                                            reinterpret_cast<float2*>(w.local.p), 0);
       eb_count_launch(ctx);
     } else if (nt > 0) {
       k_m2l<T, E><<<nt, 128, sm, st>>>(first, t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                        t.vcount.as<int>(), p, tb.binom.as<T>(), ldb,
                                        tb.dinv.as<c_t<T>>(), tb.pd.as<int>(), w.mpole.as<c_t<T>>(),
-                                       w.local.as<c_t<T>>());
+                                       w.local.as<c_t<T>>(), 0);
       eb_count_launch(ctx);
+    }
+    if (E == 2 && t.wall && t.ld >= 2) {  // the wall's reflected boxes
+      const int nimg = t.lev_off[t.ld + 1], nbi = nimg - first;
+      EB_TRY(w.mimg.ensure(sizeof(c_t<T>) * (size_t)nimg * E * p));
+      k_reflect<T><<<nblk((long long)nbi * p, 128), 128, 0, st>>>(first, nbi, t.bkey.as<unsigned long long>(), p,
+                                                                 w.mpole.as<c_t<T>>(), w.mimg.as<c_t<T>>());
+      if (sizeof(T) == 4 && p == 20)
+        k_m2l_f32p<E, 20><<<nbi, 128, 0, st>>>(first, t.ilist.as<int>(), t.icode.as<unsigned char>(),
+                                               t.icount.as<int>(), reinterpret_cast<const float*>(tb.binom.p), ldb,
+                                               reinterpret_cast<const float2*>(tb.dinv.p), tb.pd.as<int>(),
+                                               reinterpret_cast<const float2*>(w.mimg.p),
+                                               reinterpret_cast<float2*>(w.local.p), 1);
+      else
+        k_m2l<T, E><<<nbi, 128, sm, st>>>(first, t.ilist.as<int>(), t.icode.as<unsigned char>(), t.icount.as<int>(),
+                                          p, tb.binom.as<T>(), ldb, tb.dinv.as<c_t<T>>(), tb.pd.as<int>(),
+                                          w.mimg.as<c_t<T>>(), w.local.as<c_t<T>>(), 1);
+      ctx->launches += 2;
     }
     ps.done();
   }
@@ -1964,6 +2167,14 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                              w.mpole.as<float2>(), out, post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
+  if (E == 2 && t.wall) {  // the reflected near field, after the output is written
+    const int ld = t.ld, nb = t.lev_off[ld + 1] - t.lev_off[ld];
+    double2* dst = post.kind == 1 ? reinterpret_cast<double2*>(post.y) : out;
+    k_img_near<<<nb, IMG_TILE, 0, st>>>(t.lev_off[ld], nb, ld, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                        t.pt1.as<int>(), t.zs.as<double2>(), t.perm.as<int>(), dens, dz, hpt,
+                                        (double)sign, dst);
+    eb_count_launch(ctx);
+  }
   ps.done();
   ctx->last_p = tb.p;
   return eb_check_launch(ctx, "fmm apply");

@@ -14,7 +14,10 @@
 #define EB_MAX_P 60
 #define EB_VMAX 27
 #define EB_UMAX 9
-#define EB_NCODE 49
+// M2L offset codes (dx + 3) + 7 (dy + 3) of the offset d = (c_t - c_s)/r in box units:
+// dx, dy in [-3, 3] for the V lists, and dy up to 7 for the reflected boxes of a wall
+// (a source box mirrored across the wall y = 0, at level 2 anywhere in the 4 x 4 grid)
+#define EB_NCODE 77
 #define EB_GROUP 8
 #define EB_NTILE 32
 // Internal precision value (beside EB_FP64 and EB_FP32): FP64-class arithmetic in
@@ -46,8 +49,9 @@ struct DevBuf {
 // stream synchronisation covers several of them).
 struct EbTreeHost {
   double sq[4];            // the bounding square: W, x0, y0, 2^20 / W
-  int bad;                 // a non-finite coordinate
+  int bad;                 // 1: a non-finite coordinate; 2: a node below the wall
   int lmax;                // deepest leaf level
+  int lmin;                // the uniform floor level (no leaf above it)
   int hist[EB_KEY_LEVELS + 1];  // boxes per level (heads of existing boxes)
   int last[12];            // counts and scans of the last leaf or box (work items, lists)
   unsigned long long pairs[3];  // near-field, V-list and W-list (M2P) pair counts
@@ -125,6 +129,16 @@ struct EbTree {
   DevBuf chunk_box;  // int[nchunk]: the box of each chunk
   DevBuf cdone;      // int[nbox - lev_off[2]]: chunks of the box finished in the
                      // current P2M (zero between launches: the box's last chunk resets it)
+  // Wall-bounded flow (the wall is y = 0, the root square's bottom edge): the reflected
+  // source boxes of every box of levels 2..ld (ilist/icode/icount, stride EB_VMAX, like
+  // the V lists), whose multipoles are mirrored and translated by M2L; the pairs of
+  // adjacent first-row boxes of level ld are summed directly. ld is the uniform floor
+  // level (no leaf above it), or 0 when the tree has no level-2 expansions.
+  int wall = 0;
+  int ld = 0;
+  DevBuf ilist;      // int[lev_off[ld+1] * EB_VMAX] (boxes below level 2 unused)
+  DevBuf icode;      // unsigned char[same]
+  DevBuf icount;     // int[lev_off[ld+1]]
 };
 #define EB_CHUNK 64
 #define EB_DIRECT_LEVELS 3  // finest levels whose FP32 multipoles come directly from points
@@ -136,7 +150,7 @@ struct EbTree {
 struct EbTables {
   int p = 0;
   DevBuf binom;   // T[(2p+2)*(2p+2)] binomial coefficients C(i, j) at [i*(2p+2)+j]
-  DevBuf dinv;    // c_t<T>[EB_NCODE*(p+2)]: d^-j for the 49 offset codes
+  DevBuf dinv;    // c_t<T>[EB_NCODE*(p+2)]: d^-j for the offset codes
   DevBuf pd;      // int[EB_NCODE]: per-offset truncation order
   DevBuf epow;    // c_t<T>[4*(p+2)]: e_q^j for the 4 child offsets (child units)
   DevBuf einv;    // c_t<T>[4*(p+2)]: e_q^-j
@@ -158,6 +172,7 @@ struct EbFmmWork {
   DevBuf mpole;      // c_t<T>[nbox*E*p]
   DevBuf mpart;      // c_t<T>[nchunk*E*p]: per-chunk partial multipoles (FP32 direct P2M)
   DevBuf local;      // c_t<T>[nbox*E*(p+1)]
+  DevBuf mimg;       // multipoles mirrored across the wall, in the pipeline's format
 };
 
 // A GMRES cycle (or refinement step) captured as one CUDA graph: the Arnoldi steps run
@@ -199,6 +214,11 @@ struct eb_ctx {
   DevBuf pkw;                    // double2: weights of FASMVP's singular-term sums
   bool geom_valid = false;
   bool ckern_valid = false;       // ckern/tha filled by eb_extractdat
+  // wall-bounded flow (COMMON /wallinfo/, electric.f:55): the Stokes sums add the images
+  // across the wall y = 0; xleft and slength are EXTRACTDAT's (electric.f:710-711),
+  // taken from the installed nodes by the tree build
+  int iwall = 0;
+  double xleft = 0.0, slength = 0.0;
 
   EbTree tree;      // tree over the nodes
   EbTree tree_pv;   // tree over the 2N fine points of PVINTEV
@@ -312,8 +332,12 @@ inline int eb_resid_prec(const eb_ctx* ctx) { return ctx->opts.resid_df > 0 ? EB
 // tree.cu
 // root_sq (W, x0, y0) and root_level: an explicit root square whose boxes of level
 // root_level each hold one independent problem (null: the bounding square, one problem)
+// wall != 0: the root square is [xmin, xmin + S] x [0, S], S = max(xmax - xmin, ymax)
+// (EXTRACTDAT's xleft and slength, electric.f:710-711), its bottom edge the wall y = 0,
+// and the tree gets the image lists of the wall (EbTree::ilist); a node below the wall
+// is an error.
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z_dev, int n, int leaf_target, int leaf_cap,
-                  const double* root_sq = nullptr, int root_level = 0);
+                  const double* root_sq = nullptr, int root_level = 0, int wall = 0);
 // The tree's pair counts (u_pairs, v_pairs), waiting for the build if it is in flight.
 int eb_tree_pairs(eb_ctx* ctx, EbTree& t);
 

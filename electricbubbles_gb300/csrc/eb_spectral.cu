@@ -312,14 +312,38 @@ __global__ void k_dtn_post(int nbk, const double2* __restrict__ dpsi, const doub
   dphi[i] = -dpsi[i].x / dsda[i];
 }
 
-// INTERFACENEW corrections and normal velocity (electric.f:845-882), free space.
+// REFSING (reflect.f:28-86) with zb = 0, as SETVELF and INTERFACENEW call it: the images
+// across the wall y = 0 of the log sources zc at the drop centres zk, added to phi, phi'
+// and psi at z. z lies above the wall and conj(zk) below it, so z - conj(zk) has a
+// positive imaginary part and its principal logarithm needs no branch care.
+__device__ void refsing_zc(double2 z, int k, const double2* __restrict__ zk, const double2* __restrict__ zc,
+                           double2& phi, double2& phip, double2& psi) {
+  for (int j = 0; j < k; ++j) {
+    const double2 c = zc[j], kk = zk[j];
+    const double2 zd = make_double2(z.x - kk.x, z.y + kk.y);  // z - conj(zk)
+    const double2 lg = make_double2(log(hypot(zd.x, zd.y)), atan2(zd.y, zd.x));
+    const double2 r1 = cinv<double>(zd), r2 = cmul<double>(r1, r1);
+    phi = csub<double>(phi, cmul<double>(c, lg));
+    phip = csub<double>(phip, cmul<double>(c, r1));
+    psi = csub<double>(psi, cmul<double>(cconj<double>(c), lg));
+    const double2 a1 = cmul<double>(cconj<double>(c), make_double2(0.0, 2.0 * kk.y));  // conj(zc)(zk - conj(zk))
+    const double2 b1 = cadd<double>(cmul<double>(c, cconj<double>(kk)), a1);
+    const double2 b2 = cmul<double>(a1, cconj<double>(kk));
+    phi = cadd<double>(phi, cmul<double>(a1, r1));
+    phip = csub<double>(phip, cmul<double>(a1, r2));
+    psi = cadd<double>(psi, cadd<double>(cmul<double>(b1, r1), cmul<double>(b2, r2)));
+  }
+}
+
+// INTERFACENEW corrections and normal velocity (electric.f:845-882); with iwall the
+// reflected log sources of REFSING join the far field (electric.f:868-872).
 __global__ void k_velocity(int nbk, int k, const int* __restrict__ drop_of,
                            const double2* __restrict__ z, const double2* __restrict__ dz,
                            const double* __restrict__ dsda, const double* __restrict__ kappa,
                            const double* __restrict__ hpt, const double2* __restrict__ ckern,
                            const double2* __restrict__ u, const double2* __restrict__ udot,
                            const double2* __restrict__ gw, const double2* __restrict__ zc,
-                           const double2* __restrict__ zk, int any_zc, double cap,
+                           const double2* __restrict__ zk, int any_zc, int iwall, double cap,
                            double* __restrict__ un, double* __restrict__ fluxpart) {
   __shared__ double red[32];
   double fl = 0.0;
@@ -346,9 +370,15 @@ __global__ void k_velocity(int nbk, int k, const int* __restrict__ drop_of,
         zck = cadd<double>(zck, cdiv<double>(cmul<double>(cconj<double>(c), zd), cconj<double>(zd)));
       }
     }
-    // far field: zpsi = -i cap z / 2, gradwr = conj(zpsi)
+    // far field: zpsi = -i cap z / 2, gradwr = zphi + z conj(zphip) + conj(zpsi)
     double2 zpsi = make_double2(0.5 * cap * zz.y, -0.5 * cap * zz.x);
-    g = cadd<double>(g, cadd<double>(cconj<double>(zpsi), zck));
+    double2 gr = cconj<double>(zpsi);
+    if (iwall) {
+      double2 zphi = make_double2(0.0, 0.0), zphip = zphi;
+      refsing_zc(zz, k, zk, zc, zphi, zphip, zpsi);
+      gr = cadd<double>(zphi, cadd<double>(cmul<double>(zz, cconj<double>(zphip)), cconj<double>(zpsi)));
+    }
+    g = cadd<double>(g, cadd<double>(gr, zck));
     double2 zvel = make_double2(g.y, -g.x);  // -i g
     double unt = zvel.x * zn.x + zvel.y * zn.y;  // Re(zvel conj(zn))
     un[t] = unt;
@@ -678,7 +708,7 @@ static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* z
   k_velocity<<<nbv, 256, 0, s>>>(nbk, k, ctx->drop_of.as<int>(), ctx->z.as<double2>(), ctx->dz.as<double2>(),
                                  ctx->dsda.as<double>(), ctx->kappa.as<double>(), ctx->hpt.as<double>(),
                                  ctx->ckern.as<double2>(), ud, ctx->vtmp.as<double2>(), ctx->vtmp2.as<double2>(),
-                                 ctx->za.as<double2>(), ctx->zk.as<double2>(), any_zc, cap, und,
+                                 ctx->za.as<double2>(), ctx->zk.as<double2>(), any_zc, ctx->iwall, cap, und,
                                  ctx->redpart.as<double>());
   eb_count_launch(ctx);
   k_sum_final<<<1, 32, 0, s>>>(nbv, ctx->redpart.as<double>(), ctx->redpart.as<double>() + 2047);
@@ -727,30 +757,125 @@ __device__ void spectral_int(double2* a, int n) {
   __syncthreads();
 }
 
-// SETVELF (stokesbubb.f:4-135) for zbond = 0: surface tension -dz/(2|dz|), the far
-// field -conj(psi) with psi = -i cap z/2, and the electric stress i E0/4 times the
-// antiderivative of dz (dphi/dn)^2 (:110-128). As in the reference, the electric term
-// uses the `alpha` left from the previous loops, 2 pi (nd_k - 1)/nd_k of the last drop.
+// SETVELF (stokesbubb.f:4-135): surface tension -dz/(2|dz|) and the far field -zstr,
+// zstr = -conj(psi) with psi = -i cap z/2 (:61-68); for zbond != 0 the Bond-number term
+// zgrav = -(i/4)(alpha c_0 + F), F the antiderivative of zbond conj(z) dz + conj(zbond)
+// z dz (:38-56), the C_k sums (:73-102) and, on a wall, minus REFSING's reflected log
+// sources (:53-60); then the electric stress i E0/4 times the antiderivative of
+// dz (dphi/dn)^2 (:110-128). As in the reference, the electric term uses the `alpha` left
+// from the previous loops, 2 pi (nd_k - 1)/nd_k of the last drop. The wall branch of the
+// reference subtracts a `zstr` it never assigns (:67); the capillary term of the
+// free-space branch is taken, the term INTERFACENEW keeps on a wall (both agree for
+// cap = 0). One block per drop; two FFT buffers in shared memory.
 __global__ void k_setvelf(const int* __restrict__ start, const double2* __restrict__ z,
                           const double2* __restrict__ dz, const double* __restrict__ dsda,
                           const double* __restrict__ dphi, double cap, double e0,
                           double alpha_stale, const double* __restrict__ e0_drop,
-                          const double* __restrict__ alpha_drop, double2* __restrict__ rhs, int nmax) {
+                          const double* __restrict__ alpha_drop, double2 zbond, int k,
+                          const double2* __restrict__ zk, const double2* __restrict__ zc, int iwall,
+                          double2* __restrict__ rhs, int nmax) {
   extern __shared__ double2 sm[];
   __shared__ double2 s_c0, s_f0;
+  __shared__ double s_arg0;
   int b = blockIdx.x;
   int i0 = start[b], n = start[b + 1] - i0;
   if (e0_drop) e0 = e0_drop[b];  // a batch: the drop's simulation's E0 and last-drop alpha
   if (alpha_drop) alpha_stale = alpha_drop[b];
+  const bool bond = zbond.x != 0.0 || zbond.y != 0.0;
   double2* a = sm;
-  double2* tw = sm + nmax;
+  double2* c = sm + nmax;                          // the C_k sums' second buffer
+  double2* tw = c + (bond && zc ? nmax : 0);
   make_twiddles(tw, n);
+  const double inv = 1.0 / (double)n, dal = 2.0 * EB_PI / (double)n;
+  // Bond-number term (its FFT pass only for zbond != 0)
+  if (bond) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const double2 zz = z[i0 + i], d = dz[i0 + i];
+      a[i] = cadd<double>(cmul<double>(zbond, cmul<double>(cconj<double>(zz), d)),
+                          cmul<double>(cconj<double>(zbond), cmul<double>(zz, d)));
+    }
+    smem_fft(a, n, tw, n, -1);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(a[i].x * inv, a[i].y * inv);
+    __syncthreads();
+    if (threadIdx.x == 0) s_c0 = a[0];
+    __syncthreads();
+    spectral_int(a, n);
+    smem_fft(a, n, tw, n, +1);
+  }
+  const double2 g0 = bond ? s_c0 : make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int t = i0 + i;
+    double sd = dsda[t];
+    const double2 zz = z[t];
+    double2 r = make_double2(-0.5 * dz[t].x / sd, -0.5 * dz[t].y / sd);
+    if (bond) {  // zgrav = -(i/4)(alpha c_0 + F_i)
+      const double al = dal * (double)i;
+      const double2 f = make_double2(al * g0.x + a[i].x, al * g0.y + a[i].y);
+      r.x += 0.25 * f.y;
+      r.y -= 0.25 * f.x;
+    }
+    if (iwall) {  // - (zphi - z conj(zphip) - conj(zpsi)) of the reflected log sources
+      double2 zphi = make_double2(0.0, 0.0), zphip = zphi, zpsi = zphi;
+      refsing_zc(zz, k, zk, zc, zphi, zphip, zpsi);
+      const double2 ck = csub<double>(csub<double>(zphi, cmul<double>(zz, cconj<double>(zphip))), cconj<double>(zpsi));
+      r = csub<double>(r, ck);
+    }
+    // - zstr, zstr = -conj(-i cap z/2) = -i cap conj(z)/2
+    r.x += 0.5 * cap * zz.y;
+    r.y += 0.5 * cap * zz.x;
+    rhs[t] = r;
+  }
+  // C_k: the argument of z - zk(nbod) unwrapped along the drop by integrating its
+  // derivative -i (u'/u), u the unit vector, then 2 i zc arg - conj(zc) e^{2 i arg}
+  if (zc && bond) {
+    for (int nb = 0; nb < k; ++nb) {
+      const double2 cn = zc[nb], kn = zk[nb];
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 d = csub<double>(z[i0 + i], kn);
+        const double r = hypot(d.x, d.y);
+        c[i] = make_double2(d.x / r, d.y / r);
+        a[i] = c[i];
+      }
+      if (threadIdx.x == 0) {
+        const double2 d0 = csub<double>(z[i0], kn);
+        double g = asin(d0.y / hypot(d0.x, d0.y));
+        if (d0.x < 0.0) g = EB_PI - g;
+        s_arg0 = g;
+      }
+      smem_fft(a, n, tw, n, -1);
+      spectral_deriv(a, n);
+      smem_fft(a, n, tw, n, +1);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 q = cdiv<double>(a[i], c[i]);  // -i zfi / zf
+        a[i] = make_double2(q.y, -q.x);
+      }
+      smem_fft(a, n, tw, n, -1);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(a[i].x * inv, a[i].y * inv);
+      __syncthreads();
+      if (threadIdx.x == 0) s_f0 = a[0];
+      __syncthreads();
+      const double zf1 = s_f0.x;
+      spectral_int(a, n);
+      smem_fft(a, n, tw, n, +1);
+      const double arg0 = s_arg0, a0 = a[0].x;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double arg = arg0 + dal * (double)i * zf1 + (a[i].x - a0);
+        double sn, cs;
+        sincos(2.0 * arg, &sn, &cs);
+        const double2 zck = csub<double>(cmul<double>(make_double2(0.0, 2.0 * arg), cn),
+                                         cmul<double>(cconj<double>(cn), make_double2(cs, sn)));
+        rhs[i0 + i] = csub<double>(rhs[i0 + i], zck);
+      }
+    }
+  }
+  // electric stress
+  __syncthreads();
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     double d = dphi[i0 + i];
     a[i] = make_double2(dz[i0 + i].x * d * d, dz[i0 + i].y * d * d);
   }
   smem_fft(a, n, tw, n, -1);
-  double inv = 1.0 / (double)n;
   for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = make_double2(a[i].x * inv, a[i].y * inv);
   __syncthreads();
   if (threadIdx.x == 0) s_c0 = a[0];
@@ -762,30 +887,42 @@ __global__ void k_setvelf(const int* __restrict__ start, const double2* __restri
   const double2 c0 = s_c0, f0 = s_f0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     int t = i0 + i;
-    double s = dsda[t];
-    double2 r = make_double2(-0.5 * dz[t].x / s, -0.5 * dz[t].y / s);
-    // - zstr, zstr = -conj(-i cap z/2) = -i cap conj(z)/2
-    r.x += 0.5 * cap * z[t].y;
-    r.y += 0.5 * cap * z[t].x;
     double2 zs = make_double2(alpha_stale * c0.x + a[i].x - f0.x, alpha_stale * c0.y + a[i].y - f0.y);
+    double2 r = rhs[t];
     r.x += -0.25 * e0 * zs.y;  // (i E0/4) zs
     r.y += 0.25 * e0 * zs.x;
     rhs[t] = r;
   }
 }
 
-int setvelf_dev(eb_ctx* ctx, const double* dphi, double cap, double e0, double2* rhs) {
+// zc_k = i zbond area_k / (8 pi) (EXTRACTDAT, electric.f:703)
+__global__ void k_zc(int k, double2 zbond, const double* __restrict__ area, double2* __restrict__ zc) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= k) return;
+  const double f = area[b] / (8.0 * EB_PI);
+  zc[b] = make_double2(-zbond.y * f, zbond.x * f);
+}
+
+// zc: device double2[k] of C_k (used when zbond != 0), or null
+int setvelf_dev(eb_ctx* ctx, const double* dphi, double cap, double e0, double2 zbond, const double2* zc,
+                double2* rhs) {
   int nmax;
   EB_TRY(check_pow2(ctx, nmax));
   const int nlast = ctx->nd_host[ctx->k - 1];
   const double alpha_stale = 2.0 * EB_PI * (double)(nlast - 1) / (double)nlast;
-  size_t sm = sizeof(double2) * ((size_t)nmax + (size_t)nmax / 2);
+  const bool bond = zbond.x != 0.0 || zbond.y != 0.0;
+  size_t sm = sizeof(double2) * ((bond && zc ? 2 : 1) * (size_t)nmax + (size_t)nmax / 2);
   EB_TRY(set_smem((const void*)k_setvelf, sm));
+  if (ctx->iwall && !(bond && zc)) {
+    eb_set_last_error_msg("SETVELF on a wall needs zbond != 0 and its zc");
+    return EB_ERR_ARG;
+  }
   k_setvelf<<<ctx->k, SBS, sm, ctx->stream>>>(ctx->start.as<int>(), ctx->z.as<double2>(),
                                               ctx->dz.as<double2>(), ctx->dsda.as<double>(), dphi,
                                               cap, e0, alpha_stale,
                                               ctx->nsim > 0 && ctx->sim_has_e0 ? ctx->b_e0.as<double>() : nullptr,
-                                              ctx->nsim > 0 ? ctx->b_alpha.as<double>() : nullptr, rhs, nmax);
+                                              ctx->nsim > 0 ? ctx->b_alpha.as<double>() : nullptr, zbond, ctx->k,
+                                              ctx->zk.as<double2>(), bond ? zc : nullptr, ctx->iwall, rhs, nmax);
   eb_count_launch(ctx);
   return eb_check_launch(ctx, "setvelf");
 }
@@ -881,6 +1018,15 @@ __global__ void k_rk_second(int n, double dt, const double* __restrict__ phi0,
 
 int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
             eb_stage_info* info) {
+  // zbond != 0: wall-bounded (READINI's iwall, electric.f:321-326), set before the
+  // install so that the tree takes the wall
+  const double2 zb = make_double2(m->zbond[0], m->zbond[1]);
+  const int wall = zb.x != 0.0 || zb.y != 0.0;
+  if (wall && ctx->nsim > 0) {
+    eb_set_last_error_msg("wall-bounded flow is not available for a batch of simulations");
+    return EB_ERR_ARG;
+  }
+  ctx->iwall = wall;
   EB_TRY(eb_extractdat(ctx, k, nd, rku, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                        EB_DEVICE));
   int nbk = ctx->nbk, nmax;
@@ -903,10 +1049,15 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   // double-float as df64 says), refined mode the arithmetic of its FP64 residuals
   const int p64 = m->mode == EB_SOLVE_FP32_REFINED ? eb_resid_prec(ctx) : EB_FP64;
   EB_TRY(dirich_neu_map_impl(ctx, ul, phi, psi, dphi, p64, EB_DEVICE));
-  EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, ctx->st_rhs.as<double2>()));
+  if (wall) {  // zc = i zbond area / (8 pi), EXTRACTDAT (electric.f:703)
+    k_zc<<<nblk(k, 128), 128, 0, s>>>(k, zb, ctx->ex_area.as<double>(), ctx->st_zc.as<double2>());
+    eb_count_launch(ctx);
+  } else {
+    EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
+  }
+  EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, zb, ctx->st_zc.as<double2>(), ctx->st_rhs.as<double2>()));
   EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
                          EB_DEVICE));
-  EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
   double* un = rl;  // the Laplace right-hand side is no longer needed
   double flux = 0.0;
   EB_TRY(interface_velocity_impl(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, &flux,
@@ -931,32 +1082,43 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
 
 int check_model(const eb_model* m) {
   if (!m) return EB_ERR_ARG;
-  if (m->zbond[0] != 0.0 || m->zbond[1] != 0.0) {
-    eb_set_last_error_msg("wall-bounded flow (zbond != 0) is not supported");
-    return EB_ERR_ARG;
-  }
+  if (!std::isfinite(m->zbond[0]) || !std::isfinite(m->zbond[1])) return EB_ERR_ARG;
   if (m->mode != EB_SOLVE_FP64 && m->mode != EB_SOLVE_FP32_REFINED) return EB_ERR_ARG;
   return EB_OK;
 }
 
 }  // namespace
 
-int eb_setvelf(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, double* rhs, int mem) {
+int eb_setvelf_bond(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, const double* zbond,
+                    const double* zc, double* rhs, int mem) {
   if (!ctx || !dphi_dn || !rhs) return EB_ERR_ARG;
   if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
   if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  const double2 zb = zbond ? make_double2(zbond[0], zbond[1]) : make_double2(0.0, 0.0);
+  const bool bond = zb.x != 0.0 || zb.y != 0.0;
+  if (bond && !zc) return EB_ERR_ARG;
   cudaSetDevice(ctx->device);
-  if (mem == EB_DEVICE)
-    return setvelf_dev(ctx, dphi_dn, cap, e0, reinterpret_cast<double2*>(rhs));
-  int nbk = ctx->nbk;
+  int nbk = ctx->nbk, k = ctx->k;
   cudaStream_t s = ctx->stream;
+  const double2* zcd = reinterpret_cast<const double2*>(zc);
+  if (bond && mem == EB_HOST) {
+    EB_TRY(ctx->st_zc.ensure(sizeof(double2) * (size_t)k));
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->st_zc.p, zc, sizeof(double2) * k, cudaMemcpyHostToDevice, s));
+    zcd = ctx->st_zc.as<double2>();
+  }
+  if (mem == EB_DEVICE)
+    return setvelf_dev(ctx, dphi_dn, cap, e0, zb, bond ? zcd : nullptr, reinterpret_cast<double2*>(rhs));
   EB_TRY(ctx->vin.ensure(sizeof(double) * (size_t)nbk));
   EB_TRY(ctx->vout.ensure(sizeof(double2) * (size_t)nbk));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, dphi_dn, sizeof(double) * nbk, cudaMemcpyHostToDevice, s));
-  EB_TRY(setvelf_dev(ctx, ctx->vin.as<double>(), cap, e0, ctx->vout.as<double2>()));
+  EB_TRY(setvelf_dev(ctx, ctx->vin.as<double>(), cap, e0, zb, bond ? zcd : nullptr, ctx->vout.as<double2>()));
   EB_CUDA_TRY(cudaMemcpyAsync(rhs, ctx->vout.p, sizeof(double2) * nbk, cudaMemcpyDeviceToHost, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   return EB_OK;
+}
+
+int eb_setvelf(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, double* rhs, int mem) {
+  return eb_setvelf_bond(ctx, dphi_dn, cap, e0, nullptr, nullptr, rhs, mem);
 }
 
 int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* model,

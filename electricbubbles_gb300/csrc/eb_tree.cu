@@ -84,7 +84,7 @@ __global__ void k_bbox(const double2* __restrict__ z, int n, Box4* __restrict__ 
 // The bounding box and the root square sq = (W, x0, y0, 2^20 / W): the box's larger
 // side widened by 1e-9 relative, centred on the box (W = 1 for a single point).
 __global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __restrict__ out,
-                             double* __restrict__ sq) {
+                             double* __restrict__ sq, int wall, int* __restrict__ bad) {
   __shared__ Box4 sb[256];
   Box4 r = mk_box4(INFINITY, -INFINITY, INFINITY, -INFINITY);
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -104,6 +104,19 @@ __global__ void k_bbox_final(const Box4* __restrict__ part, int nb, Box4* __rest
   if (threadIdx.x != 0) return;
   r = sb[0];
   *out = r;
+  if (wall) {
+    // the square [xleft, xleft + slength] x [0, slength] of the wall-bounded CADAPDR
+    // (cadapdrop.f:142-145), widened by 1e-9 so that no key needs clamping
+    if (!(r.z >= 0.0)) atomicOr(bad, 2);
+    double w = fmax(__dadd_rn(r.y, -r.x), r.w);
+    if (!(w > 0)) w = 1.0;
+    w = __dmul_rn(w, 1.0 + 1e-9);
+    sq[0] = w;
+    sq[1] = r.x;
+    sq[2] = 0.0;
+    sq[3] = __ddiv_rn((double)(1u << EB_KEY_LEVELS), w);
+    return;
+  }
   double w = fmax(__dadd_rn(r.y, -r.x), __dadd_rn(r.w, -r.z));
   if (!(w > 0)) w = 1.0;
   w = __dmul_rn(w, 1.0 + 1e-9);
@@ -359,6 +372,49 @@ __global__ void k_vlist(const unsigned long long* __restrict__ bkey, LevOffT lo,
     cnt += __popc(m);
   }
   if (lane == 0) vcount[gid] = cnt;
+}
+
+// Image lists of the wall y = 0 (the root square's bottom edge) for the boxes of levels
+// 2..ld, one thread per box: the source boxes S of the box's level whose mirror image
+// across the wall is not adjacent to the box T but lies among the children of the
+// mirrored neighbours of T's parent, the reflected interaction list of DOINT0DR (MKINTR,
+// cadap2.f:830-877; cadapdrop2.f:159-197). On level 2 every pair is listed whose images
+// are not adjacent (it takes the pairs of level 1 as well, whose parents are the root);
+// below, only the first two rows have such pairs: T and S in rows 0-1 and S in the
+// columns of the children of T's parent's column neighbours. Mirrored, S sits at row
+// -1 - iy_S, so the offset T - S' is (ix_T - ix_S, iy_T + iy_S + 1) in box units, dy in
+// [1, 7]; the pairs with dy = 1 and |dx| <= 1 (both in row 0, columns adjacent) are left
+// to the direct sum of level ld.
+__global__ void k_imglist(const unsigned long long* __restrict__ bkey, const unsigned char* __restrict__ blev,
+                          LevOffT lo, int first, int nimg, int* __restrict__ ilist,
+                          unsigned char* __restrict__ icode, int* __restrict__ icount) {
+  const int gid = first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nimg) return;
+  const int lev = blev[gid];
+  const int off = lo.v[lev], nb = lo.v[lev + 1] - off;
+  const unsigned long long key = bkey[gid];
+  const int ix = (int)compact2(key), iy = (int)compact2(key >> 1), side = 1 << lev;
+  int cnt = 0, x0, x1, y1;
+  if (lev == 2) {
+    x0 = 0; x1 = 3; y1 = 3;
+  } else if (iy <= 1) {
+    const int px = ix >> 1;
+    x0 = max(2 * px - 2, 0); x1 = min(2 * px + 3, side - 1); y1 = 1;
+  } else {
+    icount[gid] = 0;
+    return;
+  }
+  for (int sy = 0; sy <= y1; ++sy)
+    for (int sx = x0; sx <= x1; ++sx) {
+      const int dx = ix - sx, dy = iy + sy + 1;
+      if (dy == 1 && dx >= -1 && dx <= 1) continue;  // adjacent images: direct sum
+      const int s = find_box(bkey, off, nb, morton((unsigned)sx, (unsigned)sy));
+      if (s < 0) continue;
+      ilist[(size_t)gid * EB_VMAX + cnt] = s;
+      icode[(size_t)gid * EB_VMAX + cnt] = (unsigned char)((dy + 3) * 7 + (dx + 3));
+      ++cnt;
+    }
+  icount[gid] = cnt;
 }
 
 // Leaves in point order: point i starts its leaf when it heads the box of its leaf level.
@@ -677,7 +733,7 @@ __global__ void k_leaf_coords(const int* __restrict__ leaves, const unsigned lon
 }
 
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target, int leaf_cap,
-                  const double* root_sq, int root_level) {
+                  const double* root_sq, int root_level, int wall) {
   cudaStream_t st = eb_stream(ctx);
   t.valid = false;
   if (n <= 0) return EB_ERR_ARG;
@@ -686,6 +742,8 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   t.n = n;
   t.cap = leaf_cap;
   t.R = root_sq ? root_level : 0;
+  t.wall = wall && !root_sq;
+  t.ld = 0;
   const int BS = 256;
   if (!t.host) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&t.host), sizeof(EbTreeHost)));
   EbTreeHost* H = t.host;
@@ -704,7 +762,7 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   k_bbox<<<nbb, BS, 0, st>>>(z, n, t.partial.as<Box4>(), bad);
   eb_count_launch(ctx);
   if (root_sq) k_set_square<<<1, 32, 0, st>>>(root_sq[0], root_sq[1], root_sq[2], sq);
-  else k_bbox_final<<<1, 256, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq);
+  else k_bbox_final<<<1, 256, 0, st>>>(t.partial.as<Box4>(), nbb, t.bbox.as<Box4>(), sq, t.wall, bad);
   eb_count_launch(ctx);
   // 2. keys and sort (a non-finite coordinate gives clamped keys; reported below)
   EB_TRY(t.keys.ensure(sizeof(unsigned long long) * (size_t)n));
@@ -750,10 +808,15 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
   EB_CUDA_TRY(cudaMemcpyAsync(H->sq, sq, sizeof(H->sq), cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaMemcpyAsync(&H->bad, bad, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaMemcpyAsync(H->hist, t.hist.p, sizeof(H->hist), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaMemcpyAsync(&H->lmin, lmin_d, sizeof(int), cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaStreamSynchronize(st));
-  if (H->bad) {
+  if (H->bad & 1) {
     eb_set_last_error_msg("non-finite node coordinate");
     return EB_ERR_NAN;
+  }
+  if (H->bad & 2) {
+    eb_set_last_error_msg("wall-bounded flow: a node lies below the wall y = 0");
+    return EB_ERR_ARG;
   }
   t.W = H->sq[0];
   t.x0 = H->sq[1];
@@ -821,6 +884,19 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
     k_vlist<<<nblk(32LL * (t.nbox - first), 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), lo, first, t.nbox, t.R,
                                                        t.vlist.as<int>(), t.vcode.as<unsigned char>(),
                                                        t.vcount.as<int>());
+    eb_count_launch(ctx);
+  }
+  // 7b. image lists of the wall (levels 2..ld, ld the uniform floor)
+  if (t.wall && L >= 2 && H->lmin >= 2) {
+    t.ld = std::min(H->lmin, L);
+    const int first = t.lev_off[2], nimg = t.lev_off[t.ld + 1];
+    EB_TRY(t.ilist.ensure(sizeof(int) * (size_t)nimg * EB_VMAX));
+    EB_TRY(t.icode.ensure((size_t)nimg * EB_VMAX));
+    EB_TRY(t.icount.ensure(sizeof(int) * (size_t)nimg));
+    EB_CUDA_TRY(cudaMemsetAsync(t.icount.p, 0, sizeof(int) * (size_t)nimg, st));
+    k_imglist<<<nblk(nimg - first, 128), 128, 0, st>>>(t.bkey.as<unsigned long long>(), t.blev.as<unsigned char>(),
+                                                       lo, first, nimg, t.ilist.as<int>(),
+                                                       t.icode.as<unsigned char>(), t.icount.as<int>());
     eb_count_launch(ctx);
   }
   // 8. per-leaf counts, scanned so that one synchronisation sizes them all: U and W list

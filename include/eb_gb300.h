@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define EB_GB300_VERSION 2
+#define EB_GB300_VERSION 3
 
 /* Status codes. The reference prints and STOPs on FMM/GMRES errors
  * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
@@ -103,8 +103,12 @@ typedef struct eb_tree_info {
 /* Physical parameters of the RK right-hand side F (electric.f:968-1109), the values the
  * reference keeps in COMMON: cap (strain rate of the far field psi = -i cap z / 2,
  * stokesbubb.f:64-68), e0 (electric field strength, the E0 of the electric stress,
- * stokesbubb.f:110-128) and zbond (complex Bond number; only 0, free space, is
- * supported). mode selects the solver of both GMRES solves. */
+ * stokesbubb.f:110-128) and zbond (complex Bond number). zbond != 0 is the wall-bounded
+ * flow of the reference (READINI sets iwall = 1, electric.f:321-326): the drops lie above
+ * the wall y = 0, every Stokes sum adds the images across it, and SETVELF / INTERFACENEW
+ * add the reflected log sources zc = i zbond area / (8 pi) (REFSING, reflect.f:28-86);
+ * eb_rk_f and eb_rk2_step then set the context's wall mode as eb_set_wall does (and clear
+ * it for zbond = 0). mode selects the solver of both GMRES solves. */
 typedef struct eb_model {
   double cap;
   double e0;
@@ -243,24 +247,34 @@ int eb_pvintev(eb_ctx* ctx, const double* ucmplx, double* phicmplx, int precisio
 int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi,
                       double* dphi_dn, int precision, int mem);
 
-/* INTERFACENEW (electric.f:791-912), free space: Stokes density u (complex, nbk) ->
- * interface normal velocity un and the FLUX diagnostic. zc: per-drop C_k (complex). */
+/* INTERFACENEW (electric.f:791-912): Stokes density u (complex, nbk) -> interface normal
+ * velocity un and the FLUX diagnostic. zc: per-drop C_k (complex). In wall mode
+ * (eb_set_wall) the Stokes sum adds its images and the far field the reflected log
+ * sources of REFSING (electric.f:868-872). */
 int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double cap,
                           double* un, double* flux, int precision, int mem);
 
-/* SETVELF (stokesbubb.f:4-135), free space: the right-hand side of the Stokes solve
- * (rhs, 2 nbk doubles, interleaved) from dphi_dn (nbk) on the installed geometry:
- * surface tension, the far field of strain rate cap and the electric stress of
- * strength e0. As in the reference, the electric term's `alpha` is the value left by
- * the previous loop, 2 pi (nd_k - 1) / nd_k of the last drop (stokesbubb.f:125). */
+/* SETVELF (stokesbubb.f:4-135): the right-hand side of the Stokes solve (rhs, 2 nbk
+ * doubles, interleaved) from dphi_dn (nbk) on the installed geometry: surface tension,
+ * the far field of strain rate cap and the electric stress of strength e0. As in the
+ * reference, the electric term's `alpha` is the value left by the previous loop,
+ * 2 pi (nd_k - 1) / nd_k of the last drop (stokesbubb.f:125). eb_setvelf is zbond = 0.
+ * eb_setvelf_bond takes the Bond number zbond[2] (complex; NULL: 0) and, for zbond != 0,
+ * the per-drop C_k zc (complex, k, in rhs's memory): the gravity term and the C_k sums
+ * (:38-56, :73-102), and in wall mode minus the reflected log sources of REFSING
+ * (:53-60). The wall branch of the reference subtracts a `zstr` it never assigns (:67);
+ * here it is the capillary term of the free-space branch, the term INTERFACENEW keeps on
+ * a wall (both readings agree for cap = 0). */
 int eb_setvelf(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, double* rhs,
                int mem);
+int eb_setvelf_bond(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, const double* zbond,
+                    const double* zc, double* rhs, int mem);
 
-/* F (electric.f:968-1109), free space: the RK right-hand side of the interface
- * positions. rku (interleaved x, y of all nodes, 2 nbk doubles) -> rkup (the node
- * velocities, same layout): EXTRACTDAT, Laplace solve, DIRICH_NEU_MAP, SETVELF, Stokes
- * solve, INTERFACENEW, EQUIT and the filtered node velocity, all on the GPU. Installs
- * the geometry of rku in the context. */
+/* F (electric.f:968-1109): the RK right-hand side of the interface positions. rku
+ * (interleaved x, y of all nodes, 2 nbk doubles) -> rkup (the node velocities, same
+ * layout): EXTRACTDAT, Laplace solve, DIRICH_NEU_MAP, SETVELF, Stokes solve,
+ * INTERFACENEW, EQUIT and the filtered node velocity, all on the GPU. Installs the
+ * geometry of rku in the context; model->zbond != 0 runs the wall-bounded branch. */
 int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup,
             const eb_model* model, eb_stage_info* info, int mem);
 
@@ -296,8 +310,24 @@ int eb_double(eb_ctx* ctx, int k, const int* nd, const double* rku, const int* i
  *  - FASMVP's far-field pressure is that of each simulation's first drop, and SETVELF
  *    takes E0 per simulation (e0[s]; NULL: the eb_model's e0 for all) and the alpha of
  *    each simulation's last drop (stokesbubb.f:125).
- * nsim = 0 returns the context to one simulation. */
+ * nsim = 0 returns the context to one simulation. A context in wall mode takes no
+ * batch (EB_ERR_ARG). */
 int eb_batch_define(eb_ctx* ctx, int nsim, const int* sim_k, const double* e0);
+
+/* Wall-bounded flow, the IFLAG2 = 1 branch of CADAPDR / CADAPMOD (COMMON /wallinfo/,
+ * electric.f:55; cadapdrop.f:142-145, cadapdrop2.f:159-197 and 690-721, cadap2.f:1468-1586):
+ * with iwall = 1 every Stokes sum of the installed geometry (eb_stokes_matvec,
+ * eb_stokes_sum, eb_interface_velocity, the solves) adds the sum over the images of the
+ * sources across the wall y = 0; the nodes must lie on or above it (EB_ERR_ARG otherwise,
+ * at the next install). xleft and slength, the square [xleft, xleft + slength] x
+ * [0, slength] of the reference's wall-bounded FMM, are EXTRACTDAT's (electric.f:710-711:
+ * the smallest x and max(x range, largest y) of the nodes) and are recomputed at every
+ * install; eb_get_wall reads them. The mode persists across installs; setting it on an
+ * installed geometry rebuilds its tree. Not available for a batch (EB_ERR_ARG).
+ * Replaces the reference's IFLAG2 argument of CADAPDR/CADAPMOD (cadapdrop.f:3, cadapmod.f:3)
+ * and its XLEFT/SLENGTH arguments. */
+int eb_set_wall(eb_ctx* ctx, int iwall);
+int eb_get_wall(eb_ctx* ctx, int* iwall, double* xleft, double* slength);
 
 /* Input deck and checkpoint files of the reference (host only, no context).
  * eb_bubbin_read: the first deck of a `bubbin` file as READINI reads it
