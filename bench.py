@@ -258,6 +258,46 @@ def run_gpu(args, rank, world, local):
         lap[mode + "_solves_per_s"] = world * args.steps / (ea0.elapsed_time(ea1) * 1e-3)
         lap[mode + "_info"] = linfo
 
+    # wall-bounded flow (zbond != 0): 64 drops x 512 nodes above the wall y = 0, every
+    # Stokes sum with the images across it; solves as above, and the operator with and
+    # without the images on the same geometry
+    wcfg = configs.wall_drops(k=64, n=512, seed=12, box=24.0)
+    ctx_w = Context(device=local, graphs=graphs)
+    ctx_w.set_stream(stream.cuda_stream)
+    ctx_w.set_wall(1)
+    wgeo = ctx_w.extractdat(wcfg.nd, wcfg.rku())
+    wrhs = torch.from_numpy(surface_tension_rhs(wgeo["dz"], wgeo["dsda"])).to(dev)
+    wx = torch.empty_like(wrhs)
+    wall = {"workload": wcfg.name + " above the wall y = 0", "nodes": wcfg.nbk}
+    for mode in ("fp64", "fp32_refined"):
+        for _ in range(args.warmup):
+            ctx_w.solvei(wrhs, mode, out=wx)
+        torch.cuda.synchronize()
+        ew0, ew1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ew0.record(stream)
+        for _ in range(args.steps):
+            _, winfo = ctx_w.solvei(wrhs, mode, out=wx)
+        ew1.record(stream)
+        torch.cuda.synchronize()
+        wall[mode + "_solves_per_s"] = world * args.steps / (ew0.elapsed_time(ew1) * 1e-3)
+        wall[mode + "_info"] = winfo
+    wu = torch.randn(2 * wcfg.nbk, dtype=torch.float64, device=dev)
+    wy = torch.empty_like(wu)
+    for iw in (1, 0):
+        ctx_w.set_wall(iw)
+        for prec in ("fp64", "fp32"):
+            for _ in range(3):
+                ctx_w.fasmvp(wu, prec, out=wy)
+            torch.cuda.synchronize()
+            ew0, ew1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ew0.record(stream)
+            for _ in range(10):
+                ctx_w.fasmvp(wu, prec, out=wy)
+            ew1.record(stream)
+            torch.cuda.synchronize()
+            wall["apply_us_%s_%s" % (prec, "wall" if iw else "free")] = ew0.elapsed_time(ew1) * 100.0
+    ctx_w.close()
+
     # FMM Mpts/s: single Stokes operator applies, FP64 and FP32
     u = torch.randn(n, dtype=torch.float64, device=dev)
     y = torch.empty_like(u)
@@ -522,8 +562,8 @@ def run_gpu(args, rank, world, local):
                      "achieved": dom["achieved_tflops"], "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": dom["achieved_tflops"] / fp32_peak,
                      # DRAM bytes of one k_near32<2> launch of this workload (ncu
-                     # dram__bytes_read.sum + dram__bytes_write.sum: 1,407,232 + 0)
-                     "traffic": 1407232 if WORKLOAD == "many_drops_64x512" else None,
+                     # dram__bytes_read.sum + dram__bytes_write.sum: 1,381,632 + 0)
+                     "traffic": 1381632 if WORKLOAD == "many_drops_64x512" else None,
                      "traffic_unit": "bytes per launch (ncu capture of this workload)",
                      "peak_source": "measured in-run FP32 FMA chain (MEASURED_PEAKS.json has no FP32 "
                                     "CUDA-core figure)",
@@ -531,6 +571,7 @@ def run_gpu(args, rank, world, local):
         "kernels": kern,
         "m2l_tensor_ab": m2l_ab,
         "laplace": lap,
+        "wall": wall,
         "peaks_measured_in_run": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak},
         "cpu_baseline": cpu,
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "solves/s",

@@ -10,6 +10,8 @@ Stages (all by default), on the 64-drop x 512-node workload unless named otherwi
   apply    ten FP32 Stokes operator applies, then ten double-float ones
   rk2      one FP32-refined RK2 step (the spectral kernels, SETVELF, EQUIT, both solves)
   batch    one FP32-refined RK2 step of 64 of the uneven simulations as one batch
+  wall     one FP32-refined Stokes solve (host loop) of 64 drops x 512 nodes above the
+           wall y = 0: the image lists, mirrored multipoles and reflected near field
 
 Each stage runs once; the device holds well under 1 GB. Prints "ok" at the end.
 """
@@ -65,8 +67,17 @@ def stage_batch():
     ctx.rk2(nd, 1e-3, y, mode="fp32_refined")
 
 
+def stage_wall():
+    cfg = configs.wall_drops(k=64, n=512, seed=12, box=24.0)
+    ctx = Context(graphs=-1)
+    ctx.set_wall(1)
+    g = _tree(ctx, cfg)
+    rhs = np.ascontiguousarray(-0.5 * g["dz"] / g["dsda"]).view(np.float64).copy()
+    ctx.solvei(rhs, "fp32_refined")
+
+
 STAGES = {"tree": stage_tree, "solve": stage_solve, "apply": stage_apply, "rk2": stage_rk2,
-          "batch": stage_batch}
+          "batch": stage_batch, "wall": stage_wall}
 
 
 def main(argv):
