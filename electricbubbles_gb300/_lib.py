@@ -121,6 +121,10 @@ SIGNATURES = {
     "eb_setvelf": (_I, [_P, _P, _D, _D, _P, _I]),
     "eb_setvelf_bond": (_I, [_P, _P, _D, _D, _P, _P, _P, _I]),
     "eb_set_wall": (_I, [_P, _I]),
+    "eb_stokes_matvec_adjoint": (_I, [_P, _I, _P, _P, _I, _I]),
+    "eb_laplace_matvec_adjoint": (_I, [_P, _I, _P, _P, _I, _I]),
+    "eb_stokes_solve_adjoint": (_I, [_P, _I, _P, _P, _I, ctypes.POINTER(SolveInfo), _I]),
+    "eb_laplace_solve_adjoint": (_I, [_P, _I, _P, _P, _I, ctypes.POINTER(SolveInfo), _I]),
     "eb_get_wall": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "eb_rk_f": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo), _I]),
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),

@@ -299,6 +299,32 @@ class Context:
         check(fn, st)
         return x, info.as_dict()
 
+    def fasmvp_adjoint(self, x, precision="fp64", out=None):
+        """The transpose of the Stokes operator: y = A^T x, x and y real of length 2 nbk."""
+        if not _is_device(x):
+            x = _host(x, np.float64)
+        y = out if out is not None else self._out(x, 2 * self.nbk, np.float64)
+        check("eb_stokes_matvec_adjoint", self._lib.eb_stokes_matvec_adjoint(
+            self._h, 2 * self.nbk, _ptr(x), _ptr(y), PRECISION[precision], _mem(x, y)))
+        return y
+
+    def fasmvp_lap_adjoint(self, x, precision="fp64", out=None):
+        """The transpose of the Laplace operator: y = A^T x, x and y real of length nbk."""
+        if not _is_device(x):
+            x = _host(x, np.float64)
+        y = out if out is not None else self._out(x, self.nbk, np.float64)
+        check("eb_laplace_matvec_adjoint", self._lib.eb_laplace_matvec_adjoint(
+            self._h, self.nbk, _ptr(x), _ptr(y), PRECISION[precision], _mem(x, y)))
+        return y
+
+    def solvei_adjoint(self, rhs, mode="fp64", out=None):
+        """GMRES on the transposed Stokes operator (A^T x = rhs). Returns (soln, info)."""
+        return self._solve("eb_stokes_solve_adjoint", 2 * self.nbk, rhs, mode, out)
+
+    def solve_lapl_adjoint(self, rhs, mode="fp64", out=None):
+        """GMRES on the transposed Laplace operator. Returns (soln, info)."""
+        return self._solve("eb_laplace_solve_adjoint", self.nbk, rhs, mode, out)
+
     def solvei(self, rhs, mode="fp64", out=None):
         """SOLVEI: GMRES on the Stokes operator, x0 = rhs. Returns (soln, info)."""
         return self._solve("eb_stokes_solve", 2 * self.nbk, rhs, mode, out)

@@ -63,7 +63,8 @@ __device__ __forceinline__ int quadrant(unsigned long long key) {
 // combinations P = qa + s qb, Q = qa - s qb, A = -s conj(qa).
 // ---------------------------------------------------------------------------------
 // Computed in T: the FP32 operator forms its charges in FP32 (GB300's FP64 pipe is ~1/60
-// of its FP32 rate).
+// of its FP32 rate). dz = null: the charges of the transposed operator's sum,
+// qa = -dens, qb = conj(dens).
 template <typename T>
 __global__ void k_charges_stokes(int n, const int* __restrict__ perm,
                                  const double2* __restrict__ dens, const double2* __restrict__ dz,
@@ -73,15 +74,23 @@ __global__ void k_charges_stokes(int n, const int* __restrict__ perm,
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int o = perm[i];
-  const double2 ud = dens[o], dd = dz[o];
-  const c_t<T> u = cmk<T>((T)ud.x, (T)ud.y), d = cmk<T>((T)dd.x, (T)dd.y);
+  const double2 ud = dens[o];
+  const c_t<T> u = cmk<T>((T)ud.x, (T)ud.y);
   const T s = (T)sd;
-  const T h = (T)hpt[o] * (T)(1.0 / (2.0 * EB_PI));
-  // 1/(2 pi i) = -i/(2 pi)
-  c_t<T> w = cmul<T>(u, d);
-  c_t<T> a = cmk<T>(w.y * h, -w.x * h);
-  c_t<T> v = csub<T>(cmul<T>(u, cconj<T>(d)), cmul<T>(cconj<T>(u), d));
-  c_t<T> b = cmk<T>(v.y * h, -v.x * h);
+  c_t<T> a, b;
+  if (dz) {
+    const double2 dd = dz[o];
+    const c_t<T> d = cmk<T>((T)dd.x, (T)dd.y);
+    const T h = (T)hpt[o] * (T)(1.0 / (2.0 * EB_PI));
+    // 1/(2 pi i) = -i/(2 pi)
+    c_t<T> w = cmul<T>(u, d);
+    a = cmk<T>(w.y * h, -w.x * h);
+    c_t<T> v = csub<T>(cmul<T>(u, cconj<T>(d)), cmul<T>(cconj<T>(u), d));
+    b = cmk<T>(v.y * h, -v.x * h);
+  } else {
+    a = cmk<T>(-u.x, -u.y);
+    b = cconj<T>(u);
+  }
   qa[i] = a;
   qb[i] = b;
   pq[2 * i] = cmk<T>(a.x + s * b.x, a.y + s * b.y);
@@ -104,12 +113,18 @@ __global__ void k_charges_stokes_df(int n, const int* __restrict__ perm, const d
   if (i >= n) return;
   int o = perm[i];
   const double rinv = ldexp(winv, (int)plev[i]);
-  double2 u = dens[o], d = dz[o];
-  double h = hpt[o] * (1.0 / (2.0 * EB_PI));
-  double2 w = cmul<double>(u, d);
-  double2 a = make_double2(w.y * h, -w.x * h);
-  double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
-  double2 b = make_double2(v.y * h, -v.x * h);
+  double2 u = dens[o], a, b;
+  if (dz) {
+    double2 d = dz[o];
+    double h = hpt[o] * (1.0 / (2.0 * EB_PI));
+    double2 w = cmul<double>(u, d);
+    a = make_double2(w.y * h, -w.x * h);
+    double2 v = csub<double>(cmul<double>(u, cconj<double>(d)), cmul<double>(cconj<double>(u), d));
+    b = make_double2(v.y * h, -v.x * h);
+  } else {  // the transposed operator's charges
+    a = make_double2(-u.x, -u.y);
+    b = cconj<double>(u);
+  }
   qdf[2 * i] = df4(make_double2(a.x * rinv, a.y * rinv));
   qdf[2 * i + 1] = df4(make_double2(b.x * rinv, b.y * rinv));
   pq[2 * i] = df4(make_double2((a.x + s * b.x) * rinv, (a.y + s * b.y) * rinv));
@@ -2167,7 +2182,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                              w.mpole.as<float2>(), out, post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
-  if (E == 2 && t.wall) {  // the reflected near field, after the output is written
+  if (E == 2 && t.wall && dz) {  // the reflected near field, after the output is written
     const int ld = t.ld, nb = t.lev_off[ld + 1] - t.lev_off[ld];
     double2* dst = post.kind == 1 ? reinterpret_cast<double2*>(post.y) : out;
     k_img_near<<<nb, IMG_TILE, 0, st>>>(t.lev_off[ld], nb, ld, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),

@@ -236,6 +236,7 @@ struct eb_ctx {
   // RK stage F and the RK2 step
   DevBuf st_lap;                   // double[5*nbk]: Laplace rhs/Un, density, phi, psi, dphi/dn
   DevBuf st_rhs, st_u, st_zc;      // Stokes rhs and density (double2[nbk]), C_k (double2[k])
+  DevBuf adj_a, adj_b, adj_s;      // transposed operators: two node sums, per-drop sums
   DevBuf rk_y, rk_y1, rk_d0, rk_phi;  // RK state, predictor, derivative, dt * F(y)
 
   // GMRES workspace
@@ -348,6 +349,9 @@ int eb_tables_init(eb_ctx* ctx);
 // fuses an operator's post-processing into the leaf kernels.
 // `join` (may be null): an event the leaf kernel waits for (work the caller forked onto
 // another stream whose results the post-processing reads).
+// The Stokes sum of FASMVP's charges qa = dens dz h/(2 pi i), qb = (dens conj(dz) -
+// conj(dens) dz) h/(2 pi i); dz = null: the charges qa = -dens, qb = conj(dens) of the
+// transposed operator's sums (never with a wall's images).
 int eb_fmm_apply(eb_ctx* ctx, EbTree& t, int kernel, int sign, int precision,
                  const double2* dens, const double2* dz, const double* hpt, double2* out,
                  const EbPost* post = nullptr, cudaEvent_t join = nullptr);
@@ -358,6 +362,9 @@ int eb_fmm_apply_cauchy(eb_ctx* ctx, EbTree& t, int precision, const double2* q,
 int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw, int prec);
 int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
 int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec);
+// adjoint.cu: the transposed operators
+int eb_stokes_matvec_adj_dev(eb_ctx* ctx, const double* x, double* y, int prec);
+int eb_laplace_matvec_adj_dev(eb_ctx* ctx, const double* x, double* y, int prec);
 
 // m2l_tc.cu: the FP32 M2L of order 20 on the tensor cores
 int eb_m2l_tc(eb_ctx* ctx, int E, int first, int ntarget, const int* vlist, const unsigned char* vcode,

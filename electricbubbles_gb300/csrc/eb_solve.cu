@@ -793,7 +793,8 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
 int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mode,
           eb_solve_info* info, int mem) {
   if (ctx->nsim > 0)  // a batch of simulations: GMRES per simulation, in lockstep
-    return eb_batch_solve(ctx, n, op, op == eb_stokes_matvec_dev, rhs, soln, mode, info, mem);
+    return eb_batch_solve(ctx, n, op, op == eb_stokes_matvec_dev || op == eb_stokes_matvec_adj_dev, rhs, soln,
+                          mode, info, mem);
   cudaStream_t s = ctx->stream;
   Gm g{ctx, n, std::min(nblk(n, RBS), rmaxb(ctx)), s, nullptr};
   const int maxl = ctx->opts.maxl;
@@ -917,6 +918,35 @@ int eb_laplace_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mo
   if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
   cudaSetDevice(ctx->device);
   return solve(ctx, n, eb_laplace_matvec_dev, rhs, soln, mode, info, mem);
+}
+
+// The same GMRES on the transposed operators (the adjoint solves).
+int eb_stokes_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                            eb_solve_info* info, int mem) {
+  if (!ctx || !rhs || !soln) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != 2 * ctx->nbk || (mode != EB_SOLVE_FP64 && mode != EB_SOLVE_FP32_REFINED)) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (ctx->iwall) {
+    eb_set_last_error_msg("the transposed operators do not include the wall's images");
+    return EB_ERR_ARG;
+  }
+  cudaSetDevice(ctx->device);
+  return solve(ctx, n, eb_stokes_matvec_adj_dev, rhs, soln, mode, info, mem);
+}
+
+int eb_laplace_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                             eb_solve_info* info, int mem) {
+  if (!ctx || !rhs || !soln) return EB_ERR_ARG;
+  if (!ctx->geom_valid) return EB_ERR_NOGEOM;
+  if (n != ctx->nbk || (mode != EB_SOLVE_FP64 && mode != EB_SOLVE_FP32_REFINED)) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  if (ctx->iwall) {
+    eb_set_last_error_msg("the transposed operators do not include the wall's images");
+    return EB_ERR_ARG;
+  }
+  cudaSetDevice(ctx->device);
+  return solve(ctx, n, eb_laplace_matvec_adj_dev, rhs, soln, mode, info, mem);
 }
 
 // ---------------------------------------------------------------------------------

@@ -314,6 +314,24 @@ int eb_double(eb_ctx* ctx, int k, const int* nd, const double* rku, const int* i
  * batch (EB_ERR_ARG). */
 int eb_batch_define(eb_ctx* ctx, int nsim, const int* sim_k, const double* e0);
 
+/* Transposed operators and adjoint solves, for reverse-mode gradients of what a solve
+ * produces with respect to its right-hand side (and so to the parameters that enter it
+ * linearly, such as E0 and cap through SETVELF): for J(x) with A x = b(theta),
+ * dJ/dtheta = lambda^T db/dtheta where A^T lambda = dJ/dx. No counterpart in the
+ * reference, which has no adjoint; these are the exact transposes, for the real inner
+ * product of the solver's unknowns, of FASMVP (stokesbubb.f:496-614, as MATVEC applies
+ * it) and of FASMVP_LAP's n x n operator (laplace.f:159-262, without the k constraint
+ * sums past YY(N)), formed from the same FMM (a Cauchy sum and a Stokes sum with the
+ * charges -v, conj(v) for the Stokes transpose; one Cauchy sum for the Laplace one).
+ * The solves are the same GMRES (DGMRES semantics, x0 = rhs; both modes; per simulation
+ * in a batch). Not available in wall mode (EB_ERR_ARG): the transposes hold no images. */
+int eb_stokes_matvec_adjoint(eb_ctx* ctx, int n, const double* x, double* y, int precision, int mem);
+int eb_laplace_matvec_adjoint(eb_ctx* ctx, int n, const double* x, double* y, int precision, int mem);
+int eb_stokes_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                            eb_solve_info* info, int mem);
+int eb_laplace_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
+                             eb_solve_info* info, int mem);
+
 /* Wall-bounded flow, the IFLAG2 = 1 branch of CADAPDR / CADAPMOD (COMMON /wallinfo/,
  * electric.f:55; cadapdrop.f:142-145, cadapdrop2.f:159-197 and 690-721, cadap2.f:1468-1586):
  * with iwall = 1 every Stokes sum of the installed geometry (eb_stokes_matvec,
