@@ -242,8 +242,6 @@ struct eb_ctx {
   // GMRES workspace
   DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ, gTicket;
   DevBuf gCtl, gXin, gWbuf;        // graph mode: control block, operator input and output
-  DevBuf gBar;                     // graph mode: the fused Arnoldi step's grid barrier
-  int coop = -1;                   // cooperative launches of that kernel: -1 unknown, 0 no, 1 yes
   std::vector<double> hH;
   unsigned long long geom_version = 0;  // advanced by every geometry install
   // hash of everything a captured solve graph takes from the geometry by value (counts,

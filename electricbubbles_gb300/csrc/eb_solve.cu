@@ -497,130 +497,6 @@ __global__ void k_gm_sub_arnoldi(int n, const int* __restrict__ ncol_dev, const 
   if (threadIdx.x < 32) gm_arnoldi_warp(c, hdev, h);
 }
 
-// Grid-wide barrier of the fused Arnoldi step (cooperative launch: every block is
-// resident). Thread 0 of each block arrives on a counter; the last to arrive resets it
-// and advances the generation the others wait on. The wait is bounded (~1 s): a block
-// that gives up sets err, and once err is set every barrier returns at once, so a
-// failure ends the kernel quickly and the step reports it.
-struct GridBar {
-  unsigned int count;
-  unsigned int gen;
-  int err;
-  int pad;
-};
-
-__device__ void grid_bar(GridBar* b, unsigned int nblocks) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int* vg = &b->gen;
-    volatile int* ve = &b->err;
-    if (*ve == 0) {
-      const unsigned int g = *vg;
-      __threadfence();
-      if (atomicAdd(&b->count, 1u) == nblocks - 1) {
-        atomicExch(&b->count, 0u);
-        __threadfence();
-        atomicAdd(&b->gen, 1u);
-      } else {
-        unsigned int it = 0;
-        while (*vg == g && *ve == 0) {
-          if (++it > (1u << 24)) {
-            atomicExch(&b->err, 1);
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
-      __threadfence();
-    }
-  }
-  __syncthreads();
-}
-
-// One Arnoldi step of the refined inner GMRES after the operator: w = wbuf = A v_ll.
-// Phase 1: each block's contiguous rows give partial V^T w (warps over columns, as
-// k_vtw). Barrier. Phase 2: every block adds the partials in block order (so all hold
-// the same h), w -= V h on its rows and a partial ||w||^2. Barrier. Phase 3: every block
-// adds the norm partials; block 0 writes h and ||w||^2 and ends the step (Hessenberg
-// column, DHEQR, stopping test, loop condition: gm_arnoldi_warp); every block stores
-// V[:, ll] = xin = w / ||w|| on its rows (unused when the loop stops). Two barriers
-// replace the launches of k_vtw, k_gm_sub_arnoldi and k_gm_store.
-__global__ void __launch_bounds__(256) k_gm_step_fused(int n, const int* __restrict__ ll_dev, double* V,
-                                                       size_t ldv, double* w, double* __restrict__ part,
-                                                       int maxl, double* hdev, GmCtl* c, GridBar* bar,
-                                                       double* __restrict__ xin, cudaGraphConditionalHandle hc) {
-  __shared__ double hs[EB_GM_MAXL + 2];
-  __shared__ double red[32];
-  const int ll = *ll_dev;
-  const int nb = gridDim.x;
-  const int rows = (n + nb - 1) / nb;
-  const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
-  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  double* hpart = part;
-  double* npart = part + (size_t)nb * (maxl + 1);
-  for (int j = wi; j < ll; j += nw) {
-    const double* v = V + (size_t)j * ldv;
-    double sum = 0.0;
-    for (int i = r0 + lane; i < r1; i += 32) sum = fma(v[i], w[i], sum);
-    sum = warp_sum<double>(sum);
-    if (lane == 0) hpart[(size_t)blockIdx.x * ll + j] = sum;
-  }
-  grid_bar(bar, (unsigned)nb);
-  for (int j = wi; j < ll; j += nw) {
-    double sum = 0.0;
-    for (int b = lane; b < nb; b += 32) sum += __ldcg(hpart + (size_t)b * ll + j);
-    sum = warp_sum<double>(sum);
-    if (lane == 0) hs[j] = sum;
-  }
-  __syncthreads();
-  double sq = 0.0;
-  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-    double acc = 0.0;
-    for (int j = 0; j < ll; ++j) acc = fma(V[(size_t)j * ldv + i], hs[j], acc);
-    const double v = w[i] - acc;
-    w[i] = v;
-    sq = fma(v, v, sq);
-  }
-  sq = block_sum(sq, red);
-  if (threadIdx.x == 0) npart[blockIdx.x] = sq;
-  grid_bar(bar, (unsigned)nb);
-  __shared__ double s_nrm2;
-  if (wi == 0) {
-    double sum = 0.0;
-    for (int b = lane; b < nb; b += 32) sum += __ldcg(npart + b);
-    sum = warp_sum<double>(sum);
-    if (lane == 0) s_nrm2 = sum;
-  }
-  __syncthreads();
-  const double nrm2 = s_nrm2;
-  if (blockIdx.x == 0) {
-    for (int j = threadIdx.x; j < ll; j += blockDim.x) hdev[GM_H1 + j] = hs[j];
-    if (threadIdx.x == 0) hdev[GM_NW] = nrm2;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      if (bar->err) {
-        if (threadIdx.x == 0) {
-          c->status = EB_ERR_WORKSPACE;
-          c->cont = 0;
-          cudaGraphSetConditional(hc, 0u);
-        }
-      } else {
-        gm_arnoldi_warp(c, hdev, hc);
-      }
-    }
-  }
-  const double snormw = sqrt(fmax(nrm2, 0.0));
-  if (snormw > 0.0 && isfinite(snormw)) {
-    const double sc = 1.0 / snormw;
-    double* dst = V + (size_t)ll * ldv;
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      const double v = w[i] * sc;
-      dst[i] = v;
-      xin[i] = v;
-    }
-  }
-}
-
 // DHELS (dhels.f:77-96) on the device: y = R^-1 Q^T (r0nrm e1), into ydev.
 __global__ void k_gm_finish(GmCtl* c, double* __restrict__ ydev) {
   __shared__ double y[EB_GM_MAXL + 1];
@@ -686,25 +562,6 @@ __global__ void k_gm_axpy(int n, const GmCtl* __restrict__ c, const double* __re
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += d[i];
 }
 
-// Whether the fused Arnoldi step can run: the option, the device's cooperative launch
-// support, every block of the reduction grid resident at once, and its barrier state.
-bool fused_ok(eb_ctx* ctx, int nb) {
-  if (ctx->opts.gm_fused < 0) return false;
-  if (ctx->coop < 0) {
-    int attr = 0, per_sm = 0;
-    cudaDeviceGetAttribute(&attr, cudaDevAttrCooperativeLaunch, ctx->device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gm_step_fused, RBS, 0);
-    ctx->coop = attr && per_sm * ctx->nsm >= rmaxb(ctx) ? 1 : 0;
-    cudaGetLastError();
-  }
-  if (ctx->coop != 1 || nb > rmaxb(ctx)) return false;
-  if (!ctx->gBar.p) {
-    if (ctx->gBar.ensure(sizeof(GridBar)) != EB_OK) return false;
-    if (cudaMemset(ctx->gBar.p, 0, sizeof(GridBar)) != cudaSuccess) return false;
-  }
-  return true;
-}
-
 enum { GM_PLAIN = 0, GM_REFINE = 1 };
 constexpr int GM_BUILD_FAILED = -100;  // internal: fall back to the host-driven loop
 
@@ -725,7 +582,6 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   double* wbuf = ctx->gWbuf.as<double>();
   unsigned int* ticket = ctx->gTicket.as<unsigned int>();
   const bool refine = kind == GM_REFINE;
-  const bool fused = refine && fused_ok(ctx, nb);
   const int prec = refine ? EB_FP32 : EB_FP64;
   const double tol = refine ? ctx->opts.inner_tol : ctx->opts.gmres_tol;
   double* bb = refine ? ctx->gZ.as<double>() : ctx->gR.as<double>();  // right-hand side of the cycle
@@ -772,27 +628,6 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
     k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
-    if (refine && fused) {
-      // one Gram-Schmidt pass, the norm and the next column in one cooperative kernel
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(nb);
-      cfg.blockDim = dim3(RBS);
-      cfg.stream = s;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeCooperative;
-      attr[0].val.cooperative = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      const cudaError_t le = cudaLaunchKernelEx(&cfg, k_gm_step_fused, n, lld, V, ldv, wbuf, part, maxl, hdev,
-                                                ctl, ctx->gBar.as<GridBar>(), xin, h);
-      if (le != cudaSuccess) {  // not capturable here: later graphs use the three kernels
-        ctx->coop = 0;
-        eb_set_last_cuda_error(le, "cudaLaunchKernelEx (cooperative)", __FILE__, __LINE__);
-        return EB_ERR_CUDA;
-      }
-      ctx->launches += 2;  // with the operator's count: the fused kernel stands for three
-      return eb_check_launch(ctx, "gmres graph (fused body)");
-    }
     if (refine) {
       // one Gram-Schmidt pass for the inner FP32 cycle (the H2 slots stay zero)
       k_gm_sub_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev, ticket, ctl, h);
@@ -926,11 +761,6 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
     const double itol = inner_tolerance(ctx, outer, err_prev);
     EB_CUDA_TRY(cudaMemcpyAsync(ctx->gH.as<double>() + GM_TOL, &itol, sizeof(double), cudaMemcpyHostToDevice, s));
     EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, &head));
-    if (head.status == EB_ERR_WORKSPACE) {  // a fused step's grid barrier gave up
-      cudaMemsetAsync(ctx->gBar.p, 0, sizeof(GridBar), s);
-      eb_set_last_error_msg("GMRES: the fused Arnoldi step's grid barrier timed out");
-      return head.status;
-    }
     if (head.status != EB_OK) {
       eb_set_last_error_msg("non-finite value in GMRES");
       return head.status;

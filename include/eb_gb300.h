@@ -77,10 +77,6 @@ typedef struct eb_opts {
                        arithmetic: 0 default (on), 1 on, -1 off (native FP64)   */
   int m2l_tc;       /* FP32 M2L (order 20) as a 3xTF32 contraction on the tensor
                        cores (tcgen05): 0 default (off), 1 on, -1 off          */
-  int gm_fused;     /* graph mode, refined inner GMRES: each Arnoldi step's
-                       Gram-Schmidt pass, norm and next column in one cooperative
-                       kernel with grid-wide barriers instead of three launches:
-                       0 default (on where the device allows it), 1 on, -1 off */
 } eb_opts;
 
 typedef struct eb_solve_info {
