@@ -1312,7 +1312,6 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
                                                  const float4* __restrict__ pq,
                                                  const float4* __restrict__ aa, int p, double s,
                                                  const float4* __restrict__ local,
-                                                 const int* __restrict__ anc,
                                                  double2* __restrict__ out, EbPost post,
                                                  double2* __restrict__ nearbuf) {
   const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1328,28 +1327,9 @@ __global__ void __launch_bounds__(128) k_leaf_df(int ngroup, const int* __restri
   const bool neg = s < 0.0;
   const int lt = blev[b];
   dfacc gx{0.f, 0.f}, gy{0.f, 0.f};
+  if (MODE != 1 && has_far && lt >= 2) l2p_part_df<E>(local + (size_t)b * E * (p + 1), p, sl, wi, neg, gx, gy);
   const unsigned long long kb = bkey[b];
   const int bx = (int)compact2d(kb), by = (int)compact2d(kb >> 1);
-  if (MODE != 1 && has_far && lt >= 2) {
-    // the local expansions of the leaf and of its ancestors down to the level whose
-    // locals hold the L2L-accumulated levels above (the anc list of the FP32 far
-    // field), each evaluated about its own centre: the target's offset sh levels up is
-    // u 2^-sh + (i + 1/2) 2^-sh - (i >> sh) - 1/2, the constant exact in FP32
-    const int* fb = anc + (size_t)leaf * EB_FAR_LEVELS;
-    for (int q = 0; q < EB_FAR_LEVELS; ++q) {
-      const int a = fb[q];
-      if (a < 0) break;
-      const int sh = lt - (int)blev[a];
-      cdf u = wi;
-      if (sh > 0) {
-        const float f = __int_as_float((127 - sh) << 23);  // 2^-sh
-        const float cx = fmaf((float)bx + 0.5f, f, -((float)(bx >> sh) + 0.5f));
-        const float cy = fmaf((float)by + 0.5f, f, -((float)(by >> sh) + 0.5f));
-        u = cdf{dfl_add(dfl_mul_f(wi.x, f), dfl{cx, 0.f}), dfl_add(dfl_mul_f(wi.y, f), dfl{cy, 0.f})};
-      }
-      l2p_part_df<E>(local + (size_t)a * E * (p + 1), p, sl, u, neg, gx, gy);
-    }
-  }
   if (MODE != 1 && has_far) {
     // W list: the lanes of a target take every 4th box
     for (int jw = wstart[leaf] + sl; jw < wstart[leaf + 1]; jw += 4) {
@@ -1948,9 +1928,7 @@ int fmm_expansions_df(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
     }
     ps.done();
   }
-  // L2L down to level lend only: the leaf kernel evaluates the locals of the finer
-  // levels (at most EB_FAR_LEVELS per leaf) directly, with no dependent chain of shifts
-  for (int l = 3; l <= t.lend; ++l) {
+  for (int l = 3; l <= L; ++l) {
     int nb = t.lev_off[l + 1] - t.lev_off[l];
     size_t sm = sizeof(float4) * E * (p + 1);
     k_l2l_df<E><<<nb, round32(4 * E * (p + 1)), sm, st>>>(t.lev_off[l], t.bkey.as<unsigned long long>(),
@@ -2136,7 +2114,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
           t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
           t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
           t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
-          (double)sign, w.local_df.as<float4>(), t.anc.as<int>(), out, post, w.nearbuf.as<double2>());
+          (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
     } else {
       k_near32<E><<<t.ntile, 128, 0, ss>>>(t.tiles.as<int4>(), t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
                                            t.ustart.as<int>(), t.ulist.as<int>(), t.zhl.as<float4>(),
@@ -2174,7 +2152,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.blev.as<unsigned char>(), t.pt0.as<int>(), t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
         t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
-        (double)sign, w.local_df.as<float4>(), t.anc.as<int>(), out, post, w.nearbuf.as<double2>());
+        (double)sign, w.local_df.as<float4>(), out, post, w.nearbuf.as<double2>());
   } else if (split) {
     k_far32<E><<<t.ntile, 128, far_sm, st>>>(t.tiles.as<int4>(), t.leaves.as<int>(),
                                              t.bkey.as<unsigned long long>(), t.blev.as<unsigned char>(),
@@ -2188,7 +2166,7 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
         t.wstart.as<int>(), t.wlist.as<int>(), w.mpole_df.as<float4>(), t.perm.as<int>(),
         t.wdf.as<float4>(), t.wdf_lo.as<float2>(), w.pqdf.as<float4>(), w.aadf.as<float4>(), tb.p,
         (double)sign,
-        w.local_df.as<float4>(), t.anc.as<int>(), out, post, nullptr);
+        w.local_df.as<float4>(), out, post, nullptr);
   } else if (f64) {
     k_leaf64<E><<<blocks, 128, 0, st>>>(
         t.ngroup, t.gleaf.as<int>(), t.gfirst.as<int>(), t.leaves.as<int>(), has_far, t.bkey.as<unsigned long long>(),
