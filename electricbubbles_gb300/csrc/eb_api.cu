@@ -451,7 +451,7 @@ int eb_stokes_sum_dev(eb_ctx* ctx, const double2* dens, int sign, double2* gradw
 int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   if (!ctx->geom_valid) return EB_ERR_NOGEOM;
   cudaStream_t s = ctx->stream;
-  int nbk = ctx->nbk, k = ctx->k;
+  const int k = ctx->k;
   const double2* dens = reinterpret_cast<const double2*>(x);
   EB_TRY(ctx->za.ensure(sizeof(double2) * k));
   EB_TRY(ctx->pk.ensure(sizeof(double) * k));
@@ -474,7 +474,6 @@ int eb_stokes_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
 
 int eb_laplace_matvec_dev(eb_ctx* ctx, const double* x, double* y, int prec) {
   if (!ctx->geom_valid) return EB_ERR_NOGEOM;
-  cudaStream_t s = ctx->stream;
   // the Cauchy charges q = u dz h of FASMVP_LAP (laplace.f:190-200) are formed by the
   // FMM's charge kernel from u (EbPost::u)
   EbPost post{2, nullptr, x, nullptr, ctx->dz.as<double2>(), ctx->hpt.as<double>(),

@@ -41,9 +41,13 @@ __device__ __forceinline__ double bblock_sum(double v, double* red) {
   return red[32];
 }
 
+// A simulation's bounding box: (min x, max x, min y, max y).
+struct SimBox {
+  double x, y, z, w;
+};
+
 // Per-simulation bounding boxes (block per simulation over its node range).
-__global__ void k_sim_bbox(const int* __restrict__ node0, const double2* __restrict__ z, double4* __restrict__ box) {
-  __shared__ double red[33];
+__global__ void k_sim_bbox(const int* __restrict__ node0, const double2* __restrict__ z, SimBox* __restrict__ box) {
   const int s = blockIdx.x, i0 = node0[s], i1 = node0[s + 1];
   double mnx = INFINITY, mxx = -INFINITY, mny = INFINITY, mxy = -INFINITY;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
@@ -60,12 +64,12 @@ __global__ void k_sim_bbox(const int* __restrict__ node0, const double2* __restr
     mny = fmin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
     mxy = fmax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
   }
-  __shared__ double4 wb[32];
+  __shared__ SimBox wb[32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) wb[w] = make_double4(mnx, mxx, mny, mxy);
+  if (l == 0) wb[w] = SimBox{mnx, mxx, mny, mxy};
   __syncthreads();
   if (threadIdx.x == 0) {
-    double4 r = wb[0];
+    SimBox r = wb[0];
     for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
       r.x = fmin(r.x, wb[q].x);
       r.y = fmax(r.y, wb[q].y);
@@ -418,7 +422,7 @@ int eb_batch_install(eb_ctx* ctx) {
   EB_TRY(ctx->b_seg1.ensure(sizeof(int) * (S + 1)));
   EB_TRY(ctx->b_seg2.ensure(sizeof(int) * (S + 1)));
   EB_TRY(ctx->b_sim_of_node.ensure(sizeof(int) * nbk));
-  EB_TRY(ctx->b_box.ensure(sizeof(double4) * S));
+  EB_TRY(ctx->b_box.ensure(sizeof(SimBox) * S));
   EB_TRY(ctx->b_shift.ensure(sizeof(double2) * S));
   EB_TRY(ctx->zt.ensure(sizeof(double2) * nbk));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_sim_of_drop.p, sod.data(), sizeof(int) * k, cudaMemcpyHostToDevice, st));
@@ -428,13 +432,13 @@ int eb_batch_install(eb_ctx* ctx) {
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_seg1.p, node0.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_seg2.p, seg2.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_sim_of_node.p, sonode.data(), sizeof(int) * nbk, cudaMemcpyHostToDevice, st));
-  k_sim_bbox<<<S, 256, 0, st>>>(ctx->b_seg1.as<int>(), ctx->z.as<double2>(), ctx->b_box.as<double4>());
+  k_sim_bbox<<<S, 256, 0, st>>>(ctx->b_seg1.as<int>(), ctx->z.as<double2>(), ctx->b_box.as<SimBox>());
   eb_count_launch(ctx);
-  std::vector<double4> box(S);
-  EB_CUDA_TRY(cudaMemcpyAsync(box.data(), ctx->b_box.p, sizeof(double4) * S, cudaMemcpyDeviceToHost, st));
+  std::vector<SimBox> box(S);
+  EB_CUDA_TRY(cudaMemcpyAsync(box.data(), ctx->b_box.p, sizeof(SimBox) * S, cudaMemcpyDeviceToHost, st));
   EB_CUDA_TRY(cudaStreamSynchronize(st));
   double wc = 0.0;
-  for (const double4& b : box) {
+  for (const SimBox& b : box) {
     if (!std::isfinite(b.x) || !std::isfinite(b.y) || !std::isfinite(b.z) || !std::isfinite(b.w)) {
       eb_set_last_error_msg("non-finite node coordinate");
       return EB_ERR_NAN;

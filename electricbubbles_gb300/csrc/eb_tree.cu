@@ -1015,25 +1015,29 @@ int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_targ
                                    t.pt0.as<int>(), t.pt1.as<int>(), t.zs.as<double2>(), t.x0, t.y0, t.W,
                                    t.wdf.as<float4>(), t.wdf_lo.as<float2>());
   eb_count_launch(ctx);
-  // 11. pair counts (the algorithmic work of the near field, M2P and M2L), copied to the
-  // host without waiting; eb_tree_pairs reads them
-  EB_TRY(t.pairs.ensure(3 * sizeof(unsigned long long)));
-  unsigned long long* cnt = t.pairs.as<unsigned long long>();
-  EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
-  int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
-  k_pair_counts<<<std::max(nblk(nl, BS), 1), BS, 0, st>>>(nl, t.leaves.as<int>(), t.pt0.as<int>(), t.pt1.as<int>(),
-                                                         t.ustart.as<int>(), t.ulist.as<int>(), t.wstart.as<int>(),
-                                                         vfirst, vlast, t.vcount.as<int>(), cnt);
-  eb_count_launch(ctx);
-  EB_CUDA_TRY(cudaMemcpyAsync(H->pairs, cnt, sizeof(H->pairs), cudaMemcpyDeviceToHost, st));
   EB_TRY(eb_check_launch(ctx, "tree build"));
   t.valid = true;
   return EB_OK;
 }
 
+// Pair counts (the algorithmic work of the near field, M2P and M2L), counted on the
+// device when first asked for after a build (they are statistics, not inputs of any
+// apply, so the build does not spend a launch on them).
 int eb_tree_pairs(eb_ctx* ctx, EbTree& t) {
   if (!t.pairs_read) {
-    EB_CUDA_TRY(cudaStreamSynchronize(eb_stream(ctx)));
+    if (!t.valid) return EB_ERR_NOGEOM;
+    cudaStream_t st = eb_stream(ctx);
+    const int BS = 256, nl = t.nleaf, L = t.L;
+    EB_TRY(t.pairs.ensure(3 * sizeof(unsigned long long)));
+    unsigned long long* cnt = t.pairs.as<unsigned long long>();
+    EB_CUDA_TRY(cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), st));
+    int vfirst = t.lev_off[std::min(2, L + 1)], vlast = t.nbox;
+    k_pair_counts<<<std::max(nblk(nl, BS), 1), BS, 0, st>>>(nl, t.leaves.as<int>(), t.pt0.as<int>(),
+                                                           t.pt1.as<int>(), t.ustart.as<int>(), t.ulist.as<int>(),
+                                                           t.wstart.as<int>(), vfirst, vlast, t.vcount.as<int>(), cnt);
+    eb_count_launch(ctx);
+    EB_CUDA_TRY(cudaMemcpyAsync(t.host->pairs, cnt, sizeof(t.host->pairs), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaStreamSynchronize(st));
     t.u_pairs = (long long)t.host->pairs[0];
     t.v_pairs = (long long)t.host->pairs[1];
     t.w_pairs = (long long)t.host->pairs[2];
