@@ -78,7 +78,6 @@ __global__ void k_sim_bbox(const int* __restrict__ node0, const double2* __restr
     }
     box[s] = r;
   }
-  (void)red;
 }
 
 // Moves every node of simulation s by shift[s] (the simulation's cell of the forest).
