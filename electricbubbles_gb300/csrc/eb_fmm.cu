@@ -1684,7 +1684,8 @@ __global__ void k_reflect_df(int first, int nb, const unsigned long long* __rest
 //   z conj(Phi') + conj(Psi) = (z - z_j) conj(gamma1 t^2 + 2 gamma2 t^3)
 //                              + 2 conj(gamma2 t^2) + conj(delta1 t),
 // which has no terms of size |z|. One block per box of level ld (blocks off the wall
-// return at once); sources staged through shared memory.
+// return at once); sources staged through shared memory. sorted: add into dst in the
+// sorted order (the near-field buffer of the split passes), else in node order.
 #define IMG_TILE 128
 __global__ void __launch_bounds__(IMG_TILE) k_img_near(int off, int nb, int lev,
                                                        const unsigned long long* __restrict__ bkey,
@@ -1693,7 +1694,7 @@ __global__ void __launch_bounds__(IMG_TILE) k_img_near(int off, int nb, int lev,
                                                        const double2* __restrict__ dens,
                                                        const double2* __restrict__ dz,
                                                        const double* __restrict__ hpt, double s,
-                                                       double2* __restrict__ dst) {
+                                                       double2* __restrict__ dst, int sorted) {
   __shared__ double2 sz[IMG_TILE], sg1[IMG_TILE], sg2[IMG_TILE], sd1[IMG_TILE];
   const int b = off + blockIdx.x;
   const unsigned long long key = bkey[b];
@@ -1763,7 +1764,7 @@ __global__ void __launch_bounds__(IMG_TILE) k_img_near(int off, int nb, int lev,
       }
     }
     if (act) {
-      const int o = perm[i];
+      const int o = sorted ? i : perm[i];
       dst[o] = make_double2(dst[o].x + acc.x, dst[o].y + acc.y);
     }
   }
@@ -2122,6 +2123,13 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                            w.nearbuf.as<double2>());
     }
     eb_count_launch(ctx);
+    if (E == 2 && t.wall && dz) {  // the wall's reflected near field joins the near-field sums
+      const int ld = t.ld, nbl = t.lev_off[ld + 1] - t.lev_off[ld];
+      k_img_near<<<nbl, IMG_TILE, 0, ss>>>(t.lev_off[ld], nbl, ld, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
+                                           t.pt1.as<int>(), t.zs.as<double2>(), t.perm.as<int>(), dens, dz, hpt,
+                                           (double)sign, w.nearbuf.as<double2>(), 1);
+      eb_count_launch(ctx);
+    }
     EB_CUDA_TRY(cudaEventRecord(ctx->ev_p2p, ss));
   }
   if (has_far && df) EB_TRY(fmm_expansions_df<E>(ctx, t, tb, w));
@@ -2182,12 +2190,12 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
                                              w.mpole.as<float2>(), out, post, w.nearbuf.as<double2>());
   }
   eb_count_launch(ctx);
-  if (E == 2 && t.wall && dz) {  // the reflected near field, after the output is written
+  if (E == 2 && t.wall && dz && !split) {  // the reflected near field, after the output is written
     const int ld = t.ld, nb = t.lev_off[ld + 1] - t.lev_off[ld];
     double2* dst = post.kind == 1 ? reinterpret_cast<double2*>(post.y) : out;
     k_img_near<<<nb, IMG_TILE, 0, st>>>(t.lev_off[ld], nb, ld, t.bkey.as<unsigned long long>(), t.pt0.as<int>(),
                                         t.pt1.as<int>(), t.zs.as<double2>(), t.perm.as<int>(), dens, dz, hpt,
-                                        (double)sign, dst);
+                                        (double)sign, dst, 0);
     eb_count_launch(ctx);
   }
   ps.done();
