@@ -257,6 +257,23 @@ def run_gpu(args, rank, world, local):
         torch.cuda.synchronize()
         lap[mode + "_solves_per_s"] = world * args.steps / (ea0.elapsed_time(ea1) * 1e-3)
         lap[mode + "_info"] = linfo
+    # the same solves right-preconditioned by the deflation of each drop's constant
+    # density (eb_opts.lap_deflate): same system and stopping test, fewer iterations
+    ctx_ld = Context(device=local, graphs=graphs, lap_deflate=1)
+    ctx_ld.set_stream(stream.cuda_stream)
+    ctx_ld.extractdat(cfg.nd, cfg.rku())
+    for mode in ("fp64", "fp32_refined"):
+        for _ in range(args.warmup):
+            ctx_ld.solve_lapl(rl, mode, out=xl)
+        torch.cuda.synchronize()
+        ea0, ea1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea0.record(stream)
+        for _ in range(args.steps):
+            _, linfo = ctx_ld.solve_lapl(rl, mode, out=xl)
+        ea1.record(stream)
+        torch.cuda.synchronize()
+        lap["deflated_" + mode + "_solves_per_s"] = world * args.steps / (ea0.elapsed_time(ea1) * 1e-3)
+        lap["deflated_" + mode + "_info"] = linfo
 
     # wall-bounded flow (zbond != 0): 64 drops x 512 nodes above the wall y = 0, every
     # Stokes sum with the images across it; solves as above, and the operator with and
@@ -422,15 +439,16 @@ def run_gpu(args, rank, world, local):
 
     # RK2 steps (F twice: EXTRACTDAT, Laplace solve, DtN, SETVELF, Stokes solve,
     # INTERFACENEW, EQUIT/FILTER) with the state resident on the GPU
-    def rk_rate(c, mode, steps, e0=0.5):
+    def rk_rate(c, mode, steps, e0=0.5, cx=None):
+        cx = cx or ctx
         y0 = torch.from_numpy(c.rku()).to(dev)
         y = y0.clone()
-        ctx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
+        cx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
         torch.cuda.synchronize()
         e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0_.record(stream)
         for _ in range(steps):
-            info = ctx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
+            info = cx.rk2(c.nd, 1e-3, y, e0=e0, mode=mode)
         e1_.record(stream)
         torch.cuda.synchronize()
         return steps / (e0_.elapsed_time(e1_) * 1e-3), info
@@ -439,6 +457,8 @@ def run_gpu(args, rank, world, local):
     for mode in ("fp64", "fp32_refined"):
         r, info = rk_rate(cfg, mode, 3)
         rk[WORKLOAD + "/" + mode] = {"steps_per_s": r, "last_step": info}
+        r, info = rk_rate(cfg, mode, 3, cx=ctx_ld)
+        rk[WORKLOAD + "/" + mode + "/lap_deflate"] = {"steps_per_s": r, "last_step": info}
     single = configs.single_drop(256)
     for mode in ("fp64", "fp32_refined"):
         r, info = rk_rate(single, mode, 100)

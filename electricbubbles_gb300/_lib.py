@@ -36,7 +36,8 @@ class Opts(ctypes.Structure):
                 ("maxl", ctypes.c_int), ("gmres_tol", ctypes.c_double),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
                 ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int),
-                ("resid_df", ctypes.c_int), ("m2l_tc", ctypes.c_int)]
+                ("resid_df", ctypes.c_int), ("m2l_tc", ctypes.c_int),
+                ("lap_deflate", ctypes.c_int)]
 
 
 class TuneInfo(ctypes.Structure):

@@ -175,6 +175,7 @@ void eb_opts_default(eb_opts* o) {
   o->df64 = -1;
   o->resid_df = 1;
   o->m2l_tc = -1;
+  o->lap_deflate = -1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -206,6 +207,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.df64 == 0) o.df64 = d.df64;
     if (o.resid_df == 0) o.resid_df = d.resid_df;
     if (o.m2l_tc == 0) o.m2l_tc = d.m2l_tc;
+    if (o.lap_deflate == 0) o.lap_deflate = d.lap_deflate;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {

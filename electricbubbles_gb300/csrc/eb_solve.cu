@@ -1,6 +1,7 @@
 // GMRES on the GPU with the semantics of SLATEC DGMRES as SOLVEI / SOLVE_LAPL call it
 // (stokesbubb.f:330-350, laplace.f:361-382): x0 = rhs, MAXL Krylov vectors, no
-// restart, no preconditioner, stop when the Givens estimate of ||b - A x|| / ||b||
+// restart, no preconditioner (JPRE = 0; the deflated Laplace solve below is the one
+// option that adds one), stop when the Givens estimate of ||b - A x|| / ||b||
 // (DPIGMR's RHO, dpigmr.f:340-355) is at most TOL (ISDGMR with ITOL = 0).
 //
 // The Krylov basis, residuals and the solution update stay FP64 in HBM. The Arnoldi
@@ -17,6 +18,11 @@
 // until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual. Steps after
 // the first tighten the inner tolerance (to at most a tenth) when that is expected to
 // end the solve (inner_tolerance below).
+//
+// Deflated Laplace solve (eb_opts.lap_deflate): the same GMRES, both modes, on the
+// right-preconditioned operator A M^-1 in the variable t = M x (k_deflate below), from
+// t0 = M rhs; x = M^-1 t at the end. Its residual b - A M^-1 t is b - A x, so the
+// stopping test and the reported error are those of the unpreconditioned solve.
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
@@ -241,6 +247,58 @@ void dhels(const double* hes, int ldh, int ll, const double* q, double* b) {
     double t = -b[k];
     for (int r = 0; r < k; ++r) b[r] += t * hes[(size_t)k * ldh + r];
   }
+}
+
+// Deflation of each drop's constant density for the Laplace solve. FASMVP_LAP
+// (laplace.f:159-262) maps the constant 1 on drop k to -2 h_k s'_i on that drop and to
+// zero elsewhere (the double layer of a constant vanishes off its curve and cancels the
+// identity on it, leaving the -2 h u s' term of laplace.f:235-236), so with nodes
+// equispaced in arclength the k constants are eigenvectors with the small, distinct
+// eigenvalues mu_k = -2 h_k mean_k(s'), and unpreconditioned GMRES spends about one
+// iteration on each. With P_k the mean over drop k spread over its nodes,
+//   M^-1 = I + sum_k (1/mu_k - 1) P_k,   M = I + sum_k (mu_k - 1) P_k,
+// and A M^-1 maps those modes to about 1 while leaving vectors of zero drop means alone.
+// One block per drop: y = x + c_k mean_k(x) with c_k = 1/mu_k - 1 (inverse = 1, M^-1) or
+// mu_k - 1 (inverse = 0, M). y may alias x: every read of the drop precedes the writes.
+constexpr int DEFL_BS = 256;
+__global__ void __launch_bounds__(DEFL_BS) k_deflate(const int* __restrict__ start,
+                                                     const double* __restrict__ dsda, const double* x,
+                                                     double* y, int inverse) {
+  __shared__ double red[DEFL_BS / 32];
+  __shared__ double s_add;
+  const int b = blockIdx.x, i0 = start[b], i1 = start[b + 1];
+  double sx = 0.0, ss = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += DEFL_BS) {
+    sx += x[i];
+    ss += dsda[i];
+  }
+  sx = block_sum(sx, red);
+  ss = block_sum(ss, red);
+  if (threadIdx.x == 0) {
+    const int n = i1 - i0;
+    double a = 0.0;
+    if (n > 0) {
+      const double mu = -4.0 * EB_PI * ss / ((double)n * (double)n);  // -2 (2 pi / n) (ss / n)
+      if (mu < 0.0 && isfinite(mu)) a = (inverse ? 1.0 / mu - 1.0 : mu - 1.0) * (sx / n);
+    }
+    s_add = a;
+  }
+  __syncthreads();
+  const double a = s_add;
+  for (int i = i0 + threadIdx.x; i < i1; i += DEFL_BS) y[i] = x[i] + a;
+}
+
+int deflate(eb_ctx* ctx, const double* x, double* y, int inverse) {
+  k_deflate<<<ctx->k, DEFL_BS, 0, ctx->stream>>>(ctx->start.as<int>(), ctx->dsda.as<double>(), x, y, inverse);
+  eb_count_launch(ctx);
+  return EB_OK;
+}
+
+// y = A M^-1 x: the operator of the deflated Laplace solve
+int laplace_matvec_deflated(eb_ctx* ctx, const double* x, double* y, int prec) {
+  double* t = ctx->gDefl.as<double>();
+  EB_TRY(deflate(ctx, x, t, 1));
+  return eb_laplace_matvec_dev(ctx, t, y, prec);
 }
 
 // One GMRES cycle (DGMRES with NRMAX = 0). x holds x0 on entry unless x0_zero.
@@ -811,10 +869,21 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
   EB_TRY(ctx->gX.ensure(sizeof(double) * n));
   double* b = ctx->gR.as<double>();
   double* x = ctx->gX.as<double>();
-  // SOLVEI / SOLVE_LAPL: soln = rhs as the initial guess (stokesbubb.f:346-349).
+  const bool defl = op == eb_laplace_matvec_dev && ctx->opts.lap_deflate > 0;
+  if (defl) {
+    EB_TRY(ctx->gDefl.ensure(sizeof(double) * n));
+    op = laplace_matvec_deflated;
+  }
+  // SOLVEI / SOLVE_LAPL: soln = rhs as the initial guess (stokesbubb.f:346-349); the
+  // deflated solve starts from t0 = M rhs, which is x0 = rhs.
   cudaMemcpyKind kin = mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  auto init_x = [&]() -> int {
+    EB_CUDA_TRY(cudaMemcpyAsync(x, rhs, sizeof(double) * n, kin, s));
+    if (defl) EB_TRY(deflate(ctx, x, x, 0));
+    return EB_OK;
+  };
   EB_CUDA_TRY(cudaMemcpyAsync(b, rhs, sizeof(double) * n, kin, s));
-  EB_CUDA_TRY(cudaMemcpyAsync(x, rhs, sizeof(double) * n, kin, s));
+  EB_TRY(init_x());
   eb_solve_info inf{};
   int st = EB_OK;
   bool eager = true;
@@ -825,7 +894,7 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
       ctx->opts.graphs = -1;
       inf = eb_solve_info{};
       st = EB_OK;
-      EB_CUDA_TRY(cudaMemcpyAsync(x, rhs, sizeof(double) * n, kin, s));
+      EB_TRY(init_x());
     } else {
       inf.graph = 1;
       eager = false;
@@ -882,6 +951,7 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
     }
   }
   if (st == EB_OK) {
+    if (defl) EB_TRY(deflate(ctx, x, x, 1));  // x = M^-1 t
     cudaMemcpyKind kout = mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     EB_CUDA_TRY(cudaMemcpyAsync(soln, x, sizeof(double) * n, kout, s));
     EB_CUDA_TRY(cudaStreamSynchronize(s));

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define EB_GB300_VERSION 3
+#define EB_GB300_VERSION 4
 
 /* Status codes. The reference prints and STOPs on FMM/GMRES errors
  * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
@@ -77,6 +77,12 @@ typedef struct eb_opts {
                        arithmetic: 0 default (on), 1 on, -1 off (native FP64)   */
   int m2l_tc;       /* FP32 M2L (order 20) as a 3xTF32 contraction on the tensor
                        cores (tcgen05): 0 default (off), 1 on, -1 off          */
+  int lap_deflate;  /* Laplace solves: GMRES right-preconditioned by the deflation of
+                       each drop's constant density, an eigenvector of FASMVP_LAP with
+                       eigenvalue -2 h mean(s'); same stopping test on ||b - A x||, far
+                       fewer iterations with many drops. 0 default (off: DGMRES as the
+                       reference runs it), 1 on, -1 off. Not applied to a batch of
+                       simulations or to the adjoint solve. */
 } eb_opts;
 
 typedef struct eb_solve_info {
@@ -231,7 +237,10 @@ int eb_cauchy_sum(eb_ctx* ctx, int n, const double* z, const double* q, double* 
 
 /* GMRES solves with the settings of SOLVEI (stokesbubb.f:294-415) and SOLVE_LAPL
  * (laplace.f:335-425): x0 = rhs, MAXL Krylov vectors, no restart, stop when
- * ||b - A x|| / ||b|| <= gmres_tol (DGMRES ITOL = 0). soln receives the solution. */
+ * ||b - A x|| / ||b|| <= gmres_tol (DGMRES ITOL = 0). soln receives the solution.
+ * With eb_opts.lap_deflate on, eb_laplace_solve runs the same GMRES on A M^-1 t = b,
+ * x = M^-1 t, with M^-1 = I + sum_k (1/mu_k - 1) P_k (P_k: the mean over drop k spread
+ * over its nodes, mu_k = -2 h_k mean_k(s')); t0 = M rhs, so x0 = rhs still. */
 int eb_stokes_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
                     eb_solve_info* info, int mem);
 int eb_laplace_solve(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,

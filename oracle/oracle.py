@@ -345,6 +345,34 @@ def gmres(matvec, b, x0, maxl=100, tol=1e-10):
     return x, {"iters": it.value, "err": err.value, "ierr": ierr}
 
 
+def deflate(nd, dsda, x, inverse):
+    """The per-drop deflation of the Laplace solve's right preconditioner: with P_k the
+    mean over drop k spread over its nodes and mu_k = -2 h_k mean_k(s') (FASMVP_LAP's
+    eigenvalue on the drop's constant, from its -2 h u s' term, laplace.f:235-236),
+    M^-1 x = x + sum_k (1/mu_k - 1) P_k x (inverse) or M x = x + sum_k (mu_k - 1) P_k x.
+    No counterpart in the reference (DGMRES runs with JPRE = 0); this checks the CUDA
+    path's eb_opts.lap_deflate."""
+    x = _r(x)
+    dsda = _r(dsda)
+    y = x.copy()
+    off = 0
+    for n in np.asarray(nd, dtype=np.int64):
+        s = slice(off, off + int(n))
+        mu = -2.0 * (2.0 * np.pi / n) * dsda[s].mean()
+        c = 1.0 / mu - 1.0 if inverse else mu - 1.0
+        y[s] += c * x[s].mean()
+        off += int(n)
+    return y
+
+
+def solve_lapl_deflated(g, rhs, nthreads=0, maxl=100, tol=1e-10, mode=0):
+    """SOLVE_LAPL's GMRES on A M^-1 t = rhs from t0 = M rhs; returns x = M^-1 t."""
+    t0 = deflate(g.nd, g.dsda, rhs, False)
+    t, info = gmres(lambda t: fasmvp_lap(g, deflate(g.nd, g.dsda, t, True), nthreads, mode), rhs, t0, maxl,
+                    tol)
+    return deflate(g.nd, g.dsda, t, True), info
+
+
 def solvei(g, rhs, mode=0, nthreads=0, maxl=100, tol=1e-10):
     return gmres(lambda x: fasmvp(g, x, mode, nthreads), rhs, rhs, maxl, tol)
 
