@@ -72,7 +72,7 @@ def test_laplace_check_exterior_potential(oracle):
     solve on the unit circle equals Re(z*)/|z*|^2.
 
     The double-layer part of FASMVP_LAP satisfies it to rounding. The full operator
-    also subtracts 2 h s'_i u_i on the diagonal (laplace.f:240-241, where the older
+    also subtracts 2 h s'_i u_i on the diagonal (laplace.f:235-236, where the older
     DIRECT_MATVEC subtracted the rank-one 2 sum_j h s'_j u_j / (2 pi)); that term is
     O(h), so with it the answer converges to the closed form at first order in 1/n."""
     from electricbubbles_gb300 import configs
