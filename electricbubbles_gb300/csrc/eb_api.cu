@@ -259,6 +259,7 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->ev_near1) cudaEventDestroy(ctx->ev_near1);
   for (GmGraph& g : ctx->gcache) g.destroy();
   if (ctx->b_host_act) cudaFreeHost(ctx->b_host_act);
+  if (ctx->h_flux) cudaFreeHost(ctx->h_flux);
   for (GmGraph& g : ctx->bgraph) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);

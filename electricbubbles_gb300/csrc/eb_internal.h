@@ -269,6 +269,7 @@ struct eb_ctx {
   DevBuf b_G, b_CS, b_ctl, b_misc; // batched GMRES state
   DevBuf b_st1, b_st2, b_flag;     // GETFOURIER / DOUBLE: drop starts and flags
   int* b_host_act = nullptr;       // page-locked counters read back per cycle
+  double* h_flux = nullptr;        // page-locked: an RK stage's FLUX, read after the step's synchronisation
   GmGraph bgraph[2];               // batched GMRES cycles as graphs (plain, refinement inner)
 };
 

@@ -954,7 +954,8 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
     if (defl) EB_TRY(deflate(ctx, x, x, 1));  // x = M^-1 t
     cudaMemcpyKind kout = mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     EB_CUDA_TRY(cudaMemcpyAsync(soln, x, sizeof(double) * n, kout, s));
-    EB_CUDA_TRY(cudaStreamSynchronize(s));
+    // the info is already on the host; a device solution is ready in stream order
+    if (mem == EB_HOST) EB_CUDA_TRY(cudaStreamSynchronize(s));
   }
   if (info) *info = inf;
   return st;

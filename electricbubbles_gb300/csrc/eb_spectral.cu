@@ -507,7 +507,7 @@ int eb_extractdat(eb_ctx* ctx, int k, const int* nd, const double* rku, double* 
   if (ckern) EB_CUDA_TRY(cudaMemcpyAsync(ckern, ctx->ckern.p, sizeof(double2) * nbk, ko, s));
   if (tha) EB_CUDA_TRY(cudaMemcpyAsync(tha, ctx->tha.p, sizeof(double) * nbk, ko, s));
   if (area) EB_CUDA_TRY(cudaMemcpyAsync(area, area_d.p, sizeof(double) * k, ko, s));
-  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (mem == EB_HOST) EB_CUDA_TRY(cudaStreamSynchronize(s));
   ctx->ckern_valid = true;
   return EB_OK;
 }
@@ -664,7 +664,7 @@ static int dirich_neu_map_impl(eb_ctx* ctx, const double* u, double* phi, double
   if (phi) EB_CUDA_TRY(cudaMemcpyAsync(phi, phd, sizeof(double) * nbk, ko, s));
   if (psi) EB_CUDA_TRY(cudaMemcpyAsync(psi, psd, sizeof(double) * nbk, ko, s));
   EB_CUDA_TRY(cudaMemcpyAsync(dphi_dn, dpd, sizeof(double) * nbk, ko, s));
-  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (mem == EB_HOST) EB_CUDA_TRY(cudaStreamSynchronize(s));
   return EB_OK;
 }
 
@@ -678,9 +678,12 @@ int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, do
   return dirich_neu_map_impl(ctx, u, phi, psi, dphi_dn, prec, mem);
 }
 
-// INTERFACENEW with any internal precision (EB_FP64, EB_FP32 or EB_PREC_DF)
+// INTERFACENEW with any internal precision (EB_FP64, EB_FP32 or EB_PREC_DF). zc_any: 1 if
+// some C_k is nonzero, 0 if all are, -1 to look (device zc: one readback). flux_async:
+// FLUX goes to ctx->h_flux without a synchronisation (the caller reads it after its own).
 static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
-                                   double* flux, int prec, int mem) {
+                                   double* flux, int prec, int mem, int zc_any = -1,
+                                   bool flux_async = false) {
   int nbk = ctx->nbk, k = ctx->k;
   cudaStream_t s = ctx->stream;
   EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
@@ -694,13 +697,23 @@ static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* z
     EB_CUDA_TRY(cudaMemcpyAsync(ctx->vin.p, u, sizeof(double2) * nbk, cudaMemcpyHostToDevice, s));
     ud = ctx->vin.as<double2>();
   }
-  std::vector<double> zch(2 * (size_t)k);
-  EB_CUDA_TRY(cudaMemcpyAsync(zch.data(), zc, sizeof(double2) * k,
-                              mem == EB_HOST ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, s));
-  EB_CUDA_TRY(cudaStreamSynchronize(s));
-  int any_zc = 0;
-  for (double v : zch) if (v != 0.0) any_zc = 1;
-  EB_CUDA_TRY(cudaMemcpyAsync(ctx->za.p, zch.data(), sizeof(double2) * k, cudaMemcpyHostToDevice, s));
+  int any_zc = zc_any;
+  if (mem == EB_HOST) {
+    if (any_zc < 0) {
+      any_zc = 0;
+      for (size_t i = 0; i < 2 * (size_t)k; ++i) if (zc[i] != 0.0) any_zc = 1;
+    }
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->za.p, zc, sizeof(double2) * k, cudaMemcpyHostToDevice, s));
+  } else {
+    if (any_zc < 0) {
+      std::vector<double> zch(2 * (size_t)k);
+      EB_CUDA_TRY(cudaMemcpyAsync(zch.data(), zc, sizeof(double2) * k, cudaMemcpyDeviceToHost, s));
+      EB_CUDA_TRY(cudaStreamSynchronize(s));
+      any_zc = 0;
+      for (double v : zch) if (v != 0.0) any_zc = 1;
+    }
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->za.p, zc, sizeof(double2) * k, cudaMemcpyDeviceToDevice, s));
+  }
   EB_TRY(fdiff_dev(ctx, ud, ctx->vtmp.as<double2>()));
   EB_TRY(eb_stokes_sum_dev(ctx, ud, +1, ctx->vtmp2.as<double2>(), prec));
   int nbv = std::min(nblk(nbk, 256), 2048);
@@ -715,6 +728,12 @@ static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* z
   eb_count_launch(ctx);
   EB_TRY(eb_check_launch(ctx, "interface velocity"));
   if (mem == EB_HOST) EB_CUDA_TRY(cudaMemcpyAsync(un, und, sizeof(double) * nbk, cudaMemcpyDeviceToHost, s));
+  if (flux_async) {
+    if (!ctx->h_flux) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&ctx->h_flux), sizeof(double)));
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->h_flux, ctx->redpart.as<double>() + 2047, sizeof(double),
+                                cudaMemcpyDeviceToHost, s));
+    return EB_OK;
+  }
   double fl = 0.0;
   EB_CUDA_TRY(cudaMemcpyAsync(&fl, ctx->redpart.as<double>() + 2047, sizeof(double), cudaMemcpyDeviceToHost, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1059,9 +1078,11 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
                          EB_DEVICE));
   double* un = rl;  // the Laplace right-hand side is no longer needed
-  double flux = 0.0;
-  EB_TRY(interface_velocity_impl(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, &flux,
-                                 p64, EB_DEVICE));
+  // C_k is nonzero exactly in wall mode; FLUX is read by the caller after its
+  // synchronisation (the stage itself waits on the host only inside the tree builds
+  // and the solves)
+  EB_TRY(interface_velocity_impl(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, nullptr,
+                                 p64, EB_DEVICE, wall ? 1 : 0, true));
   size_t sm2 = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax / 2);
   EB_TRY(set_smem((const void*)k_equit_rkup, sm2));
   k_equit_rkup<<<k, SBS, sm2, s>>>(ctx->start.as<int>(), ctx->tha.as<double>(), un, ctx->dz.as<double2>(),
@@ -1073,7 +1094,6 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
     info->stokes_iters += si.iters;
     info->lap_err = li.err;
     info->stokes_err = si.err;
-    info->flux = flux;
     info->lap_ierr = li.ierr;
     info->stokes_ierr = si.ierr;
   }
@@ -1131,13 +1151,17 @@ int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   for (int b = 0; b < k; ++b) nbk += nd[b];
   cudaStream_t s = ctx->stream;
   if (info) *info = eb_stage_info{};
-  if (mem == EB_DEVICE) return stage_f(ctx, k, nd, rku, rkup, model, info);
-  EB_TRY(ctx->rk_y.ensure(sizeof(double) * 2 * (size_t)nbk));
-  EB_TRY(ctx->rk_d0.ensure(sizeof(double) * 2 * (size_t)nbk));
-  EB_CUDA_TRY(cudaMemcpyAsync(ctx->rk_y.p, rku, sizeof(double) * 2 * nbk, cudaMemcpyHostToDevice, s));
-  EB_TRY(stage_f(ctx, k, nd, ctx->rk_y.as<double>(), ctx->rk_d0.as<double>(), model, info));
-  EB_CUDA_TRY(cudaMemcpyAsync(rkup, ctx->rk_d0.p, sizeof(double) * 2 * nbk, cudaMemcpyDeviceToHost, s));
+  if (mem == EB_DEVICE) {
+    EB_TRY(stage_f(ctx, k, nd, rku, rkup, model, info));
+  } else {
+    EB_TRY(ctx->rk_y.ensure(sizeof(double) * 2 * (size_t)nbk));
+    EB_TRY(ctx->rk_d0.ensure(sizeof(double) * 2 * (size_t)nbk));
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->rk_y.p, rku, sizeof(double) * 2 * nbk, cudaMemcpyHostToDevice, s));
+    EB_TRY(stage_f(ctx, k, nd, ctx->rk_y.as<double>(), ctx->rk_d0.as<double>(), model, info));
+    EB_CUDA_TRY(cudaMemcpyAsync(rkup, ctx->rk_d0.p, sizeof(double) * 2 * nbk, cudaMemcpyDeviceToHost, s));
+  }
   EB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (info) info->flux = *ctx->h_flux;
   return EB_OK;
 }
 
@@ -1170,5 +1194,6 @@ int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar, cons
   EB_CUDA_TRY(cudaMemcpyAsync(ybar, y, sizeof(double) * neq,
                               mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (info) info->flux = *ctx->h_flux;  // the second stage's
   return EB_OK;
 }

@@ -14,7 +14,11 @@
  *  - Nodes of k drops are concatenated in drop order (nd[0] nodes of drop 0, ...).
  *  - `mem` says whether the array arguments are host (EB_HOST) or device
  *    (EB_DEVICE, allocated on the context's GPU) pointers. Host calls copy in,
- *    compute, copy out, and return when the result is in host memory.
+ *    compute, copy out, and return when the result is in host memory. Device calls
+ *    return once their work is enqueued on the context's stream (waiting on the host
+ *    only where sizes or loop decisions need it: tree builds, GMRES steps); a device
+ *    result is ready in that stream's order (eb_ctx_sync waits for it). The RK calls
+ *    (eb_rk_f, eb_rk2_step) return with their stage info, so after the stream's work.
  *  - Every function returns an eb_status; the library never calls exit().
  *    eb_last_error() describes the last failure of the calling thread.
  */
