@@ -17,7 +17,10 @@
 //   solve A32 d = r to inner_tol with the same GMRES;  x += d;  r = b - A64 x,
 // until ||r|| / ||b|| <= TOL; the reported error is the true FP64 residual. Steps after
 // the first tighten the inner tolerance (to at most a tenth) when that is expected to
-// end the solve (inner_tolerance below).
+// end the solve (inner_tolerance below). The inner cycle orthogonalises with one
+// Gram-Schmidt pass (its tolerance is far above the loss of orthogonality) and takes
+// the new vector's norm by Pythagoras, ||w - V h||^2 = w.w - h.h, from the reduction
+// that forms h = V^T w, so that a step is the apply, one reduction and one update.
 //
 // Deflated Laplace solve (eb_opts.lap_deflate): the same GMRES, both modes, on the
 // right-preconditioned operator A M^-1 in the variable t = M x (k_deflate below), from
@@ -75,24 +78,65 @@ __device__ bool finish_columns(int nb, int ncol, const double* part, double* out
   return true;
 }
 
-// out[j] = V[:, j] . w for j < ncol. Each block takes a contiguous range of rows and
-// each of its warps a subset of the columns; partial sums per block go to `part` and
-// the last block to finish adds them in block order.
-__global__ void k_vtw(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
-                      size_t ldv, const double* __restrict__ w, double* __restrict__ part,
-                      double* __restrict__ out, unsigned int* __restrict__ ticket) {
-  if (ncol_dev) ncol = *ncol_dev;
+// The block's partial sums of V[:, j] . w for j < ncol, and with with_w of w . w as
+// column ncol, into part[blockIdx.x * (ncol + with_w) + j]. Each block takes a
+// contiguous range of rows and each of its warps a subset of the columns.
+__device__ __forceinline__ void vtw_partials(int n, int ncol, int with_w, const double* __restrict__ V,
+                                             size_t ldv, const double* __restrict__ w,
+                                             double* __restrict__ part) {
+  const int nc = ncol + with_w;
   const int rows = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int j = wi; j < ncol; j += nw) {
-    const double* v = V + (size_t)j * ldv;
+  for (int j = wi; j < nc; j += nw) {
+    const double* v = j < ncol ? V + (size_t)j * ldv : w;
     double s = 0.0;
     for (int i = r0 + lane; i < r1; i += 32) s = fma(v[i], w[i], s);
     s = warp_sum<double>(s);
-    if (lane == 0) part[(size_t)blockIdx.x * ncol + j] = s;
+    if (lane == 0) part[(size_t)blockIdx.x * nc + j] = s;
   }
-  finish_columns(gridDim.x, ncol, part, out, ticket);
+}
+
+// out[j] = V[:, j] . w for j < ncol (and out[ncol] = w . w with with_w); partial sums
+// per block go to `part` and the last block to finish adds them in block order.
+__global__ void k_vtw(int n, int ncol, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                      size_t ldv, const double* __restrict__ w, double* __restrict__ part,
+                      double* __restrict__ out, unsigned int* __restrict__ ticket, int with_w = 0) {
+  if (ncol_dev) ncol = *ncol_dev;
+  vtw_partials(n, ncol, with_w, V, ldv, w, part);
+  finish_columns(gridDim.x, ncol + with_w, part, out, ticket);
+}
+
+// Norm of the new Arnoldi vector w - V h of one Gram-Schmidt pass, from h = V^T w and
+// s = w . w (Pythagoras, V orthonormal): ||w - V h||^2 = s - sum h_i^2. The same
+// explicit fma sequence on the host and the device. With the difference at most 1e-12 s
+// (the new direction is lost in rounding) the vector counts as zero: the Krylov space
+// is invariant to working precision (DPIGMR's SNORMW = 0).
+__host__ __device__ inline double pyth_norm2(const double* h, int ncol, double s) {
+  double t = s;
+  for (int i = 0; i < ncol; ++i) t = fma(-h[i], h[i], t);
+  return t > 1e-12 * s ? t : 0.0;
+}
+
+// dst = (w - V[:, 0:ncol] h) * scale, and xin = the same when xin != nullptr (dst may be w).
+__device__ __forceinline__ void sub_scale_store(int n, int ncol, const double* __restrict__ V, size_t ldv,
+                                                const double* __restrict__ h, const double* w, double scale,
+                                                double* dst, double* __restrict__ xin) {
+  __shared__ double hs[128];
+  for (int j = threadIdx.x; j < ncol; j += blockDim.x) hs[j] = h[j];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < ncol; ++j) acc = fma(V[(size_t)j * ldv + i], hs[j], acc);
+    const double v = (w[i] - acc) * scale;
+    dst[i] = v;
+    if (xin) xin[i] = v;
+  }
+}
+
+__global__ void k_sub_scale(int n, int ncol, const double* __restrict__ V, size_t ldv,
+                            const double* __restrict__ h, double* w, double scale) {
+  sub_scale_store(n, ncol, V, ldv, h, w, scale, w, nullptr);
 }
 
 // Pass-1 update fused with the pass-2 projection of classical Gram-Schmidt: each block
@@ -371,24 +415,29 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     double* w = V + (size_t)ll * ldv;
     EB_TRY(op(ctx, V + (size_t)(ll - 1) * ldv, w, prec));
     (*nmv)++;
-    // pass 1: h1 = V^T w; w -= V h1
-    k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket);
+    double* col = hes.data() + (size_t)(ll - 1) * ldh;
+    double snormw;
     if (cgs2) {
-      // w -= V h1; pass 2: h2 = V^T w; w -= V h2 with ||w||^2
+      // pass 1: h1 = V^T w; w -= V h1; pass 2: h2 = V^T w; w -= V h2 with ||w||^2
+      k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket);
       k_update_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + (maxl + 2), g.ticket);
       k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev + (maxl + 2), w, part,
                                         hdev + 2 * (maxl + 2), g.ticket);
+      ctx->launches += 3;
+      EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
+                                  cudaMemcpyDeviceToHost, g.s));
+      EB_CUDA_TRY(cudaStreamSynchronize(g.s));
+      for (int i = 0; i < ll; ++i) col[i] = hbuf[i] + hbuf[(maxl + 2) + i];
+      snormw = std::sqrt(std::max(hbuf[2 * (maxl + 2)], 0.0));
     } else {
-      k_gemv_sub<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, hdev, w, part, hdev + 2 * (maxl + 2),
-                                        g.ticket);
+      // one pass: h = V^T w and w . w; the update waits for the decision below
+      k_vtw<<<g.nb, RBS, 0, g.s>>>(n, ll, nullptr, V, ldv, w, part, hdev, g.ticket, 1);
+      eb_count_launch(ctx);
+      EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * (ll + 1), cudaMemcpyDeviceToHost, g.s));
+      EB_CUDA_TRY(cudaStreamSynchronize(g.s));
+      for (int i = 0; i < ll; ++i) col[i] = hbuf[i];
+      snormw = std::sqrt(pyth_norm2(hbuf.data(), ll, hbuf[ll]));
     }
-    ctx->launches += cgs2 ? 3 : 2;
-    EB_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), hdev, sizeof(double) * 3 * (maxl + 2),
-                                cudaMemcpyDeviceToHost, g.s));
-    EB_CUDA_TRY(cudaStreamSynchronize(g.s));
-    double* col = hes.data() + (size_t)(ll - 1) * ldh;
-    for (int i = 0; i < ll; ++i) col[i] = hbuf[i] + (cgs2 ? hbuf[(maxl + 2) + i] : 0.0);
-    double snormw = std::sqrt(std::max(hbuf[2 * (maxl + 2)], 0.0));
     col[ll] = snormw;
     if (!std::isfinite(snormw)) {
       eb_set_last_error_msg("non-finite Arnoldi vector");
@@ -402,7 +451,11 @@ int gmres_cycle(Gm& g, op_fn op, int prec, const double* b, double* x, bool x0_z
     if (*err <= tol) { iflag = 0; break; }
     if (ll == maxl) break;
     if (snormw == 0.0) { iflag = 2; break; }
-    k_scale<<<g.nb, RBS, 0, g.s>>>(n, 1.0 / snormw, w);
+    if (cgs2) {
+      k_scale<<<g.nb, RBS, 0, g.s>>>(n, 1.0 / snormw, w);
+    } else {
+      k_sub_scale<<<g.nb, RBS, 0, g.s>>>(n, ll, V, ldv, hdev, w, 1.0 / snormw);
+    }
     eb_count_launch(ctx);
   }
   if (iflag != 0 && iflag != 2) iflag = (rho < r0nrm) ? 1 : 2;
@@ -555,6 +608,31 @@ __global__ void k_gm_sub_arnoldi(int n, const int* __restrict__ ncol_dev, const 
   if (threadIdx.x < 32) gm_arnoldi_warp(c, hdev, h);
 }
 
+// One-pass Arnoldi step of the refined inner cycle: h = V^T w and w . w in one
+// reduction; the last block forms the norm of w - V h by Pythagoras (pyth_norm2) and
+// ends the step with its first warp. k_gm_sub_store then forms the new column.
+__global__ void k_gm_vtw_arnoldi(int n, const int* __restrict__ ncol_dev, const double* __restrict__ V,
+                                 size_t ldv, const double* __restrict__ w, double* __restrict__ part,
+                                 double* hdev, unsigned int* __restrict__ ticket, GmCtl* c,
+                                 cudaGraphConditionalHandle h) {
+  const int ncol = *ncol_dev;
+  vtw_partials(n, ncol, 1, V, ldv, w, part);
+  if (!finish_columns(gridDim.x, ncol + 1, part, hdev + GM_H1, ticket)) return;
+  __syncthreads();
+  if (threadIdx.x == 0) hdev[GM_NW] = pyth_norm2(hdev + GM_H1, ncol, hdev[GM_H1 + ncol]);
+  __syncthreads();
+  if (threadIdx.x < 32) gm_arnoldi_warp(c, hdev, h);
+}
+
+// V[:, store_col] = xin = (w - V[:, 0:store_col] h) * scale while the iteration continues
+__global__ void k_gm_sub_store(int n, const GmCtl* __restrict__ c, double* V, size_t ldv,
+                               const double* __restrict__ h, const double* __restrict__ w,
+                               double* __restrict__ xin) {
+  if (!c->cont) return;
+  const int col = c->store_col;  // columns 0..col-1 are read, column col written
+  sub_scale_store(n, col, V, ldv, h, w, c->scale, V + (size_t)col * ldv, xin);
+}
+
 // DHELS (dhels.f:77-96) on the device: y = R^-1 Q^T (r0nrm e1), into ydev.
 __global__ void k_gm_finish(GmCtl* c, double* __restrict__ ydev) {
   __shared__ double y[EB_GM_MAXL + 1];
@@ -685,16 +763,18 @@ int build_graph(eb_ctx* ctx, GmGraph& G, int kind, op_fn op, int n, int maxl) {
   cst = eb_capture_into(ctx, body, nullptr, 0, nullptr, &G.n_body, &body_lost, [&]() -> int {
     cudaStream_t s = ctx->stream;
     EB_TRY(op(ctx, xin, wbuf, prec));
-    k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
     if (refine) {
-      // one Gram-Schmidt pass for the inner FP32 cycle (the H2 slots stay zero)
-      k_gm_sub_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev, ticket, ctl, h);
+      // one Gram-Schmidt pass for the inner FP32 cycle (the H2 slots stay zero), its
+      // norm by Pythagoras from the same reduction, the update fused with the store
+      k_gm_vtw_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, wbuf, part, hdev, ticket, ctl, h);
+      k_gm_sub_store<<<nb, RBS, 0, s>>>(n, ctl, V, ldv, hdev + GM_H1, wbuf, xin);
     } else {
+      k_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, wbuf, part, hdev + GM_H1, ticket);
       k_update_vtw<<<nb, RBS, 0, s>>>(n, 0, lld, V, ldv, hdev + GM_H1, wbuf, part, hdev + GM_H2, ticket);
       k_gm_sub_arnoldi<<<nb, RBS, 0, s>>>(n, lld, V, ldv, hdev + GM_H2, wbuf, part, hdev, ticket, ctl, h);
+      k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
     }
-    k_gm_store<<<nb, RBS, 0, s>>>(n, ctl, wbuf, V, ldv, xin);
-    ctx->launches += refine ? 3 : 4;
+    ctx->launches += refine ? 2 : 4;
     return eb_check_launch(ctx, "gmres graph (body)");
   });
   if (body_lost) lost = true;  // the body belongs to the graph; leave the whole graph alone
