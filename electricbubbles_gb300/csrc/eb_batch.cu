@@ -148,49 +148,83 @@ __global__ void k_bg_init(const int* __restrict__ seg, const double* __restrict_
   }
 }
 
-// One Arnoldi step j for every active simulation: classical Gram-Schmidt applied twice
-// on w = A V[:, j] against V[:, 0..j] within the simulation's segment, the new column
-// of the Hessenberg matrix, DHEQR's Givens update (dheqr.f:82-176) and the stopping
-// test on |g_(j+1)| (DPIGMR's RHO, dpigmr.f:340-355). nact counts the simulations still
-// active after the step.
+// One Arnoldi step j for every active simulation: classical Gram-Schmidt on
+// w = A V[:, j] against V[:, 0..j] within the simulation's segment, the new column of
+// the Hessenberg matrix, DHEQR's Givens update (dheqr.f:82-176) and the stopping test on
+// |g_(j+1)| (DPIGMR's RHO, dpigmr.f:340-355). nact counts the simulations still active
+// after the step. Two passes for the FP64 cycle; for the inner FP32 cycle of refinement
+// (one_pass) a single pass whose norm comes by Pythagoras from the same sweep,
+// ||w - V h||^2 = w.w - h.h (within 1e-12 of w.w the vector counts as zero), and one
+// sweep that forms and normalises the new column.
 __global__ void __launch_bounds__(BBS) k_bg_arnoldi(const int* __restrict__ jdev, const int* __restrict__ seg,
                                                     double* __restrict__ V, size_t ldv, double* __restrict__ w,
                                                     BCtl* __restrict__ ctl, double* __restrict__ Hh,
                                                     double* __restrict__ G, double* __restrict__ CS, int maxl,
-                                                    int* __restrict__ nact) {
+                                                    int* __restrict__ nact, int one_pass) {
   const int j = *jdev;
   __shared__ double red[33];
   __shared__ double h1[EB_GM_MAXL + 2];
   __shared__ double h2[EB_GM_MAXL + 2];
+  __shared__ double s_hn;
   const int s = blockIdx.x;
   BCtl& c = ctl[s];
   if (!c.active) return;
   const int i0 = seg[s], i1 = seg[s + 1];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  double* hp[2] = {h1, h2};
-  for (int pass = 0; pass < 2; ++pass) {
-    double* h = hp[pass];
-    for (int q = wi; q <= j; q += nw) {
-      const double* v = V + (size_t)q * ldv;
+  double* vn = V + (size_t)(j + 1) * ldv;
+  double hn;
+  if (one_pass) {
+    for (int q = wi; q <= j + 1; q += nw) {  // column j + 1: w . w
+      const double* v = q <= j ? V + (size_t)q * ldv : w;
       double acc = 0.0;
       for (int i = i0 + lane; i < i1; i += 32) acc = fma(v[i], w[i], acc);
       acc = warp_sum<double>(acc);
-      if (lane == 0) h[q] = acc;
+      if (lane == 0) h1[q] = acc;
     }
     __syncthreads();
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      double acc = 0.0;
-      for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h[q], acc);
-      w[i] -= acc;
+    if (threadIdx.x == 0) {
+      const double ww = h1[j + 1];
+      double t = ww;
+      for (int q = 0; q <= j; ++q) {
+        t = fma(-h1[q], h1[q], t);
+        h2[q] = 0.0;
+      }
+      s_hn = t > 1e-12 * ww ? sqrt(t) : 0.0;
     }
     __syncthreads();
+    hn = s_hn;
+    if (hn > 0.0) {
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        double acc = 0.0;
+        for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h1[q], acc);
+        vn[i] = (w[i] - acc) / hn;
+      }
+    }
+  } else {
+    double* hp[2] = {h1, h2};
+    for (int pass = 0; pass < 2; ++pass) {
+      double* h = hp[pass];
+      for (int q = wi; q <= j; q += nw) {
+        const double* v = V + (size_t)q * ldv;
+        double acc = 0.0;
+        for (int i = i0 + lane; i < i1; i += 32) acc = fma(v[i], w[i], acc);
+        acc = warp_sum<double>(acc);
+        if (lane == 0) h[q] = acc;
+      }
+      __syncthreads();
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        double acc = 0.0;
+        for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h[q], acc);
+        w[i] -= acc;
+      }
+      __syncthreads();
+    }
+    double nn = 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) nn = fma(w[i], w[i], nn);
+    hn = sqrt(bblock_sum(nn, red));
+    if (hn > 0.0)
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] / hn;
   }
-  double nn = 0.0;
-  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) nn = fma(w[i], w[i], nn);
-  const double hn = sqrt(bblock_sum(nn, red));
-  double* vn = V + (size_t)(j + 1) * ldv;
-  if (hn > 0.0)
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] / hn;
   if (threadIdx.x == 0) {
     double* H = Hh + (size_t)s * (maxl + 1) * maxl;  // column-major, ld maxl + 1
     double* g = G + (size_t)s * (maxl + 1);
@@ -512,7 +546,8 @@ int bg_enqueue_step(BatchWork& B, eb_op_fn op, int prec, cudaGraphConditionalHan
   k_bg_col<<<std::min(nblk(B.n, 256), 2 * ctx->nsm), 256, 0, st>>>(B.n, B.jdev, B.V, ldv, B.xin);
   eb_count_launch(ctx);
   EB_TRY(op(ctx, B.xin, B.w, prec));
-  k_bg_arnoldi<<<B.S, BBS, 0, st>>>(B.jdev, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact);
+  k_bg_arnoldi<<<B.S, BBS, 0, st>>>(B.jdev, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact,
+                                    prec == EB_FP32 ? 1 : 0);
   k_bg_next<<<1, 32, 0, st>>>(B.maxl, B.jdev, B.nact, h, use_h);
   ctx->launches += 2;
   return eb_check_launch(ctx, "batched gmres (step)");

@@ -12,6 +12,9 @@ Stages (all by default), on the 64-drop x 512-node workload unless named otherwi
   batch    one FP32-refined RK2 step of 64 of the uneven simulations as one batch
   wall     one FP32-refined Stokes solve (host loop) of 64 drops x 512 nodes above the
            wall y = 0: the image lists, mirrored multipoles and reflected near field
+  lapsolve one FP32-refined Laplace solve (host loop) with the per-drop deflation
+           (eb_opts.lap_deflate): k_deflate and the one-pass inner Arnoldi kernels
+  single   one plain FP64 RK2 step of the single 256-node drop
 
 Each stage runs once; the device holds well under 1 GB. Prints "ok" at the end.
 """
@@ -76,8 +79,22 @@ def stage_wall():
     ctx.solvei(rhs, "fp32_refined")
 
 
+def stage_lapsolve():
+    cfg = configs.many_drops()
+    ctx = Context(graphs=-1, lap_deflate=1)
+    g = _tree(ctx, cfg)
+    ctx.solve_lapl(-2.0 * np.asarray(g["z"]).real, "fp32_refined")
+
+
+def stage_single():
+    cfg = configs.single_drop(256)
+    ctx = Context()
+    y = cfg.rku()
+    ctx.rk2(cfg.nd, 1e-3, y, e0=0.5, mode="fp64")
+
+
 STAGES = {"tree": stage_tree, "solve": stage_solve, "apply": stage_apply, "rk2": stage_rk2,
-          "batch": stage_batch, "wall": stage_wall}
+          "batch": stage_batch, "wall": stage_wall, "lapsolve": stage_lapsolve, "single": stage_single}
 
 
 def main(argv):
