@@ -134,8 +134,10 @@ __global__ void k_bg_init(const int* __restrict__ seg, const double* __restrict_
   BCtl& c = ctl[s];
   const bool off = skip && skip[s];
   const bool done = off || !(beta > c.tol * bn) || !(bn > 0.0);
-  if (!done)
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) V[i] /= beta;
+  if (!done) {  // one reciprocal: an FP64 division per element is slow on this GPU
+    const double rb = 1.0 / beta;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) V[i] *= rb;
+  }
   if (threadIdx.x == 0) {
     c.bnrm = bn;
     c.rho = off ? 0.0 : beta;
@@ -194,10 +196,11 @@ __global__ void __launch_bounds__(BBS) k_bg_arnoldi(const int* __restrict__ jdev
     __syncthreads();
     hn = s_hn;
     if (hn > 0.0) {
+      const double rh = 1.0 / hn;
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         double acc = 0.0;
         for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h1[q], acc);
-        vn[i] = (w[i] - acc) / hn;
+        vn[i] = (w[i] - acc) * rh;
       }
     }
   } else {
@@ -222,8 +225,10 @@ __global__ void __launch_bounds__(BBS) k_bg_arnoldi(const int* __restrict__ jdev
     double nn = 0.0;
     for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) nn = fma(w[i], w[i], nn);
     hn = sqrt(bblock_sum(nn, red));
-    if (hn > 0.0)
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] / hn;
+    if (hn > 0.0) {
+      const double rh = 1.0 / hn;
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] * rh;
+    }
   }
   if (threadIdx.x == 0) {
     double* H = Hh + (size_t)s * (maxl + 1) * maxl;  // column-major, ld maxl + 1
