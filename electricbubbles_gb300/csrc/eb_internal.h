@@ -242,7 +242,7 @@ struct eb_ctx {
   // GMRES workspace
   DevBuf gV, gW, gH, gPart, gX, gR, gD, gZ, gTicket;
   DevBuf gCtl, gXin, gWbuf;        // graph mode: control block, operator input and output
-  DevBuf gDefl;                    // deflated Laplace solve: M^-1 of the operator's input
+  DevBuf gDefl, gDeflC;            // deflated Laplace solve: M^-1 of the operator's input, coefficients
   std::vector<double> hH;
   unsigned long long geom_version = 0;  // advanced by every geometry install
   // hash of everything a captured solve graph takes from the geometry by value (counts,

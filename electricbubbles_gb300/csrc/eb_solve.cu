@@ -302,30 +302,43 @@ void dhels(const double* hes, int ldh, int ll, const double* q, double* b) {
 // iteration on each. With P_k the mean over drop k spread over its nodes,
 //   M^-1 = I + sum_k (1/mu_k - 1) P_k,   M = I + sum_k (mu_k - 1) P_k,
 // and A M^-1 maps those modes to about 1 while leaving vectors of zero drop means alone.
-// One block per drop: y = x + c_k mean_k(x) with c_k = 1/mu_k - 1 (inverse = 1, M^-1) or
-// mu_k - 1 (inverse = 0, M). y may alias x: every read of the drop precedes the writes.
+// The coefficients are formed once per solve (k_deflate_coef: coef_k = (1/mu_k - 1,
+// mu_k - 1), zero for a drop whose mu_k is not negative and finite); every application
+// is then one block per drop: y = x + c_k mean_k(x) with c_k = coef_k.x (inverse = 1, M^-1)
+// or coef_k.y (inverse = 0, M). y may alias x: every read of the drop precedes the writes.
 constexpr int DEFL_BS = 256;
+__global__ void __launch_bounds__(DEFL_BS) k_deflate_coef(const int* __restrict__ start,
+                                                          const double* __restrict__ dsda,
+                                                          double2* __restrict__ coef) {
+  __shared__ double red[DEFL_BS / 32];
+  const int b = blockIdx.x, i0 = start[b], i1 = start[b + 1];
+  double ss = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += DEFL_BS) ss += dsda[i];
+  ss = block_sum(ss, red);
+  if (threadIdx.x == 0) {
+    const int n = i1 - i0;
+    double2 c = make_double2(0.0, 0.0);
+    if (n > 0) {
+      const double mu = -4.0 * EB_PI * ss / ((double)n * (double)n);  // -2 (2 pi / n) (ss / n)
+      if (mu < 0.0 && isfinite(mu)) c = make_double2(1.0 / mu - 1.0, mu - 1.0);
+    }
+    coef[b] = c;
+  }
+}
+
 __global__ void __launch_bounds__(DEFL_BS) k_deflate(const int* __restrict__ start,
-                                                     const double* __restrict__ dsda, const double* x,
+                                                     const double2* __restrict__ coef, const double* x,
                                                      double* y, int inverse) {
   __shared__ double red[DEFL_BS / 32];
   __shared__ double s_add;
   const int b = blockIdx.x, i0 = start[b], i1 = start[b + 1];
-  double sx = 0.0, ss = 0.0;
-  for (int i = i0 + threadIdx.x; i < i1; i += DEFL_BS) {
-    sx += x[i];
-    ss += dsda[i];
-  }
+  double sx = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += DEFL_BS) sx += x[i];
   sx = block_sum(sx, red);
-  ss = block_sum(ss, red);
   if (threadIdx.x == 0) {
     const int n = i1 - i0;
-    double a = 0.0;
-    if (n > 0) {
-      const double mu = -4.0 * EB_PI * ss / ((double)n * (double)n);  // -2 (2 pi / n) (ss / n)
-      if (mu < 0.0 && isfinite(mu)) a = (inverse ? 1.0 / mu - 1.0 : mu - 1.0) * (sx / n);
-    }
-    s_add = a;
+    const double2 c = coef[b];
+    s_add = n > 0 ? (inverse ? c.x : c.y) * (sx / n) : 0.0;
   }
   __syncthreads();
   const double a = s_add;
@@ -333,7 +346,7 @@ __global__ void __launch_bounds__(DEFL_BS) k_deflate(const int* __restrict__ sta
 }
 
 int deflate(eb_ctx* ctx, const double* x, double* y, int inverse) {
-  k_deflate<<<ctx->k, DEFL_BS, 0, ctx->stream>>>(ctx->start.as<int>(), ctx->dsda.as<double>(), x, y, inverse);
+  k_deflate<<<ctx->k, DEFL_BS, 0, ctx->stream>>>(ctx->start.as<int>(), ctx->gDeflC.as<double2>(), x, y, inverse);
   eb_count_launch(ctx);
   return EB_OK;
 }
@@ -952,6 +965,10 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
   const bool defl = op == eb_laplace_matvec_dev && ctx->opts.lap_deflate > 0;
   if (defl) {
     EB_TRY(ctx->gDefl.ensure(sizeof(double) * n));
+    EB_TRY(ctx->gDeflC.ensure(sizeof(double2) * (size_t)ctx->k));
+    k_deflate_coef<<<ctx->k, DEFL_BS, 0, s>>>(ctx->start.as<int>(), ctx->dsda.as<double>(),
+                                              ctx->gDeflC.as<double2>());
+    eb_count_launch(ctx);
     op = laplace_matvec_deflated;
   }
   // SOLVEI / SOLVE_LAPL: soln = rhs as the initial guess (stokesbubb.f:346-349); the
