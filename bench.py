@@ -477,6 +477,10 @@ def run_gpu(args, rank, world, local):
     bctx.batch_define([sm.k for sm in sims], be0)
     uneven_steps = 50
     binfo = bctx.rk2(bnd, 1e-3, by, mode="fp32_refined")
+    # leaf sizes picked for this forest by the autotuner (FP32 operator timed per
+    # candidate), once, before the timed steps; every later stage's tree uses them
+    btune = bctx.autotune()
+    binfo = bctx.rk2(bnd, 1e-3, by, mode="fp32_refined")
     torch.cuda.synchronize()
     ea_, eb2_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ea_.record(stream)
@@ -492,7 +496,10 @@ def run_gpu(args, rank, world, local):
               "ms_per_step": bms / uneven_steps,
               "sim_steps_per_s": len(sims) * uneven_steps / (bms * 1e-3),
               "launches_per_step": (bctx.launch_count() - l0) / uneven_steps,
-              "last_step": binfo, "tree": bctx.tree_info()}
+              "last_step": binfo, "tree": bctx.tree_info(),
+              "autotuned": {"leaf64": btune["leaf64"], "leaf_cap": btune["leaf_cap"],
+                            "fp32_apply_us": {"%d/%d" % (c["leaf64"], c["leaf_cap"]): round(c["apply_us"], 1)
+                                              for c in btune["candidates"]}}}
     bctx.close()
 
     # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
