@@ -23,7 +23,8 @@
 namespace {
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
-constexpr int BBS = 256;  // threads per simulation block
+constexpr int BBS = 256;   // threads per simulation block
+constexpr int BCH = 1024;  // rows per work item of the inner Arnoldi steps
 
 __device__ __forceinline__ double bblock_sum(double v, double* red) {
   v = warp_sum<double>(v);
@@ -150,120 +151,171 @@ __global__ void k_bg_init(const int* __restrict__ seg, const double* __restrict_
   }
 }
 
-// One Arnoldi step j for every active simulation: classical Gram-Schmidt on
-// w = A V[:, j] against V[:, 0..j] within the simulation's segment, the new column of
-// the Hessenberg matrix, DHEQR's Givens update (dheqr.f:82-176) and the stopping test on
-// |g_(j+1)| (DPIGMR's RHO, dpigmr.f:340-355). nact counts the simulations still active
-// after the step. Two passes for the FP64 cycle; for the inner FP32 cycle of refinement
-// (one_pass) a single pass whose norm comes by Pythagoras from the same sweep,
-// ||w - V h||^2 = w.w - h.h (within 1e-12 of w.w the vector counts as zero), and one
-// sweep that forms and normalises the new column.
+// The end of Arnoldi step j of simulation s (one thread): the Hessenberg column h (plus
+// h2 when given) with ||w'|| = hn below it, DHEQR's Givens update (dheqr.f:82-176), the
+// residual estimate and the stopping test (DPIGMR's RHO, dpigmr.f:340-355).
+__device__ void bg_step_end(int s, int j, const double* h, const double* h2, double hn, BCtl& c,
+                            double* __restrict__ Hh, double* __restrict__ G, double* __restrict__ CS, int maxl,
+                            int* __restrict__ nact) {
+  double* H = Hh + (size_t)s * (maxl + 1) * maxl;  // column-major, ld maxl + 1
+  double* g = G + (size_t)s * (maxl + 1);
+  double* cs = CS + (size_t)s * 2 * maxl;
+  double* col = H + (size_t)j * (maxl + 1);
+  for (int q = 0; q <= j; ++q) col[q] = h2 ? h[q] + h2[q] : h[q];
+  col[j + 1] = hn;
+  for (int q = 0; q < j; ++q) {  // earlier rotations
+    const double cq = cs[2 * q], sq = cs[2 * q + 1];
+    const double t1 = col[q], t2 = col[q + 1];
+    col[q] = cq * t1 - sq * t2;
+    col[q + 1] = sq * t1 + cq * t2;
+  }
+  const double d = hypot(col[j], col[j + 1]);
+  const double cj = d > 0.0 ? col[j] / d : 1.0, sj = d > 0.0 ? -col[j + 1] / d : 0.0;
+  cs[2 * j] = cj;
+  cs[2 * j + 1] = sj;
+  col[j] = d;
+  col[j + 1] = 0.0;
+  g[j + 1] = sj * g[j];
+  g[j] = cj * g[j];
+  c.rho = fabs(g[j + 1]);
+  c.lgmr = j + 1;
+  if (!isfinite(c.rho)) {
+    c.iflag = 2;
+    c.active = 0;
+  } else if (c.rho <= c.tol * c.bnrm || !(hn > 0.0)) {
+    c.active = 0;
+  } else if (j + 1 >= maxl) {
+    c.iflag = 1;
+    c.active = 0;
+  } else {
+    atomicAdd(nact, 1);
+  }
+}
+
+// One Arnoldi step j for every active simulation of an FP64 cycle: classical Gram-Schmidt
+// applied twice on w = A V[:, j] against V[:, 0..j] within the simulation's segment, the
+// new column of the Hessenberg matrix, DHEQR's Givens update (dheqr.f:82-176) and the
+// stopping test on |g_(j+1)| (DPIGMR's RHO, dpigmr.f:340-355). nact counts the
+// simulations still active after the step.
 __global__ void __launch_bounds__(BBS) k_bg_arnoldi(const int* __restrict__ jdev, const int* __restrict__ seg,
                                                     double* __restrict__ V, size_t ldv, double* __restrict__ w,
                                                     BCtl* __restrict__ ctl, double* __restrict__ Hh,
                                                     double* __restrict__ G, double* __restrict__ CS, int maxl,
-                                                    int* __restrict__ nact, int one_pass) {
+                                                    int* __restrict__ nact) {
   const int j = *jdev;
   __shared__ double red[33];
   __shared__ double h1[EB_GM_MAXL + 2];
   __shared__ double h2[EB_GM_MAXL + 2];
-  __shared__ double s_hn;
   const int s = blockIdx.x;
   BCtl& c = ctl[s];
   if (!c.active) return;
   const int i0 = seg[s], i1 = seg[s + 1];
   const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double* vn = V + (size_t)(j + 1) * ldv;
-  double hn;
-  if (one_pass) {
-    for (int q = wi; q <= j + 1; q += nw) {  // column j + 1: w . w
-      const double* v = q <= j ? V + (size_t)q * ldv : w;
+  double* hp[2] = {h1, h2};
+  for (int pass = 0; pass < 2; ++pass) {
+    double* h = hp[pass];
+    for (int q = wi; q <= j; q += nw) {
+      const double* v = V + (size_t)q * ldv;
       double acc = 0.0;
       for (int i = i0 + lane; i < i1; i += 32) acc = fma(v[i], w[i], acc);
       acc = warp_sum<double>(acc);
-      if (lane == 0) h1[q] = acc;
+      if (lane == 0) h[q] = acc;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      const double ww = h1[j + 1];
-      double t = ww;
-      for (int q = 0; q <= j; ++q) {
-        t = fma(-h1[q], h1[q], t);
-        h2[q] = 0.0;
-      }
-      s_hn = t > 1e-12 * ww ? sqrt(t) : 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      double acc = 0.0;
+      for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h[q], acc);
+      w[i] -= acc;
     }
     __syncthreads();
-    hn = s_hn;
-    if (hn > 0.0) {
-      const double rh = 1.0 / hn;
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        double acc = 0.0;
-        for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h1[q], acc);
-        vn[i] = (w[i] - acc) * rh;
-      }
-    }
-  } else {
-    double* hp[2] = {h1, h2};
-    for (int pass = 0; pass < 2; ++pass) {
-      double* h = hp[pass];
-      for (int q = wi; q <= j; q += nw) {
-        const double* v = V + (size_t)q * ldv;
-        double acc = 0.0;
-        for (int i = i0 + lane; i < i1; i += 32) acc = fma(v[i], w[i], acc);
-        acc = warp_sum<double>(acc);
-        if (lane == 0) h[q] = acc;
-      }
-      __syncthreads();
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        double acc = 0.0;
-        for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], h[q], acc);
-        w[i] -= acc;
-      }
-      __syncthreads();
-    }
-    double nn = 0.0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) nn = fma(w[i], w[i], nn);
-    hn = sqrt(bblock_sum(nn, red));
-    if (hn > 0.0) {
-      const double rh = 1.0 / hn;
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] * rh;
-    }
   }
-  if (threadIdx.x == 0) {
-    double* H = Hh + (size_t)s * (maxl + 1) * maxl;  // column-major, ld maxl + 1
-    double* g = G + (size_t)s * (maxl + 1);
-    double* cs = CS + (size_t)s * 2 * maxl;
-    double* col = H + (size_t)j * (maxl + 1);
-    for (int q = 0; q <= j; ++q) col[q] = h1[q] + h2[q];
-    col[j + 1] = hn;
-    for (int q = 0; q < j; ++q) {  // earlier rotations
-      const double cq = cs[2 * q], sq = cs[2 * q + 1];
-      const double t1 = col[q], t2 = col[q + 1];
-      col[q] = cq * t1 - sq * t2;
-      col[q + 1] = sq * t1 + cq * t2;
-    }
-    const double d = hypot(col[j], col[j + 1]);
-    const double cj = d > 0.0 ? col[j] / d : 1.0, sj = d > 0.0 ? -col[j + 1] / d : 0.0;
-    cs[2 * j] = cj;
-    cs[2 * j + 1] = sj;
-    col[j] = d;
-    col[j + 1] = 0.0;
-    g[j + 1] = sj * g[j];
-    g[j] = cj * g[j];
-    c.rho = fabs(g[j + 1]);
-    c.lgmr = j + 1;
-    if (!isfinite(c.rho)) {
-      c.iflag = 2;
-      c.active = 0;
-    } else if (c.rho <= c.tol * c.bnrm || !(hn > 0.0)) {
-      c.active = 0;
-    } else if (j + 1 >= maxl) {
-      c.iflag = 1;
-      c.active = 0;
-    } else {
-      atomicAdd(nact, 1);
-    }
+  double nn = 0.0;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) nn = fma(w[i], w[i], nn);
+  const double hn = sqrt(bblock_sum(nn, red));
+  if (hn > 0.0) {
+    const double rh = 1.0 / hn;  // one reciprocal: an FP64 division per element is slow on this GPU
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) vn[i] = w[i] * rh;
+  }
+  if (threadIdx.x == 0) bg_step_end(s, j, h1, h2, hn, c, Hh, G, CS, maxl, nact);
+}
+
+// The inner FP32 cycle's Arnoldi step j over work items (chunks of BCH rows of one
+// simulation), so that a large simulation's FP64 reductions spread over several SMs
+// instead of one block: partial sums of h_q = V[:, q] . w (q <= j) and of w . w per item;
+// the last item of a simulation to finish (a per-simulation ticket) adds its items'
+// partials in item order, forms ||w - V h|| by Pythagoras (within 1e-12 of w.w the
+// vector counts as zero), the Hessenberg column, DHEQR's Givens update and the stopping
+// test, as k_bg_arnoldi does, and leaves h and the norm in hbuf for k_bg_upd1.
+__global__ void __launch_bounds__(BBS) k_bg_dots1(const int* __restrict__ jdev, const int4* __restrict__ items,
+                                                  const int2* __restrict__ sitem, const double* __restrict__ V,
+                                                  size_t ldv, const double* __restrict__ w, BCtl* __restrict__ ctl,
+                                                  double* __restrict__ part, int* __restrict__ tick,
+                                                  double* __restrict__ hbuf, double* __restrict__ Hh,
+                                                  double* __restrict__ G, double* __restrict__ CS, int maxl,
+                                                  int* __restrict__ nact) {
+  const int j = *jdev;
+  const int4 it = items[blockIdx.x];
+  const int s = it.x;
+  BCtl& c = ctl[s];
+  if (!c.active) return;
+  const int nc = j + 2, ldp = maxl + 2;
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int q = wi; q < nc; q += nw) {  // column j + 1: w . w
+    const double* v = q <= j ? V + (size_t)q * ldv : w;
+    double acc = 0.0;
+    for (int i = it.y + lane; i < it.z; i += 32) acc = fma(v[i], w[i], acc);
+    acc = warp_sum<double>(acc);
+    if (lane == 0) part[(size_t)blockIdx.x * ldp + q] = acc;
+  }
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  const int2 si = sitem[s];
+  if (threadIdx.x == 0) s_last = atomicAdd(&tick[s], 1) == si.y - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  __shared__ double h1[EB_GM_MAXL + 2];
+  for (int q = wi; q < nc; q += nw) {
+    double acc = 0.0;
+    for (int b = si.x + lane; b < si.x + si.y; b += 32) acc += __ldcg(part + (size_t)b * ldp + q);
+    acc = warp_sum<double>(acc);
+    if (lane == 0) h1[q] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  tick[s] = 0;
+  const double ww = h1[j + 1];
+  double t = ww;
+  for (int q = 0; q <= j; ++q) t = fma(-h1[q], h1[q], t);
+  const double hn = t > 1e-12 * ww ? sqrt(t) : 0.0;
+  double* hb = hbuf + (size_t)s * ldp;
+  for (int q = 0; q <= j; ++q) hb[q] = h1[q];
+  hb[maxl + 1] = hn;
+  bg_step_end(s, j, h1, nullptr, hn, c, Hh, G, CS, maxl, nact);
+}
+
+// V[:, j + 1] = (w - V[:, 0..j] h) / ||.|| over each work item of a simulation that
+// continues (its h and norm from k_bg_dots1).
+__global__ void __launch_bounds__(BBS) k_bg_upd1(const int* __restrict__ jdev, const int4* __restrict__ items,
+                                                 double* __restrict__ V, size_t ldv, const double* __restrict__ w,
+                                                 const BCtl* __restrict__ ctl, const double* __restrict__ hbuf,
+                                                 int maxl) {
+  const int j = *jdev;
+  const int4 it = items[blockIdx.x];
+  const int s = it.x;
+  if (!ctl[s].active) return;
+  __shared__ double hs[EB_GM_MAXL + 2];
+  const double* hb = hbuf + (size_t)s * (maxl + 2);
+  for (int q = threadIdx.x; q <= j; q += blockDim.x) hs[q] = hb[q];
+  __syncthreads();
+  const double rh = 1.0 / hb[maxl + 1];
+  double* vn = V + (size_t)(j + 1) * ldv;
+  for (int i = it.y + threadIdx.x; i < it.z; i += blockDim.x) {
+    double acc = 0.0;
+    for (int q = 0; q <= j; ++q) acc = fma(V[(size_t)q * ldv + i], hs[q], acc);
+    vn[i] = (w[i] - acc) * rh;
   }
 }
 
@@ -470,6 +522,24 @@ int eb_batch_install(eb_ctx* ctx) {
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_seg1.p, node0.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_seg2.p, seg2.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, st));
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_sim_of_node.p, sonode.data(), sizeof(int) * nbk, cudaMemcpyHostToDevice, st));
+  // work items of the inner Arnoldi steps: each simulation's segment in chunks of BCH rows
+  for (int e = 1; e <= 2; ++e) {
+    std::vector<int4> items;
+    std::vector<int2> sitem(S);
+    for (int sm = 0; sm < S; ++sm) {
+      const int r0 = e * node0[sm], r1 = e * node0[sm + 1];
+      sitem[sm].x = (int)items.size();
+      for (int r = r0; r < r1; r += BCH) items.push_back(make_int4(sm, r, std::min(r1, r + BCH), 0));
+      sitem[sm].y = (int)items.size() - sitem[sm].x;
+    }
+    DevBuf& bi = e == 1 ? ctx->b_items1 : ctx->b_items2;
+    DevBuf& bs = e == 1 ? ctx->b_sitem1 : ctx->b_sitem2;
+    EB_TRY(bi.ensure(sizeof(int4) * items.size()));
+    EB_TRY(bs.ensure(sizeof(int2) * (size_t)S));
+    EB_CUDA_TRY(cudaMemcpyAsync(bi.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st));
+    EB_CUDA_TRY(cudaMemcpyAsync(bs.p, sitem.data(), sizeof(int2) * (size_t)S, cudaMemcpyHostToDevice, st));
+    (e == 1 ? ctx->b_nitem1 : ctx->b_nitem2) = (int)items.size();
+  }
   k_sim_bbox<<<S, 256, 0, st>>>(ctx->b_seg1.as<int>(), ctx->z.as<double2>(), ctx->b_box.as<SimBox>());
   eb_count_launch(ctx);
   std::vector<SimBox> box(S);
@@ -523,6 +593,11 @@ struct BatchWork {
   eb_ctx* ctx;
   int n, S, maxl;
   const int* seg;
+  const int4* items;  // work items of the inner Arnoldi steps
+  const int2* sitem;
+  int nitem;
+  double *part, *hbuf;
+  int* tick;
   double *V, *H, *G, *CS, *w, *xin;
   BCtl* ctl;
   int* nact;
@@ -551,10 +626,18 @@ int bg_enqueue_step(BatchWork& B, eb_op_fn op, int prec, cudaGraphConditionalHan
   k_bg_col<<<std::min(nblk(B.n, 256), 2 * ctx->nsm), 256, 0, st>>>(B.n, B.jdev, B.V, ldv, B.xin);
   eb_count_launch(ctx);
   EB_TRY(op(ctx, B.xin, B.w, prec));
-  k_bg_arnoldi<<<B.S, BBS, 0, st>>>(B.jdev, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact,
-                                    prec == EB_FP32 ? 1 : 0);
+  if (prec == EB_FP32) {
+    // one-pass step over work items: partial sums, then the update
+    k_bg_dots1<<<B.nitem, BBS, 0, st>>>(B.jdev, B.items, B.sitem, B.V, ldv, B.w, B.ctl, B.part, B.tick, B.hbuf,
+                                        B.H, B.G, B.CS, B.maxl, B.nact);
+    k_bg_upd1<<<B.nitem, BBS, 0, st>>>(B.jdev, B.items, B.V, ldv, B.w, B.ctl, B.hbuf, B.maxl);
+    ctx->launches += 2;
+  } else {
+    k_bg_arnoldi<<<B.S, BBS, 0, st>>>(B.jdev, B.seg, B.V, ldv, B.w, B.ctl, B.H, B.G, B.CS, B.maxl, B.nact);
+    eb_count_launch(ctx);
+  }
   k_bg_next<<<1, 32, 0, st>>>(B.maxl, B.jdev, B.nact, h, use_h);
-  ctx->launches += 2;
+  eb_count_launch(ctx);
   return eb_check_launch(ctx, "batched gmres (step)");
 }
 
@@ -661,6 +744,16 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
   B.S = S;
   B.maxl = maxl;
   B.seg = stokes ? ctx->b_seg2.as<int>() : ctx->b_seg1.as<int>();
+  B.items = stokes ? ctx->b_items2.as<int4>() : ctx->b_items1.as<int4>();
+  B.sitem = stokes ? ctx->b_sitem2.as<int2>() : ctx->b_sitem1.as<int2>();
+  B.nitem = stokes ? ctx->b_nitem2 : ctx->b_nitem1;
+  EB_TRY(ctx->b_part.ensure(sizeof(double) * (size_t)std::max(ctx->b_nitem2, 1) * (maxl + 2)));
+  EB_TRY(ctx->b_hbuf.ensure(sizeof(double) * (size_t)S * (maxl + 2)));
+  EB_TRY(ctx->b_tick.ensure(sizeof(int) * (size_t)S));
+  EB_CUDA_TRY(cudaMemsetAsync(ctx->b_tick.p, 0, sizeof(int) * (size_t)S, st));
+  B.part = ctx->b_part.as<double>();
+  B.hbuf = ctx->b_hbuf.as<double>();
+  B.tick = ctx->b_tick.as<int>();
   EB_TRY(ctx->gV.ensure(sizeof(double) * (size_t)n * (maxl + 1)));
   EB_TRY(ctx->gH.ensure(sizeof(double) * (size_t)S * (maxl + 1) * (maxl + 1)));
   EB_TRY(ctx->b_G.ensure(sizeof(double) * (size_t)S * (maxl + 1)));

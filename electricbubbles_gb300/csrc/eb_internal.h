@@ -267,6 +267,11 @@ struct eb_ctx {
   int b_R = 0;                     // the forest's cells are the boxes of level b_R
   double b_sq[3] = {1, 0, 0};      // the forest's root square (W, x0, y0)
   DevBuf b_G, b_CS, b_ctl, b_misc; // batched GMRES state
+  // inner FP32 Arnoldi steps over chunks of rows: work items (sim, row0, row1, 0) of the
+  // Laplace (1) and Stokes (2) segments, per simulation its first item and count, the
+  // partial sums per item, h and the norm per simulation, and per-simulation tickets
+  DevBuf b_items1, b_items2, b_sitem1, b_sitem2, b_part, b_hbuf, b_tick;
+  int b_nitem1 = 0, b_nitem2 = 0;
   DevBuf b_st1, b_st2, b_flag;     // GETFOURIER / DOUBLE: drop starts and flags
   int* b_host_act = nullptr;       // page-locked counters read back per cycle
   double* h_flux = nullptr;        // page-locked: an RK stage's FLUX, read after the step's synchronisation
