@@ -527,6 +527,22 @@ def run_gpu(args, rank, world, local):
         torch.cuda.synchronize()
         large["solve_ms_" + mode] = ea.elapsed_time(eb_)
         large["solve_info_" + mode] = info
+    # the Laplace solve (GETBCs' -2 Re z) on the 1,024 drops: each drop adds one small,
+    # distinct eigenvalue to FASMVP_LAP, more than the MAXL = 100 Krylov vectors of a
+    # GMRES cycle resolve; with the per-drop deflation (eb_opts.lap_deflate) it converges
+    rlb = torch.from_numpy(np.ascontiguousarray(-2.0 * np.ascontiguousarray(gb["z"]).real)).to(dev)
+    xlb = torch.empty_like(rlb)
+    ctx_ldb = Context(device=local, graphs=graphs, lap_deflate=1)
+    ctx_ldb.set_stream(stream.cuda_stream)
+    ctx_ldb.extractdat(big.nd, big.rku())
+    for lab, cx in (("laplace_refined", ctx), ("laplace_refined_deflated", ctx_ldb)):
+        ea.record(stream)
+        _, info = cx.solve_lapl(rlb, "fp32_refined", out=xlb)
+        eb_.record(stream)
+        torch.cuda.synchronize()
+        large[lab + "_ms"] = ea.elapsed_time(eb_)
+        large[lab + "_info"] = info
+    ctx_ldb.close()
 
     cpu = None
     if rank == 0:
