@@ -171,10 +171,13 @@ __global__ void k_extractdat(const int* __restrict__ start, const double2* __res
 
 // PVINTEV interpolation (pv_integral.f:143-166): per drop, FINTERC of ucmplx and FINTER
 // of x and y from n to 2n points; charges QA = U2 h on the odd fine nodes (0-based),
-// zero on the even ones (the original nodes).
+// zero on the even ones (the original nodes). One block per (drop, component):
+// blockIdx.y = 0 the density, 1 and 2 the x and y of the fine points (launched when the
+// positions are wanted). The three transforms are independent, and a drop's FP64
+// transforms are bound by the FP64 rate of one SM, so each gets its own.
 __global__ void k_pv_interp(const int* __restrict__ start, const double2* __restrict__ z,
                             const double2* __restrict__ uc, double2* __restrict__ zf,
-                            double2* __restrict__ qf, int nmax, int want_positions) {
+                            double2* __restrict__ qf, int nmax) {
   extern __shared__ double2 sm[];
   int b = blockIdx.x;
   int i0 = start[b], n = start[b + 1] - i0, nf = 2 * n;
@@ -183,8 +186,8 @@ __global__ void k_pv_interp(const int* __restrict__ start, const double2* __rest
   make_twiddles(tw, nf);
   double h = 2.0 * EB_PI / (double)n, inv = 1.0 / (double)n;
   int ny = n / 2;
-  int ncomp = want_positions ? 3 : 1;
-  for (int comp = 0; comp < ncomp; ++comp) {
+  const int comp = blockIdx.y;
+  {
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       double2 v;
@@ -435,9 +438,8 @@ int pvintev_dev(eb_ctx* ctx, const double2* uc, double2* phi, int prec) {
   size_t sm = sizeof(double2) * (size_t)nmax * 3;
   EB_TRY(set_smem((const void*)k_pv_interp, sm));
   bool need_tree = !ctx->tree_pv.valid;
-  k_pv_interp<<<ctx->k, SBS, sm, s>>>(ctx->start.as<int>(), ctx->z.as<double2>(), uc,
-                                      ctx->pvz.as<double2>(), ctx->pvq.as<double2>(), nmax,
-                                      need_tree ? 1 : 0);
+  k_pv_interp<<<dim3(ctx->k, need_tree ? 3 : 1), SBS, sm, s>>>(ctx->start.as<int>(), ctx->z.as<double2>(), uc,
+                                                                ctx->pvz.as<double2>(), ctx->pvq.as<double2>(), nmax);
   eb_count_launch(ctx);
   if (need_tree && ctx->nsim > 0) {
     EB_TRY(eb_batch_translate_fine(ctx, ctx->pvz.as<double2>()));
