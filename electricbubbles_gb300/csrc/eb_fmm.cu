@@ -1605,6 +1605,79 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
 }
 
 // ---------------------------------------------------------------------------------
+// Direct sums for small point sets (at most eb_opts.direct_max points, one problem, free
+// space). Every pair by the near-field formula of the leaf kernels, with the FMM's charges
+// (sorted order) and its fused post-processing; one warp per target, lanes over the
+// sources, the lanes' partial sums added by a butterfly. On a few hundred points the
+// FMM's chain of about a dozen dependent launches, each on a handful of SMs, costs far
+// more than all N^2 pairs: an FP64 pair is ~35 FP64 instructions, so 1,024 points take
+// ~60 us of the GPU's FP64 rate. The sums are exact up to rounding (no truncation).
+// ---------------------------------------------------------------------------------
+template <int E>
+__global__ void __launch_bounds__(128) k_direct64(int n, const double2* __restrict__ zs,
+                                                  const double2* __restrict__ pq,
+                                                  const double2* __restrict__ aa,
+                                                  const double2* __restrict__ qa, const int* __restrict__ perm,
+                                                  double2* __restrict__ out, EbPost post) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per target
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const double2 zi = zs[i];
+  double gx = 0.0, gy = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    if (j == i) continue;
+    const double2 zj = zs[j];
+    const double dx = zj.x - zi.x, dy = zj.y - zi.y;
+    const double rr = rcp_nr(fma(dx, dx, dy * dy));
+    const double ix = dx * rr, iy = -dy * rr;  // 1/D
+    if (E == 2) {
+      const double2 P = pq[2 * j], Q = pq[2 * j + 1], A = aa[j];
+      gx = fma(P.x, ix, fma(-P.y, iy, gx));  // qa/D + s conj(qb/D)
+      gy = fma(Q.x, iy, fma(Q.y, ix, gy));
+      const double w2x = fma(ix, ix, -iy * iy), w2y = -2.0 * ix * iy;  // conj(1/D)^2
+      const double tx = fma(dx, w2x, -dy * w2y), ty = fma(dx, w2y, dy * w2x);
+      gx = fma(A.x, tx, fma(-A.y, ty, gx));  // - s D conj(qa) conj(1/D)^2
+      gy = fma(A.x, ty, fma(A.y, tx, gy));
+    } else {
+      const double2 q = qa[j];
+      gx = fma(-q.x, ix, fma(q.y, iy, gx));  // q/(z_i - z_j) = -q/D
+      gy = fma(-q.x, iy, fma(-q.y, ix, gy));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+  }
+  if (lane == 0) eb_post_store(post, perm[i], make_double2(gx, gy), out);
+}
+
+// The FP32 operator's direct sums: positions as float hi + lo, the pair of k_near32.
+template <int E>
+__global__ void __launch_bounds__(128) k_direct32(int n, const float4* __restrict__ zhl,
+                                                  const float4* __restrict__ pq, const float2* __restrict__ aa,
+                                                  const float2* __restrict__ qa, const int* __restrict__ perm,
+                                                  double2* __restrict__ out, EbPost post) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const float4 hi = zhl[i];
+  float gx = 0.f, gy = 0.f;
+  for (int j = lane; j < n; j += 32) {
+    if (j == i) continue;
+    const float4 PQ = E == 2 ? pq[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 A = E == 2 ? aa[j] : qa[j];
+    near_pair<E>(zhl[j], PQ, A, hi, gx, gy);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+  }
+  if (lane == 0) eb_post_store_f32(post, perm[i], make_float2(gx, gy), out);
+}
+
+// ---------------------------------------------------------------------------------
 // Wall-bounded flow (IFLAG2 = 1 of CADAPDR / CADAPMOD): the images of the sources across
 // the wall y = 0, the bottom edge of the root square.
 // ---------------------------------------------------------------------------------
@@ -2059,10 +2132,60 @@ int fmm_expansions(eb_ctx* ctx, EbTree& t, EbTables& tb, EbFmmWork& w) {
   return EB_OK;
 }
 
+// The direct path of a small problem: the FMM's charges, k_direct64 / k_direct32, and
+// the post-processing. FP64-class requests (native or double-float) run in native FP64.
+template <int E>
+int direct_run(eb_ctx* ctx, EbTree& t, bool f32, int sign, const double2* dens, const double2* dz,
+               const double* hpt, const double2* q, double2* out, const EbPost* postp, cudaEvent_t join) {
+  EbPost post{};
+  if (postp) post = *postp;
+  cudaStream_t st = eb_stream(ctx);
+  const int n = t.n;
+  EbFmmWork& w = f32 ? ctx->work32 : ctx->work64;
+  const size_t cs = f32 ? sizeof(float2) : sizeof(double2);
+  EB_TRY(w.qa.ensure(cs * (size_t)n));
+  EB_TRY(w.qb.ensure(cs * (size_t)n));
+  EB_TRY(w.pq.ensure(cs * 2 * (size_t)n));
+  EB_TRY(w.aa.ensure(cs * (size_t)n));
+  const int g = nblk((long long)n * 32, 128);
+  if (f32) {
+    if (E == 2)
+      k_charges_stokes<float><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
+                                                            w.qa.as<float2>(), w.qb.as<float2>(),
+                                                            w.pq.as<float2>(), w.aa.as<float2>());
+    else
+      k_charges_cauchy<float><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, post.u, post.dz, post.hpt,
+                                                            w.qa.as<float2>());
+    if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
+    k_direct32<E><<<g, 128, 0, st>>>(n, t.zhl.as<float4>(), reinterpret_cast<const float4*>(w.pq.p),
+                                     w.aa.as<float2>(), w.qa.as<float2>(), t.perm.as<int>(), out, post);
+  } else {
+    if (E == 2)
+      k_charges_stokes<double><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
+                                                             w.qa.as<double2>(), w.qb.as<double2>(),
+                                                             w.pq.as<double2>(), w.aa.as<double2>());
+    else
+      k_charges_cauchy<double><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), q, post.u, post.dz, post.hpt,
+                                                             w.qa.as<double2>());
+    if (join) EB_CUDA_TRY(cudaStreamWaitEvent(st, join, 0));
+    k_direct64<E><<<g, 128, 0, st>>>(n, t.zs.as<double2>(), w.pq.as<double2>(), w.aa.as<double2>(),
+                                     w.qa.as<double2>(), t.perm.as<int>(), out, post);
+  }
+  ctx->launches += 2;
+  return eb_check_launch(ctx, "direct sum");
+}
+
+// A problem small enough for the direct sums: at most eb_opts.direct_max points, one
+// problem (a batch's forest keeps its simulations apart through the tree), no wall.
+bool use_direct(const eb_ctx* ctx, const EbTree& t) {
+  return ctx->opts.direct_max > 0 && t.n <= ctx->opts.direct_max && !t.wall && ctx->nsim == 0;
+}
+
 template <typename T, int E>
 int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2* dz,
             const double* hpt, const double2* q, double2* out, const EbPost* postp,
             cudaEvent_t join, bool df_req) {
+  if (use_direct(ctx, t)) return direct_run<E>(ctx, t, sizeof(T) == 4, sign, dens, dz, hpt, q, out, postp, join);
   EbPost post{};
   if (postp) post = *postp;
   cudaStream_t st = eb_stream(ctx);

@@ -87,6 +87,10 @@ typedef struct eb_opts {
                        fewer iterations with many drops. 0 default (off: DGMRES as the
                        reference runs it), 1 on, -1 off. Not applied to a batch of
                        simulations or to the adjoint solve. */
+  int direct_max;   /* layer sums over at most this many points (one problem, no wall)
+                       are direct O(N^2) sums in one kernel instead of the FMM: exact up
+                       to rounding, and faster on few points (0: default 1024; -1: the
+                       FMM always) */
 } eb_opts;
 
 typedef struct eb_solve_info {

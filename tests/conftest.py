@@ -33,6 +33,8 @@ def gpu_ctx_factory(eblib):
     made = []
 
     def make(**kw):
+        # the FMM unless a test asks for the small-problem direct sums (test_gpu_direct.py)
+        kw.setdefault("direct_max", -1)
         c = Context(**kw)
         made.append(c)
         return c

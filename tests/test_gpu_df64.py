@@ -18,8 +18,8 @@ def relmax(a, b):
 
 @pytest.fixture(scope="module")
 def pair():
-    d = Context(df64=1)
-    n = Context(df64=-1)
+    d = Context(df64=1, direct_max=-1)
+    n = Context(df64=-1, direct_max=-1)
     yield d, n
     d.close()
     n.close()

@@ -20,8 +20,8 @@ def relmax(a, b):
 
 @pytest.fixture(scope="module")
 def pair():
-    g = Context(graphs=1)
-    e = Context(graphs=-1)
+    g = Context(graphs=1, direct_max=-1)
+    e = Context(graphs=-1, direct_max=-1)
     yield g, e
     g.close()
     e.close()
@@ -94,8 +94,8 @@ def test_graph_across_geometry_installs(mode):
     for bit, and a different geometry of the same sizes solves as in a fresh context."""
     a = configs.many_drops(8, 128, seed=21, box=5.0)
     b = configs.many_drops(8, 128, seed=22, box=5.0)
-    g = Context(graphs=1)
-    f = Context(graphs=1)
+    g = Context(graphs=1, direct_max=-1)
+    f = Context(graphs=1, direct_max=-1)
     try:
         def solve(ctx, cfg):
             ex = ctx.extractdat(cfg.nd, cfg.rku())
