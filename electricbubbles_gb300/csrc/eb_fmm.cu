@@ -2175,17 +2175,13 @@ int direct_run(eb_ctx* ctx, EbTree& t, bool f32, int sign, const double2* dens, 
   return eb_check_launch(ctx, "direct sum");
 }
 
-// A problem small enough for the direct sums: at most eb_opts.direct_max points, one
-// problem (a batch's forest keeps its simulations apart through the tree), no wall.
-bool use_direct(const eb_ctx* ctx, const EbTree& t) {
-  return ctx->opts.direct_max > 0 && t.n <= ctx->opts.direct_max && !t.wall && ctx->nsim == 0;
-}
-
 template <typename T, int E>
 int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2* dz,
             const double* hpt, const double2* q, double2* out, const EbPost* postp,
             cudaEvent_t join, bool df_req) {
-  if (use_direct(ctx, t)) return direct_run<E>(ctx, t, sizeof(T) == 4, sign, dens, dz, hpt, q, out, postp, join);
+  // a direct tree (eb_tree_build: at most eb_opts.direct_max points, one problem -- a
+  // batch's forest keeps its simulations apart through the tree -- and no wall)
+  if (t.direct) return direct_run<E>(ctx, t, sizeof(T) == 4, sign, dens, dz, hpt, q, out, postp, join);
   EbPost post{};
   if (postp) post = *postp;
   cudaStream_t st = eb_stream(ctx);

@@ -80,6 +80,9 @@ struct EbTree {
   long long nu = 0, nw = 0;  // lengths of the U and W lists
   bool pairs_read = false;
   bool valid = false;
+  // a problem small enough for the direct sums (eb_opts.direct_max; one problem, no
+  // wall): the points in their given order (perm, zs, zhl) and no boxes or lists
+  bool direct = false;
   EbTreeHost* host = nullptr;  // page-locked (cudaMallocHost), freed with the tree
   ~EbTree();
 

@@ -159,6 +159,20 @@ __global__ void k_gather_points(const double2* __restrict__ z, const int* __rest
   zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
 }
 
+// The points of a direct tree in their given order, with the float hi + lo copies, and a
+// flag for a non-finite coordinate.
+__global__ void k_direct_points(const double2* __restrict__ z, int n, int* __restrict__ perm,
+                                double2* __restrict__ zs, float4* __restrict__ zhl, int* __restrict__ bad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 p = z[i];
+  if (!isfinite(p.x) || !isfinite(p.y)) atomicOr(bad, 1);
+  perm[i] = i;
+  zs[i] = p;
+  float hx = (float)p.x, hy = (float)p.y;
+  zhl[i] = make_float4(hx, hy, (float)(p.x - (double)hx), (float)(p.y - (double)hy));
+}
+
 // Histogram of the first level at which consecutive sorted keys fall in different boxes:
 // the occupied boxes of level l in a uniform tree number 1 + sum_{l' <= l} hist[l'].
 __global__ void k_level_hist(const unsigned long long* __restrict__ keys, int n, int* __restrict__ hist) {
@@ -732,11 +746,60 @@ __global__ void k_leaf_coords(const int* __restrict__ leaves, const unsigned lon
   }
 }
 
+// The tree of a problem that takes the direct sums: one kernel and one readback (the
+// finiteness check) instead of the build; the FMM's apply then sums all pairs.
+static int direct_tree(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_cap) {
+  cudaStream_t st = eb_stream(ctx);
+  t.direct = true;
+  t.n = n;
+  t.cap = leaf_cap;
+  t.R = 0;
+  t.wall = 0;
+  t.ld = 0;
+  t.L = 0;
+  t.nbox = 1;
+  t.nleaf = 1;
+  t.ngroup = 0;
+  t.ntile = 0;
+  t.nchunk = 0;
+  t.chunk_lmin = 2;
+  t.lend = 2;
+  t.nu = t.nw = 0;
+  t.lev_off[0] = 0;
+  for (int l = 1; l < EB_KEY_LEVELS + 2; ++l) t.lev_off[l] = 1;
+  t.x0 = t.y0 = 0.0;
+  t.W = 1.0;
+  if (!t.host) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&t.host), sizeof(EbTreeHost)));
+  EB_TRY(t.perm.ensure(sizeof(int) * (size_t)n));
+  EB_TRY(t.zs.ensure(sizeof(double2) * (size_t)n));
+  EB_TRY(t.zhl.ensure(sizeof(float4) * (size_t)n));
+  EB_TRY(t.bbox.ensure(sizeof(int)));
+  int* bad = t.bbox.as<int>();
+  EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  k_direct_points<<<nblk(n, 256), 256, 0, st>>>(z, n, t.perm.as<int>(), t.zs.as<double2>(), t.zhl.as<float4>(),
+                                                bad);
+  eb_count_launch(ctx);
+  EB_CUDA_TRY(cudaMemcpyAsync(&t.host->bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (t.host->bad & 1) {
+    eb_set_last_error_msg("non-finite node coordinate");
+    return EB_ERR_NAN;
+  }
+  t.u_pairs = (long long)n * (n - 1);
+  t.v_pairs = t.w_pairs = 0;
+  t.pairs_read = true;
+  t.valid = true;
+  return eb_check_launch(ctx, "direct tree");
+}
+
 int eb_tree_build(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf_target, int leaf_cap,
                   const double* root_sq, int root_level, int wall) {
   cudaStream_t st = eb_stream(ctx);
   t.valid = false;
   if (n <= 0) return EB_ERR_ARG;
+  if (!root_sq && !wall && ctx->nsim == 0 && ctx->opts.direct_max > 0 && n <= ctx->opts.direct_max)
+    return direct_tree(ctx, t, z, n, leaf_cap < 1 ? EB_LEAF_CAP : leaf_cap);
+  t.direct = false;
   if (leaf_target < 1) leaf_target = 32;
   if (leaf_cap < 1) leaf_cap = EB_LEAF_CAP;
   t.n = n;

@@ -152,3 +152,21 @@ def test_wall_and_batch_keep_the_fmm(gpu_ctx_factory, oracle):
         xs, _ = one.solvei(rhs[off:off + 2 * s.nbk], "fp64")
         assert relmax(xb[off:off + 2 * s.nbk], xs) < 1e-9
         off += 2 * s.nbk
+
+
+def test_direct_install_checks_and_reports(gpu_ctx_factory, oracle):
+    """A direct problem installs no tree: the install still rejects a non-finite node
+    (EB_ERR_NAN) and the tree info reports one box whose pairs are all summed directly."""
+    from electricbubbles_gb300.api import EbError
+    cfg = configs.single_drop(64)
+    ex = oracle.extractdat(cfg.nd, cfg.rku())
+    ctx = direct_ctx(gpu_ctx_factory)
+    ctx.set_geometry(cfg.nd, ex["z"], ex["dz"], ex["dsda"], ex["kappa"], ex["zk"])
+    info = ctx.tree_info()
+    assert info["npoints"] == 64 and info["nboxes"] == 1 and info["levels"] == 0
+    assert info["u_pairs"] == 64 * 63 and info["v_pairs"] == 0
+    z = ex["z"].copy()
+    z[5] = np.nan
+    with pytest.raises(EbError) as e:
+        ctx.set_geometry(cfg.nd, z, ex["dz"], ex["dsda"], ex["kappa"], ex["zk"])
+    assert e.value.status == 6  # EB_ERR_NAN
