@@ -464,6 +464,39 @@ def run_gpu(args, rank, world, local):
         r, info = rk_rate(single, mode, 100)
         rk["single_drop_n256/" + mode] = {"steps_per_s": r, "last_step": info, "steps": 100}
 
+    # the single drop (N = 256, E0 = 0.5): plain FP64 Stokes and Laplace solves/s and
+    # F-evaluations/s (the RK right-hand side: EXTRACTDAT, both solves, DtN, SETVELF,
+    # INTERFACENEW, EQUIT), with the small-problem direct sums (the default below 1,024
+    # points) and with the FMM at every size
+    def single_rates(cx, reps=50):
+        sg = cx.extractdat(single.nd, single.rku())
+        srhs = torch.from_numpy(surface_tension_rhs(sg["dz"], sg["dsda"])).to(dev)
+        srl = torch.from_numpy(np.ascontiguousarray(-2.0 * np.ascontiguousarray(sg["z"]).real)).to(dev)
+        sx, sxl = torch.empty_like(srhs), torch.empty_like(srl)
+        sy = torch.from_numpy(single.rku()).to(dev)
+        sd = torch.empty_like(sy)
+        out = {}
+        for lab, fn in (("stokes_solves_per_s", lambda: cx.solvei(srhs, "fp64", out=sx)),
+                        ("laplace_solves_per_s", lambda: cx.solve_lapl(srl, "fp64", out=sxl)),
+                        ("f_evals_per_s", lambda: cx.f(single.nd, sy, e0=0.5, mode="fp64", out=sd))):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0_.record(stream)
+            for _ in range(reps):
+                fn()
+            e1_.record(stream)
+            torch.cuda.synchronize()
+            out[lab] = reps / (e0_.elapsed_time(e1_) * 1e-3)
+        return out
+    single_fp64 = {"workload": "single_drop_n256 (E0 = 0.5, plain FP64)"}
+    for lab, dm in (("direct", 0), ("fmm", -1)):
+        cx = Context(device=local, graphs=graphs, direct_max=dm)
+        cx.set_stream(stream.cuda_stream)
+        single_fp64[lab] = single_rates(cx)
+        cx.close()
+
     # the 256 independent single-drop simulations of uneven sizes (N log-uniform in
     # [128, 4096], E0 U[0.1, 1], seed 4) as one batch in one context: every kernel
     # launch covers all simulations, GMRES per simulation; 50 FP32-refined RK2 steps
@@ -623,6 +656,7 @@ def run_gpu(args, rank, world, local):
         "clocks": clk,
         "gpu_launches": launches,
         "rk2": rk,
+        "single_drop": single_fp64,
         "uneven": uneven,
         "large": large,
     }
