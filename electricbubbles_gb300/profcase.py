@@ -14,7 +14,10 @@ Stages (all by default), on the 64-drop x 512-node workload unless named otherwi
            wall y = 0: the image lists, mirrored multipoles and reflected near field
   lapsolve one FP32-refined Laplace solve (host loop) with the per-drop deflation
            (eb_opts.lap_deflate): k_deflate and the one-pass inner Arnoldi kernels
-  single   one plain FP64 RK2 step of the single 256-node drop
+  single   one plain FP64 RK2 step of the single 256-node drop (direct sums: at most
+           1,024 points)
+  batchloop one FP32-refined RK2 step of 64 of the uneven simulations as one batch with
+           the GMRES loops driven from the host (the batched Arnoldi kernels as launches)
 
 Each stage runs once; the device holds well under 1 GB. Prints "ok" at the end.
 """
@@ -93,8 +96,18 @@ def stage_single():
     ctx.rk2(cfg.nd, 1e-3, y, e0=0.5, mode="fp64")
 
 
+def stage_batchloop():
+    sims = configs.uneven_simulations()[:64]
+    ctx = Context(graphs=-1)
+    ctx.batch_define([s.k for s in sims], np.array([s.params["E0"] for s in sims]))
+    nd = np.concatenate([s.nd for s in sims])
+    y = np.concatenate([s.rku() for s in sims])
+    ctx.rk2(nd, 1e-3, y, mode="fp32_refined")
+
+
 STAGES = {"tree": stage_tree, "solve": stage_solve, "apply": stage_apply, "rk2": stage_rk2,
-          "batch": stage_batch, "wall": stage_wall, "lapsolve": stage_lapsolve, "single": stage_single}
+          "batch": stage_batch, "wall": stage_wall, "lapsolve": stage_lapsolve, "single": stage_single,
+          "batchloop": stage_batchloop}
 
 
 def main(argv):
