@@ -1607,24 +1607,44 @@ __global__ void __launch_bounds__(128, 8) k_near32(const int4* __restrict__ tile
 // ---------------------------------------------------------------------------------
 // Direct sums for small point sets (at most eb_opts.direct_max points, one problem, free
 // space). Every pair by the near-field formula of the leaf kernels, with the FMM's charges
-// (sorted order) and its fused post-processing; one warp per target, lanes over the
-// sources, the lanes' partial sums added by a butterfly. On a few hundred points the
+// (sorted order) and its fused post-processing; one block of 128 threads per target, the
+// threads over the sources, their partial sums added in a fixed order (direct_block_sum). On a few hundred points the
 // FMM's chain of about a dozen dependent launches, each on a handful of SMs, costs far
 // more than all N^2 pairs: an FP64 pair is ~35 FP64 instructions, so 1,024 points take
 // ~60 us of the GPU's FP64 rate. The sums are exact up to rounding (no truncation).
 // ---------------------------------------------------------------------------------
+// The sum of a block's partial sums, in thread 0 (warp butterflies, then the warps in
+// order through shared memory).
+template <typename T>
+__device__ __forceinline__ void direct_block_sum(T& gx, T& gy) {
+  __shared__ T sx[4], sy[4];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sx[w] = gx;
+    sy[w] = gy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    gx = sx[0] + sx[1] + sx[2] + sx[3];
+    gy = sy[0] + sy[1] + sy[2] + sy[3];
+  }
+}
+
 template <int E>
 __global__ void __launch_bounds__(128) k_direct64(int n, const double2* __restrict__ zs,
                                                   const double2* __restrict__ pq,
                                                   const double2* __restrict__ aa,
                                                   const double2* __restrict__ qa, const int* __restrict__ perm,
                                                   double2* __restrict__ out, EbPost post) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per target
-  const int lane = threadIdx.x & 31;
-  if (i >= n) return;
+  const int i = blockIdx.x;  // one block of 128 threads per target, the threads over the sources
   const double2 zi = zs[i];
   double gx = 0.0, gy = 0.0;
-  for (int j = lane; j < n; j += 32) {
+  for (int j = threadIdx.x; j < n; j += 128) {
     if (j == i) continue;
     const double2 zj = zs[j];
     const double dx = zj.x - zi.x, dy = zj.y - zi.y;
@@ -1644,12 +1664,8 @@ __global__ void __launch_bounds__(128) k_direct64(int n, const double2* __restri
       gy = fma(-q.x, iy, fma(-q.y, ix, gy));
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    gx += __shfl_xor_sync(0xffffffffu, gx, o);
-    gy += __shfl_xor_sync(0xffffffffu, gy, o);
-  }
-  if (lane == 0) eb_post_store(post, perm[i], make_double2(gx, gy), out);
+  direct_block_sum<double>(gx, gy);
+  if (threadIdx.x == 0) eb_post_store(post, perm[i], make_double2(gx, gy), out);
 }
 
 // The FP32 operator's direct sums: positions as float hi + lo, the pair of k_near32.
@@ -1658,23 +1674,17 @@ __global__ void __launch_bounds__(128) k_direct32(int n, const float4* __restric
                                                   const float4* __restrict__ pq, const float2* __restrict__ aa,
                                                   const float2* __restrict__ qa, const int* __restrict__ perm,
                                                   double2* __restrict__ out, EbPost post) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= n) return;
+  const int i = blockIdx.x;
   const float4 hi = zhl[i];
   float gx = 0.f, gy = 0.f;
-  for (int j = lane; j < n; j += 32) {
+  for (int j = threadIdx.x; j < n; j += 128) {
     if (j == i) continue;
     const float4 PQ = E == 2 ? pq[j] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 A = E == 2 ? aa[j] : qa[j];
     near_pair<E>(zhl[j], PQ, A, hi, gx, gy);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    gx += __shfl_xor_sync(0xffffffffu, gx, o);
-    gy += __shfl_xor_sync(0xffffffffu, gy, o);
-  }
-  if (lane == 0) eb_post_store_f32(post, perm[i], make_float2(gx, gy), out);
+  direct_block_sum<float>(gx, gy);
+  if (threadIdx.x == 0) eb_post_store_f32(post, perm[i], make_float2(gx, gy), out);
 }
 
 // ---------------------------------------------------------------------------------
@@ -2147,7 +2157,7 @@ int direct_run(eb_ctx* ctx, EbTree& t, bool f32, int sign, const double2* dens, 
   EB_TRY(w.qb.ensure(cs * (size_t)n));
   EB_TRY(w.pq.ensure(cs * 2 * (size_t)n));
   EB_TRY(w.aa.ensure(cs * (size_t)n));
-  const int g = nblk((long long)n * 32, 128);
+  const int g = n;  // one block of 128 threads per target
   if (f32) {
     if (E == 2)
       k_charges_stokes<float><<<nblk(n, 256), 256, 0, st>>>(n, t.perm.as<int>(), dens, dz, hpt, (double)sign,
