@@ -190,6 +190,7 @@ struct GmGraph {
 };
 #define EB_GRAPH_CACHE 4
 #define EB_GM_MAXL 126
+#define EB_DEFER_SLOTS 8
 
 struct eb_ctx {
   eb_opts opts;
@@ -278,6 +279,16 @@ struct eb_ctx {
   DevBuf b_st1, b_st2, b_flag;     // GETFOURIER / DOUBLE: drop starts and flags
   int* b_host_act = nullptr;       // page-locked counters read back per cycle
   double* h_flux = nullptr;        // page-locked: an RK stage's FLUX, read after the step's synchronisation
+  // Deferred waits inside an RK call in plain mode (eb_rk2_step, eb_rk_f): the GMRES graph
+  // solves queue their control blocks to page-locked slots and the installs of direct
+  // trees their finiteness flags to d_bad; the call reads both after its one
+  // synchronisation (eb_defer_info)
+  bool defer = false;
+  int ndefer = 0;                  // slots used by this call
+  unsigned char* h_defer = nullptr; // page-locked: EB_DEFER_SLOTS control-block heads
+  long long defer_body[8] = {0};    // kernel launches per Arnoldi step of each slot's graph
+  DevBuf d_bad;                    // int: a direct tree's non-finite node (deferred)
+  int* h_bad = nullptr;            // page-locked copy of d_bad
   GmGraph bgraph[2];               // batched GMRES cycles as graphs (plain, refinement inner)
 };
 
@@ -333,6 +344,8 @@ inline int eb_capture_into(eb_ctx* ctx, cudaGraph_t gr, const cudaGraphNode_t* d
 // batch.cu
 int eb_batch_install(eb_ctx* ctx);
 int eb_batch_translate_fine(eb_ctx* ctx, double2* zf);
+// solve.cu: the info of deferred plain solve `slot` (after the caller's synchronisation)
+int eb_defer_info(eb_ctx* ctx, int slot, eb_solve_info* inf);
 int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* rhs, double* soln, int mode,
                    eb_solve_info* info, int mem);
 

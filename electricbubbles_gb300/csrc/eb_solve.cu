@@ -861,6 +861,14 @@ int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
   }
   cudaStream_t s = ctx->stream;
   EB_CUDA_TRY(cudaGraphLaunch(G->exec, s));
+  if (!head) {  // deferred: the control block goes to the next page-locked slot
+    const int slot = ctx->ndefer++;
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->h_defer + (size_t)slot * GM_HEAD, ctx->gCtl.p, GM_HEAD,
+                                cudaMemcpyDeviceToHost, s));
+    ctx->launches += G->n_pre + G->n_post;
+    ctx->defer_body[slot] = G->n_body;
+    return EB_OK;
+  }
   EB_CUDA_TRY(cudaMemcpyAsync(head, ctx->gCtl.p, GM_HEAD, cudaMemcpyDeviceToHost, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   ctx->launches += G->n_pre + G->n_post + G->n_body * (long long)head->lgmr;
@@ -888,6 +896,14 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
   EB_TRY(ctx->gD.ensure(sizeof(double) * n));
   EB_TRY(ctx->gZ.ensure(sizeof(double) * n));
   GmCtl head;
+  if (mode == EB_SOLVE_FP64 && ctx->defer && ctx->ndefer < EB_DEFER_SLOTS) {
+    // inside an RK call: no wait here; eb_defer_info reads the control block later
+    if (!ctx->h_defer)
+      EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&ctx->h_defer), GM_HEAD * (size_t)EB_DEFER_SLOTS));
+    EB_TRY(run_graph(ctx, GM_PLAIN, op, n, maxl, nullptr));
+    inf->outer = 1;
+    return EB_OK;
+  }
   if (mode == EB_SOLVE_FP64) {
     EB_TRY(run_graph(ctx, GM_PLAIN, op, n, maxl, &head));
     if (head.status != EB_OK) {
@@ -1059,6 +1075,24 @@ int solve(eb_ctx* ctx, int n, op_fn op, const double* rhs, double* soln, int mod
 }
 
 }  // namespace
+
+int eb_defer_info(eb_ctx* ctx, int slot, eb_solve_info* inf) {
+  if (slot < 0 || slot >= ctx->ndefer) return EB_ERR_ARG;
+  GmCtl head;
+  memcpy(&head, ctx->h_defer + (size_t)slot * GM_HEAD, GM_HEAD);
+  ctx->launches += ctx->defer_body[slot] * (long long)head.lgmr;
+  if (head.status != EB_OK) {
+    eb_set_last_error_msg("non-finite value in GMRES");
+    return head.status;
+  }
+  inf->iters = head.iters;
+  inf->err = head.err;
+  inf->ierr = head.lgmr > 0 ? head.iflag : 0;
+  inf->outer = 1;
+  inf->matvecs64 = 1 + head.lgmr;
+  inf->graph = 1;
+  return EB_OK;
+}
 
 void GmGraph::destroy() {
   if (exec) cudaGraphExecDestroy(exec);

@@ -1037,8 +1037,14 @@ __global__ void k_rk_second(int n, double dt, const double* __restrict__ phi0,
   y[i] = y[i] + 0.5 * phi0[i] + 0.5 * (dt * d[i]);
 }
 
+// Deferred solves of a stage (ctx->defer): their control-block slots, -1 when a solve
+// filled its info at once (refined mode, the host-driven loop)
+struct StageSlots {
+  int lap = -1, stokes = -1;
+};
+
 int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
-            eb_stage_info* info) {
+            eb_stage_info* info, StageSlots* slots = nullptr) {
   // zbond != 0: wall-bounded (READINI's iwall, electric.f:321-326), set before the
   // install so that the tree takes the wall
   const double2 zb = make_double2(m->zbond[0], m->zbond[1]);
@@ -1065,7 +1071,9 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   eb_solve_info li{}, si{};
   k_lap_bc<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->z.as<double2>(), rl);
   eb_count_launch(ctx);
+  int s0 = ctx->ndefer;
   EB_TRY(eb_laplace_solve(ctx, nbk, rl, ul, m->mode, &li, EB_DEVICE));
+  const int lap_slot = ctx->ndefer > s0 ? s0 : -1;
   // the FP64 sums of the stage outside the solves: plain mode FP64 (native or
   // double-float as df64 says), refined mode the arithmetic of its FP64 residuals
   const int p64 = m->mode == EB_SOLVE_FP32_REFINED ? eb_resid_prec(ctx) : EB_FP64;
@@ -1077,8 +1085,14 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
     EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
   }
   EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, zb, ctx->st_zc.as<double2>(), ctx->st_rhs.as<double2>()));
+  s0 = ctx->ndefer;
   EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
                          EB_DEVICE));
+  const int stokes_slot = ctx->ndefer > s0 ? s0 : -1;
+  if (slots) {
+    slots->lap = lap_slot;
+    slots->stokes = stokes_slot;
+  }
   double* un = rl;  // the Laplace right-hand side is no longer needed
   // C_k is nonzero exactly in wall mode; FLUX is read by the caller after its
   // synchronisation (the stage itself waits on the host only inside the tree builds
@@ -1091,13 +1105,68 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
                                    ctx->dsda.as<double>(), reinterpret_cast<double2*>(rkup), nmax);
   eb_count_launch(ctx);
   EB_TRY(eb_check_launch(ctx, "stage F"));
-  if (info) {
-    info->lap_iters += li.iters;
-    info->stokes_iters += si.iters;
-    info->lap_err = li.err;
-    info->stokes_err = si.err;
-    info->lap_ierr = li.ierr;
-    info->stokes_ierr = si.ierr;
+  if (info) {  // a deferred solve's part comes from collect_stage after the caller's wait
+    if (lap_slot < 0) {
+      info->lap_iters += li.iters;
+      info->lap_err = li.err;
+      info->lap_ierr = li.ierr;
+    }
+    if (stokes_slot < 0) {
+      info->stokes_iters += si.iters;
+      info->stokes_err = si.err;
+      info->stokes_ierr = si.ierr;
+    }
+  }
+  return EB_OK;
+}
+
+// An RK call's deferred waits (ctx->defer, for its duration): solves and direct trees
+// queue their results to page-locked memory; start clears the finiteness flag, finish
+// queues its copy before the call's synchronisation, and collect_stage adds a stage's
+// deferred solve infos after it.
+struct DeferScope {
+  eb_ctx* c;
+  explicit DeferScope(eb_ctx* ctx) : c(ctx) {}
+  int start() {
+    EB_TRY(c->d_bad.ensure(sizeof(int)));
+    if (!c->h_bad) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&c->h_bad), sizeof(int)));
+    EB_CUDA_TRY(cudaMemsetAsync(c->d_bad.p, 0, sizeof(int), c->stream));
+    c->defer = true;
+    c->ndefer = 0;
+    return EB_OK;
+  }
+  int finish() {
+    return cudaMemcpyAsync(c->h_bad, c->d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream) == cudaSuccess
+               ? EB_OK
+               : EB_ERR_CUDA;
+  }
+  ~DeferScope() {
+    c->defer = false;
+    c->ndefer = 0;
+  }
+};
+
+int collect_stage(eb_ctx* ctx, const StageSlots& sl, eb_stage_info* info) {
+  if (*ctx->h_bad & 1) {
+    eb_set_last_error_msg("non-finite node coordinate");
+    return EB_ERR_NAN;
+  }
+  eb_solve_info li{}, si{};
+  if (sl.lap >= 0) {
+    EB_TRY(eb_defer_info(ctx, sl.lap, &li));
+    if (info) {
+      info->lap_iters += li.iters;
+      info->lap_err = li.err;
+      info->lap_ierr = li.ierr;
+    }
+  }
+  if (sl.stokes >= 0) {
+    EB_TRY(eb_defer_info(ctx, sl.stokes, &si));
+    if (info) {
+      info->stokes_iters += si.iters;
+      info->stokes_err = si.err;
+      info->stokes_ierr = si.ierr;
+    }
   }
   return EB_OK;
 }
@@ -1153,16 +1222,21 @@ int eb_rk_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   for (int b = 0; b < k; ++b) nbk += nd[b];
   cudaStream_t s = ctx->stream;
   if (info) *info = eb_stage_info{};
+  DeferScope dsc(ctx);
+  EB_TRY(dsc.start());
+  StageSlots sl;
   if (mem == EB_DEVICE) {
-    EB_TRY(stage_f(ctx, k, nd, rku, rkup, model, info));
+    EB_TRY(stage_f(ctx, k, nd, rku, rkup, model, info, &sl));
   } else {
     EB_TRY(ctx->rk_y.ensure(sizeof(double) * 2 * (size_t)nbk));
     EB_TRY(ctx->rk_d0.ensure(sizeof(double) * 2 * (size_t)nbk));
     EB_CUDA_TRY(cudaMemcpyAsync(ctx->rk_y.p, rku, sizeof(double) * 2 * nbk, cudaMemcpyHostToDevice, s));
-    EB_TRY(stage_f(ctx, k, nd, ctx->rk_y.as<double>(), ctx->rk_d0.as<double>(), model, info));
+    EB_TRY(stage_f(ctx, k, nd, ctx->rk_y.as<double>(), ctx->rk_d0.as<double>(), model, info, &sl));
     EB_CUDA_TRY(cudaMemcpyAsync(rkup, ctx->rk_d0.p, sizeof(double) * 2 * nbk, cudaMemcpyDeviceToHost, s));
   }
+  EB_TRY(dsc.finish());
   EB_CUDA_TRY(cudaStreamSynchronize(s));
+  EB_TRY(collect_stage(ctx, sl, info));
   if (info) info->flux = *ctx->h_flux;
   return EB_OK;
 }
@@ -1185,17 +1259,24 @@ int eb_rk2_step(eb_ctx* ctx, int k, const int* nd, double dt, double* ybar, cons
   double* y = ctx->rk_y.as<double>();
   EB_CUDA_TRY(cudaMemcpyAsync(y, ybar, sizeof(double) * neq,
                               mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-  EB_TRY(stage_f(ctx, k, nd, y, ctx->rk_d0.as<double>(), model, info));
+  // plain-mode solves and direct-sum installs wait on the host only once, at the end
+  DeferScope dsc(ctx);
+  EB_TRY(dsc.start());
+  StageSlots sl1, sl2;
+  EB_TRY(stage_f(ctx, k, nd, y, ctx->rk_d0.as<double>(), model, info, &sl1));
   k_rk_first<<<nblk(neq, 256), 256, 0, s>>>(neq, dt, y, ctx->rk_d0.as<double>(), ctx->rk_phi.as<double>(),
                                             ctx->rk_y1.as<double>());
   eb_count_launch(ctx);
-  EB_TRY(stage_f(ctx, k, nd, ctx->rk_y1.as<double>(), ctx->rk_d0.as<double>(), model, info));
+  EB_TRY(stage_f(ctx, k, nd, ctx->rk_y1.as<double>(), ctx->rk_d0.as<double>(), model, info, &sl2));
   k_rk_second<<<nblk(neq, 256), 256, 0, s>>>(neq, dt, ctx->rk_phi.as<double>(), ctx->rk_d0.as<double>(), y);
   eb_count_launch(ctx);
   EB_TRY(eb_check_launch(ctx, "rk2 step"));
   EB_CUDA_TRY(cudaMemcpyAsync(ybar, y, sizeof(double) * neq,
                               mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  EB_TRY(dsc.finish());
   EB_CUDA_TRY(cudaStreamSynchronize(s));
+  EB_TRY(collect_stage(ctx, sl1, info));
+  EB_TRY(collect_stage(ctx, sl2, info));
   if (info) info->flux = *ctx->h_flux;  // the second stage's
   return EB_OK;
 }

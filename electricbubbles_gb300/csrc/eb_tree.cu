@@ -774,16 +774,19 @@ static int direct_tree(eb_ctx* ctx, EbTree& t, const double2* z, int n, int leaf
   EB_TRY(t.zs.ensure(sizeof(double2) * (size_t)n));
   EB_TRY(t.zhl.ensure(sizeof(float4) * (size_t)n));
   EB_TRY(t.bbox.ensure(sizeof(int)));
-  int* bad = t.bbox.as<int>();
-  EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  // inside an RK call (ctx->defer) the flag accumulates in ctx->d_bad, read after the call
+  int* bad = ctx->defer ? ctx->d_bad.as<int>() : t.bbox.as<int>();
+  if (!ctx->defer) EB_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
   k_direct_points<<<nblk(n, 256), 256, 0, st>>>(z, n, t.perm.as<int>(), t.zs.as<double2>(), t.zhl.as<float4>(),
                                                 bad);
   eb_count_launch(ctx);
-  EB_CUDA_TRY(cudaMemcpyAsync(&t.host->bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EB_CUDA_TRY(cudaStreamSynchronize(st));
-  if (t.host->bad & 1) {
-    eb_set_last_error_msg("non-finite node coordinate");
-    return EB_ERR_NAN;
+  if (!ctx->defer) {
+    EB_CUDA_TRY(cudaMemcpyAsync(&t.host->bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EB_CUDA_TRY(cudaStreamSynchronize(st));
+    if (t.host->bad & 1) {
+      eb_set_last_error_msg("non-finite node coordinate");
+      return EB_ERR_NAN;
+    }
   }
   t.u_pairs = (long long)n * (n - 1);
   t.v_pairs = t.w_pairs = 0;

@@ -170,3 +170,22 @@ def test_direct_install_checks_and_reports(gpu_ctx_factory, oracle):
     with pytest.raises(EbError) as e:
         ctx.set_geometry(cfg.nd, z, ex["dz"], ex["dsda"], ex["kappa"], ex["zk"])
     assert e.value.status == 6  # EB_ERR_NAN
+
+
+@pytest.mark.parametrize("direct_max", [0, -1])
+@pytest.mark.parametrize("mode", ["fp64", "fp32_refined"])
+def test_rk2_nonfinite_state_is_an_error(gpu_ctx_factory, direct_max, mode):
+    """A non-finite node in the RK state is EB_ERR_NAN, whether the install checks it at
+    once (a tree build) or after the step (a direct-sum install inside the RK call), and
+    the context stays usable."""
+    from electricbubbles_gb300.api import EbError
+    cfg = configs.single_drop(128)
+    ctx = gpu_ctx_factory(direct_max=direct_max)
+    y = cfg.rku()
+    y[10] = np.nan
+    with pytest.raises(EbError) as e:
+        ctx.rk2(cfg.nd, 1e-3, y, e0=0.5, mode=mode)
+    assert e.value.status == 6  # EB_ERR_NAN
+    y = cfg.rku()
+    info = ctx.rk2(cfg.nd, 1e-3, y, e0=0.5, mode=mode)
+    assert info["lap_ierr"] == 0 and info["stokes_ierr"] == 0 and np.isfinite(y).all()
