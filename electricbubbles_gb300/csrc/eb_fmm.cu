@@ -2229,10 +2229,12 @@ int fmm_run(eb_ctx* ctx, EbTree& t, int sign, const double2* dens, const double2
   const int has_far = t.L >= 2;
   int blocks = nblk((long long)t.ngroup * 32, 128);
   // FP32 and double-float: the near field runs on the side stream while the expansion
-  // passes run on the main stream, and the far-field kernel adds both. This pays while
-  // the passes are latency-bound (up to ~256K nodes); above that each kernel fills the
-  // GPU by itself. The per-kernel profiling timer times the combined kernel.
-  const bool split = has_far && (df || !f64) && !ctx->profiling && n <= (1 << 18);
+  // passes run on the main stream, and the far-field kernel adds both. Measured up to
+  // 2^20 nodes it pays at every size (the expansion passes' coarse levels stay
+  // latency-bound): against a limit of 2^18, the 285,440-node batch's RK2 step 35.1 →
+  // 33.6 ms and the 1,048,576-node refined solve 45.7 → 44.3 ms. The per-kernel profiling
+  // timer times the combined kernel.
+  const bool split = has_far && (df || !f64) && !ctx->profiling && n <= (1 << 20);
   if (split) {
     EB_TRY(w.nearbuf.ensure(sizeof(double2) * (size_t)n));
     EB_CUDA_TRY(cudaEventRecord(ctx->ev_c, st));
