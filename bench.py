@@ -551,6 +551,23 @@ def run_gpu(args, rank, world, local):
         eb_.record(stream)
         torch.cuda.synchronize()
         large["fmm_mpts_per_s_" + prec] = big.nbk / (ea.elapsed_time(eb_) / 3 * 1e-3) / 1e6
+    # the FP32 kernels at this size (near and far field, M2L; timed in profiling mode, where
+    # the near field runs on the main stream) against the FP32 peak: where the 64 x 512
+    # kernels are latency-bound, these fill the GPU
+    btree = large["tree"]
+    ctx.set_profiling(True)
+    for _ in range(3):
+        ctx.fasmvp(ub, "fp32", out=yb)
+    nl, leaf_ms = ctx.kernel_time(0)
+    nm, m2l_ms = ctx.kernel_time(1)
+    nn, near_ms = ctx.kernel_time(2)
+    ctx.set_profiling(False)
+    bkern = {"k_near32<2>": kentry(near_ms, nn, 40.0 * btree["u_pairs"]),
+             "k_far32<2>": kentry(leaf_ms, nl, 8.0 * 20 * 2 * btree["npoints"] * min(max(btree["levels"] - 1, 1), 6)),
+             "k_m2l_f32p<2, 20>": kentry(m2l_ms, nm, 2 * 8.0 * 20 * 20 * btree["v_pairs"])}
+    for v in bkern.values():
+        v["frac_of_fp32_peak"] = v["achieved_tflops"] / fp32_peak
+    large["kernels_fp32"] = bkern
     rb = torch.from_numpy(surface_tension_rhs(gb["dz"], gb["dsda"])).to(dev)
     xb = torch.empty_like(rb)
     for mode in ("fp64", "fp32_refined"):
