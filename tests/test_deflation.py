@@ -147,3 +147,22 @@ def test_gpu_deflation_leaves_stokes_and_adjoint_alone(gpu_ctx_factory):
     la, ja = a.solve_lapl_adjoint(rl)
     lb, jb = b.solve_lapl_adjoint(rl)
     assert ja["iters"] == jb["iters"] and np.array_equal(la, lb)
+
+
+@pytest.mark.gpu
+def test_gpu_deflation_in_wall_mode(gpu_ctx_factory):
+    """The wall's images enter the Stokes sums only; the Laplace operator and its drop
+    constants are unchanged, and the deflated solve gives the plain one's density."""
+    cfg = configs.wall_drops()
+    plain = gpu_ctx_factory()
+    defl = gpu_ctx_factory(lap_deflate=1)
+    for c in (plain, defl):
+        c.set_wall(1)
+    ex = plain.extractdat(cfg.nd, cfg.rku())
+    defl.extractdat(cfg.nd, cfg.rku())
+    b = -2.0 * np.asarray(ex["z"]).real
+    xp, ip = plain.solve_lapl(b, "fp64")
+    xd, idf = defl.solve_lapl(b, "fp64")
+    assert ip["ierr"] == 0 and idf["ierr"] == 0
+    assert relmax(xd, xp) < 1e-9
+    assert idf["iters"] < ip["iters"]

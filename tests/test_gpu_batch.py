@@ -143,3 +143,25 @@ def test_batch_define_errors(bctx):
     assert e.value.status == 1  # EB_ERR_ARG
     bctx.batch_define([])
     bctx.extractdat(nd, y)  # back to one simulation
+
+
+def test_autotuned_batch_step_matches(gpu_ctx_factory):
+    """eb_autotune on a batch's forest picks leaf sizes; an RK2 step with them gives the
+    positions of the untuned step (the same operators to FMM accuracy)."""
+    sims = configs.uneven_simulations(count=8, seed=17)
+    nd = np.concatenate([s.nd for s in sims])
+    e0 = np.array([s.params["E0"] for s in sims])
+    ys = []
+    for tune in (False, True):
+        b = gpu_ctx_factory()
+        b.batch_define([s.k for s in sims], e0)
+        y = np.concatenate([s.rku() for s in sims])
+        b.extractdat(nd, y.copy())
+        if tune:
+            info = b.autotune()
+            assert len(info["candidates"]) >= 2 and (info["leaf64"], info["leaf_cap"]) in \
+                [(c["leaf64"], c["leaf_cap"]) for c in info["candidates"]]
+        step = b.rk2(nd, 1e-3, y, mode="fp64")
+        assert step["lap_ierr"] == 0 and step["stokes_ierr"] == 0
+        ys.append(y)
+    assert np.abs(ys[0] - ys[1]).max() < 1e-10
