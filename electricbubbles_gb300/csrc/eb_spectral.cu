@@ -1136,9 +1136,8 @@ struct DeferScope {
     return EB_OK;
   }
   int finish() {
-    return cudaMemcpyAsync(c->h_bad, c->d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream) == cudaSuccess
-               ? EB_OK
-               : EB_ERR_CUDA;
+    EB_CUDA_TRY(cudaMemcpyAsync(c->h_bad, c->d_bad.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    return EB_OK;
   }
   ~DeferScope() {
     c->defer = false;
