@@ -85,6 +85,15 @@ class StageInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class AdjointInfo(ctypes.Structure):
+    _fields_ = [("lap_iters", ctypes.c_int), ("stokes_iters", ctypes.c_int),
+                ("lap_adj_iters", ctypes.c_int), ("stokes_adj_iters", ctypes.c_int),
+                ("ierr", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -130,6 +139,11 @@ SIGNATURES = {
     "eb_rk_f": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo), _I]),
     "eb_rk2_step": (_I, [_P, _I, _P, _D, _P, ctypes.POINTER(Model), ctypes.POINTER(StageInfo),
                          _I]),
+    "eb_rk_f_vjp": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(Model), _P, _P,
+                         ctypes.POINTER(AdjointInfo), _I]),
+    "eb_rk2_step_vjp": (_I, [_P, _I, _P, _D, _P, _P, ctypes.POINTER(Model), _P,
+                             ctypes.POINTER(AdjointInfo), _I]),
+    "eb_deformation": (_I, [_P, _I, _P, _P, ctypes.POINTER(_D), _P, _I]),
     "eb_batch_define": (_I, [_P, _I, _P, _P]),
     "eb_getfourier": (_I, [_P, _I, _P, _P, _P, _P, _I]),
     "eb_double": (_I, [_P, _I, _P, _P, _P, _P, _I]),

@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (EB_DEVICE, EB_FP32, EB_FP64, EB_HOST, EB_SOLVE_FP32_REFINED, EB_SOLVE_FP64,
-                   EbError, Model, Opts, SolveInfo, StageInfo, TreeInfo, check)
+                   AdjointInfo, EbError, Model, Opts, SolveInfo, StageInfo, TreeInfo, check)
 
 PRECISION = {"fp64": EB_FP64, "fp32": EB_FP32}
 SOLVE_MODE = {"fp64": EB_SOLVE_FP64, "fp32_refined": EB_SOLVE_FP32_REFINED}
@@ -439,6 +439,78 @@ class Context:
                                                    ctypes.byref(info), _mem(ybar)))
         self._set_drops(nd)
         return info.as_dict()
+
+    # ---- reverse mode through the time stepper -------------------------------
+    def f_vjp(self, nd, rku, v, cap=0.0, e0=0.0, mode="fp64"):
+        """v^T dF/drku at the RK state rku (free space, one simulation): returns
+        (rku_bar, {"e0": v^T dF/dE0, "cap": v^T dF/dcap}, info)."""
+        nd = _host(nd, np.int32)
+        if not _is_device(rku):
+            rku = _host(rku, np.float64)
+            v = _host(v, np.float64)
+        out = self._out(rku, 2 * int(nd.sum()), np.float64)
+        pb = np.zeros(2)
+        info = AdjointInfo()
+        m = self._model(cap, e0, 0.0, mode)
+        check("eb_rk_f_vjp", self._lib.eb_rk_f_vjp(self._h, int(nd.shape[0]), _ptr(nd), _ptr(rku),
+                                                   _ptr(v), ctypes.byref(m), _ptr(out), _ptr(pb),
+                                                   ctypes.byref(info), _mem(rku, v, out)))
+        self._set_drops(nd)
+        return out, {"e0": float(pb[0]), "cap": float(pb[1])}, info.as_dict()
+
+    def rk2_vjp(self, nd, dt, ybar, rbar, cap=0.0, e0=0.0, mode="fp64"):
+        """The transpose of one RK2 step from the state ybar: rbar (dJ/dy after the step,
+        float64, updated in place to dJ/dy before it). Returns ({"e0", "cap"} parts, info)."""
+        nd = _host(nd, np.int32)
+        if not _is_device(ybar):
+            ybar = _host(ybar, np.float64)
+            if not (isinstance(rbar, np.ndarray) and rbar.dtype == np.float64
+                    and rbar.flags["C_CONTIGUOUS"]):
+                raise TypeError("rbar must be a C-contiguous float64 array (updated in place)")
+        pb = np.zeros(2)
+        info = AdjointInfo()
+        m = self._model(cap, e0, 0.0, mode)
+        check("eb_rk2_step_vjp", self._lib.eb_rk2_step_vjp(self._h, int(nd.shape[0]), _ptr(nd), float(dt),
+                                                           _ptr(ybar), _ptr(rbar), ctypes.byref(m),
+                                                           _ptr(pb), ctypes.byref(info), _mem(ybar, rbar)))
+        self._set_drops(nd)
+        return {"e0": float(pb[0]), "cap": float(pb[1])}, info.as_dict()
+
+    def deformation(self, nd, rku, grad=True):
+        """The summed Taylor deformation (L - B)/(L + B) of the drops of rku, and its
+        gradient with respect to rku (None when grad is False)."""
+        nd = _host(nd, np.int32)
+        if not _is_device(rku):
+            rku = _host(rku, np.float64)
+        g = self._out(rku, 2 * int(nd.sum()), np.float64) if grad else None
+        val = ctypes.c_double(0.0)
+        check("eb_deformation", self._lib.eb_deformation(self._h, int(nd.shape[0]), _ptr(nd), _ptr(rku),
+                                                         ctypes.byref(val), _ptr(g) if grad else None,
+                                                         _mem(rku)))
+        return float(val.value), g
+
+    def rk2_gradient(self, nd, dt, y0, steps, cap=0.0, e0=0.0, mode="fp64"):
+        """J = the deformation after `steps` RK2 steps from y0, and dJ/dy0, dJ/dE0 and
+        dJ/dcap by reverse mode: the forward steps keep one checkpoint (the state) per
+        step, the reverse pass recomputes each step's stages from its checkpoint."""
+        nd = _host(nd, np.int32)
+        y = np.array(y0, dtype=np.float64, copy=True)
+        ckpt = []
+        for _ in range(int(steps)):
+            ckpt.append(y.copy())
+            self.rk2(nd, dt, y, cap=cap, e0=e0, mode=mode)
+        J, rbar = self.deformation(nd, y)
+        pe, pc = 0.0, 0.0
+        iters = {"lap_iters": 0, "stokes_iters": 0, "lap_adj_iters": 0, "stokes_adj_iters": 0, "ierr": 0}
+        for yc in reversed(ckpt):
+            p, info = self.rk2_vjp(nd, dt, yc, rbar, cap=cap, e0=e0, mode=mode)
+            pe += p["e0"]
+            pc += p["cap"]
+            for key in ("lap_iters", "stokes_iters", "lap_adj_iters", "stokes_adj_iters"):
+                iters[key] += info[key]
+            if iters["ierr"] == 0:
+                iters["ierr"] = info["ierr"]
+        return {"J": J, "y0": rbar, "e0": pe, "cap": pc, "info": iters}
 
 
 def geometry_from_extract(ctx, cfg):

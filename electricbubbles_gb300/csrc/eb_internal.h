@@ -241,6 +241,7 @@ struct eb_ctx {
   DevBuf st_lap;                   // double[5*nbk]: Laplace rhs/Un, density, phi, psi, dphi/dn
   DevBuf st_rhs, st_u, st_zc;      // Stokes rhs and density (double2[nbk]), C_k (double2[k])
   DevBuf adj_a, adj_b, adj_s;      // transposed operators: two node sums, per-drop sums
+  DevBuf aj, aj_part, aj_rk;       // adjoint of F: cotangents, per-drop partials, RK2 step state
   DevBuf rk_y, rk_y1, rk_d0, rk_phi;  // RK state, predictor, derivative, dt * F(y)
 
   // GMRES workspace
@@ -346,6 +347,13 @@ int eb_batch_install(eb_ctx* ctx);
 int eb_batch_translate_fine(eb_ctx* ctx, double2* zf);
 // solve.cu: the info of deferred plain solve `slot` (after the caller's synchronisation)
 int eb_defer_info(eb_ctx* ctx, int slot, eb_solve_info* inf);
+// One RK stage F (eb_spectral.cu) with synchronous solves; gout (device, optional)
+// receives INTERFACENEW's full velocity sum g (Un = Re(-i g conj(zn))).
+int eb_stage_f_keep(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
+                    eb_stage_info* info, double2* gout);
+// PVINTEV's fine points and charges of the Laplace density ul (charges of ul dz, as
+// DIRICH_NEU_MAP forms them) into ctx->pvz / ctx->pvq, interleaved even/odd fine nodes.
+int eb_pv_fine(eb_ctx* ctx, const double* ul);
 int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* rhs, double* soln, int mode,
                    eb_solve_info* info, int mem);
 

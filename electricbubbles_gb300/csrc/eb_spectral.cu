@@ -11,68 +11,13 @@
 #include <cmath>
 #include <vector>
 
+#include "eb_fft.cuh"
 #include "eb_internal.h"
 
 namespace {
 
 inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 constexpr int SBS = 512;
-
-// tw[j] = exp(+2 pi i j / N), j < N/2: one table serves both directions (the forward
-// transform uses the conjugate) and every size n dividing N.
-__device__ __forceinline__ void make_twiddles(double2* tw, int N) {
-  for (int j = threadIdx.x; j < N / 2; j += blockDim.x) {
-    double s, c;
-    sincospi(2.0 * (double)j / (double)N, &s, &c);
-    tw[j] = make_double2(c, s);
-  }
-}
-
-// In-place FFT of a[0..n): sign = -1 is DCFFTF's exp(-i..), +1 is DCFFTB's exp(+i..).
-__device__ void smem_fft(double2* a, int n, const double2* tw, int N, int sign) {
-  int logn = 31 - __clz(n);
-  int mult = N / n;
-  __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    int j = (int)(__brev((unsigned)i) >> (32 - logn));
-    if (i < j) {
-      double2 t = a[i];
-      a[i] = a[j];
-      a[j] = t;
-    }
-  }
-  __syncthreads();
-  for (int len = 2; len <= n; len <<= 1) {
-    int half = len >> 1, step = (n / len) * mult;
-    for (int b = threadIdx.x; b < n / 2; b += blockDim.x) {
-      int grp = b / half, j = b - grp * half;
-      int i = grp * len + j;
-      double2 t = tw[j * step];
-      if (sign < 0) t.y = -t.y;
-      double2 u = a[i], v = cmul<double>(a[i + half], t);
-      a[i] = make_double2(u.x + v.x, u.y + v.y);
-      a[i + half] = make_double2(u.x - v.x, u.y - v.y);
-    }
-    __syncthreads();
-  }
-}
-
-// Derivative in Fourier space: c_k -> i k c_k / n for |k| < n/2, Nyquist and mean zeroed
-// (FDIFFF, dcfft.f:1395-1425).
-__device__ void spectral_deriv(double2* a, int n) {
-  double inv = 1.0 / (double)n;
-  for (int m = threadIdx.x; m < n; m += blockDim.x) {
-    int k = (m <= n / 2) ? m : m - n;
-    if (m == n / 2 || m == 0) {
-      a[m] = make_double2(0.0, 0.0);
-    } else {
-      double2 c = a[m];
-      double f = (double)k * inv;
-      a[m] = make_double2(-f * c.y, f * c.x);
-    }
-  }
-  __syncthreads();
-}
 
 // FDIFFF of each drop's complex samples.
 __global__ void k_fdiff(const int* __restrict__ start, const double2* __restrict__ f,
@@ -104,23 +49,6 @@ __global__ void k_fdiff_real(const int* __restrict__ start, const double* __rest
   spectral_deriv(a, n);
   smem_fft(a, n, tw, n, +1);
   for (int i = threadIdx.x; i < n; i += blockDim.x) df[i0 + i] = a[i];
-}
-
-__device__ double block_sum_d(double v, double* red) {
-  v = warp_sum<double>(v);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (w == 0) {
-    r = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
-    r = warp_sum<double>(r);
-    if (l == 0) red[0] = r;
-  }
-  __syncthreads();
-  r = red[0];
-  __syncthreads();
-  return r;
 }
 
 // EXTRACTDAT per drop: zk = mean of z (its zero Fourier mode / n), z' = FDIFFF(z),
@@ -347,7 +275,7 @@ __global__ void k_velocity(int nbk, int k, const int* __restrict__ drop_of,
                            const double2* __restrict__ u, const double2* __restrict__ udot,
                            const double2* __restrict__ gw, const double2* __restrict__ zc,
                            const double2* __restrict__ zk, int any_zc, int iwall, double cap,
-                           double* __restrict__ un, double* __restrict__ fluxpart) {
+                           double* __restrict__ un, double* __restrict__ fluxpart, double2* __restrict__ gout) {
   __shared__ double red[32];
   double fl = 0.0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbk; t += gridDim.x * blockDim.x) {
@@ -382,6 +310,7 @@ __global__ void k_velocity(int nbk, int k, const int* __restrict__ drop_of,
       gr = cadd<double>(zphi, cadd<double>(cmul<double>(zz, cconj<double>(zphip)), cconj<double>(zpsi)));
     }
     g = cadd<double>(g, cadd<double>(gr, zck));
+    if (gout) gout[t] = g;
     double2 zvel = make_double2(g.y, -g.x);  // -i g
     double unt = zvel.x * zn.x + zvel.y * zn.y;  // Re(zvel conj(zn))
     un[t] = unt;
@@ -683,9 +612,10 @@ int eb_dirich_neu_map(eb_ctx* ctx, const double* u, double* phi, double* psi, do
 // INTERFACENEW with any internal precision (EB_FP64, EB_FP32 or EB_PREC_DF). zc_any: 1 if
 // some C_k is nonzero, 0 if all are, -1 to look (device zc: one readback). flux_async:
 // FLUX goes to ctx->h_flux without a synchronisation (the caller reads it after its own).
+// gout (device, optional) receives the full sum g of which Un = Re(-i g conj(zn)).
 static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* zc, double cap, double* un,
                                    double* flux, int prec, int mem, int zc_any = -1,
-                                   bool flux_async = false) {
+                                   bool flux_async = false, double2* gout = nullptr) {
   int nbk = ctx->nbk, k = ctx->k;
   cudaStream_t s = ctx->stream;
   EB_TRY(ctx->vin.ensure(sizeof(double2) * nbk));
@@ -724,7 +654,7 @@ static int interface_velocity_impl(eb_ctx* ctx, const double* u, const double* z
                                  ctx->dsda.as<double>(), ctx->kappa.as<double>(), ctx->hpt.as<double>(),
                                  ctx->ckern.as<double2>(), ud, ctx->vtmp.as<double2>(), ctx->vtmp2.as<double2>(),
                                  ctx->za.as<double2>(), ctx->zk.as<double2>(), any_zc, ctx->iwall, cap, und,
-                                 ctx->redpart.as<double>());
+                                 ctx->redpart.as<double>(), gout);
   eb_count_launch(ctx);
   k_sum_final<<<1, 32, 0, s>>>(nbv, ctx->redpart.as<double>(), ctx->redpart.as<double>() + 2047);
   eb_count_launch(ctx);
@@ -762,21 +692,6 @@ int eb_interface_velocity(eb_ctx* ctx, const double* u, const double* zc, double
 // space (zbond = 0), with everything resident on the GPU.
 // =================================================================================
 namespace {
-
-// Antiderivative in Fourier space (FOURINT, electric.f:1307-1331): c_k -> c_k/(i k),
-// mean and Nyquist dropped.
-__device__ void spectral_int(double2* a, int n) {
-  for (int m = threadIdx.x; m < n; m += blockDim.x) {
-    if (m == 0 || m == n / 2) {
-      a[m] = make_double2(0.0, 0.0);
-    } else {
-      double k = (double)((m <= n / 2) ? m : m - n);
-      double2 c = a[m];
-      a[m] = make_double2(c.y / k, -c.x / k);  // c / (i k)
-    }
-  }
-  __syncthreads();
-}
 
 // SETVELF (stokesbubb.f:4-135): surface tension -dz/(2|dz|) and the far field -zstr,
 // zstr = -conj(psi) with psi = -i cap z/2 (:61-68); for zbond != 0 the Bond-number term
@@ -948,17 +863,6 @@ int setvelf_dev(eb_ctx* ctx, const double* dphi, double cap, double e0, double2 
   return eb_check_launch(ctx, "setvelf");
 }
 
-__device__ __forceinline__ double powi25(double x) {
-  double r = 1.0;
-  int e = 25;
-  while (e > 0) {
-    if (e & 1) r *= x;
-    x *= x;
-    e >>= 1;
-  }
-  return r;
-}
-
 // EQUIT (electric.f:1270-1302), then the velocity of the nodes
 // (-Un i dz - T dz)/|dz|, Fourier filtered (FILTER, electric.f:1152-1187, with k/n
 // formed in single precision as the reference does) and transformed back
@@ -1043,8 +947,9 @@ struct StageSlots {
   int lap = -1, stokes = -1;
 };
 
+// gout (device, optional): INTERFACENEW's full velocity sum (interface_velocity_impl)
 int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
-            eb_stage_info* info, StageSlots* slots = nullptr) {
+            eb_stage_info* info, StageSlots* slots = nullptr, double2* gout = nullptr) {
   // zbond != 0: wall-bounded (READINI's iwall, electric.f:321-326), set before the
   // install so that the tree takes the wall
   const double2 zb = make_double2(m->zbond[0], m->zbond[1]);
@@ -1098,7 +1003,7 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   // synchronisation (the stage itself waits on the host only inside the tree builds
   // and the solves)
   EB_TRY(interface_velocity_impl(ctx, ctx->st_u.as<double>(), ctx->st_zc.as<double>(), m->cap, un, nullptr,
-                                 p64, EB_DEVICE, wall ? 1 : 0, true));
+                                 p64, EB_DEVICE, wall ? 1 : 0, true, gout));
   size_t sm2 = sizeof(double2) * ((size_t)nmax * 2 + (size_t)nmax / 2);
   EB_TRY(set_smem((const void*)k_equit_rkup, sm2));
   k_equit_rkup<<<k, SBS, sm2, s>>>(ctx->start.as<int>(), ctx->tha.as<double>(), un, ctx->dz.as<double2>(),
@@ -1178,6 +1083,30 @@ int check_model(const eb_model* m) {
 }
 
 }  // namespace
+
+int eb_stage_f_keep(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
+                    eb_stage_info* info, double2* gout) {
+  EB_TRY(check_model(m));
+  return stage_f(ctx, k, nd, rku, rkup, m, info, nullptr, gout);
+}
+
+int eb_pv_fine(eb_ctx* ctx, const double* ul) {
+  int nmax;
+  EB_TRY(check_pow2(ctx, nmax));
+  const int nbk = ctx->nbk;
+  cudaStream_t s = ctx->stream;
+  EB_TRY(ctx->vtmp.ensure(sizeof(double2) * nbk));
+  EB_TRY(ctx->pvz.ensure(sizeof(double2) * 2 * (size_t)nbk));
+  EB_TRY(ctx->pvq.ensure(sizeof(double2) * 2 * (size_t)nbk));
+  k_dtn_pre<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ul, ctx->dz.as<double2>(), ctx->vtmp.as<double2>());
+  eb_count_launch(ctx);
+  size_t sm = sizeof(double2) * (size_t)nmax * 3;
+  EB_TRY(set_smem((const void*)k_pv_interp, sm));
+  k_pv_interp<<<dim3(ctx->k, 3), SBS, sm, s>>>(ctx->start.as<int>(), ctx->z.as<double2>(), ctx->vtmp.as<double2>(),
+                                                ctx->pvz.as<double2>(), ctx->pvq.as<double2>(), nmax);
+  eb_count_launch(ctx);
+  return eb_check_launch(ctx, "pv fine points");
+}
 
 int eb_setvelf_bond(eb_ctx* ctx, const double* dphi_dn, double cap, double e0, const double* zbond,
                     const double* zc, double* rhs, int mem) {

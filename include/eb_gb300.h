@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EB_GB300_VERSION 4
+#define EB_GB300_VERSION 5
 
 /* Status codes. The reference prints and STOPs on FMM/GMRES errors
  * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
@@ -348,6 +348,44 @@ int eb_stokes_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln,
                             eb_solve_info* info, int mem);
 int eb_laplace_solve_adjoint(eb_ctx* ctx, int n, const double* rhs, double* soln, int mode,
                              eb_solve_info* info, int mem);
+
+/* Reverse mode through the time stepper: the adjoint of F and of the RK2 step with
+ * respect to the node positions, E0 and cap (no counterpart in the reference). Free
+ * space and one simulation only (model->zbond = 0, no batch; EB_ERR_ARG otherwise).
+ *
+ * eb_rk_f_vjp: rku_bar = v^T dF/drku (2 nbk doubles), and param_bar[0] += v^T dF/dE0,
+ * param_bar[1] += v^T dF/dcap (param_bar may be NULL). F is differentiated as the map
+ * with exact solves: the call reruns the stage at rku (its solves with model->mode and
+ * the context's gmres_tol), then solves with the transposed Stokes and Laplace operators
+ * (eb_stokes_solve_adjoint, eb_laplace_solve_adjoint) and adds the derivatives of every
+ * layer sum with respect to its targets, sources and weights (direct O(nbk^2) sums in
+ * FP64), of the spectral derivatives, interpolations and Fourier integrals (their
+ * transposes), and of the pointwise geometry. FILTER's zeroing of coefficient parts
+ * below 1e-13 is differentiated as the identity (it moves F by at most 1e-13 per
+ * coefficient; differences of F at steps above about 1e-7 see those parts move).
+ *
+ * eb_rk2_step_vjp: the transpose of one eb_rk2_step from the state ybar: rbar (in: dJ/dy
+ * after the step, out: dJ/dy before it), param_bar accumulated. The stage states are
+ * recomputed from ybar (checkpointed by the caller, one state per step).
+ *
+ * eb_deformation: value = sum over drops of (L - B)/(L + B), L and B the largest and
+ * smallest distance of a drop's nodes from its centroid (the mean of its nodes), the
+ * Taylor deformation; rku_bar (optional) = its gradient with respect to rku. */
+typedef struct eb_adjoint_info {
+  int lap_iters;        /* Krylov iterations of the forward Laplace solves           */
+  int stokes_iters;     /* Krylov iterations of the forward Stokes solves            */
+  int lap_adj_iters;    /* Krylov iterations of the transposed Laplace solves        */
+  int stokes_adj_iters; /* Krylov iterations of the transposed Stokes solves         */
+  int ierr;             /* 0 when all four solves converged, else the first nonzero IERR */
+} eb_adjoint_info;
+
+int eb_rk_f_vjp(eb_ctx* ctx, int k, const int* nd, const double* rku, const double* v,
+                const eb_model* model, double* rku_bar, double* param_bar, eb_adjoint_info* info,
+                int mem);
+int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* ybar, double* rbar,
+                    const eb_model* model, double* param_bar, eb_adjoint_info* info, int mem);
+int eb_deformation(eb_ctx* ctx, int k, const int* nd, const double* rku, double* value, double* rku_bar,
+                   int mem);
 
 /* Wall-bounded flow, the IFLAG2 = 1 branch of CADAPDR / CADAPMOD (COMMON /wallinfo/,
  * electric.f:55; cadapdrop.f:142-145, cadapdrop2.f:159-197 and 690-721, cadap2.f:1468-1586):

@@ -1,7 +1,8 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/eb_oracle.c into oracle/_build/libeb_oracle.so with gcc. The
-reference itself is Fortran 77 and no Fortran compiler exists on either machine,
+Compiles oracle/eb_oracle.c into oracle/_build/libeb_oracle.so with gcc, without
+fused multiply-add contraction (-ffp-contract=off), so that the x86 and Arm builds round
+alike (gcc contracts a*b+c on Arm by default). The reference itself is Fortran 77 and no Fortran compiler exists on either machine,
 so there is no oracle/_ref build of the reference sources.
 """
 import os
@@ -20,7 +21,7 @@ def build(force=False):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = ["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
+    cmd = ["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
            "-fcx-fortran-rules", "-o", tmp, src, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)

@@ -1174,6 +1174,7 @@ static void pvintev_impl(int k, const int* nd, const cplx* z, const cplx* ucmplx
   int nbk = 0, ndmax = 0;
   for (int b = 0; b < k; ++b) { nbk += nd[b]; ndmax = nd[b] > ndmax ? nd[b] : ndmax; }
   cplx* zsrc = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
+  cplx* ztgt = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
   cplx* qs = (cplx*)malloc(sizeof(cplx) * (size_t)nbk);
   cplx* u2 = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)ndmax);
   double* xc = (double*)malloc(sizeof(double) * (size_t)ndmax);
@@ -1191,14 +1192,16 @@ static void pvintev_impl(int k, const int* nd, const cplx* z, const cplx* ucmplx
     eb_or_finter(n, yc, y2);
     for (int i = 0; i < n; ++i) {
       zsrc[ist + i] = x2[2 * i + 1] + y2[2 * i + 1] * I;
+      ztgt[ist + i] = x2[2 * i] + y2[2 * i] * I;
       qs[ist + i] = u2[2 * i + 1] * hb;
     }
     ist += n;
   }
-  /* DAPIF2 runs on all 2N fine points; the even ones carry zero charge and the odd
-   * ones are never targets, so only odd-source -> original-node pairs contribute.
-   * The evaluation points are FINTER's even fine nodes, equal to z up to roundoff;
-   * the original nodes are used. */
+  /* DAPIF2 runs on all 2N fine points X2, Y2 (pv_integral.f:174-176); the even ones
+   * carry zero charge and the odd ones are never read, so only odd-source -> even-node
+   * pairs contribute. The field is read at the even fine nodes (CFIELD(2I-1),
+   * :192-201), FINTER's interpolated positions: they differ from the original nodes by
+   * FINTER's zeroed parts of modes nd/2-1 and nd/2 (pv_integral.f:235-236). */
   if (mode == EB_OR_CADAP) {
     /* DAPIF2 on all 2N fine points, TOL 1e-10 (pv_integral.f:176): charges on the odd
      * fine nodes, the field read at the even ones (the original nodes) */
@@ -1206,7 +1209,7 @@ static void pvintev_impl(int k, const int* nd, const cplx* z, const cplx* ucmplx
     cplx* qall = (cplx*)calloc(2 * (size_t)nbk, sizeof(cplx));
     cplx* fall = (cplx*)malloc(sizeof(cplx) * 2 * (size_t)nbk);
     for (int i = 0; i < nbk; ++i) {
-      zall[2 * i] = z[i];
+      zall[2 * i] = ztgt[i];
       zall[2 * i + 1] = zsrc[i];
       qall[2 * i + 1] = qs[i];
     }
@@ -1214,11 +1217,11 @@ static void pvintev_impl(int k, const int* nd, const cplx* z, const cplx* ucmplx
     for (int i = 0; i < nbk; ++i) cf[i] = fall[2 * i];
     free(zall); free(qall); free(fall);
   } else {
-    eb_or_cauchy_direct(nbk, z, nbk, zsrc, qs, 0, cf, nthreads);
+    eb_or_cauchy_direct(nbk, ztgt, nbk, zsrc, qs, 0, cf, nthreads);
   }
   const cplx z2pii = 1.0 / (2.0 * EB_PI * I);
   for (int i = 0; i < nbk; ++i) phicmplx[i] = -z2pii * cf[i];
-  free(zsrc); free(qs); free(u2); free(xc); free(yc); free(x2); free(y2); free(cf);
+  free(zsrc); free(ztgt); free(qs); free(u2); free(xc); free(yc); free(x2); free(y2); free(cf);
 }
 
 void eb_or_pvintev(int k, const int* nd, const cplx* z, const cplx* ucmplx, cplx* phicmplx,

@@ -7,6 +7,11 @@ both sides solve to ||b - A x|| / ||b|| <= 1e-14 and the oracle applies the oper
 exact O(N^2) direct summation (SOLVEI's GMRES, stokesbubb.f:294-415, and SOLVE_LAPL's,
 laplace.f:335-425, with x0 = b; INTERFACENEW, electric.f:791-912).
 
+Iteration counts are compared at DGMRES's own tolerance 1e-10 (within one of the
+oracle's): at 1e-14 the last iterations sit at the rounding floor, where the count follows
+the last bits of the arithmetic (the oracle's own x86 and Arm builds take 14 and 26
+iterations for the 3 x 128 Stokes solve).
+
 Native FP64 (the default plain path) is held to 1e-12. The double-float FP64-class
 operators (eb_opts.df64 = 1) round each pair term at about 2^-48 instead of 2^-53; their
 solves are held to 1e-11 (measured 1e-12 and below on these cases).
@@ -34,7 +39,9 @@ def relmax(a, b):
 @pytest.fixture(scope="module")
 def ctxs(gpu_ctx_factory):
     return {"native": gpu_ctx_factory(df64=-1, gmres_tol=TOL_SOLVE),
-            "df": gpu_ctx_factory(df64=1, gmres_tol=TOL_SOLVE)}
+            "df": gpu_ctx_factory(df64=1, gmres_tol=TOL_SOLVE),
+            "native10": gpu_ctx_factory(df64=-1, gmres_tol=1e-10),
+            "df10": gpu_ctx_factory(df64=1, gmres_tol=1e-10)}
 
 
 @pytest.fixture(scope="module")
@@ -53,9 +60,11 @@ def reference(oracle):
         zc = np.zeros(cfg.k, complex)
         rhs = oracle.setvelf(g, zc, 0j, 0.0, 0.5, dphi)
         us, sinfo = oracle.solvei(g, rhs, tol=TOL_SOLVE)
+        _, linfo10 = oracle.solve_lapl(g, rl, tol=1e-10)
+        _, sinfo10 = oracle.solvei(g, rhs, tol=1e-10)
         un, flux = oracle.interfacenew(g, ex["ckern"], zc, 0.0, us.view(np.complex128))
         out[name] = dict(cfg=cfg, ex=ex, rl=rl, ul=ul, linfo=linfo, rhs=rhs, us=us, sinfo=sinfo,
-                         un=un, zc=zc)
+                         un=un, zc=zc, linfo10=linfo10, sinfo10=sinfo10)
     return out
 
 
@@ -67,8 +76,11 @@ def test_laplace_density_per_solve(ctxs, reference, case, arith):
     ctx.extractdat(r["cfg"].nd, r["cfg"].rku())
     ul, info = ctx.solve_lapl(r["rl"], "fp64")
     assert info["ierr"] == 0 and info["err"] <= TOL_SOLVE
-    assert abs(info["iters"] - r["linfo"]["iters"]) <= 1
     assert relmax(ul, r["ul"]) < BAR[arith]
+    c10 = ctxs[arith + "10"]
+    c10.extractdat(r["cfg"].nd, r["cfg"].rku())
+    _, i10 = c10.solve_lapl(r["rl"], "fp64")
+    assert abs(i10["iters"] - r["linfo10"]["iters"]) <= 1
 
 
 @pytest.mark.parametrize("arith", ["native", "df"])
@@ -79,10 +91,13 @@ def test_stokes_density_and_velocity_per_solve(ctxs, reference, case, arith):
     ctx.extractdat(r["cfg"].nd, r["cfg"].rku())
     us, info = ctx.solvei(r["rhs"], "fp64")
     assert info["ierr"] == 0 and info["err"] <= TOL_SOLVE
-    assert abs(info["iters"] - r["sinfo"]["iters"]) <= 1
     assert relmax(us, r["us"]) < BAR[arith]
     un, _ = ctx.interfacenew(us.view(np.complex128), r["zc"], cap=0.0)
     assert relmax(un, r["un"]) < BAR[arith]
+    c10 = ctxs[arith + "10"]
+    c10.extractdat(r["cfg"].nd, r["cfg"].rku())
+    _, i10 = c10.solvei(r["rhs"], "fp64")
+    assert abs(i10["iters"] - r["sinfo10"]["iters"]) <= 1
 
 
 @pytest.mark.parametrize("case", list(CASES))
