@@ -535,6 +535,56 @@ def run_gpu(args, rank, world, local):
                                               for c in btune["candidates"]}}}
     bctx.close()
 
+    # the gradient workload (16 drops x 512, radii U[0.6, 1], seed 5): J = the summed
+    # Taylor deformation (L - B)/(L + B) after 50 RK2 steps (dt = 1e-3, E0 = 0.5, plain
+    # FP64, GMRES 1e-10), and dJ/dy0, dJ/dE0, dJ/dcap by reverse mode (checkpointed states,
+    # hand-written adjoint kernels, transposed solves); wall time of the whole gradient,
+    # host state. Checked against central differences (step 1e-4) of the forward steps
+    # along E0 and along a smooth node displacement (drop modes 1 to 5).
+    gcfg = configs.gradient_drops()
+    gsteps, gdt, ge0 = 50, 1e-3, 0.5
+    gctx = Context(device=local, graphs=graphs)
+    gctx.set_stream(stream.cuda_stream)
+    gy0 = gcfg.rku()
+    gctx.rk2_gradient(gcfg.nd, gdt, gy0, 1, e0=ge0)  # warm-up (allocations, graphs)
+    torch.cuda.synchronize()
+    t0g = time.perf_counter()
+    grad = gctx.rk2_gradient(gcfg.nd, gdt, gy0, gsteps, e0=ge0)
+    torch.cuda.synchronize()
+    grad_s = time.perf_counter() - t0g
+
+    def g_loss(yv, e):
+        yv = yv.copy()
+        for _ in range(gsteps):
+            gctx.rk2(gcfg.nd, gdt, yv, e0=e)
+        return gctx.deformation(gcfg.nd, yv, grad=False)[0]
+
+    t0f = time.perf_counter()
+    g_loss(gy0, ge0)
+    fwd_s = time.perf_counter() - t0f
+    hfd = 1e-4
+    fd_e0 = (g_loss(gy0, ge0 + hfd) - g_loss(gy0, ge0 - hfd)) / (2 * hfd)
+    grng = np.random.default_rng(96)
+    dz_ = np.zeros(gcfg.nbk, complex)
+    for b in range(gcfg.k):
+        th = 2 * np.pi * np.arange(512) / 512
+        for m in range(1, 6):
+            ca, cb = grng.standard_normal(2) + 1j * grng.standard_normal(2)
+            dz_[512 * b:512 * (b + 1)] += ca * np.exp(1j * m * th) + cb * np.exp(-1j * m * th)
+    gd = np.stack([dz_.real, dz_.imag], 1).reshape(-1)
+    gd /= np.linalg.norm(gd)
+    fd_dir = (g_loss(gy0 + hfd * gd, ge0) - g_loss(gy0 - hfd * gd, ge0)) / (2 * hfd)
+    ad_dir = float(grad["y0"] @ gd)
+    gradient = {"workload": "gradient_drops_16x512 (seed 5), 50 RK2 steps, dt 1e-3, E0 0.5, plain FP64, GMRES 1e-10",
+                "loss": "sum over drops of (L - B)/(L + B)", "J": grad["J"],
+                "gradient_wall_s": grad_s, "forward_wall_s": fwd_s, "gradient_over_forward": grad_s / fwd_s,
+                "dJ_dE0": grad["e0"], "dJ_dcap": grad["cap"], "dJ_dy0_norm": float(np.linalg.norm(grad["y0"])),
+                "fd_check_h": hfd,
+                "dJ_dE0_vs_central_difference_rel": abs(grad["e0"] - fd_e0) / abs(fd_e0),
+                "smooth_direction_vs_central_difference_rel": abs(ad_dir - fd_dir) / abs(fd_dir),
+                "solves": grad["info"]}
+    gctx.close()
+
     # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
     big = configs.large_drops()
     gb = ctx.extractdat(big.nd, big.rku())
@@ -675,6 +725,7 @@ def run_gpu(args, rank, world, local):
         "rk2": rk,
         "single_drop": single_fp64,
         "uneven": uneven,
+        "gradient": gradient,
         "large": large,
     }
     if rank == 0:

@@ -12,8 +12,9 @@
 //   k_aj_rkup       FILTER (its 1e-13 zeroing passed through), the node velocity
 //                   -(Un i dz + T dz)/|dz| and EQUIT -> dz, |dz|, tha, Un
 //   k_aj_vel_local  INTERFACENEW's pointwise terms and the transpose of udot = D u
-//   k_aj_stokes_*   every Stokes sum's derivative with respect to targets, sources and
-//                   charges (direct O(N^2), a block per target or per source)
+//   k_aj_stokes_*   the Stokes sums' derivatives with respect to targets, sources and
+//                   charges (direct O(N^2), a block per target or per source; the
+//                   target side of both sums in one pass after the transposed solve)
 //   (solve)         lambda = A_S^-T ubar: eb_stokes_solve_adjoint
 //   k_aj_op_local   FASMVP's drop sums (pk, za) and self terms at the density u, with
 //                   cotangent -lambda; the Stokes sums follow with the same cotangent
@@ -225,15 +226,17 @@ __global__ void k_aj_charges(int nbk, const double2* __restrict__ dens, const do
   qb[t] = c0 * (u * cj(d) - cj(u) * d);
 }
 
-// Target side of a Stokes sum's derivative, gradw_t = sum_{j != t} qa_j/D + s conj(qb_j/D)
-// - s D conj(qa_j/D^2), D = z_j - z_t: zb_t -= G_t (-Ta - s Tb) + conj(G_t) (2 s Tc - s Td),
-// Ta = sum conj(qa/D^2), Tb = sum qa/D^2, Tc = sum conj(qa) D conj(1/D)^3,
-// Td = sum conj(qb/D^2); the cotangent of gradw_t is gs G_t.
-template <int SIG>
+// Target side of the derivatives of the two Stokes sums of the adjoint at the density u,
+// gradw_t = sum_{j != t} qa_j/D + s conj(qb_j/D) - s D conj(qa_j/D^2), D = z_j - z_t, with
+// s = +1 (INTERFACENEW, cotangent G1) and s = -1 (FASMVP, cotangent -G2 = -lambda): the
+// sums Ta = sum conj(qa/D^2), Tb = sum qa/D^2, Tc = sum conj(qa) D conj(1/D)^3 and
+// Td = sum conj(qb/D^2) do not depend on s or the cotangent, so one pass serves both:
+// zb_t -= G (-Ta - s Tb) + conj(G) (2 s Tc - s Td) for each (s, G).
 __global__ void __launch_bounds__(PBS) k_aj_stokes_tgt(int nbk, const double2* __restrict__ z,
                                                        const double2* __restrict__ qa,
                                                        const double2* __restrict__ qb,
-                                                       const double2* __restrict__ G, double gs,
+                                                       const double2* __restrict__ G1,
+                                                       const double2* __restrict__ G2,
                                                        double2* __restrict__ zb) {
   __shared__ double red[8 * 32];
   const int t = blockIdx.x;
@@ -252,14 +255,14 @@ __global__ void __launch_bounds__(PBS) k_aj_stokes_tgt(int nbk, const double2* _
   double v[8] = {Ta.x, Ta.y, Tb.x, Tb.y, Tc.x, Tc.y, Td.x, Td.y};
   block_sums<8>(v, red);
   if (threadIdx.x == 0) {
-    const double s = (double)SIG;
     Ta = cmk2(v[0], v[1]);
     Tb = cmk2(v[2], v[3]);
     Tc = cmk2(v[4], v[5]);
     Td = cmk2(v[6], v[7]);
-    const double2 g = gs * G[t];
-    const double2 r = g * (-Ta - s * Tb) + cj(g) * ((2.0 * s) * Tc - s * Td);
-    zb[t] = zb[t] - r;
+    const double2 g1 = G1[t], g2 = -G2[t];
+    const double2 r1 = g1 * (-Ta - Tb) + cj(g1) * (2.0 * Tc - Td);
+    const double2 r2 = g2 * (Tb - Ta) + cj(g2) * (Td - 2.0 * Tc);
+    zb[t] = zb[t] - r1 - r2;
   }
 }
 
@@ -836,9 +839,8 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   k_aj_vel_local<<<k, SBS, sm1, s>>>(st, z, dz, ds, ka, hp, ck, u, un, B.gw, B.unb, m->cap, B.gwb, B.uB, B.kb,
                                      B.ckb, B.zb, B.dzb, B.sb, part, nmax);
   k_aj_charges<<<nblk(nbk, 256), 256, 0, s>>>(nbk, u, dz, hp, B.qa, B.qb);
-  k_aj_stokes_tgt<1><<<nbk, PBS, 0, s>>>(nbk, z, B.qa, B.qb, B.gwb, 1.0, B.zb);
   k_aj_stokes_src<1, true><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.gwb, 1.0, B.zb, B.dzb, B.uB);
-  ctx->launches += 5;
+  ctx->launches += 4;
   EB_TRY(eb_check_launch(ctx, "adjoint: velocity"));
   // Stokes solve: lambda = A_S^-T ubar
   eb_solve_info ai{};
@@ -847,7 +849,8 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   if (info) info->stokes_adj_iters += ai.iters;
   note_ierr(info, ai.ierr);
   k_aj_op_local<<<k, SBS, 0, s>>>(st, z, dz, ds, ka, hp, zk, u, B.lam, B.zb, B.dzb, B.sb, B.kb, B.zkb);
-  k_aj_stokes_tgt<-1><<<nbk, PBS, 0, s>>>(nbk, z, B.qa, B.qb, B.lam, -1.0, B.zb);
+  // the target side of both Stokes sums (INTERFACENEW's and FASMVP's) in one pass
+  k_aj_stokes_tgt<<<nbk, PBS, 0, s>>>(nbk, z, B.qa, B.qb, B.gwb, B.lam, B.zb);
   k_aj_stokes_src<-1, false><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.lam, -1.0, B.zb, B.dzb, nullptr);
   const double alpha_c = 2.0 * EB_PI * (double)(nd[k - 1] - 1) / (double)nd[k - 1];
   k_aj_setvelf<<<k, SBS, sm1, s>>>(st, z, dz, ds, dphi, B.lam, m->e0, m->cap, alpha_c, B.dzb, B.sb, B.zb, B.dphib,

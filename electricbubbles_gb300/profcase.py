@@ -18,6 +18,9 @@ Stages (all by default), on the 64-drop x 512-node workload unless named otherwi
            1,024 points)
   batchloop one FP32-refined RK2 step of 64 of the uneven simulations as one batch with
            the GMRES loops driven from the host (the batched Arnoldi kernels as launches)
+  vjp      one adjoint of F (eb_rk_f_vjp) on the 16-drop x 512-node gradient workload,
+           plain FP64 with the GMRES loops driven from the host: the stage's forward rerun,
+           the transposed solves and the adjoint kernels
 
 Each stage runs once; the device holds well under 1 GB. Prints "ok" at the end.
 """
@@ -105,9 +108,17 @@ def stage_batchloop():
     ctx.rk2(nd, 1e-3, y, mode="fp32_refined")
 
 
+def stage_vjp():
+    cfg = configs.gradient_drops()
+    ctx = Context(graphs=-1)
+    v = np.random.default_rng(1).standard_normal(2 * cfg.nbk)
+    ctx.f_vjp(cfg.nd, cfg.rku(), v, e0=0.5)
+    ctx.close()
+
+
 STAGES = {"tree": stage_tree, "solve": stage_solve, "apply": stage_apply, "rk2": stage_rk2,
           "batch": stage_batch, "wall": stage_wall, "lapsolve": stage_lapsolve, "single": stage_single,
-          "batchloop": stage_batchloop}
+          "batchloop": stage_batchloop, "vjp": stage_vjp}
 
 
 def main(argv):
