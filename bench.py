@@ -575,6 +575,13 @@ def run_gpu(args, rank, world, local):
     gd /= np.linalg.norm(gd)
     fd_dir = (g_loss(gy0 + hfd * gd, ge0) - g_loss(gy0 - hfd * gd, ge0)) / (2 * hfd)
     ad_dir = float(grad["y0"] @ gd)
+    # the same gradient with FP32-refined forward and transposed solves
+    gctx.rk2_gradient(gcfg.nd, gdt, gy0, 1, e0=ge0, mode="fp32_refined")
+    torch.cuda.synchronize()
+    t0g = time.perf_counter()
+    grad32 = gctx.rk2_gradient(gcfg.nd, gdt, gy0, gsteps, e0=ge0, mode="fp32_refined")
+    torch.cuda.synchronize()
+    grad32_s = time.perf_counter() - t0g
     gradient = {"workload": "gradient_drops_16x512 (seed 5), 50 RK2 steps, dt 1e-3, E0 0.5, plain FP64, GMRES 1e-10",
                 "loss": "sum over drops of (L - B)/(L + B)", "J": grad["J"],
                 "gradient_wall_s": grad_s, "forward_wall_s": fwd_s, "gradient_over_forward": grad_s / fwd_s,
@@ -582,7 +589,11 @@ def run_gpu(args, rank, world, local):
                 "fd_check_h": hfd,
                 "dJ_dE0_vs_central_difference_rel": abs(grad["e0"] - fd_e0) / abs(fd_e0),
                 "smooth_direction_vs_central_difference_rel": abs(ad_dir - fd_dir) / abs(fd_dir),
-                "solves": grad["info"]}
+                "solves": grad["info"],
+                "fp32_refined": {"gradient_wall_s": grad32_s,
+                                 "dJ_dy0_rel_vs_fp64": float(np.linalg.norm(grad32["y0"] - grad["y0"])
+                                                             / np.linalg.norm(grad["y0"])),
+                                 "dJ_dE0_rel_vs_fp64": abs(grad32["e0"] - grad["e0"]) / abs(grad["e0"])}}
     gctx.close()
 
     # the 1,024 x 1,024 workload (N = 1,048,576): FMM Mpts/s and one full solve per mode
