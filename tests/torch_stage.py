@@ -16,6 +16,7 @@ import numpy as np
 import torch
 
 PI = math.pi
+DEV = "cpu"  # the device of the tensors the helpers create (set by f_vjp)
 
 
 def _fft(x):
@@ -27,7 +28,7 @@ def _bfft(x):
 
 
 def _wavenum(n):
-    m = torch.arange(n, dtype=torch.float64)
+    m = torch.arange(n, dtype=torch.float64, device=DEV)
     k = torch.where(m <= n // 2, m, m - n)
     k[n // 2] = 0.0
     return k
@@ -58,8 +59,8 @@ def finterc(f):
     """FINTERC (pv_integral.f:276-328): complex samples n -> 2n, Nyquist dropped."""
     n = f.shape[-1]
     c = _fft(f)
-    c = torch.cat([c[: n // 2], torch.zeros(1, dtype=c.dtype), c[n // 2 + 1:]])
-    w = torch.cat([c[: n // 2 + 1], torch.zeros(n, dtype=c.dtype), c[n // 2 + 1:]])
+    c = torch.cat([c[: n // 2], torch.zeros(1, dtype=c.dtype, device=DEV), c[n // 2 + 1:]])
+    w = torch.cat([c[: n // 2 + 1], torch.zeros(n, dtype=c.dtype, device=DEV), c[n // 2 + 1:]])
     return _bfft(w / n)
 
 
@@ -71,7 +72,7 @@ def finter(x):
     ny = n // 2
     c = torch.cat([c[: ny - 1], c[ny - 1: ny].real.to(torch.complex128),
                    1j * c[ny: ny + 1].imag, c[ny + 1:]])
-    w = torch.cat([c[: ny + 1], torch.zeros(n, dtype=c.dtype), c[ny + 1:]])
+    w = torch.cat([c[: ny + 1], torch.zeros(n, dtype=c.dtype, device=DEV), c[ny + 1:]])
     return _bfft(w / n).real
 
 
@@ -84,13 +85,13 @@ def filter_(c):
     m = np.arange(n)
     i = np.where(m <= h, m, n - m)
     ratio = (i.astype(np.float32) / np.float32(h)).astype(np.float64)
-    sig = torch.tensor(np.exp(-10.0 * ratio ** 25))
+    sig = torch.tensor(np.exp(-10.0 * ratio ** 25), device=DEV)
     v = c * sig
     re, im = v.real, v.imag
     re = re + (torch.where(re.abs() < 1e-13, torch.zeros_like(re), re) - re).detach()
     im = im + (torch.where(im.abs() < 1e-13, torch.zeros_like(im), im) - im).detach()
     out = torch.complex(re, im)
-    out = torch.cat([out[:h], torch.zeros(1, dtype=out.dtype), out[h + 1:]])
+    out = torch.cat([out[:h], torch.zeros(1, dtype=out.dtype, device=DEV), out[h + 1:]])
     return out
 
 
@@ -117,16 +118,16 @@ def extractdat(nd, z):
 
 
 def point_h(nd):
-    return torch.tensor(np.concatenate([np.full(n, 2.0 * PI / n) for n in nd]))
+    return torch.tensor(np.concatenate([np.full(n, 2.0 * PI / n) for n in nd]), device=DEV)
 
 
 def drop_index(nd):
-    return torch.tensor(np.concatenate([np.full(n, b) for b, n in enumerate(nd)]))
+    return torch.tensor(np.concatenate([np.full(n, b) for b, n in enumerate(nd)]), device=DEV)
 
 
 def _offdiag_inv(zt, zs):
     d = zt[:, None] - zs[None, :]
-    eye = torch.eye(d.shape[0], dtype=torch.bool)
+    eye = torch.eye(d.shape[0], dtype=torch.bool, device=DEV)
     d = torch.where(eye, torch.ones_like(d), d)
     return torch.where(eye, torch.zeros_like(d), 1.0 / d)
 
@@ -146,7 +147,7 @@ def stokes_pq(z, dz, h, sign):
     c0 = h / (2 pi i), as gradw = P dens + Q conj(dens)."""
     n = z.shape[0]
     D = z[None, :] - z[:, None]
-    eye = torch.eye(n, dtype=torch.bool)
+    eye = torch.eye(n, dtype=torch.bool, device=DEV)
     Ds = torch.where(eye, torch.ones_like(D), D)
     c0 = (h / (2j * PI))[None, :]
     dzj = dz[None, :]
@@ -160,7 +161,7 @@ def _real_matrix(P, Q):
     """The real 2n x 2n matrix (interleaved Re/Im) of dens -> P dens + Q conj(dens)."""
     A, B = P + Q, P - Q
     n = P.shape[0]
-    R = torch.zeros(2 * n, 2 * n, dtype=torch.float64)
+    R = torch.zeros(2 * n, 2 * n, dtype=torch.float64, device=DEV)
     R[0::2, 0::2] = A.real
     R[0::2, 1::2] = -B.imag
     R[1::2, 0::2] = A.imag
@@ -253,14 +254,20 @@ def deformation(nd, y):
     return tot
 
 
-def f_vjp(nd, y, v, e0, cap):
-    """(F(y), v^T dF/dy, v^T dF/dE0, v^T dF/dcap) by autograd."""
-    yt = torch.tensor(np.asarray(y, dtype=np.float64), requires_grad=True)
-    e0t = torch.tensor(float(e0), dtype=torch.float64, requires_grad=True)
-    capt = torch.tensor(float(cap), dtype=torch.float64, requires_grad=True)
-    f = f_stage(nd, yt, e0t, capt)
-    gy, ge, gc = torch.autograd.grad(f, (yt, e0t, capt), torch.tensor(np.asarray(v, dtype=np.float64)))
-    return f.detach().numpy(), gy.numpy(), float(ge), float(gc)
+def f_vjp(nd, y, v, e0, cap, device="cpu"):
+    """(F(y), v^T dF/dy, v^T dF/dE0, v^T dF/dcap) by autograd, on `device`."""
+    global DEV
+    DEV = device
+    try:
+        yt = torch.tensor(np.asarray(y, dtype=np.float64), requires_grad=True, device=device)
+        e0t = torch.tensor(float(e0), dtype=torch.float64, requires_grad=True, device=device)
+        capt = torch.tensor(float(cap), dtype=torch.float64, requires_grad=True, device=device)
+        f = f_stage(nd, yt, e0t, capt)
+        gy, ge, gc = torch.autograd.grad(f, (yt, e0t, capt),
+                                         torch.tensor(np.asarray(v, dtype=np.float64), device=device))
+        return f.detach().cpu().numpy(), gy.cpu().numpy(), float(ge), float(gc)
+    finally:
+        DEV = "cpu"
 
 
 def rk2_gradient(nd, dt, y0, steps, e0, cap):
@@ -276,4 +283,4 @@ def rk2_gradient(nd, dt, y0, steps, e0, cap):
         y = y + 0.5 * dt * k1 + 0.5 * dt * k2
     J = deformation(nd, y)
     gy, ge, gc = torch.autograd.grad(J, (yt, e0t, capt))
-    return float(J), gy.numpy(), float(ge), float(gc)
+    return float(J.detach()), gy.numpy(), float(ge), float(gc)
