@@ -263,6 +263,7 @@ int eb_ctx_destroy(eb_ctx* ctx) {
   if (ctx->b_host_act) cudaFreeHost(ctx->b_host_act);
   if (ctx->h_flux) cudaFreeHost(ctx->h_flux);
   if (ctx->h_defer) cudaFreeHost(ctx->h_defer);
+  if (ctx->h_spec) cudaFreeHost(ctx->h_spec);
   if (ctx->h_bad) cudaFreeHost(ctx->h_bad);
   for (GmGraph& g : ctx->bgraph) g.destroy();
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

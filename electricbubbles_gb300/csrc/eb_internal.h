@@ -287,6 +287,7 @@ struct eb_ctx {
   bool defer = false;
   int ndefer = 0;                  // slots used by this call
   unsigned char* h_defer = nullptr; // page-locked: EB_DEFER_SLOTS control-block heads
+  unsigned char* h_spec = nullptr;  // page-locked: the heads of refinement steps 1 and 2 (one wait)
   long long defer_body[8] = {0};    // kernel launches per Arnoldi step of each slot's graph
   DevBuf d_bad;                    // int: a direct tree's non-finite node (deferred)
   int* h_bad = nullptr;            // page-locked copy of d_bad

@@ -711,6 +711,21 @@ __global__ void k_gm_axpy(int n, const GmCtl* __restrict__ c, const double* __re
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += d[i];
 }
 
+// The inner tolerance of refinement step 2 from step 1's control block, formed as
+// inner_tolerance() forms it on the host (the same operations, so the same value). A
+// step 1 that ended the solve (converged, b = 0, a non-finite value) makes step 2 a
+// no-op: tolerance 1e300, so no inner iteration and x += 0.
+__global__ void k_gm_next_tol(const GmCtl* __restrict__ c, double* __restrict__ tol_out, double inner_tol,
+                              double gmres_tol) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 1e300;
+  if (c->status == EB_OK && !c->zero_x) {
+    const double err = sqrt(fmax(c->rnrm2, 0.0)) / c->bnrm;
+    if (err > gmres_tol) t = fmin(inner_tol, fmax(0.1 * inner_tol, 0.5 * gmres_tol / err));
+  }
+  *tol_out = t;
+}
+
 enum { GM_PLAIN = 0, GM_REFINE = 1 };
 constexpr int GM_BUILD_FAILED = -100;  // internal: fall back to the host-driven loop
 
@@ -820,8 +835,11 @@ GmGraph* find_graph(eb_ctx* ctx, const unsigned long long* key) {
   return nullptr;
 }
 
-// Runs one graph launch (building it on first use) and reads the control block back.
-int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
+// Runs one graph launch (building it on first use) and reads the control block back:
+// into head after a synchronisation; with wait = false into head (page-locked) without
+// one, the caller synchronising and adding the launches (*base + *per_step * lgmr).
+int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head, bool wait = true,
+              long long* base = nullptr, long long* per_step = nullptr) {
   unsigned long long key[8];
   auto fill_key = [&](unsigned long long epoch) {
     double t1 = ctx->opts.gmres_tol, t2 = ctx->opts.inner_tol;
@@ -870,6 +888,11 @@ int run_graph(eb_ctx* ctx, int kind, op_fn op, int n, int maxl, GmCtl* head) {
     return EB_OK;
   }
   EB_CUDA_TRY(cudaMemcpyAsync(head, ctx->gCtl.p, GM_HEAD, cudaMemcpyDeviceToHost, s));
+  if (!wait) {
+    *base = G->n_pre + G->n_post;
+    *per_step = G->n_body;
+    return EB_OK;
+  }
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   ctx->launches += G->n_pre + G->n_post + G->n_body * (long long)head->lgmr;
   return EB_OK;
@@ -923,27 +946,28 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
   inf->ierr = 1;
   double bnrm = 0.0;
   double err_prev = 1.0;
-  for (int outer = 1; outer <= ctx->opts.max_outer; ++outer) {
+  // the host's part of refinement step `outer` once its control block is read: returns
+  // EB_OK with *done set when the solve ended, or an error
+  auto step_done = [&](int outer, const GmCtl& h, bool* done) -> int {
+    *done = false;
     inf->outer = outer;
-    const double itol = inner_tolerance(ctx, outer, err_prev);
-    EB_CUDA_TRY(cudaMemcpyAsync(ctx->gH.as<double>() + GM_TOL, &itol, sizeof(double), cudaMemcpyHostToDevice, s));
-    EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, &head));
-    if (head.status != EB_OK) {
+    if (h.status != EB_OK) {
       eb_set_last_error_msg("non-finite value in GMRES");
-      return head.status;
+      return h.status;
     }
-    inf->iters += head.iters;
-    inf->matvecs32 += head.lgmr;
+    inf->iters += h.iters;
+    inf->matvecs32 += h.lgmr;
     inf->matvecs64 += 1;
     if (outer == 1) {
-      bnrm = head.bnrm;  // the first inner right-hand side is b itself
-      if (head.zero_x) {
+      bnrm = h.bnrm;  // the first inner right-hand side is b itself
+      if (h.zero_x) {
         inf->err = 0.0;
         inf->ierr = 0;
-        break;
+        *done = true;
+        return EB_OK;
       }
     }
-    inf->err = std::sqrt(std::max(head.rnrm2, 0.0)) / bnrm;
+    inf->err = std::sqrt(std::max(h.rnrm2, 0.0)) / bnrm;
     err_prev = inf->err;
     if (!std::isfinite(inf->err)) {
       eb_set_last_error_msg("non-finite residual");
@@ -951,8 +975,45 @@ int solve_graph(eb_ctx* ctx, int n, op_fn op, int mode, int maxl, eb_solve_info*
     }
     if (inf->err <= ctx->opts.gmres_tol) {
       inf->ierr = 0;
-      break;
+      *done = true;
     }
+    return EB_OK;
+  };
+  int first = 1;
+  if (ctx->opts.max_outer >= 2) {
+    // steps 1 and 2 back to back with one wait: step 2's inner tolerance is formed on the
+    // device from step 1's residual (k_gm_next_tol), and a step 1 that ended the solve
+    // leaves step 2 nothing to do
+    if (!ctx->h_spec) EB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&ctx->h_spec), 2 * GM_HEAD));
+    GmCtl* h1 = reinterpret_cast<GmCtl*>(ctx->h_spec);
+    GmCtl* h2 = reinterpret_cast<GmCtl*>(ctx->h_spec + GM_HEAD);
+    const double itol = inner_tolerance(ctx, 1, err_prev);
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->gH.as<double>() + GM_TOL, &itol, sizeof(double), cudaMemcpyHostToDevice, s));
+    long long b1 = 0, p1 = 0, b2 = 0, p2 = 0;
+    EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, h1, false, &b1, &p1));
+    k_gm_next_tol<<<1, 32, 0, s>>>(ctx->gCtl.as<GmCtl>(), ctx->gH.as<double>() + GM_TOL, ctx->opts.inner_tol,
+                                   ctx->opts.gmres_tol);
+    eb_count_launch(ctx);
+    EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, h2, false, &b2, &p2));
+    EB_CUDA_TRY(cudaStreamSynchronize(s));
+    GmCtl hd1, hd2;
+    memcpy(&hd1, h1, GM_HEAD);
+    memcpy(&hd2, h2, GM_HEAD);
+    ctx->launches += b1 + p1 * (long long)hd1.lgmr + b2 + p2 * (long long)hd2.lgmr;
+    bool done = false;
+    EB_TRY(step_done(1, hd1, &done));
+    if (done) return EB_OK;
+    EB_TRY(step_done(2, hd2, &done));
+    if (done) return EB_OK;
+    first = 3;
+  }
+  for (int outer = first; outer <= ctx->opts.max_outer; ++outer) {
+    const double itol = inner_tolerance(ctx, outer, err_prev);
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->gH.as<double>() + GM_TOL, &itol, sizeof(double), cudaMemcpyHostToDevice, s));
+    EB_TRY(run_graph(ctx, GM_REFINE, op, n, maxl, &head));
+    bool done = false;
+    EB_TRY(step_done(outer, head, &done));
+    if (done) break;
   }
   return EB_OK;
 }
