@@ -37,7 +37,7 @@ class Opts(ctypes.Structure):
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
                 ("device", ctypes.c_int), ("graphs", ctypes.c_int), ("df64", ctypes.c_int),
                 ("resid_df", ctypes.c_int), ("m2l_tc", ctypes.c_int),
-                ("lap_deflate", ctypes.c_int), ("direct_max", ctypes.c_int)]
+                ("lap_deflate", ctypes.c_int), ("direct_max", ctypes.c_int), ("adj_df", ctypes.c_int)]
 
 
 class TuneInfo(ctypes.Structure):

@@ -65,7 +65,7 @@ class Context:
 
     def __init__(self, p64=0, p32=0, leaf64=0, leaf_cap=0, tol64=0.0, tol32=0.0, maxl=0,
                  gmres_tol=0.0, inner_tol=0.0, max_outer=0, device=0, graphs=0, df64=0,
-                 resid_df=0, m2l_tc=0, lap_deflate=0, direct_max=0):
+                 resid_df=0, m2l_tc=0, lap_deflate=0, direct_max=0, adj_df=0):
         self._lib = _lib.load()
         o = Opts()
         self._lib.eb_opts_default(ctypes.byref(o))
@@ -74,7 +74,7 @@ class Context:
                         ("gmres_tol", gmres_tol), ("inner_tol", inner_tol),
                         ("max_outer", max_outer), ("graphs", graphs), ("df64", df64),
                         ("resid_df", resid_df), ("m2l_tc", m2l_tc),
-                        ("lap_deflate", lap_deflate), ("direct_max", direct_max)):
+                        ("lap_deflate", lap_deflate), ("direct_max", direct_max), ("adj_df", adj_df)):
             if v:
                 setattr(o, name, v)
         o.device = device

@@ -177,6 +177,7 @@ void eb_opts_default(eb_opts* o) {
   o->m2l_tc = -1;
   o->lap_deflate = -1;
   o->direct_max = 1024;
+  o->adj_df = 1;
 }
 
 int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
@@ -210,6 +211,7 @@ int eb_ctx_create(eb_ctx** out, const eb_opts* opts) {
     if (o.m2l_tc == 0) o.m2l_tc = d.m2l_tc;
     if (o.lap_deflate == 0) o.lap_deflate = d.lap_deflate;
     if (o.direct_max == 0) o.direct_max = d.direct_max;
+    if (o.adj_df == 0) o.adj_df = d.adj_df;
     c->opts = o;
   }
   if (c->opts.device < 0 || c->opts.device >= ndev) {

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <vector>
 
+#include "eb_df.cuh"
 #include "eb_fft.cuh"
 #include "eb_internal.h"
 
@@ -728,6 +729,203 @@ __global__ void k_deformation(const int* __restrict__ start, const double* __res
   }
 }
 
+// ---------------------------------------------------------------------------------
+// The pair sums in double-float arithmetic (eb_opts.adj_df): the same sums as the FP64
+// kernels above, each pair's terms in about 48 bits on the FP32 pipes (GB300 issues some
+// 60 times more FP32 than FP64 operations), positions relative to the first node (the
+// nearest pairs then keep ~1e-11 relative), compensated accumulators; the sums are
+// finished in FP64 as above.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ cdf c4(float4 v) { return cdf{{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return cdf{dfl_sub(a.x, b.x), dfl_sub(a.y, b.y)}; }
+__device__ __forceinline__ cdf cdf_conj(cdf a) { return cdf{a.x, dfl_neg(a.y)}; }
+__device__ __forceinline__ cdf cdf_inv(cdf a) {
+  const dfl r = dfl_rcp(dfl_add(dfl_sqr(a.x), dfl_sqr(a.y)));
+  return cdf{dfl_mul(a.x, r), dfl_neg(dfl_mul(a.y, r))};
+}
+__device__ __forceinline__ cdf cdf_scale(dfl s, cdf a) { return cdf{dfl_mul(s, a.x), dfl_mul(s, a.y)}; }
+struct cacc {
+  dfacc x, y;
+};
+__device__ __forceinline__ void cacc_add(cacc& a, cdf v) {
+  acc_dfl(a.x, v.x);
+  acc_dfl(a.y, v.y);
+}
+__device__ __forceinline__ void cacc_put(const cacc& a, double* v) {
+  v[0] = (double)a.x.s + (double)a.x.c;
+  v[1] = (double)a.y.s + (double)a.y.c;
+}
+
+// out_i = the double-float form of in[i stride] - *shift (shift may be null)
+__global__ void k_df4(int n, const double2* __restrict__ in, int stride, const double2* __restrict__ shift,
+                      float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 v = in[(size_t)i * stride];
+  if (shift) {
+    v.x -= shift->x;
+    v.y -= shift->y;
+  }
+  const dfl a = dfl_from_double(v.x), b = dfl_from_double(v.y);
+  out[i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+}
+
+__global__ void k_df2(int n, const double* __restrict__ in, float2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const dfl a = dfl_from_double(in[i]);
+  out[i] = make_float2(a.hi, a.lo);
+}
+
+// k_aj_stokes_tgt in double-float (Ta = conj(Tb) is not summed separately)
+__global__ void __launch_bounds__(PBS) k_aj_stokes_tgt_df(int nbk, const float4* __restrict__ zd,
+                                                          const float4* __restrict__ qad,
+                                                          const float4* __restrict__ qbd,
+                                                          const double2* __restrict__ G1,
+                                                          const double2* __restrict__ G2,
+                                                          double2* __restrict__ zb) {
+  __shared__ double red[6 * 32];
+  const int t = blockIdx.x;
+  const cdf zt = c4(zd[t]);
+  cacc Tb{}, Tc{}, Td{};
+  for (int j = threadIdx.x; j < nbk; j += blockDim.x) {
+    if (j == t) continue;
+    const cdf D = cdf_sub(c4(zd[j]), zt);
+    const cdf iv = cdf_inv(D), iv2 = cdf_mul(iv, iv);
+    const cdf qa = c4(qad[j]);
+    cacc_add(Tb, cdf_mul(qa, iv2));
+    cacc_add(Td, cdf_conj(cdf_mul(c4(qbd[j]), iv2)));
+    cacc_add(Tc, cdf_mul(cdf_mul(cdf_conj(qa), D), cdf_conj(cdf_mul(iv2, iv))));
+  }
+  double v[6];
+  cacc_put(Tb, v);
+  cacc_put(Tc, v + 2);
+  cacc_put(Td, v + 4);
+  block_sums<6>(v, red);
+  if (threadIdx.x == 0) {
+    const double2 Tbv = cmk2(v[0], v[1]), Tcv = cmk2(v[2], v[3]), Tdv = cmk2(v[4], v[5]), Tav = cj(Tbv);
+    const double2 g1 = G1[t], g2 = -G2[t];
+    const double2 r1 = g1 * (-Tav - Tbv) + cj(g1) * (2.0 * Tcv - Tdv);
+    const double2 r2 = g2 * (Tbv - Tav) + cj(g2) * (Tdv - 2.0 * Tcv);
+    zb[t] = zb[t] - r1 - r2;
+  }
+}
+
+// k_aj_stokes_src in double-float; Gd = the double-float form of the cotangent, scaled
+// by gs in the FP64 finish
+template <int SIG, bool DENS>
+__global__ void __launch_bounds__(PBS) k_aj_stokes_src_df(int nbk, const float4* __restrict__ zd,
+                                                          const float4* __restrict__ Gd, double gs,
+                                                          const double2* __restrict__ dz,
+                                                          const double* __restrict__ hpt,
+                                                          const double2* __restrict__ dens,
+                                                          const double2* __restrict__ qa,
+                                                          const double2* __restrict__ qb,
+                                                          double2* __restrict__ zb, double2* __restrict__ dzb,
+                                                          double2* __restrict__ uB) {
+  __shared__ double red[12 * 32];
+  const int j = blockIdx.x;
+  const cdf zj = c4(zd[j]);
+  cacc Sa{}, Sb{}, Sc{}, Sq1{}, Sq2{}, Sd{};
+  for (int t = threadIdx.x; t < nbk; t += blockDim.x) {
+    if (t == j) continue;
+    const cdf D = cdf_sub(zj, c4(zd[t]));
+    const cdf iv = cdf_inv(D), iv2 = cdf_mul(iv, iv);
+    const cdf g = c4(Gd[t]);
+    const cdf ci2 = cdf_conj(iv2);
+    cacc_add(Sa, cdf_mul(g, ci2));
+    cacc_add(Sb, cdf_mul(g, iv2));
+    const cdf Dg = cdf_mul(D, cdf_conj(g));
+    cacc_add(Sc, cdf_mul(Dg, cdf_conj(cdf_mul(iv2, iv))));
+    cacc_add(Sq1, cdf_mul(g, cdf_conj(iv)));
+    cacc_add(Sq2, cdf_mul(Dg, ci2));
+    cacc_add(Sd, cdf_mul(g, iv));
+  }
+  double v[12];
+  cacc_put(Sa, v);
+  cacc_put(Sb, v + 2);
+  cacc_put(Sc, v + 4);
+  cacc_put(Sq1, v + 6);
+  cacc_put(Sq2, v + 8);
+  cacc_put(Sd, v + 10);
+  block_sums<12>(v, red);
+  if (threadIdx.x == 0) {
+    const double s = (double)SIG;
+    const double2 Sav = gs * cmk2(v[0], v[1]), Sbv = gs * cmk2(v[2], v[3]), Scv = gs * cmk2(v[4], v[5]);
+    const double2 Sq1v = gs * cmk2(v[6], v[7]), Sq2v = gs * cmk2(v[8], v[9]), Sdv = gs * cmk2(v[10], v[11]);
+    const double2 a = qa[j], bq = qb[j];
+    zb[j] = zb[j] + (-(cj(a) * Sav) - s * (a * Sbv) + (2.0 * s) * (cj(a) * Scv) - s * (cj(bq) * cj(Sbv)));
+    const double2 qab = Sq1v - s * Sq2v, qbb = s * cj(Sdv);
+    const double2 c0 = cmk2(0.0, -hpt[j] / (2.0 * EB_PI));
+    const double2 u = dens[j], d = dz[j];
+    dzb[j] = dzb[j] + (cj(c0 * u) * qab - (cj(c0) * u) * qbb + (c0 * u) * cj(qbb));
+    if (DENS) uB[j] = uB[j] + (cj(c0 * d) * qab + (cj(c0) * d) * qbb - (c0 * d) * cj(qbb));
+  }
+}
+
+// k_aj_cauchy_tgt in double-float
+template <bool SELF, bool ADD>
+__global__ void __launch_bounds__(PBS) k_aj_cauchy_tgt_df(int nt, const float4* __restrict__ ztd, int ns,
+                                                          const float4* __restrict__ zsd,
+                                                          const float4* __restrict__ qd,
+                                                          const double* __restrict__ x, double2 coef,
+                                                          double2* __restrict__ zb) {
+  __shared__ double red[2 * 32];
+  const int t = blockIdx.x;
+  const cdf z = c4(ztd[t]);
+  cacc A{};
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    if (SELF && j == t) continue;
+    const cdf iv = cdf_inv(cdf_sub(z, c4(zsd[j])));
+    cacc_add(A, cdf_mul(c4(qd[j]), cdf_mul(iv, iv)));
+  }
+  double v[2];
+  cacc_put(A, v);
+  block_sums<2>(v, red);
+  if (threadIdx.x == 0) {
+    const double2 r = cj(-cmk2(v[0], v[1])) * (x[t] * coef);
+    zb[t] = ADD ? zb[t] + r : r;
+  }
+}
+
+// k_aj_cauchy_src in double-float (xd: the double-float form of x)
+template <bool SELF, bool LAP>
+__global__ void __launch_bounds__(PBS) k_aj_cauchy_src_df(int nt, const float4* __restrict__ ztd, int ns,
+                                                          const float4* __restrict__ zsd,
+                                                          const float2* __restrict__ xd, double2 coef,
+                                                          const double2* __restrict__ q, int qs,
+                                                          const double* __restrict__ ul,
+                                                          const double* __restrict__ hpt,
+                                                          double2* __restrict__ zb, double2* __restrict__ dzb,
+                                                          double2* __restrict__ qsb, double2* __restrict__ zsb) {
+  __shared__ double red[4 * 32];
+  const int j = blockIdx.x;
+  const cdf zj = c4(zsd[j]);
+  cacc S1{}, S2{};
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    if (SELF && t == j) continue;
+    const cdf iv = cdf_conj(cdf_inv(cdf_sub(c4(ztd[t]), zj)));
+    const dfl xt = dfl{xd[t].x, xd[t].y};
+    cacc_add(S1, cdf_scale(xt, iv));
+    cacc_add(S2, cdf_scale(xt, cdf_mul(iv, iv)));
+  }
+  double v[4];
+  cacc_put(S1, v);
+  cacc_put(S2, v + 2);
+  block_sums<4>(v, red);
+  if (threadIdx.x == 0) {
+    const double2 qb = cmk2(v[0], v[1]) * coef;
+    const double2 zsbar = cj(q[(size_t)j * qs]) * (cmk2(v[2], v[3]) * coef);
+    if (LAP) {
+      zb[j] = zb[j] + zsbar;
+      dzb[j] = dzb[j] + (ul[j] * hpt[j]) * qb;
+    } else {
+      qsb[j] = qb;
+      zsb[j] = zsbar;
+    }
+  }
+}
+
 __global__ void k_axpby(int n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
                         double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -839,7 +1037,30 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   k_aj_vel_local<<<k, SBS, sm1, s>>>(st, z, dz, ds, ka, hp, ck, u, un, B.gw, B.unb, m->cap, B.gwb, B.uB, B.kb,
                                      B.ckb, B.zb, B.dzb, B.sb, part, nmax);
   k_aj_charges<<<nblk(nbk, 256), 256, 0, s>>>(nbk, u, dz, hp, B.qa, B.qb);
-  k_aj_stokes_src<1, true><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.gwb, 1.0, B.zb, B.dzb, B.uB);
+  // double-float pair sums: positions relative to the first node, charges and cotangents
+  const bool dfp = ctx->opts.adj_df > 0;
+  float4 *zd = nullptr, *qad = nullptr, *qbd = nullptr, *g1d = nullptr, *g2d = nullptr, *ptd = nullptr,
+         *psd = nullptr, *pqd = nullptr, *qld = nullptr;
+  float2* xd = nullptr;
+  const int nb = nblk(nbk, 256);
+  if (dfp) {
+    EB_TRY(ctx->aj_df.ensure(sizeof(float4) * 9 * (size_t)nbk + sizeof(float2) * (size_t)nbk));
+    float4* p4 = ctx->aj_df.as<float4>();
+    float4** c4s[] = {&zd, &qad, &qbd, &g1d, &g2d, &ptd, &psd, &pqd, &qld};
+    for (float4** q : c4s) {
+      *q = p4;
+      p4 += nbk;
+    }
+    xd = reinterpret_cast<float2*>(p4);
+    k_df4<<<nb, 256, 0, s>>>(nbk, z, 1, z, zd);
+    k_df4<<<nb, 256, 0, s>>>(nbk, B.qa, 1, nullptr, qad);
+    k_df4<<<nb, 256, 0, s>>>(nbk, B.qb, 1, nullptr, qbd);
+    k_df4<<<nb, 256, 0, s>>>(nbk, B.gwb, 1, nullptr, g1d);
+    k_aj_stokes_src_df<1, true><<<nbk, PBS, 0, s>>>(nbk, zd, g1d, 1.0, dz, hp, u, B.qa, B.qb, B.zb, B.dzb, B.uB);
+    ctx->launches += 4;
+  } else {
+    k_aj_stokes_src<1, true><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.gwb, 1.0, B.zb, B.dzb, B.uB);
+  }
   ctx->launches += 4;
   EB_TRY(eb_check_launch(ctx, "adjoint: velocity"));
   // Stokes solve: lambda = A_S^-T ubar
@@ -850,8 +1071,16 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   note_ierr(info, ai.ierr);
   k_aj_op_local<<<k, SBS, 0, s>>>(st, z, dz, ds, ka, hp, zk, u, B.lam, B.zb, B.dzb, B.sb, B.kb, B.zkb);
   // the target side of both Stokes sums (INTERFACENEW's and FASMVP's) in one pass
-  k_aj_stokes_tgt<<<nbk, PBS, 0, s>>>(nbk, z, B.qa, B.qb, B.gwb, B.lam, B.zb);
-  k_aj_stokes_src<-1, false><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.lam, -1.0, B.zb, B.dzb, nullptr);
+  if (dfp) {
+    k_df4<<<nb, 256, 0, s>>>(nbk, B.lam, 1, nullptr, g2d);
+    k_aj_stokes_tgt_df<<<nbk, PBS, 0, s>>>(nbk, zd, qad, qbd, B.gwb, B.lam, B.zb);
+    k_aj_stokes_src_df<-1, false><<<nbk, PBS, 0, s>>>(nbk, zd, g2d, -1.0, dz, hp, u, B.qa, B.qb, B.zb, B.dzb,
+                                                      nullptr);
+    eb_count_launch(ctx);
+  } else {
+    k_aj_stokes_tgt<<<nbk, PBS, 0, s>>>(nbk, z, B.qa, B.qb, B.gwb, B.lam, B.zb);
+    k_aj_stokes_src<-1, false><<<nbk, PBS, 0, s>>>(nbk, z, dz, hp, u, B.qa, B.qb, B.lam, -1.0, B.zb, B.dzb, nullptr);
+  }
   const double alpha_c = 2.0 * EB_PI * (double)(nd[k - 1] - 1) / (double)nd[k - 1];
   k_aj_setvelf<<<k, SBS, sm1, s>>>(st, z, dz, ds, dphi, B.lam, m->e0, m->cap, alpha_c, B.dzb, B.sb, B.zb, B.dphib,
                                    part, nmax);
@@ -864,9 +1093,20 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   const double2* pvq = ctx->pvq.as<double2>();
   const double2 cpv = make_double2(-1.0 / (2.0 * EB_PI), 0.0);
   // (evaluation points: the even fine nodes; sources and charges: the odd ones)
-  k_aj_cauchy_tgt<false, false><<<nbk, PBS, 0, s>>>(nbk, pvz, 2, nbk, pvz + 1, 2, pvq + 1, 2, B.psib, cpv, B.ztb);
-  k_aj_cauchy_src<false, false><<<nbk, PBS, 0, s>>>(nbk, pvz, 2, nbk, pvz + 1, 2, pvq + 1, 2, B.psib, cpv, nullptr,
-                                                    nullptr, nullptr, nullptr, B.qsb, B.zsb);
+  if (dfp) {
+    k_df4<<<nb, 256, 0, s>>>(nbk, pvz, 2, z, ptd);
+    k_df4<<<nb, 256, 0, s>>>(nbk, pvz + 1, 2, z, psd);
+    k_df4<<<nb, 256, 0, s>>>(nbk, pvq + 1, 2, nullptr, pqd);
+    k_df2<<<nb, 256, 0, s>>>(nbk, B.psib, xd);
+    k_aj_cauchy_tgt_df<false, false><<<nbk, PBS, 0, s>>>(nbk, ptd, nbk, psd, pqd, B.psib, cpv, B.ztb);
+    k_aj_cauchy_src_df<false, false><<<nbk, PBS, 0, s>>>(nbk, ptd, nbk, psd, xd, cpv, pvq + 1, 2, nullptr, nullptr,
+                                                         nullptr, nullptr, B.qsb, B.zsb);
+    ctx->launches += 4;
+  } else {
+    k_aj_cauchy_tgt<false, false><<<nbk, PBS, 0, s>>>(nbk, pvz, 2, nbk, pvz + 1, 2, pvq + 1, 2, B.psib, cpv, B.ztb);
+    k_aj_cauchy_src<false, false><<<nbk, PBS, 0, s>>>(nbk, pvz, 2, nbk, pvz + 1, 2, pvq + 1, 2, B.psib, cpv, nullptr,
+                                                      nullptr, nullptr, nullptr, B.qsb, B.zsb);
+  }
   k_aj_pv_fine<<<dim3(k, 3), SBS, smf, s>>>(st, dz, ul, hp, B.qsb, B.zsb, B.ztb, B.ulb, B.dzb, B.zb, nmax);
   ctx->launches += 3;
   EB_TRY(eb_check_launch(ctx, "adjoint: PV integral"));
@@ -876,9 +1116,18 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   note_ierr(info, ai.ierr);
   k_aj_lap_local<<<nblk(nbk, 256), 256, 0, s>>>(nbk, dz, ds, ka, hp, ul, B.laml, B.zb, B.kb, B.sb, B.ql);
   const double2 clp = make_double2(0.0, 1.0 / EB_PI);
-  k_aj_cauchy_tgt<true, true><<<nbk, PBS, 0, s>>>(nbk, z, 1, nbk, z, 1, B.ql, 1, B.laml, clp, B.zb);
-  k_aj_cauchy_src<true, true><<<nbk, PBS, 0, s>>>(nbk, z, 1, nbk, z, 1, B.ql, 1, B.laml, clp, ul, hp, B.zb, B.dzb,
-                                                  nullptr, nullptr);
+  if (dfp) {
+    k_df4<<<nb, 256, 0, s>>>(nbk, B.ql, 1, nullptr, qld);
+    k_df2<<<nb, 256, 0, s>>>(nbk, B.laml, xd);
+    k_aj_cauchy_tgt_df<true, true><<<nbk, PBS, 0, s>>>(nbk, zd, nbk, zd, qld, B.laml, clp, B.zb);
+    k_aj_cauchy_src_df<true, true><<<nbk, PBS, 0, s>>>(nbk, zd, nbk, zd, xd, clp, B.ql, 1, ul, hp, B.zb, B.dzb,
+                                                       nullptr, nullptr);
+    ctx->launches += 2;
+  } else {
+    k_aj_cauchy_tgt<true, true><<<nbk, PBS, 0, s>>>(nbk, z, 1, nbk, z, 1, B.ql, 1, B.laml, clp, B.zb);
+    k_aj_cauchy_src<true, true><<<nbk, PBS, 0, s>>>(nbk, z, 1, nbk, z, 1, B.ql, 1, B.laml, clp, ul, hp, B.zb, B.dzb,
+                                                    nullptr, nullptr);
+  }
   k_aj_extract<<<k, SBS, sm2, s>>>(st, z, B.zb, B.dzb, B.sb, B.kb, B.thb, B.ckb, B.zkb, yb_out, nmax);
   ctx->launches += 4;
   EB_TRY(eb_check_launch(ctx, "adjoint: Laplace operator and EXTRACTDAT"));

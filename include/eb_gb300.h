@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define EB_GB300_VERSION 5
+#define EB_GB300_VERSION 6
 
 /* Status codes. The reference prints and STOPs on FMM/GMRES errors
  * (stokesbubb.f:573-579, laplace.f:217-222, 395-398, pv_integral.f:183-188);
@@ -91,6 +91,10 @@ typedef struct eb_opts {
                        are direct O(N^2) sums in one kernel instead of the FMM: exact up
                        to rounding, and faster on few points (0: default 1024; -1: the
                        FMM always) */
+  int adj_df;       /* reverse mode (eb_rk_f_vjp): the O(nbk^2) derivative sums in
+                       double-float arithmetic on the FP32 pipes (about 48 bits; the
+                       positions relative to the first node): 0 default (on), 1 on,
+                       -1 off (native FP64) */
 } eb_opts;
 
 typedef struct eb_solve_info {

@@ -33,7 +33,7 @@ def test_python_binding_covers_header():
 
 def test_status_strings(eblib):
     assert eblib.eb_status_string(0) == b"ok"
-    assert eblib.eb_version() == 5
+    assert eblib.eb_version() == 6
 
 
 def test_context_without_device_fails_loudly(eblib):

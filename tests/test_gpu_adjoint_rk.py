@@ -48,11 +48,14 @@ def untied(cfg, seed, amp=1e-3):
     return np.ascontiguousarray(np.stack([z.real, z.imag], 1).reshape(-1))
 
 
+@pytest.mark.parametrize("pairs", ["df", "fp64"])
 @pytest.mark.parametrize("sums", ["direct", "fmm"])
 @pytest.mark.parametrize("case", list(CASES))
-def test_f_vjp_matches_autograd(gpu_ctx_factory, case, sums):
+def test_f_vjp_matches_autograd(gpu_ctx_factory, case, sums, pairs):
+    """pairs: the derivative sums in double-float (the default) or native FP64."""
     cfg = CASES[case]()
-    ctx = gpu_ctx_factory(gmres_tol=1e-14, direct_max=0 if sums == "direct" else -1)
+    ctx = gpu_ctx_factory(gmres_tol=1e-14, direct_max=0 if sums == "direct" else -1,
+                          adj_df=1 if pairs == "df" else -1)
     y = cfg.rku()
     rng = np.random.default_rng(90)
     v = rng.standard_normal(2 * cfg.nbk)
