@@ -144,6 +144,8 @@ SIGNATURES = {
     "eb_rk2_step_vjp": (_I, [_P, _I, _P, _D, _P, _P, ctypes.POINTER(Model), _P,
                              ctypes.POINTER(AdjointInfo), _I]),
     "eb_deformation": (_I, [_P, _I, _P, _P, ctypes.POINTER(_D), _P, _I]),
+    "eb_rk2_gradient": (_I, [_P, _I, _P, _D, _I, _P, ctypes.POINTER(Model), ctypes.POINTER(_D), _P, _P,
+                             ctypes.POINTER(AdjointInfo), _I]),
     "eb_batch_define": (_I, [_P, _I, _P, _P]),
     "eb_getfourier": (_I, [_P, _I, _P, _P, _P, _P, _I]),
     "eb_double": (_I, [_P, _I, _P, _P, _P, _P, _I]),

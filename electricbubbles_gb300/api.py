@@ -491,27 +491,22 @@ class Context:
 
     def rk2_gradient(self, nd, dt, y0, steps, cap=0.0, e0=0.0, mode="fp64"):
         """J = the deformation after `steps` RK2 steps from y0, and dJ/dy0, dJ/dE0 and
-        dJ/dcap by reverse mode: the forward steps keep one checkpoint (the state) per
-        step, the reverse pass recomputes each step's stages from its checkpoint."""
+        dJ/dcap by reverse mode (eb_rk2_gradient: one checkpoint, the state, per step on
+        the device; the reverse pass recomputes each step's stages from its checkpoint)."""
         nd = _host(nd, np.int32)
-        y = np.array(y0, dtype=np.float64, copy=True)
-        ckpt = []
-        for _ in range(int(steps)):
-            ckpt.append(y.copy())
-            self.rk2(nd, dt, y, cap=cap, e0=e0, mode=mode)
-        J, rbar = self.deformation(nd, y)
-        pe, pc = 0.0, 0.0
-        iters = {"lap_iters": 0, "stokes_iters": 0, "lap_adj_iters": 0, "stokes_adj_iters": 0, "ierr": 0}
-        for yc in reversed(ckpt):
-            p, info = self.rk2_vjp(nd, dt, yc, rbar, cap=cap, e0=e0, mode=mode)
-            pe += p["e0"]
-            pc += p["cap"]
-            for key in ("lap_iters", "stokes_iters", "lap_adj_iters", "stokes_adj_iters"):
-                iters[key] += info[key]
-            if iters["ierr"] == 0:
-                iters["ierr"] = info["ierr"]
-        return {"J": J, "y0": rbar, "e0": pe, "cap": pc, "info": iters}
-
+        if not _is_device(y0):
+            y0 = _host(y0, np.float64)
+        g = self._out(y0, 2 * int(nd.sum()), np.float64)
+        pb = np.zeros(2)
+        val = ctypes.c_double(0.0)
+        info = AdjointInfo()
+        m = self._model(cap, e0, 0.0, mode)
+        check("eb_rk2_gradient", self._lib.eb_rk2_gradient(self._h, int(nd.shape[0]), _ptr(nd), float(dt),
+                                                           int(steps), _ptr(y0), ctypes.byref(m),
+                                                           ctypes.byref(val), _ptr(g), _ptr(pb),
+                                                           ctypes.byref(info), _mem(y0, g)))
+        self._set_drops(nd)
+        return {"J": float(val.value), "y0": g, "e0": float(pb[0]), "cap": float(pb[1]), "info": info.as_dict()}
 
 def geometry_from_extract(ctx, cfg):
     """Install cfg's geometry by EXTRACTDAT on the GPU; returns the geometry dict."""

@@ -243,6 +243,7 @@ struct eb_ctx {
   DevBuf adj_a, adj_b, adj_s;      // transposed operators: two node sums, per-drop sums
   DevBuf aj, aj_part, aj_rk;       // adjoint of F: cotangents, per-drop partials, RK2 step state
   DevBuf aj_df;                    // adjoint of F: double-float positions, charges and cotangents
+  DevBuf aj_ck;                    // eb_rk2_gradient: the checkpointed states and the cotangent
   DevBuf rk_y, rk_y1, rk_d0, rk_phi;  // RK state, predictor, derivative, dt * F(y)
 
   // GMRES workspace

@@ -1273,3 +1273,50 @@ int eb_deformation(eb_ctx* ctx, int k, const int* nd, const double* rku, double*
   *value = J;
   return EB_OK;
 }
+
+int eb_rk2_gradient(eb_ctx* ctx, int k, const int* nd, double dt, int nsteps, const double* y0,
+                    const eb_model* model, double* value, double* y0_bar, double* param_bar,
+                    eb_adjoint_info* info, int mem) {
+  if (!ctx || k <= 0 || !nd || !y0 || !value || !y0_bar || nsteps < 0) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  EB_TRY(check_adjoint_model(ctx, model));
+  EB_TRY(check_drops(k, nd));
+  cudaSetDevice(ctx->device);
+  if (info) *info = eb_adjoint_info{};
+  int nbk = 0;
+  for (int b = 0; b < k; ++b) nbk += nd[b];
+  const size_t neq = 2 * (size_t)nbk, bytes = sizeof(double) * neq;
+  cudaStream_t s = ctx->stream;
+  // checkpoints: the state before each step, then the final state; and the cotangent
+  EB_TRY(ctx->aj_ck.ensure(bytes * ((size_t)nsteps + 2)));
+  double* ck = ctx->aj_ck.as<double>();
+  double* rb = ck + neq * ((size_t)nsteps + 1);
+  EB_CUDA_TRY(cudaMemcpyAsync(ck, y0, bytes, mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+  for (int st = 0; st < nsteps; ++st) {
+    double* y = ck + neq * (size_t)(st + 1);
+    EB_CUDA_TRY(cudaMemcpyAsync(y, ck + neq * (size_t)st, bytes, cudaMemcpyDeviceToDevice, s));
+    eb_stage_info si{};
+    EB_TRY(eb_rk2_step(ctx, k, nd, dt, y, model, &si, EB_DEVICE));
+    if (info) {
+      info->lap_iters += si.lap_iters;
+      info->stokes_iters += si.stokes_iters;
+    }
+    note_ierr(info, si.lap_ierr);
+    note_ierr(info, si.stokes_ierr);
+  }
+  EB_TRY(eb_deformation(ctx, k, nd, ck + neq * (size_t)nsteps, value, rb, EB_DEVICE));
+  for (int st = nsteps - 1; st >= 0; --st) {
+    eb_adjoint_info ai{};
+    EB_TRY(eb_rk2_step_vjp(ctx, k, nd, dt, ck + neq * (size_t)st, rb, model, param_bar, &ai, EB_DEVICE));
+    if (info) {
+      info->lap_iters += ai.lap_iters;
+      info->stokes_iters += ai.stokes_iters;
+      info->lap_adj_iters += ai.lap_adj_iters;
+      info->stokes_adj_iters += ai.stokes_adj_iters;
+    }
+    note_ierr(info, ai.ierr);
+  }
+  EB_CUDA_TRY(cudaMemcpyAsync(y0_bar, rb, bytes, mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  EB_CUDA_TRY(cudaStreamSynchronize(s));
+  return EB_OK;
+}

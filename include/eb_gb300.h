@@ -391,6 +391,14 @@ int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* 
 int eb_deformation(eb_ctx* ctx, int k, const int* nd, const double* rku, double* value, double* rku_bar,
                    int mem);
 
+/* The whole reverse pass: value = the deformation after nsteps RK2 steps of size dt from
+ * y0; y0_bar = its gradient with respect to y0, param_bar[0] += dJ/dE0, param_bar[1] +=
+ * dJ/dcap (param_bar may be NULL). The states before each step are kept on the device
+ * (nsteps + 2 vectors of 2 nbk doubles), each step's stages recomputed on the way back. */
+int eb_rk2_gradient(eb_ctx* ctx, int k, const int* nd, double dt, int nsteps, const double* y0,
+                    const eb_model* model, double* value, double* y0_bar, double* param_bar,
+                    eb_adjoint_info* info, int mem);
+
 /* Wall-bounded flow, the IFLAG2 = 1 branch of CADAPDR / CADAPMOD (COMMON /wallinfo/,
  * electric.f:55; cadapdrop.f:142-145, cadapdrop2.f:159-197 and 690-721, cadap2.f:1468-1586):
  * with iwall = 1 every Stokes sum of the installed geometry (eb_stokes_matvec,
