@@ -14,7 +14,9 @@
 //   k_aj_vel_local  INTERFACENEW's pointwise terms and the transpose of udot = D u
 //   k_aj_stokes_*   the Stokes sums' derivatives with respect to targets, sources and
 //                   charges (direct O(N^2), a block per target or per source; the
-//                   target side of both sums in one pass after the transposed solve)
+//                   target side of both sums in one pass after the transposed solve;
+//                   the _df forms, in double-float on the FP32 pipes, unless
+//                   eb_opts.adj_df = -1)
 //   (solve)         lambda = A_S^-T ubar: eb_stokes_solve_adjoint
 //   k_aj_op_local   FASMVP's drop sums (pk, za) and self terms at the density u, with
 //                   cotangent -lambda; the Stokes sums follow with the same cotangent
@@ -30,6 +32,8 @@
 // The forward values come from one rerun of the stage (eb_stage_f_keep): the geometry in
 // the context, the Laplace density, psi and dphi/dn in st_lap, the Stokes density in
 // st_u, INTERFACENEW's full sum g; PVINTEV's fine points from eb_pv_fine.
+// eb_rk2_step_vjp transposes one RK2 step from its start state, eb_rk2_gradient runs the
+// forward steps, keeps each step's start state on the device and walks them back.
 #include <algorithm>
 #include <cmath>
 #include <vector>
