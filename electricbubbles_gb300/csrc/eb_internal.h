@@ -351,9 +351,12 @@ int eb_batch_translate_fine(eb_ctx* ctx, double2* zf);
 // solve.cu: the info of deferred plain solve `slot` (after the caller's synchronisation)
 int eb_defer_info(eb_ctx* ctx, int slot, eb_solve_info* inf);
 // One RK stage F (eb_spectral.cu) with synchronous solves; gout (device, optional)
-// receives INTERFACENEW's full velocity sum g (Un = Re(-i g conj(zn))).
+// receives INTERFACENEW's full velocity sum g (Un = Re(-i g conj(zn))). ul_in / u_in
+// (device, optional) stand in for the Laplace / Stokes solve with kept solutions; ul_out /
+// u_out receive the solutions.
 int eb_stage_f_keep(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
-                    eb_stage_info* info, double2* gout);
+                    eb_stage_info* info, double2* gout, const double* ul_in = nullptr,
+                    const double* u_in = nullptr, double* ul_out = nullptr, double* u_out = nullptr);
 // PVINTEV's fine points and charges of the Laplace density ul (charges of ul dz, as
 // DIRICH_NEU_MAP forms them) into ctx->pvz / ctx->pvq, interleaved even/odd fine nodes.
 int eb_pv_fine(eb_ctx* ctx, const double* ul);

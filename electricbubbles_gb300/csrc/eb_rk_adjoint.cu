@@ -936,6 +936,23 @@ __global__ void k_axpby(int n, double a, const double* __restrict__ x, double b,
   if (i < n) out[i] = a * x[i] + b * y[i];
 }
 
+// RK2 as eb_rk2_step forms it: phi0 = dt d0, y1 = y + phi0; y_next = y + phi0/2 + (dt d1)/2
+__global__ void k_rk_pred(int n, double dt, const double* __restrict__ y, const double* __restrict__ d0,
+                          double* __restrict__ phi0, double* __restrict__ y1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p = dt * d0[i];
+  phi0[i] = p;
+  y1[i] = y[i] + p;
+}
+
+__global__ void k_rk_corr(int n, double dt, const double* __restrict__ y, const double* __restrict__ phi0,
+                          const double* __restrict__ d1, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = y[i] + 0.5 * phi0[i] + 0.5 * (dt * d1[i]);
+}
+
 __global__ void k_sum3(int n, const double* __restrict__ x, const double* __restrict__ y,
                        const double* __restrict__ z, double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -997,8 +1014,11 @@ void note_ierr(eb_adjoint_info* info, int ierr) {
 
 // v^T dF at y (device arrays, 2 nbk each) into yb_out (device); param_bar (host, 2) += the
 // E0 and cap parts.
+// ul_in / u_in (device, optional): the stage's solutions kept from its forward run, which
+// the stage's rerun then replays instead of solving
 int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* v, const eb_model* m,
-              double* yb_out, double* param_bar, eb_adjoint_info* info) {
+              double* yb_out, double* param_bar, eb_adjoint_info* info, const double* ul_in = nullptr,
+              const double* u_in = nullptr) {
   cudaStream_t s = ctx->stream;
   int nbk = 0, nmax = 0;
   for (int b = 0; b < k; ++b) {
@@ -1009,7 +1029,7 @@ int f_vjp_dev(eb_ctx* ctx, int k, const int* nd, const double* y, const double* 
   AjBufs B;
   EB_TRY(aj_bufs(ctx, nbk, k, B));
   eb_stage_info si{};
-  EB_TRY(eb_stage_f_keep(ctx, k, nd, y, reinterpret_cast<double*>(B.f), m, &si, B.gw));
+  EB_TRY(eb_stage_f_keep(ctx, k, nd, y, reinterpret_cast<double*>(B.f), m, &si, B.gw, ul_in, u_in));
   if (info) {
     info->lap_iters += si.lap_iters;
     info->stokes_iters += si.stokes_iters;
@@ -1187,14 +1207,17 @@ int eb_rk_f_vjp(eb_ctx* ctx, int k, const int* nd, const double* rku, const doub
   return EB_OK;
 }
 
-int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* ybar, double* rbar,
-                    const eb_model* model, double* param_bar, eb_adjoint_info* info, int mem) {
-  if (!ctx || k <= 0 || !nd || !ybar || !rbar) return EB_ERR_ARG;
-  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
-  EB_TRY(check_adjoint_model(ctx, model));
-  EB_TRY(check_drops(k, nd));
-  cudaSetDevice(ctx->device);
-  if (info) *info = eb_adjoint_info{};
+namespace {
+
+// Kept solutions of one RK2 step's two stages (device, nbk + 2 nbk doubles each), or null.
+struct StepSolutions {
+  const double *ul0, *u0, *ul1, *u1;
+};
+
+// The transpose of one RK2 step on device arrays: rb (2 nbk, in: dJ/dy after the step,
+// out: before it) from the step's start state y (2 nbk).
+int step_vjp_dev(eb_ctx* ctx, int k, const int* nd, double dt, const double* y, double* rb_io,
+                 const eb_model* model, double* param_bar, eb_adjoint_info* info, const StepSolutions& ss) {
   int nbk = 0;
   for (int b = 0; b < k; ++b) nbk += nd[b];
   const int neq = 2 * nbk;
@@ -1208,12 +1231,11 @@ int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* 
   double* vv = rb + neq;
   double* g2 = vv + neq;
   double* g1 = g2 + neq;
-  const cudaMemcpyKind kin = mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  EB_CUDA_TRY(cudaMemcpyAsync(y0, ybar, bytes, kin, s));
-  EB_CUDA_TRY(cudaMemcpyAsync(rb, rbar, bytes, kin, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(y0, y, bytes, cudaMemcpyDeviceToDevice, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(rb, rb_io, bytes, cudaMemcpyDeviceToDevice, s));
   // the predictor y1 = y0 + dt F(y0)
   eb_stage_info si{};
-  EB_TRY(eb_stage_f_keep(ctx, k, nd, y0, y1, model, &si, nullptr));
+  EB_TRY(eb_stage_f_keep(ctx, k, nd, y0, y1, model, &si, nullptr, ss.ul0, ss.u0));
   if (info) {
     info->lap_iters += si.lap_iters;
     info->stokes_iters += si.stokes_iters;
@@ -1226,14 +1248,44 @@ int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* 
   // g1 = J(y0)^T (dt/2 rbar + dt g2), rbar_out = rbar + g2 + g1
   k_axpby<<<nb, 256, 0, s>>>(neq, 0.5 * dt, rb, 0.0, rb, vv);
   ctx->launches += 2;
-  EB_TRY(f_vjp_dev(ctx, k, nd, y1, vv, model, g2, param_bar, info));
+  EB_TRY(f_vjp_dev(ctx, k, nd, y1, vv, model, g2, param_bar, info, ss.ul1, ss.u1));
   k_axpby<<<nb, 256, 0, s>>>(neq, 0.5 * dt, rb, dt, g2, vv);
   eb_count_launch(ctx);
-  EB_TRY(f_vjp_dev(ctx, k, nd, y0, vv, model, g1, param_bar, info));
+  EB_TRY(f_vjp_dev(ctx, k, nd, y0, vv, model, g1, param_bar, info, ss.ul0, ss.u0));
   k_sum3<<<nb, 256, 0, s>>>(neq, rb, g2, g1, rb);
   eb_count_launch(ctx);
   EB_TRY(eb_check_launch(ctx, "rk2 step adjoint"));
-  EB_CUDA_TRY(cudaMemcpyAsync(rbar, rb, bytes, mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+  EB_CUDA_TRY(cudaMemcpyAsync(rb_io, rb, bytes, cudaMemcpyDeviceToDevice, s));
+  return EB_OK;
+}
+
+}  // namespace
+
+int eb_rk2_step_vjp(eb_ctx* ctx, int k, const int* nd, double dt, const double* ybar, double* rbar,
+                    const eb_model* model, double* param_bar, eb_adjoint_info* info, int mem) {
+  if (!ctx || k <= 0 || !nd || !ybar || !rbar) return EB_ERR_ARG;
+  if (mem != EB_HOST && mem != EB_DEVICE) return EB_ERR_ARG;
+  EB_TRY(check_adjoint_model(ctx, model));
+  EB_TRY(check_drops(k, nd));
+  cudaSetDevice(ctx->device);
+  if (info) *info = eb_adjoint_info{};
+  int nbk = 0;
+  for (int b = 0; b < k; ++b) nbk += nd[b];
+  const size_t bytes = sizeof(double) * 2 * (size_t)nbk;
+  cudaStream_t s = ctx->stream;
+  const double* y = ybar;
+  double* r = rbar;
+  if (mem == EB_HOST) {  // staged through the checkpoint buffer
+    EB_TRY(ctx->aj_ck.ensure(2 * bytes));
+    double* yd = ctx->aj_ck.as<double>();
+    double* rd = yd + 2 * (size_t)nbk;
+    EB_CUDA_TRY(cudaMemcpyAsync(yd, ybar, bytes, cudaMemcpyHostToDevice, s));
+    EB_CUDA_TRY(cudaMemcpyAsync(rd, rbar, bytes, cudaMemcpyHostToDevice, s));
+    y = yd;
+    r = rd;
+  }
+  EB_TRY(step_vjp_dev(ctx, k, nd, dt, y, r, model, param_bar, info, StepSolutions{}));
+  if (mem == EB_HOST) EB_CUDA_TRY(cudaMemcpyAsync(rbar, r, bytes, cudaMemcpyDeviceToHost, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));
   return EB_OK;
 }
@@ -1289,36 +1341,51 @@ int eb_rk2_gradient(eb_ctx* ctx, int k, const int* nd, double dt, int nsteps, co
   if (info) *info = eb_adjoint_info{};
   int nbk = 0;
   for (int b = 0; b < k; ++b) nbk += nd[b];
-  const size_t neq = 2 * (size_t)nbk, bytes = sizeof(double) * neq;
+  const size_t n = (size_t)nbk, neq = 2 * n, bytes = sizeof(double) * neq;
   cudaStream_t s = ctx->stream;
-  // checkpoints: the state before each step, then the final state; and the cotangent
-  EB_TRY(ctx->aj_ck.ensure(bytes * ((size_t)nsteps + 2)));
+  // per step: its start state and its two stages' Laplace (nbk) and Stokes (2 nbk)
+  // solutions; then the final state, the cotangent and two stage derivatives
+  const size_t per_step = neq + 2 * (n + neq);
+  EB_TRY(ctx->aj_ck.ensure(sizeof(double) * (per_step * (size_t)nsteps + 4 * neq)));
   double* ck = ctx->aj_ck.as<double>();
-  double* rb = ck + neq * ((size_t)nsteps + 1);
-  EB_CUDA_TRY(cudaMemcpyAsync(ck, y0, bytes, mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-  for (int st = 0; st < nsteps; ++st) {
-    double* y = ck + neq * (size_t)(st + 1);
-    EB_CUDA_TRY(cudaMemcpyAsync(y, ck + neq * (size_t)st, bytes, cudaMemcpyDeviceToDevice, s));
-    eb_stage_info si{};
-    EB_TRY(eb_rk2_step(ctx, k, nd, dt, y, model, &si, EB_DEVICE));
+  auto state = [&](int st) { return ck + per_step * (size_t)st; };
+  auto sol = [&](int st, int which) { return ck + per_step * (size_t)st + neq + (size_t)which * (n + neq); };
+  double* yfin = ck + per_step * (size_t)nsteps;
+  double* rb = yfin + neq;
+  double* d0 = rb + neq;
+  double* d1 = d0 + neq;
+  EB_CUDA_TRY(cudaMemcpyAsync(nsteps > 0 ? state(0) : yfin, y0, bytes,
+                              mem == EB_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+  const int nb = nblk((long long)neq, 256);
+  auto add_info = [&](const eb_stage_info& si) {
     if (info) {
       info->lap_iters += si.lap_iters;
       info->stokes_iters += si.stokes_iters;
     }
     note_ierr(info, si.lap_ierr);
     note_ierr(info, si.stokes_ierr);
+  };
+  // forward: the RK2 steps (electric.f:762-786), each stage's solutions kept
+  for (int st = 0; st < nsteps; ++st) {
+    double* y = state(st);
+    double* ynext = st + 1 < nsteps ? state(st + 1) : yfin;
+    eb_stage_info si{};
+    EB_TRY(eb_stage_f_keep(ctx, k, nd, y, d0, model, &si, nullptr, nullptr, nullptr, sol(st, 0), sol(st, 0) + n));
+    add_info(si);
+    k_rk_pred<<<nb, 256, 0, s>>>((int)neq, dt, y, d0, d0, ynext);  // phi0 in d0, the predictor in ynext
+    eb_count_launch(ctx);
+    si = eb_stage_info{};
+    EB_TRY(eb_stage_f_keep(ctx, k, nd, ynext, d1, model, &si, nullptr, nullptr, nullptr, sol(st, 1),
+                           sol(st, 1) + n));
+    add_info(si);
+    k_rk_corr<<<nb, 256, 0, s>>>((int)neq, dt, y, d0, d1, ynext);
+    eb_count_launch(ctx);
   }
-  EB_TRY(eb_deformation(ctx, k, nd, ck + neq * (size_t)nsteps, value, rb, EB_DEVICE));
+  EB_TRY(eb_deformation(ctx, k, nd, yfin, value, rb, EB_DEVICE));
+  // reverse: each step's stages replayed with their kept solutions
   for (int st = nsteps - 1; st >= 0; --st) {
-    eb_adjoint_info ai{};
-    EB_TRY(eb_rk2_step_vjp(ctx, k, nd, dt, ck + neq * (size_t)st, rb, model, param_bar, &ai, EB_DEVICE));
-    if (info) {
-      info->lap_iters += ai.lap_iters;
-      info->stokes_iters += ai.stokes_iters;
-      info->lap_adj_iters += ai.lap_adj_iters;
-      info->stokes_adj_iters += ai.stokes_adj_iters;
-    }
-    note_ierr(info, ai.ierr);
+    const StepSolutions ss{sol(st, 0), sol(st, 0) + n, sol(st, 1), sol(st, 1) + n};
+    EB_TRY(step_vjp_dev(ctx, k, nd, dt, state(st), rb, model, param_bar, info, ss));
   }
   EB_CUDA_TRY(cudaMemcpyAsync(y0_bar, rb, bytes, mem == EB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   EB_CUDA_TRY(cudaStreamSynchronize(s));

@@ -947,9 +947,14 @@ struct StageSlots {
   int lap = -1, stokes = -1;
 };
 
-// gout (device, optional): INTERFACENEW's full velocity sum (interface_velocity_impl)
+// gout (device, optional): INTERFACENEW's full velocity sum (interface_velocity_impl).
+// Solutions (device, optional): ul_in / u_in replace the Laplace / Stokes solve by a
+// solution kept from an earlier run of the same stage (the reverse pass replays a stage
+// without its solves); ul_out / u_out receive this run's solutions.
 int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
-            eb_stage_info* info, StageSlots* slots = nullptr, double2* gout = nullptr) {
+            eb_stage_info* info, StageSlots* slots = nullptr, double2* gout = nullptr,
+            const double* ul_in = nullptr, const double* u_in = nullptr, double* ul_out = nullptr,
+            double* u_out = nullptr) {
   // zbond != 0: wall-bounded (READINI's iwall, electric.f:321-326), set before the
   // install so that the tree takes the wall
   const double2 zb = make_double2(m->zbond[0], m->zbond[1]);
@@ -974,10 +979,15 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   double* psi = phi + nbk;
   double* dphi = psi + nbk;
   eb_solve_info li{}, si{};
-  k_lap_bc<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->z.as<double2>(), rl);
-  eb_count_launch(ctx);
   int s0 = ctx->ndefer;
-  EB_TRY(eb_laplace_solve(ctx, nbk, rl, ul, m->mode, &li, EB_DEVICE));
+  if (ul_in) {
+    EB_CUDA_TRY(cudaMemcpyAsync(ul, ul_in, sizeof(double) * nbk, cudaMemcpyDeviceToDevice, s));
+  } else {
+    k_lap_bc<<<nblk(nbk, 256), 256, 0, s>>>(nbk, ctx->z.as<double2>(), rl);
+    eb_count_launch(ctx);
+    EB_TRY(eb_laplace_solve(ctx, nbk, rl, ul, m->mode, &li, EB_DEVICE));
+    if (ul_out) EB_CUDA_TRY(cudaMemcpyAsync(ul_out, ul, sizeof(double) * nbk, cudaMemcpyDeviceToDevice, s));
+  }
   const int lap_slot = ctx->ndefer > s0 ? s0 : -1;
   // the FP64 sums of the stage outside the solves: plain mode FP64 (native or
   // double-float as df64 says), refined mode the arithmetic of its FP64 residuals
@@ -989,10 +999,15 @@ int stage_f(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, 
   } else {
     EB_CUDA_TRY(cudaMemsetAsync(ctx->st_zc.p, 0, sizeof(double2) * (size_t)k, s));
   }
-  EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, zb, ctx->st_zc.as<double2>(), ctx->st_rhs.as<double2>()));
   s0 = ctx->ndefer;
-  EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
-                         EB_DEVICE));
+  if (u_in) {
+    EB_CUDA_TRY(cudaMemcpyAsync(ctx->st_u.p, u_in, sizeof(double2) * nbk, cudaMemcpyDeviceToDevice, s));
+  } else {
+    EB_TRY(setvelf_dev(ctx, dphi, m->cap, m->e0, zb, ctx->st_zc.as<double2>(), ctx->st_rhs.as<double2>()));
+    EB_TRY(eb_stokes_solve(ctx, 2 * nbk, ctx->st_rhs.as<double>(), ctx->st_u.as<double>(), m->mode, &si,
+                           EB_DEVICE));
+    if (u_out) EB_CUDA_TRY(cudaMemcpyAsync(u_out, ctx->st_u.p, sizeof(double2) * nbk, cudaMemcpyDeviceToDevice, s));
+  }
   const int stokes_slot = ctx->ndefer > s0 ? s0 : -1;
   if (slots) {
     slots->lap = lap_slot;
@@ -1085,9 +1100,10 @@ int check_model(const eb_model* m) {
 }  // namespace
 
 int eb_stage_f_keep(eb_ctx* ctx, int k, const int* nd, const double* rku, double* rkup, const eb_model* m,
-                    eb_stage_info* info, double2* gout) {
+                    eb_stage_info* info, double2* gout, const double* ul_in, const double* u_in, double* ul_out,
+                    double* u_out) {
   EB_TRY(check_model(m));
-  return stage_f(ctx, k, nd, rku, rkup, m, info, nullptr, gout);
+  return stage_f(ctx, k, nd, rku, rkup, m, info, nullptr, gout, ul_in, u_in, ul_out, u_out);
 }
 
 int eb_pv_fine(eb_ctx* ctx, const double* ul) {

@@ -393,8 +393,9 @@ int eb_deformation(eb_ctx* ctx, int k, const int* nd, const double* rku, double*
 
 /* The whole reverse pass: value = the deformation after nsteps RK2 steps of size dt from
  * y0; y0_bar = its gradient with respect to y0, param_bar[0] += dJ/dE0, param_bar[1] +=
- * dJ/dcap (param_bar may be NULL). The states before each step are kept on the device
- * (nsteps + 2 vectors of 2 nbk doubles), each step's stages recomputed on the way back. */
+ * dJ/dcap (param_bar may be NULL). The state before each step and its two stages' Laplace
+ * and Stokes solutions are kept on the device (8 nbk doubles per step, plus 8 nbk), and the
+ * reverse pass replays each step's stages with those solutions. */
 int eb_rk2_gradient(eb_ctx* ctx, int k, const int* nd, double dt, int nsteps, const double* y0,
                     const eb_model* model, double* value, double* y0_bar, double* param_bar,
                     eb_adjoint_info* info, int mem);
