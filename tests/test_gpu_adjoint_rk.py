@@ -162,6 +162,31 @@ def test_rk2_gradient_matches_autograd(gpu_ctx_factory):
     assert abs(g["cap"] - gc) < 1e-8 * abs(gc)
 
 
+def test_rk2_gradient_equals_its_steps(gpu_ctx_factory):
+    """eb_rk2_gradient (stages replayed with the solutions kept from the forward pass, on
+    device arrays) against the composition of eb_rk2_step, eb_deformation and
+    eb_rk2_step_vjp (stages re-solved, host arrays), three steps."""
+    cfg = CASES["3x64"]()
+    ctx = gpu_ctx_factory(gmres_tol=1e-14)
+    y0 = untied(cfg, 99)
+    dt, e0, cap, steps = 1e-2, 0.6, 0.2, 3
+    ys = [y0.copy()]
+    for _ in range(steps):
+        y = ys[-1].copy()
+        ctx.rk2(cfg.nd, dt, y, cap=cap, e0=e0)
+        ys.append(y)
+    J, rbar = ctx.deformation(cfg.nd, ys[-1])
+    pe = pc = 0.0
+    for yc in reversed(ys[:-1]):
+        p, _ = ctx.rk2_vjp(cfg.nd, dt, yc, rbar, cap=cap, e0=e0)
+        pe += p["e0"]
+        pc += p["cap"]
+    g = ctx.rk2_gradient(cfg.nd, dt, torch.from_numpy(y0).cuda(), steps, cap=cap, e0=e0)
+    assert abs(g["J"] - J) < 1e-13 * abs(J)
+    assert relmax(g["y0"].cpu().numpy(), rbar) < 1e-9
+    assert abs(g["e0"] - pe) < 1e-10 * abs(pe) and abs(g["cap"] - pc) < 1e-10 * abs(pc)
+
+
 def smooth_direction(cfg, rng):
     """A unit node displacement made of each drop's Fourier modes 1 to 5."""
     z = np.zeros(cfg.nbk, complex)
