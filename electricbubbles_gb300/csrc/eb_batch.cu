@@ -702,8 +702,10 @@ int bg_cycle_graph(BatchWork& B, eb_op_fn op, int prec, const double* b, double*
   return EB_OK;
 }
 
+// defer_iters: the cycle's iteration count is queued to ctx->b_host_act[2] without a wait
+// (the caller reads it after its own synchronisation) instead of added to *total_iters.
 int bg_cycle(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bool have_x0,
-             const int* skip, int* total_iters, int slot) {
+             const int* skip, int* total_iters, int slot, bool defer_iters = false) {
   eb_ctx* ctx = B.ctx;
   cudaStream_t st = ctx->stream;
   const long long l0 = ctx->launches;
@@ -726,6 +728,7 @@ int bg_cycle(BatchWork& B, eb_op_fn op, int prec, const double* b, double* x, bo
     EB_TRY(bg_enqueue_post(B, have_x0, skip, x));
   }
   EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_host_act + 2, B.jdev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (defer_iters) return EB_OK;
   EB_CUDA_TRY(cudaStreamSynchronize(st));
   *total_iters += ctx->b_host_act[2];
   return EB_OK;
@@ -817,10 +820,8 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
     for (outer = 1; outer <= ctx->opts.max_outer && left > 0; ++outer) {
       k_bg_set_tol<<<nblk(S, 128), 128, 0, st>>>(S, B.ctl, ctx->opts.inner_tol, outer > 1 ? itol : nullptr);
       eb_count_launch(ctx);
-      int its = 0;
-      EB_TRY(bg_cycle(B, op, EB_FP32, r, dd, false, skip, &its, 1));
-      inf.iters += its;
-      inf.matvecs32 += its;
+      // the cycle's iteration count is read after this step's one wait (below)
+      EB_TRY(bg_cycle(B, op, EB_FP32, r, dd, false, skip, nullptr, 1, true));
       // x += d on the simulations that took part
       k_bg_axpy<<<S, BBS, 0, st>>>(B.seg, skip, dd, x);
       eb_count_launch(ctx);
@@ -833,6 +834,8 @@ int eb_batch_solve(eb_ctx* ctx, int n, eb_op_fn op, bool stokes, const double* r
       EB_CUDA_TRY(cudaMemcpyAsync(ctx->b_host_act + 1, nleft, sizeof(int), cudaMemcpyDeviceToHost, st));
       EB_CUDA_TRY(cudaStreamSynchronize(st));
       left = ctx->b_host_act[1];
+      inf.iters += ctx->b_host_act[2];
+      inf.matvecs32 += ctx->b_host_act[2];
     }
     std::vector<double> he(S);
     EB_CUDA_TRY(cudaMemcpyAsync(he.data(), err, sizeof(double) * S, cudaMemcpyDeviceToHost, st));
